@@ -1,0 +1,268 @@
+"""Host-side Python mirror of the dccm_gb300 C ABI.
+
+The product is the C-ABI library ``libdccm_gb300.so`` (CUDA kernels for
+sm_103a behind ``include/dccm_gb300.h``).  This module loads it with ctypes
+and exposes the reference's procedure names with the reference's argument
+meaning, so that tests and the benchmark read like calls into the Fortran
+modules they replace:
+
+* ``DSFCM_Util_SfcBulkFlux_Get`` (sfc/DSFCM_Util_SfcBulkFlux_mod.f90:108-151)
+* ``gen_gridmapfile_lonlat2lonlat`` and ``set_mappingTable_interpCoef``
+  (common/grid_mapping_util_jones99.f90:35-41, :446-462)
+* ``RemapPlan`` / ``interpolate_data`` (common/interpolation_data_latlon_mod.f90:116-306,
+  common/interpolate_data.f90:1-15)
+* ``ShtPlan`` (SPML w_Initial + transforms, tool/gmapgen/gmapgen_main.f90:262-305)
+
+There is no fallback: if the library is missing or cannot be loaded every
+call raises.  Errors from the library (negative status codes) raise
+``DccmError``.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libdccm_gb300.so")
+
+FLUX_ARGS = [
+    "WindStressX", "WindStressY", "SenHFlx", "QVapMFlx", "LatHFlx",
+    "SfcVelTransCoef", "SfcTempTransCoef", "SfcQVapTransCoef",
+    "DelVarImplCPL", "SUwRFlx", "LUwRFlx", "SfcHFlx_ns", "SfcHFlx_sr",
+    "DSfcHFlxDTs", "WindU", "WindV", "SfcAirTemp", "QVap1", "SDwRFlx",
+    "LDwRFlx", "ImplCplCoef1", "ImplCplCoef2", "SfcTemp", "SfcAlbedo",
+    "SIceCon", "a_Sig1Info", "SfcHeight", "SfcPress",
+]
+FLUX_OUT = FLUX_ARGS[:14]
+FLUX_IN = FLUX_ARGS[14:]
+FLUX_SLOTS = {n: 3 for n in FLUX_OUT}
+FLUX_SLOTS.update({"DelVarImplCPL": 4, "ImplCplCoef1": 4, "ImplCplCoef2": 4,
+                   "SfcTemp": 3, "SfcAlbedo": 3})
+
+J99_REF, J99_CONSERVE = 0, 1
+SHT_FP64, SHT_MIXED = 0, 1
+
+
+class DccmError(RuntimeError):
+    def __init__(self, status, what=""):
+        self.status = status
+        msg = _lib.dccm_status_string(status).decode() if _lib is not None else str(status)
+        super().__init__("%s: %s (status %d, cuda %d)" % (what, msg, status,
+                                                          _lib.dccm_last_cuda_error() if _lib else 0))
+
+
+class FluxArgs(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_void_p) for n in FLUX_ARGS]
+
+
+class SfcGrid(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int) for n in ("IA", "JA", "IS", "IE", "JS", "JE")]
+
+
+_lib = None
+_SIGS = {
+    "dccm_status_string": (ctypes.c_char_p, [ctypes.c_int]),
+    "dccm_abi_version": (ctypes.c_int, []),
+    "dccm_last_cuda_error": (ctypes.c_int, []),
+    "dccm_sfc_bulk_flux_get": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "dccm_sfc_bulk_flux_get_dev": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "dccm_j99_generate": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
+                                         ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
+                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                         ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]),
+    "dccm_remap_table_size": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "dccm_remap_table_rows": (ctypes.c_int, [ctypes.c_void_p] * 6),
+    "dccm_remap_table_write": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
+    "dccm_remap_table_read": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_void_p]),
+    "dccm_remap_table_index": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                              ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "dccm_remap_table_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "dccm_remap_plan_create": (ctypes.c_int, [ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
+                                              ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                              ctypes.c_void_p]),
+    "dccm_remap_plan_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "dccm_remap_plan_info": (ctypes.c_int, [ctypes.c_void_p] * 4),
+    "dccm_interpolate_data": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p,
+                                             ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int]),
+    "dccm_remap_apply_dev": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+                                            ctypes.c_int64, ctypes.c_int, ctypes.c_void_p]),
+    "dccm_area_integral_dev": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+                                              ctypes.c_void_p, ctypes.c_void_p]),
+}
+
+
+def exported_symbols():
+    """Names the C ABI exports (the declarations of include/dccm_gb300.h)."""
+    return sorted(_SIGS)
+
+
+def load(path=None):
+    """Load the library (raises if it is missing: there is no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise ImportError("libdccm_gb300.so not built (%s); run __graft_entry__.build()" % path)
+    L = ctypes.CDLL(path)
+    for name, (res, args) in _SIGS.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def _check(st, what):
+    if st != 0:
+        raise DccmError(st, what)
+
+
+def _p(a):
+    """Pointer of a numpy array or a torch tensor (device or host)."""
+    if a is None:
+        return None
+    if hasattr(a, "data_ptr"):
+        return ctypes.c_void_p(a.data_ptr())
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _stream(s):
+    if s is None:
+        return None
+    if hasattr(s, "cuda_stream"):
+        return ctypes.c_void_p(s.cuda_stream)
+    return ctypes.c_void_p(int(s))
+
+
+# ------------------------------------------------------------- bulk flux
+def DSFCM_Util_SfcBulkFlux_Get(arrays, IA, JA, IS, IE, JS, JE, device=False, stream=None):
+    """Run the bulk flux on a dict of Fortran-ordered arrays (names of the
+    reference's dummy arguments without the xy_/xya_/a_ prefixes, except
+    a_Sig1Info).  Host numpy arrays use the host entry point; torch CUDA
+    tensors with device=True use the device entry point."""
+    L = load()
+    a = FluxArgs()
+    keep = []
+    for n in FLUX_ARGS:
+        arr = arrays[n]
+        if n == "a_Sig1Info" and device:
+            arr = np.ascontiguousarray(np.asarray(arr.cpu() if hasattr(arr, "cpu") else arr, np.float64))
+            keep.append(arr)
+        setattr(a, n, _p(arr).value)
+    g = SfcGrid(IA, JA, IS, IE, JS, JE)
+    if device:
+        _check(L.dccm_sfc_bulk_flux_get_dev(ctypes.byref(a), ctypes.byref(g), _stream(stream)),
+               "dccm_sfc_bulk_flux_get_dev")
+    else:
+        _check(L.dccm_sfc_bulk_flux_get(ctypes.byref(a), ctypes.byref(g)), "dccm_sfc_bulk_flux_get")
+
+
+# ------------------------------------------------------------- remap table
+class RemapTable:
+    """Rows (iD, jD, iS, jS, w) of a Jones-99 table held by the library."""
+
+    def __init__(self, handle):
+        self.h = handle
+
+    @property
+    def nrow(self):
+        n = ctypes.c_int64(0)
+        _check(load().dccm_remap_table_size(self.h, ctypes.byref(n)), "dccm_remap_table_size")
+        return n.value
+
+    def rows(self):
+        n = self.nrow
+        bufs = [np.zeros(n, np.int32) for _ in range(4)] + [np.zeros(n, np.float64)]
+        _check(load().dccm_remap_table_rows(self.h, *[_p(b) for b in bufs]), "dccm_remap_table_rows")
+        return tuple(bufs)
+
+    def write(self, path):
+        _check(load().dccm_remap_table_write(self.h, path.encode()), "dccm_remap_table_write")
+
+    def index(self, GNXS, GNXR):
+        """set_mappingTable_interpCoef: (send_index, recv_index, coef), 1-based."""
+        n = self.nrow
+        s = np.zeros(n, np.int32)
+        r = np.zeros(n, np.int32)
+        c = np.zeros(n, np.float64)
+        _check(load().dccm_remap_table_index(self.h, GNXS, GNXR, _p(s), _p(r), _p(c)), "dccm_remap_table_index")
+        return s, r, c
+
+    def __del__(self):
+        if self.h and _lib is not None:
+            _lib.dccm_remap_table_destroy(self.h)
+            self.h = None
+
+
+def gen_gridmapfile_lonlat2lonlat(x_LonS, y_LatS, x_LonD, y_LatD, x_LonIntWtS, y_LatIntWtS,
+                                  x_LonIntWtD, y_LatIntWtD, accuracy_order=1, weight_mode=J99_REF,
+                                  dst_mask=None):
+    """Jones-99 table on the GPU (grid_mapping_util_jones99.f90:35-41)."""
+    L = load()
+    arrs = [np.ascontiguousarray(x, np.float64) for x in
+            (x_LonS, y_LatS, x_LonD, y_LatD, x_LonIntWtS, y_LatIntWtS, x_LonIntWtD, y_LatIntWtD)]
+    m = None if dst_mask is None else np.ascontiguousarray(dst_mask, np.uint8)
+    h = ctypes.c_void_p()
+    _check(L.dccm_j99_generate(_p(arrs[0]), len(arrs[0]), _p(arrs[1]), len(arrs[1]),
+                               _p(arrs[2]), len(arrs[2]), _p(arrs[3]), len(arrs[3]),
+                               _p(arrs[4]), _p(arrs[5]), _p(arrs[6]), _p(arrs[7]),
+                               accuracy_order, weight_mode, _p(m), ctypes.byref(h)), "dccm_j99_generate")
+    return RemapTable(h)
+
+
+def read_table(path):
+    h = ctypes.c_void_p()
+    _check(load().dccm_remap_table_read(path.encode(), ctypes.byref(h)), "dccm_remap_table_read")
+    return RemapTable(h)
+
+
+def set_mappingTable_interpCoef(gridmapfile, GNXS, GNXR):
+    """Reader of the reference text format (:446-506): (send_index, recv_index, coef)."""
+    return read_table(gridmapfile).index(GNXS, GNXR)
+
+
+# ------------------------------------------------------------- remap apply
+class RemapPlan:
+    """Operation list of one (recv, send, mapping_tag) triple on the device."""
+
+    def __init__(self, n_send_points, n_recv_points, send_index, recv_index, coef):
+        L = load()
+        si = np.ascontiguousarray(send_index, np.int32)
+        ri = np.ascontiguousarray(recv_index, np.int32)
+        cf = np.ascontiguousarray(coef, np.float64)
+        self.h = ctypes.c_void_p()
+        self.n_send, self.n_recv = int(n_send_points), int(n_recv_points)
+        _check(L.dccm_remap_plan_create(self.n_send, self.n_recv, len(si), _p(si), _p(ri), _p(cf),
+                                        ctypes.byref(self.h)), "dccm_remap_plan_create")
+
+    def info(self):
+        a, b, c = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        _check(load().dccm_remap_plan_info(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)),
+               "dccm_remap_plan_info")
+        return a.value, b.value, c.value
+
+    def interpolate_data(self, send_data, recv_data, num_of_data):
+        """interpolate_data (interpolate_data.f90:1-15) on host arrays
+        send_data(sn1,sn2), recv_data(rn1,rn2), Fortran order (modified in place)."""
+        assert send_data.flags.f_contiguous and recv_data.flags.f_contiguous
+        sn1, sn2 = send_data.shape
+        rn1, rn2 = recv_data.shape
+        _check(load().dccm_interpolate_data(self.h, sn1, sn2, _p(send_data), rn1, rn2, _p(recv_data),
+                                            int(num_of_data)), "dccm_interpolate_data")
+
+    def apply_dev(self, src, ld_src, dst, ld_dst, nfields, stream=None):
+        _check(load().dccm_remap_apply_dev(self.h, _p(src), ld_src, _p(dst), ld_dst, nfields,
+                                           _stream(stream)), "dccm_remap_apply_dev")
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.dccm_remap_plan_destroy(self.h)
+            self.h = None
+
+
+def area_integral_dev(f, area, stream=None):
+    out = ctypes.c_double(0.0)
+    _check(load().dccm_area_integral_dev(_p(f), _p(area), f.numel(), ctypes.byref(out), _stream(stream)),
+           "dccm_area_integral_dev")
+    return out.value

@@ -1,0 +1,63 @@
+// Shared helpers of the dccm_gb300 library (internal header).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+
+#include "dccm_gb300.h"
+
+namespace dccm {
+
+// Records the CUDA error of the calling thread for dccm_last_cuda_error().
+void set_cuda_error(cudaError_t e);
+
+// Evaluate a CUDA runtime call; on failure record it and return DCCM_ERR_CUDA.
+#define DCCM_CUDA(call)                                   \
+  do {                                                    \
+    cudaError_t e_ = (call);                              \
+    if (e_ != cudaSuccess) {                              \
+      ::dccm::set_cuda_error(e_);                         \
+      return DCCM_ERR_CUDA;                               \
+    }                                                     \
+  } while (0)
+
+// Check the launch status of the preceding kernel launch.
+#define DCCM_LAUNCH_CHECK() DCCM_CUDA(cudaGetLastError())
+
+#define DCCM_TRY(expr)           \
+  do {                           \
+    int st_ = (expr);            \
+    if (st_ != DCCM_OK) return st_; \
+  } while (0)
+
+inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// Number of SMs of the current device (cached per device).
+int sm_count();
+
+// Device buffer that grows on demand (never shrinks); used for the host
+// entry points' staging copies.
+struct DevBuf {
+  void *ptr = nullptr;
+  size_t bytes = 0;
+  int ensure(size_t n) {
+    if (n <= bytes) return DCCM_OK;
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+    cudaError_t e = cudaMalloc(&ptr, n);
+    if (e != cudaSuccess) {
+      set_cuda_error(e);
+      return DCCM_ERR_NOMEM;
+    }
+    bytes = n;
+    return DCCM_OK;
+  }
+  void release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+  }
+};
+
+}  // namespace dccm

@@ -1,0 +1,381 @@
+// Surface bulk flux: one fused FP64 column kernel.
+//
+// Replaces DSFCM_Util_SfcBulkFlux_Get + BulkCoefL82
+// (sfc/DSFCM_Util_SfcBulkFlux_mod.f90:108-572; constants :35-58; limits
+// :574-591).  The reference runs four OpenMP loop nests over the grid and
+// keeps ~25 full-grid temporaries; here every statement is column-local,
+// so one thread evaluates the whole routine for one column in registers:
+// 21 FP64 reads and 42 FP64 writes per column, nothing else touches HBM.
+// Expressions keep the reference's evaluation order.  The two reference
+// behaviours without a single defined result are given the meaning stated
+// in dccm_gb300.h (per-type sea-ice flag in the final loop; slot-3 latent
+// heat flux as the fraction-weighted merge of slots 1 and 2).
+#include "common.cuh"
+
+namespace dccm {
+namespace flux {
+
+// Constants (:35-58) and read_config limits (:574-591).
+constexpr double FKarm = 0.4;
+constexpr double GasRUniv = 8.3144621;
+constexpr double StB = 5.670373e-8;
+constexpr double Grav = 9.8;
+constexpr double MolWtDry = 1.8e-2;
+constexpr double MolWtWet = 1.8e-2;
+constexpr double CpDry = 1616.0;
+constexpr double LatentHeat = 2425300.0;
+constexpr double LatentHeatFusion = 334000.0;
+constexpr double RefPress = 1e5;
+constexpr double Es0 = 611.0;
+constexpr double RoughLength = 1e-4;
+constexpr double RoughLenHeatFactor = 1.0;
+constexpr double VelMinForRi = 0.01, VelMinForVel = 0.01, VelMinForTemp = 0.01,
+                 VelMinForQVap = 0.01;
+constexpr double VelMaxForVel = 1000.0, VelMaxForTemp = 1000.0, VelMaxForQVap = 1000.0;
+constexpr double VelBulkCoefMin = 0.0, TempBulkCoefMin = 0.0, QVapBulkCoefMin = 0.0;
+constexpr double VelBulkCoefMax = 1.0, TempBulkCoefMax = 1.0, QVapBulkCoefMax = 1.0;
+
+struct Ptrs {
+  double *__restrict__ WSX, *__restrict__ WSY, *__restrict__ Sen, *__restrict__ QV,
+      *__restrict__ Lat, *__restrict__ CVel, *__restrict__ CTemp, *__restrict__ CQ,
+      *__restrict__ DelV, *__restrict__ SUw, *__restrict__ LUw, *__restrict__ Fns,
+      *__restrict__ Fsr, *__restrict__ DFdT;
+  const double *__restrict__ U, *__restrict__ V, *__restrict__ Ta, *__restrict__ q1,
+      *__restrict__ SDw, *__restrict__ LDw, *__restrict__ C1, *__restrict__ C2;
+  double *__restrict__ Ts, *__restrict__ Alb;
+  const double *__restrict__ Ice, *__restrict__ Zs, *__restrict__ Ps;
+};
+
+struct Geom {
+  int64_t plane;  // IA*JA
+  int IA, IS, JS, NI;
+  int64_t ncol;  // NI*NJ
+  double sig1;
+};
+
+__device__ __forceinline__ void bulk_coef_l82(double Ri, double z0m, double z0h, double zs,
+                                              double z, double cmn, double chn, bool flag,
+                                              double &cm, double &ch, double &cq) {
+  double vm, th;
+  if (flag) {
+    if (Ri > 0.0) {
+      const double r = sqrt(1.0 + 5.0 * Ri);
+      vm = cmn / (1.0 + 10.0 * Ri / r);
+      th = chn / (1.0 + 15.0 * Ri * r);
+    } else {
+      vm = cmn * (1.0 - 10.0 * Ri / (1.0 + 75.0 * cmn * sqrt(-(z - zs + z0m) / z0m * Ri)));
+      th = chn * (1.0 - 15.0 * Ri / (1.0 + 75.0 * chn * sqrt(-(z - zs + z0h) / z0h * Ri)));
+    }
+  } else {
+    vm = 0.0;
+    th = 0.0;
+  }
+  cm = fmax(fmin(vm, VelBulkCoefMax), VelBulkCoefMin);
+  ch = fmax(fmin(th, TempBulkCoefMax), TempBulkCoefMin);
+  cq = fmax(fmin(th, QVapBulkCoefMax), QVapBulkCoefMin);
+}
+
+__global__ void __launch_bounds__(128) bulk_flux_column(Ptrs p, Geom g) {
+  constexpr double GasRDry = GasRUniv / MolWtDry;
+  constexpr double GasRWet = GasRUniv / MolWtWet;
+  constexpr double EpsV = MolWtWet / MolWtDry;
+  const double aL[2] = {LatentHeat, LatentHeat + LatentHeatFusion};
+
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < g.ncol;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int ii = (int)(t % g.NI);
+    const int jj = (int)(t / g.NI);
+    const int64_t c = (int64_t)(g.IS - 1 + ii) + (int64_t)g.IA * (g.JS - 1 + jj);
+    const int64_t P = g.plane;
+
+    const double SIceCon = p.Ice[c];
+    const double Ps = p.Ps[c];
+    const double Ta = p.Ta[c];
+    const double q1 = p.q1[c];
+    const double U = p.U[c], V = p.V[c];
+    const double zs = p.Zs[c];
+    const double SDw = p.SDw[c], LDw = p.LDw[c];
+    const double z0m = RoughLength;
+    const double z0h = RoughLenHeatFactor * z0m;
+    const double humd = 1.0;
+
+    double Frac[2], QSat[2], SVT[2], Tsn[2], Albn[2];
+    Frac[0] = 1.0 - SIceCon;
+    Frac[1] = SIceCon;
+#pragma unroll
+    for (int n = 0; n < 2; ++n) {
+      Tsn[n] = p.Ts[c + P * n];
+      Albn[n] = p.Alb[c + P * n];
+      QSat[n] = EpsV * Es0 / Ps * exp(aL[n] / GasRWet * (1.0 / 273.0 - 1.0 / Tsn[n]));
+      SVT[n] = Tsn[n] * (1.0 + (((1.0 / EpsV) - 1.0) * QSat[n]));
+    }
+    const double VirTemp = Ta * (1.0 + (((1.0 / EpsV) - 1.0) * q1));
+    const double Press1 = Ps * g.sig1;
+    const double Exner = pow(Press1 / RefPress, GasRDry / CpDry);
+    const double SfcExner = pow(Ps / RefPress, GasRDry / CpDry);
+    const double VelAbs = sqrt(U * U + V * V);
+    const double Height = zs + GasRDry / Grav * VirTemp * (1.0 - g.sig1);
+
+    // Neutral coefficients (:250-260) depend only on the column (the
+    // roughness lengths are the same constants for both surface types).
+    const double tmp = (FKarm / log((Height - zs + z0m) / z0m));
+    const double cmn = tmp * tmp;
+    const double chn = tmp * (FKarm / log((Height - zs + z0h) / z0h));
+    const double vmx = fmax(VelAbs, VelMinForRi);
+
+    double CVel[2], CTemp[2], CQ[2], WSX[2], WSY[2], Sen[2], QV[2], LatH[2], LUw[2], SUw[2];
+    bool flag[2];
+    double WSX3 = 0.0, WSY3 = 0.0, Sen3 = 0.0, QV3 = 0.0, SUw3 = 0.0, LUw3 = 0.0, Ts3 = 0.0,
+           Alb3 = 0.0, CVel3 = 0.0, CTemp3 = 0.0, CQ3 = 0.0;
+#pragma unroll
+    for (int n = 0; n < 2; ++n) {
+      const double Ri = Grav / (SVT[n] / SfcExner) * (VirTemp / Exner - SVT[n] / SfcExner) /
+                        (vmx * vmx) * (Height - zs);
+      const bool f = (n == 0) ? true : (Frac[n] > 1e-12);
+      flag[n] = f;
+      double cm, ch, cq;
+      bulk_coef_l82(Ri, z0m, z0h, zs, Height, cmn, chn, f, cm, ch, cq);
+      CVel[n] = cm * Ps / (GasRDry * SVT[n]) * fmin(fmax(VelAbs, VelMinForVel), VelMaxForVel);
+      CTemp[n] = ch * Ps / (GasRDry * SVT[n]) * fmin(fmax(VelAbs, VelMinForTemp), VelMaxForTemp);
+      CQ[n] = cq * Ps / (GasRDry * SVT[n]) * fmin(fmax(VelAbs, VelMinForQVap), VelMaxForQVap);
+      if (f) {
+        WSX[n] = -CVel[n] * U;
+        WSY[n] = -CVel[n] * V;
+        Sen[n] = -CpDry * SfcExner * CTemp[n] * (Ta / Exner - Tsn[n] / SfcExner);
+        QV[n] = -humd * CQ[n] * (q1 - QSat[n]);
+        LatH[n] = aL[n] * QV[n];
+        const double T2 = Tsn[n] * Tsn[n];
+        const double T4 = T2 * T2;
+        LUw[n] = StB * T4;
+        SUw[n] = Albn[n] * SDw;
+        Ts3 = Ts3 + Frac[n] * T4;
+        Alb3 = Alb3 + Frac[n] * Albn[n];
+        WSX3 = WSX3 + Frac[n] * WSX[n];
+        WSY3 = WSY3 + Frac[n] * WSY[n];
+        Sen3 = Sen3 + Frac[n] * Sen[n];
+        QV3 = QV3 + Frac[n] * QV[n];
+        LUw3 = LUw3 + Frac[n] * LUw[n];
+        SUw3 = SUw3 + Frac[n] * SUw[n];
+        CVel3 = CVel3 + Frac[n] * CVel[n];
+        CTemp3 = CTemp3 + Frac[n] * CTemp[n];
+        CQ3 = CQ3 + Frac[n] * CQ[n];
+      } else {
+        WSX[n] = WSY[n] = Sen[n] = QV[n] = LatH[n] = LUw[n] = SUw[n] = 0.0;
+      }
+    }
+
+    // Implicit-coupling back-substitution (:355-382).
+    const double c11 = p.C1[c], c12 = p.C1[c + P], c13 = p.C1[c + 2 * P], c14 = p.C1[c + 3 * P];
+    const double c21 = p.C2[c], c22 = p.C2[c + P], c23 = p.C2[c + 2 * P], c24 = p.C2[c + 3 * P];
+    const double DFsDT1 = -CpDry * SfcExner * CTemp3 / Exner;
+    const double f1 = 1.0 / (c11 + CVel3) * (WSX3 + c21);
+    const double f2 = 1.0 / (c12 + CVel3) * (WSY3 + c22);
+    const double f3 = 1.0 / (c13 - DFsDT1) * (Sen3 + c23);
+    const double f4 = 1.0 / (c14 + humd * CQ3) * (QV3 + c24);
+    p.DelV[c] = f1;
+    p.DelV[c + P] = f2;
+    p.DelV[c + 2 * P] = f3;
+    p.DelV[c + 3 * P] = f4;
+
+    const double sfac = CpDry * SfcExner / Exner;
+    double Lat3 = 0.0;
+#pragma unroll
+    for (int n = 0; n < 2; ++n) {
+      WSX[n] = WSX[n] - CVel[n] * f1;
+      WSY[n] = WSY[n] - CVel[n] * f2;
+      Sen[n] = Sen[n] - sfac * CTemp[n] * f3;
+      QV[n] = QV[n] - humd * CQ[n] * f4;
+      LatH[n] = aL[n] * QV[n];
+      if (flag[n]) Lat3 = Lat3 + Frac[n] * LatH[n];
+    }
+    WSX3 = WSX3 - CVel3 * f1;
+    WSY3 = WSY3 - CVel3 * f2;
+    Sen3 = Sen3 - sfac * CTemp3 * f3;
+    QV3 = QV3 - humd * CQ3 * f4;
+
+    // Net heat fluxes and dF/dTs (:384-415), flag per surface type.
+#pragma unroll
+    for (int n = 0; n < 2; ++n) {
+      double fns = 0.0, fsr = 0.0, dfdt = 0.0;
+      if (flag[n]) {
+        fns = +LUw[n] - LDw + LatH[n] + Sen[n];
+        fsr = SUw[n] - SDw;
+        dfdt = +4.0 * StB * (Tsn[n] * Tsn[n] * Tsn[n]) + CpDry * CTemp[n] +
+               aL[n] * humd * CQ[n] * (aL[n] * QSat[n] / (GasRWet * (Tsn[n] * Tsn[n])));
+      }
+      p.Fns[c + P * n] = fns;
+      p.Fsr[c + P * n] = fsr;
+      p.DFdT[c + P * n] = dfdt;
+      p.WSX[c + P * n] = WSX[n];
+      p.WSY[c + P * n] = WSY[n];
+      p.Sen[c + P * n] = Sen[n];
+      p.QV[c + P * n] = QV[n];
+      p.Lat[c + P * n] = LatH[n];
+      p.CVel[c + P * n] = CVel[n];
+      p.CTemp[c + P * n] = CTemp[n];
+      p.CQ[c + P * n] = CQ[n];
+      p.SUw[c + P * n] = SUw[n];
+      p.LUw[c + P * n] = LUw[n];
+    }
+    p.WSX[c + 2 * P] = WSX3;
+    p.WSY[c + 2 * P] = WSY3;
+    p.Sen[c + 2 * P] = Sen3;
+    p.QV[c + 2 * P] = QV3;
+    p.Lat[c + 2 * P] = Lat3;
+    p.CVel[c + 2 * P] = CVel3;
+    p.CTemp[c + 2 * P] = CTemp3;
+    p.CQ[c + 2 * P] = CQ3;
+    p.SUw[c + 2 * P] = SUw3;
+    p.LUw[c + 2 * P] = LUw3;
+    p.Ts[c + 2 * P] = Ts3;
+    p.Alb[c + 2 * P] = Alb3;
+  }
+}
+
+static int check_grid(const dccm_sfc_grid *g) {
+  if (!g) return DCCM_ERR_INVALID_ARG;
+  if (g->IA <= 0 || g->JA <= 0) return DCCM_ERR_SHAPE;
+  if (g->IS < 1 || g->JS < 1 || g->IE > g->IA || g->JE > g->JA) return DCCM_ERR_SHAPE;
+  return DCCM_OK;
+}
+
+static int check_args(const dccm_sfc_bulk_flux_args *a) {
+  if (!a) return DCCM_ERR_INVALID_ARG;
+  const void *const ptrs[] = {a->WindStressX, a->WindStressY, a->SenHFlx, a->QVapMFlx,
+                              a->LatHFlx, a->SfcVelTransCoef, a->SfcTempTransCoef,
+                              a->SfcQVapTransCoef, a->DelVarImplCPL, a->SUwRFlx, a->LUwRFlx,
+                              a->SfcHFlx_ns, a->SfcHFlx_sr, a->DSfcHFlxDTs, a->WindU,
+                              a->WindV, a->SfcAirTemp, a->QVap1, a->SDwRFlx, a->LDwRFlx,
+                              a->ImplCplCoef1, a->ImplCplCoef2, a->SfcTemp, a->SfcAlbedo,
+                              a->SIceCon, a->a_Sig1Info, a->SfcHeight, a->SfcPress};
+  for (const void *q : ptrs)
+    if (!q) return DCCM_ERR_INVALID_ARG;
+  return DCCM_OK;
+}
+
+static Ptrs make_ptrs(const dccm_sfc_bulk_flux_args *a) {
+  Ptrs p;
+  p.WSX = a->WindStressX; p.WSY = a->WindStressY; p.Sen = a->SenHFlx; p.QV = a->QVapMFlx;
+  p.Lat = a->LatHFlx; p.CVel = a->SfcVelTransCoef; p.CTemp = a->SfcTempTransCoef;
+  p.CQ = a->SfcQVapTransCoef; p.DelV = a->DelVarImplCPL; p.SUw = a->SUwRFlx;
+  p.LUw = a->LUwRFlx; p.Fns = a->SfcHFlx_ns; p.Fsr = a->SfcHFlx_sr; p.DFdT = a->DSfcHFlxDTs;
+  p.U = a->WindU; p.V = a->WindV; p.Ta = a->SfcAirTemp; p.q1 = a->QVap1; p.SDw = a->SDwRFlx;
+  p.LDw = a->LDwRFlx; p.C1 = a->ImplCplCoef1; p.C2 = a->ImplCplCoef2; p.Ts = a->SfcTemp;
+  p.Alb = a->SfcAlbedo; p.Ice = a->SIceCon; p.Zs = a->SfcHeight; p.Ps = a->SfcPress;
+  return p;
+}
+
+int launch(const Ptrs &p, const dccm_sfc_grid *g, double sig1, cudaStream_t s) {
+  Geom geo;
+  geo.plane = (int64_t)g->IA * g->JA;
+  geo.IA = g->IA;
+  geo.IS = g->IS;
+  geo.JS = g->JS;
+  geo.NI = g->IE - g->IS + 1;
+  const int NJ = g->JE - g->JS + 1;
+  if (geo.NI <= 0 || NJ <= 0) return DCCM_OK;
+  geo.ncol = (int64_t)geo.NI * NJ;
+  geo.sig1 = sig1;
+  const int threads = 128;
+  int64_t blocks = (geo.ncol + threads - 1) / threads;
+  const int64_t cap = (int64_t)sm_count() * 16;
+  if (blocks > cap) blocks = cap;
+  bulk_flux_column<<<(unsigned)blocks, threads, 0, s>>>(p, geo);
+  DCCM_LAUNCH_CHECK();
+  return DCCM_OK;
+}
+
+// Host entry point state: one device staging area per process.
+static DevBuf g_stage;
+static cudaStream_t g_stream = nullptr;
+
+}  // namespace flux
+}  // namespace dccm
+
+using namespace dccm;
+
+extern "C" int dccm_sfc_bulk_flux_get_dev(const dccm_sfc_bulk_flux_args *a,
+                                          const dccm_sfc_grid *g, void *stream) {
+  DCCM_TRY(flux::check_args(a));
+  DCCM_TRY(flux::check_grid(g));
+  return flux::launch(flux::make_ptrs(a), g, a->a_Sig1Info[0], as_stream(stream));
+}
+
+// Copy the interior IS..IE x JS..JE of nk planes between a host and a device
+// (IA,JA,nk) array, starting at plane k0.
+static int copy_interior(void *dst, const void *src, const dccm_sfc_grid *g, int k0, int nk,
+                         cudaMemcpyKind kind, cudaStream_t s) {
+  cudaMemcpy3DParms prm = {};
+  const size_t pitch = (size_t)g->IA * sizeof(double);
+  prm.srcPtr = make_cudaPitchedPtr(const_cast<void *>(src), pitch, g->IA, g->JA);
+  prm.dstPtr = make_cudaPitchedPtr(dst, pitch, g->IA, g->JA);
+  prm.srcPos = make_cudaPos((size_t)(g->IS - 1) * sizeof(double), g->JS - 1, k0);
+  prm.dstPos = prm.srcPos;
+  prm.extent = make_cudaExtent((size_t)(g->IE - g->IS + 1) * sizeof(double),
+                               g->JE - g->JS + 1, nk);
+  prm.kind = kind;
+  DCCM_CUDA(cudaMemcpy3DAsync(&prm, s));
+  return DCCM_OK;
+}
+
+extern "C" int dccm_sfc_bulk_flux_get(const dccm_sfc_bulk_flux_args *a, const dccm_sfc_grid *g) {
+  DCCM_TRY(flux::check_args(a));
+  DCCM_TRY(flux::check_grid(g));
+  if (g->IE < g->IS || g->JE < g->JS) return DCCM_OK;
+  if (!flux::g_stream) DCCM_CUDA(cudaStreamCreateWithFlags(&flux::g_stream, cudaStreamNonBlocking));
+  cudaStream_t s = flux::g_stream;
+  const size_t plane = (size_t)g->IA * g->JA;
+  // Device layout: 10 out x3, DelV x4, Fns/Fsr/DFdT x3, 6 in x1, C1/C2 x4,
+  // Ts/Alb x3, Ice/Zs/Ps x1  -> 72 planes.
+  DCCM_TRY(flux::g_stage.ensure(plane * sizeof(double) * 72));
+  double *base = (double *)flux::g_stage.ptr;
+  size_t off = 0;
+  auto take = [&](int k) { double *q = base + off; off += plane * k; return q; };
+  dccm_sfc_bulk_flux_args d = *a;
+  d.WindStressX = take(3); d.WindStressY = take(3); d.SenHFlx = take(3); d.QVapMFlx = take(3);
+  d.LatHFlx = take(3); d.SfcVelTransCoef = take(3); d.SfcTempTransCoef = take(3);
+  d.SfcQVapTransCoef = take(3); d.DelVarImplCPL = take(4); d.SUwRFlx = take(3);
+  d.LUwRFlx = take(3); d.SfcHFlx_ns = take(3); d.SfcHFlx_sr = take(3); d.DSfcHFlxDTs = take(3);
+  double *U = take(1), *V = take(1), *Ta = take(1), *q1 = take(1), *SDw = take(1), *LDw = take(1);
+  double *C1 = take(4), *C2 = take(4);
+  d.SfcTemp = take(3); d.SfcAlbedo = take(3);
+  double *Ice = take(1), *Zs = take(1), *Ps = take(1);
+  d.WindU = U; d.WindV = V; d.SfcAirTemp = Ta; d.QVap1 = q1; d.SDwRFlx = SDw; d.LDwRFlx = LDw;
+  d.ImplCplCoef1 = C1; d.ImplCplCoef2 = C2; d.SIceCon = Ice; d.SfcHeight = Zs; d.SfcPress = Ps;
+
+  const cudaMemcpyKind H2D = cudaMemcpyHostToDevice, D2H = cudaMemcpyDeviceToHost;
+  DCCM_TRY(copy_interior(U, a->WindU, g, 0, 1, H2D, s));
+  DCCM_TRY(copy_interior(V, a->WindV, g, 0, 1, H2D, s));
+  DCCM_TRY(copy_interior(Ta, a->SfcAirTemp, g, 0, 1, H2D, s));
+  DCCM_TRY(copy_interior(q1, a->QVap1, g, 0, 1, H2D, s));
+  DCCM_TRY(copy_interior(SDw, a->SDwRFlx, g, 0, 1, H2D, s));
+  DCCM_TRY(copy_interior(LDw, a->LDwRFlx, g, 0, 1, H2D, s));
+  DCCM_TRY(copy_interior(C1, a->ImplCplCoef1, g, 0, 4, H2D, s));
+  DCCM_TRY(copy_interior(C2, a->ImplCplCoef2, g, 0, 4, H2D, s));
+  DCCM_TRY(copy_interior(d.SfcTemp, a->SfcTemp, g, 0, 2, H2D, s));
+  DCCM_TRY(copy_interior(d.SfcAlbedo, a->SfcAlbedo, g, 0, 2, H2D, s));
+  DCCM_TRY(copy_interior(Ice, a->SIceCon, g, 0, 1, H2D, s));
+  DCCM_TRY(copy_interior(Zs, a->SfcHeight, g, 0, 1, H2D, s));
+  DCCM_TRY(copy_interior(Ps, a->SfcPress, g, 0, 1, H2D, s));
+
+  DCCM_TRY(flux::launch(flux::make_ptrs(&d), g, a->a_Sig1Info[0], s));
+
+  DCCM_TRY(copy_interior(a->WindStressX, d.WindStressX, g, 0, 3, D2H, s));
+  DCCM_TRY(copy_interior(a->WindStressY, d.WindStressY, g, 0, 3, D2H, s));
+  DCCM_TRY(copy_interior(a->SenHFlx, d.SenHFlx, g, 0, 3, D2H, s));
+  DCCM_TRY(copy_interior(a->QVapMFlx, d.QVapMFlx, g, 0, 3, D2H, s));
+  DCCM_TRY(copy_interior(a->LatHFlx, d.LatHFlx, g, 0, 3, D2H, s));
+  DCCM_TRY(copy_interior(a->SfcVelTransCoef, d.SfcVelTransCoef, g, 0, 3, D2H, s));
+  DCCM_TRY(copy_interior(a->SfcTempTransCoef, d.SfcTempTransCoef, g, 0, 3, D2H, s));
+  DCCM_TRY(copy_interior(a->SfcQVapTransCoef, d.SfcQVapTransCoef, g, 0, 3, D2H, s));
+  DCCM_TRY(copy_interior(a->DelVarImplCPL, d.DelVarImplCPL, g, 0, 4, D2H, s));
+  DCCM_TRY(copy_interior(a->SUwRFlx, d.SUwRFlx, g, 0, 3, D2H, s));
+  DCCM_TRY(copy_interior(a->LUwRFlx, d.LUwRFlx, g, 0, 3, D2H, s));
+  DCCM_TRY(copy_interior(a->SfcHFlx_ns, d.SfcHFlx_ns, g, 0, 2, D2H, s));
+  DCCM_TRY(copy_interior(a->SfcHFlx_sr, d.SfcHFlx_sr, g, 0, 2, D2H, s));
+  DCCM_TRY(copy_interior(a->DSfcHFlxDTs, d.DSfcHFlxDTs, g, 0, 2, D2H, s));
+  DCCM_TRY(copy_interior(a->SfcTemp, d.SfcTemp, g, 2, 1, D2H, s));
+  DCCM_TRY(copy_interior(a->SfcAlbedo, d.SfcAlbedo, g, 2, 1, D2H, s));
+  DCCM_CUDA(cudaStreamSynchronize(s));
+  return DCCM_OK;
+}

@@ -1,0 +1,183 @@
+/*
+ * dccm_gb300 — C ABI of the GB300 (sm_103a) implementation of the
+ * Dennou-CCM per-coupling-step hot path:
+ *   - surface bulk flux        (replaces sfc/DSFCM_Util_SfcBulkFlux_mod.f90)
+ *   - Jones-99 remap table and its apply (replaces
+ *     common/grid_mapping_util_jones99.f90 and
+ *     common/interpolation_data_latlon_mod.f90 / interpolate_data.f90)
+ *   - spherical-harmonic transform pair on the Gaussian grid (replaces the
+ *     SPML w_module transforms that the atmosphere dynamics call)
+ *   - the fused coupling step (all of the above, captured as a CUDA graph).
+ *
+ * Conventions shared by every entry point:
+ *   - plain C types only; every function returns an int status
+ *     (DCCM_OK = 0, negative on error; nothing aborts or throws);
+ *   - arrays are Fortran column-major FP64 as in the reference;
+ *   - "_dev" entry points take device pointers and a CUDA stream
+ *     (passed as void*, NULL = default stream) and are stream-ordered;
+ *     the others take host pointers and return when the results are in
+ *     host memory (what a Fortran caller through iso_c_binding passes);
+ *   - plans own their device memory and are not safe to use from two
+ *     threads at once.
+ */
+#ifndef DCCM_GB300_H
+#define DCCM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DCCM_ABI_VERSION 1
+
+enum dccm_status {
+  DCCM_OK = 0,
+  DCCM_ERR_INVALID_ARG = -1,  /* null pointer, negative size, bad enum */
+  DCCM_ERR_SHAPE = -2,        /* sizes inconsistent with the plan */
+  DCCM_ERR_CUDA = -3,         /* a CUDA runtime call failed */
+  DCCM_ERR_INDEX_RANGE = -4,  /* a table index outside the grid */
+  DCCM_ERR_SEARCH = -5,       /* overlap search failed (the reference stops) */
+  DCCM_ERR_IO = -6,           /* table file could not be read or written */
+  DCCM_ERR_NOMEM = -7,        /* host or device allocation failed */
+  DCCM_ERR_TIMEOUT = -8,      /* a bounded device wait gave up */
+  DCCM_ERR_UNSUPPORTED = -9   /* size or mode this build does not handle */
+};
+
+/* Message for a status code (static storage). */
+const char *dccm_status_string(int status);
+/* DCCM_ABI_VERSION of the loaded library. */
+int dccm_abi_version(void);
+/* The last CUDA error code seen by the library on this thread (0 if none). */
+int dccm_last_cuda_error(void);
+
+/* =====================================================================
+ * Surface bulk flux
+ * Replaces DSFCM_Util_SfcBulkFlux_Get (sfc/DSFCM_Util_SfcBulkFlux_mod.f90:108-151)
+ * and its module state IA, IS, IE, JA, JS, JE (sfc/DSFCM_Admin_Grid_mod.f90:35-52).
+ * Members are in the Fortran dummy-argument order.  Arrays are (IA,JA),
+ * (IA,JA,3) or (IA,JA,4) column-major; only the interior IS..IE x JS..JE
+ * (1-based, inclusive) is read or written.  a_Sig1Info always points to
+ * two host doubles.  Slot 3 of SfcHFlx_ns, SfcHFlx_sr and DSfcHFlxDTs is
+ * left untouched, as in the reference.  Two reference behaviours are
+ * given one defined meaning: the sea-ice flag of the final loop is taken
+ * per surface type (the reference's OpenMP loop shares it between types,
+ * :384-393), and slot 3 of LatHFlx after the implicit correction is the
+ * fraction-weighted merge of slots 1 and 2 (the reference reads a
+ * latent-heat array of extent 2 at index 3, :379).
+ * ===================================================================== */
+typedef struct dccm_sfc_bulk_flux_args {
+  double *WindStressX, *WindStressY;                          /* out (IA,JA,3) */
+  double *SenHFlx, *QVapMFlx, *LatHFlx;                       /* out (IA,JA,3) */
+  double *SfcVelTransCoef, *SfcTempTransCoef, *SfcQVapTransCoef; /* out (IA,JA,3) */
+  double *DelVarImplCPL;                                      /* out (IA,JA,4) */
+  double *SUwRFlx, *LUwRFlx;                                  /* out (IA,JA,3) */
+  double *SfcHFlx_ns, *SfcHFlx_sr, *DSfcHFlxDTs;              /* out (IA,JA,3), slot 3 untouched */
+  const double *WindU, *WindV, *SfcAirTemp, *QVap1;           /* in (IA,JA) */
+  const double *SDwRFlx, *LDwRFlx;                            /* in (IA,JA) */
+  const double *ImplCplCoef1, *ImplCplCoef2;                  /* in (IA,JA,4) */
+  double *SfcTemp, *SfcAlbedo;                                /* inout (IA,JA,3) */
+  const double *SIceCon;                                      /* in (IA,JA) */
+  const double *a_Sig1Info;                                   /* in, 2 host doubles */
+  const double *SfcHeight, *SfcPress;                         /* in (IA,JA) */
+} dccm_sfc_bulk_flux_args;
+
+typedef struct dccm_sfc_grid {
+  int IA, JA; /* array extents including halo */
+  int IS, IE; /* interior, 1-based inclusive */
+  int JS, JE;
+} dccm_sfc_grid;
+
+/* Host arrays; returns after the outputs are back in host memory. */
+int dccm_sfc_bulk_flux_get(const dccm_sfc_bulk_flux_args *args,
+                           const dccm_sfc_grid *grid);
+/* Device arrays (a_Sig1Info stays a host pointer); stream-ordered. */
+int dccm_sfc_bulk_flux_get_dev(const dccm_sfc_bulk_flux_args *args,
+                               const dccm_sfc_grid *grid, void *stream);
+
+/* =====================================================================
+ * Jones-99 remap table
+ * dccm_j99_generate replaces gen_gridmapfile_lonlat2lonlat
+ * (common/grid_mapping_util_jones99.f90:35-41, body :78-442); the table is
+ * built on the GPU and returned in host memory instead of a text file.
+ * Grid arguments are those of the reference: centre longitudes and
+ * latitudes (radians, latitudes ascending south to north) and integration
+ * weights (x_*IntWt* is accepted and unused, as in the reference; y_*IntWt*
+ * are the sin-latitude widths, sum 2).
+ *   weight_mode DCCM_J99_REF      the reference's weights and pattern,
+ *                                 rows identical to the reference file;
+ *   weight_mode DCCM_J99_CONSERVE true longitude overlaps: row sums 1 and
+ *                                 global integrals conserved for any grids.
+ * dst_mask (nxd*nyd bytes, i fastest, or NULL) drops rows of destination
+ * cells whose mask is 0 (land); the reference's masks are all true.
+ * accuracy_order 1 or 2 (second-order adds the latitude-gradient rows).
+ * ===================================================================== */
+enum { DCCM_J99_REF = 0, DCCM_J99_CONSERVE = 1 };
+
+typedef struct dccm_remap_table dccm_remap_table;
+
+int dccm_j99_generate(const double *x_LonS, int nxs, const double *y_LatS, int nys,
+                      const double *x_LonD, int nxd, const double *y_LatD, int nyd,
+                      const double *x_LonIntWtS, const double *y_LatIntWtS,
+                      const double *x_LonIntWtD, const double *y_LatIntWtD,
+                      int accuracy_order, int weight_mode, const uint8_t *dst_mask,
+                      dccm_remap_table **table);
+/* Number of rows (iD, jD, iS, jS, w). */
+int dccm_remap_table_size(const dccm_remap_table *table, int64_t *nrow);
+/* Copies the rows out (1-based grid indices as in the reference file). */
+int dccm_remap_table_rows(const dccm_remap_table *table, int32_t *iD, int32_t *jD,
+                          int32_t *iS, int32_t *jS, double *w);
+/* Writes / reads the reference's text format: one "iD jD iS jS w" row per
+ * line (written by :246-247, read by :485/:497). */
+int dccm_remap_table_write(const dccm_remap_table *table, const char *path);
+int dccm_remap_table_read(const char *path, dccm_remap_table **table);
+/* set_mappingTable_interpCoef (common/grid_mapping_util_jones99.f90:446-506):
+ * recv_index = iD + GNXR*(jD-1), send_index = iS + GNXS*(jS-1), 1-based. */
+int dccm_remap_table_index(const dccm_remap_table *table, int GNXS, int GNXR,
+                           int32_t *send_index, int32_t *recv_index, double *coef);
+int dccm_remap_table_destroy(dccm_remap_table *table);
+
+/* =====================================================================
+ * Remap apply (the jcup interpolation callback)
+ * dccm_remap_plan_create takes the operation list of set_operation_index /
+ * set_interpolate_coef (common/interpolation_data_latlon_mod.f90:116-270):
+ * 1-based send/recv point indices and coefficients, in table order.  It
+ * validates every index (the reference reads out of bounds instead) and
+ * builds a CSR matrix on the device whose per-row order is the table order.
+ * dccm_interpolate_data replaces interpolate_data
+ * (common/interpolate_data.f90:1-15 -> interpolate_data_latlon,
+ * common/interpolation_data_latlon_mod.f90:274-306): recv_data(:,:) is
+ * zeroed and then recv(r,d) += send(s,d)*coef in table order, with the
+ * product and the sum rounded separately, so results are bit-identical to
+ * the reference loop.  mapping/exchange tags select the plan on the
+ * caller's side and are not arguments here.
+ * ===================================================================== */
+typedef struct dccm_remap_plan dccm_remap_plan;
+
+int dccm_remap_plan_create(int64_t n_send_points, int64_t n_recv_points,
+                           int64_t num_of_operation, const int32_t *send_index,
+                           const int32_t *recv_index, const double *coef,
+                           dccm_remap_plan **plan);
+int dccm_remap_plan_destroy(dccm_remap_plan *plan);
+int dccm_remap_plan_info(const dccm_remap_plan *plan, int64_t *nnz,
+                         int64_t *n_send_points, int64_t *n_recv_points);
+/* Host arrays send_data(sn1,sn2), recv_data(rn1,rn2); num_of_data <= sn2, rn2. */
+int dccm_interpolate_data(dccm_remap_plan *plan, int64_t sn1, int64_t sn2,
+                          const double *send_data, int64_t rn1, int64_t rn2,
+                          double *recv_data, int num_of_data);
+/* Device arrays; field d of src starts at src + d*ld_src. */
+int dccm_remap_apply_dev(dccm_remap_plan *plan, const double *src, int64_t ld_src,
+                         double *dst, int64_t ld_dst, int nfields, void *stream);
+
+/* Compensated FP64 global integral sum_i f[i]*area[i] of a device array
+ * (IntLonLat_xy, used by atm/dccm_atm_mod.f90:668-669 and
+ * ocn/dccm_ocn_mod.f90:803-804; external in the reference).  The result is
+ * written to *result (host) after the stream has synchronised. */
+int dccm_area_integral_dev(const double *f, const double *area, int64_t n,
+                           double *result, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DCCM_GB300_H */

@@ -1,0 +1,173 @@
+"""ctypes bindings of the CPU oracle (test infrastructure only).
+
+The oracle is the checker: tests, ``__graft_entry__.smoke()`` and the CPU
+baseline of ``bench.py`` call it; the product library never does.  See
+``oracle.h`` for what each function restates and why parity is unpinned.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "liboracle.so")
+_lib = None
+
+FLUX_ARGS = [
+    "WindStressX", "WindStressY", "SenHFlx", "QVapMFlx", "LatHFlx",
+    "SfcVelTransCoef", "SfcTempTransCoef", "SfcQVapTransCoef",
+    "DelVarImplCPL", "SUwRFlx", "LUwRFlx", "SfcHFlx_ns", "SfcHFlx_sr",
+    "DSfcHFlxDTs", "WindU", "WindV", "SfcAirTemp", "QVap1", "SDwRFlx",
+    "LDwRFlx", "ImplCplCoef1", "ImplCplCoef2", "SfcTemp", "SfcAlbedo",
+    "SIceCon", "a_Sig1Info", "SfcHeight", "SfcPress",
+]
+
+
+def build(force=False):
+    """Compile liboracle.so with make (gcc, FP64, OpenMP)."""
+    if force or not os.path.exists(_LIB_PATH):
+        subprocess.check_call(["make", "-s", "-C", _HERE, "-B" if force else "liboracle.so"])
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(_LIB_PATH)
+        P = ctypes.c_void_p
+        i32, i64, f64 = ctypes.c_int, ctypes.c_int64, ctypes.c_double
+        L.oracle_sfc_bulk_flux.argtypes = [P, i32, i32, i32, i32, i32, i32]
+        L.oracle_j99_gen.argtypes = [P, i32, P, i32, P, i32, P, i32, P, P, i32, i32,
+                                     i64, P, P, P, P, P, P]
+        L.oracle_j99_gen.restype = i32
+        L.oracle_table_to_index.argtypes = [i64, P, P, P, P, i32, i32, P, P]
+        L.oracle_remap_apply.argtypes = [i64, P, P, P, i64, P, i64, P, i32]
+        L.oracle_remap_apply.restype = i32
+        L.oracle_area_integral.argtypes = [i64, P, P]
+        L.oracle_area_integral.restype = f64
+        L.oracle_gauss_nodes.argtypes = [i32, P, P]
+        L.oracle_pnm.argtypes = [i32, i32, P, P]
+        L.oracle_sht_inverse.argtypes = [i32, i32, i32, i32, P, P]
+        L.oracle_sht_forward.argtypes = [i32, i32, i32, i32, P, P]
+        L.oracle_rfft_row.argtypes = [i32, P, i32, P]
+        L.oracle_set_threads.argtypes = [i32]
+        L.oracle_get_threads.restype = i32
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def set_threads(n):
+    lib().oracle_set_threads(int(n))
+
+
+def get_threads():
+    return int(lib().oracle_get_threads())
+
+
+# ------------------------------------------------------------------ flux
+def sfc_bulk_flux(arrays, IA, JA, IS, IE, JS, JE):
+    """arrays: dict name -> Fortran-ordered float64 array (modified in place)."""
+    ptrs = (ctypes.c_void_p * len(FLUX_ARGS))()
+    for k, name in enumerate(FLUX_ARGS):
+        a = arrays[name]
+        assert a.dtype == np.float64 and (a.flags.f_contiguous or a.ndim == 1)
+        ptrs[k] = a.ctypes.data
+    lib().oracle_sfc_bulk_flux(ctypes.cast(ptrs, ctypes.c_void_p), IA, JA, IS, IE, JS, JE)
+
+
+# ----------------------------------------------------------------- remap
+def j99_gen(lonS, latS, lonD, latD, latwtS, latwtD, order=1, mode=0):
+    """Rows (iD, jD, iS, jS, w) of the Jones-99 table in the reference's order."""
+    args = [np.ascontiguousarray(x, dtype=np.float64) for x in (lonS, latS, lonD, latD, latwtS, latwtD)]
+    lonS, latS, lonD, latD, latwtS, latwtD = args
+    cap = 0
+    nrow = ctypes.c_int64(0)
+    while True:
+        bufs = [np.zeros(max(cap, 1), np.int32) for _ in range(4)] + [np.zeros(max(cap, 1), np.float64)]
+        st = lib().oracle_j99_gen(_p(lonS), len(lonS), _p(latS), len(latS), _p(lonD), len(lonD),
+                                  _p(latD), len(latD), _p(latwtS), _p(latwtD), int(order), int(mode),
+                                  cap, *[_p(b) for b in bufs], ctypes.byref(nrow))
+        if st < 0:
+            raise RuntimeError("oracle_j99_gen: search failed (%d)" % st)
+        if st == 0:
+            n = nrow.value
+            return tuple(b[:n] for b in bufs)
+        cap = nrow.value
+
+
+def table_to_index(iD, jD, iS, jS, GNXS, GNXR):
+    n = len(iD)
+    send = np.zeros(n, np.int32)
+    recv = np.zeros(n, np.int32)
+    c = [np.ascontiguousarray(x, dtype=np.int32) for x in (iD, jD, iS, jS)]
+    lib().oracle_table_to_index(n, *[_p(x) for x in c], GNXS, GNXR, _p(send), _p(recv))
+    return send, recv
+
+
+def remap_apply(send_index, recv_index, coef, send, rn1):
+    """send: (sn1, nd) Fortran order.  Returns recv (rn1, nd) Fortran order."""
+    send = np.asfortranarray(send, dtype=np.float64)
+    sn1, nd = send.shape
+    recv = np.zeros((rn1, nd), np.float64, order="F")
+    si = np.ascontiguousarray(send_index, np.int32)
+    ri = np.ascontiguousarray(recv_index, np.int32)
+    cf = np.ascontiguousarray(coef, np.float64)
+    st = lib().oracle_remap_apply(len(si), _p(si), _p(ri), _p(cf), sn1, _p(send), rn1, _p(recv), nd)
+    if st != 0:
+        raise ValueError("index out of range")
+    return recv
+
+
+def area_integral(f, area):
+    f = np.ascontiguousarray(f, np.float64).ravel()
+    area = np.ascontiguousarray(area, np.float64).ravel()
+    return lib().oracle_area_integral(len(f), _p(f), _p(area))
+
+
+# ------------------------------------------------------------------- SHT
+def ncoef(N):
+    return (N + 1) * (N + 2) // 2
+
+
+def gauss_nodes(J):
+    mu = np.zeros(J)
+    w = np.zeros(J)
+    lib().oracle_gauss_nodes(J, _p(mu), _p(w))
+    return mu, w
+
+
+def pnm(N, J):
+    mu, _ = gauss_nodes(J)
+    p = np.zeros(ncoef(N) * J)
+    lib().oracle_pnm(N, J, _p(mu), _p(p))
+    return p.reshape(ncoef(N), J)
+
+
+def sht_inverse(N, I, J, spec):
+    """spec: complex128 [batch, ncoef] -> grid float64 [batch, J, I]."""
+    spec = np.ascontiguousarray(spec, np.complex128)
+    B = spec.shape[0]
+    grid = np.zeros((B, J, I))
+    lib().oracle_sht_inverse(N, I, J, B, _p(spec), _p(grid))
+    return grid
+
+
+def sht_forward(N, I, J, grid):
+    grid = np.ascontiguousarray(grid, np.float64)
+    B = grid.shape[0]
+    spec = np.zeros((B, ncoef(N)), np.complex128)
+    lib().oracle_sht_forward(N, I, J, B, _p(grid), _p(spec))
+    return spec
+
+
+def rfft_row(g, M):
+    g = np.ascontiguousarray(g, np.float64)
+    out = np.zeros(M, np.complex128)
+    lib().oracle_rfft_row(len(g), _p(g), M, _p(out))
+    return out

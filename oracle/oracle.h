@@ -1,0 +1,99 @@
+/*
+ * CPU oracle for the Dennou-CCM coupling-step hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker that the CUDA
+ * library is compared against, and the timed CPU baseline of bench.py.  No
+ * product code path loads it.
+ *
+ * It is a plain-C FP64 restatement of the reference algorithms:
+ *   - surface bulk flux:  sfc/DSFCM_Util_SfcBulkFlux_mod.f90:35-58,108-591
+ *   - Jones-99 table:     common/grid_mapping_util_jones99.f90:35-442
+ *   - table reader:       common/grid_mapping_util_jones99.f90:446-506
+ *   - remap apply:        common/interpolation_data_latlon_mod.f90:274-306
+ *   - spherical-harmonic transform: SPML/ISPACK (external, not vendored);
+ *     restated from the mathematics with the convention documented in
+ *     oracle_sht.c.
+ *
+ * PARITY UNPINNED: the reference is Fortran 90 and no Fortran compiler,
+ * nor its libraries (jcup, gtool5, SPML, ISPACK), exists where this is
+ * built, and the reference ships no golden vectors or tests.  The oracle
+ * is cross-checked instead against an independent numpy restatement
+ * (tests/golden/make_golden.py), numpy's Gauss-Legendre nodes, and
+ * analytic known answers.
+ *
+ * Compile with -ffp-contract=off so that results do not depend on whether
+ * the host compiler fuses multiply-adds (GCC fuses by default on aarch64).
+ */
+#ifndef DCCM_ORACLE_H
+#define DCCM_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- flux */
+/* Pointer table in the dummy-argument order of DSFCM_Util_SfcBulkFlux_Get
+ * (sfc/DSFCM_Util_SfcBulkFlux_mod.f90:108-120).  Index: */
+enum {
+  OF_WindStressX = 0, OF_WindStressY, OF_SenHFlx, OF_QVapMFlx, OF_LatHFlx,
+  OF_SfcVelTransCoef, OF_SfcTempTransCoef, OF_SfcQVapTransCoef,
+  OF_DelVarImplCPL, OF_SUwRFlx, OF_LUwRFlx, OF_SfcHFlx_ns, OF_SfcHFlx_sr,
+  OF_DSfcHFlxDTs, OF_WindU, OF_WindV, OF_SfcAirTemp, OF_QVap1, OF_SDwRFlx,
+  OF_LDwRFlx, OF_ImplCplCoef1, OF_ImplCplCoef2, OF_SfcTemp, OF_SfcAlbedo,
+  OF_SIceCon, OF_Sig1Info, OF_SfcHeight, OF_SfcPress, OF_NARGS
+};
+/* Fortran bounds IS..IE, JS..JE (1-based) inside arrays of shape (IA,JA[,k]). */
+void oracle_sfc_bulk_flux(double *const *args, int IA, int JA, int IS, int IE,
+                          int JS, int JE);
+
+/* --------------------------------------------------------------- remap */
+/* Jones-99 table generation.  mode 0 = the reference's weights (REF),
+ * mode 1 = true longitude overlap (conservative).  order 1 or 2.
+ * Rows are (iD, jD, iS, jS, w) with 1-based grid indices exactly as the
+ * reference writes them.  If cap is too small, *nrow is set to the needed
+ * count and 1 is returned.  Returns <0 on a failed search (the reference
+ * stops there). */
+int oracle_j99_gen(const double *lonS, int nxs, const double *latS, int nys,
+                   const double *lonD, int nxd, const double *latD, int nyd,
+                   const double *latwtS, const double *latwtD, int order,
+                   int mode, int64_t cap, int32_t *iD, int32_t *jD, int32_t *iS,
+                   int32_t *jS, double *w, int64_t *nrow);
+
+/* set_mappingTable_interpCoef: 1-based linear indices. */
+void oracle_table_to_index(int64_t n, const int32_t *iD, const int32_t *jD,
+                           const int32_t *iS, const int32_t *jS, int GNXS,
+                           int GNXR, int32_t *send_index, int32_t *recv_index);
+
+/* interpolate_data_latlon: recv(:,:)=0 then COO scatter-add in table order.
+ * send is (sn1, num_of_data), recv is (rn1, num_of_data), column-major.
+ * Returns -1 if an index is outside 1..sn1 or 1..rn1. */
+int oracle_remap_apply(int64_t nop, const int32_t *send_index,
+                       const int32_t *recv_index, const double *coef,
+                       int64_t sn1, const double *send, int64_t rn1,
+                       double *recv, int num_of_data);
+
+/* Compensated (Neumaier) FP64 sum of f[i]*area[i]. */
+double oracle_area_integral(int64_t n, const double *f, const double *area);
+
+/* ----------------------------------------------------------------- SHT */
+void oracle_gauss_nodes(int J, double *mu, double *w);
+/* P-bar table, m-major: p[(idx(m,n))*J + j] for the J Gaussian nodes. */
+void oracle_pnm(int N, int J, const double *mu, double *p);
+/* Inverse: spec[b][ncoef] complex (re,im interleaved) -> grid[b][J][I]. */
+void oracle_sht_inverse(int N, int I, int J, int batch, const double *spec,
+                        double *grid);
+/* Forward: grid[b][J][I] -> spec[b][ncoef] complex. */
+void oracle_sht_forward(int N, int I, int J, int batch, const double *grid,
+                        double *spec);
+/* Real DFT of one row (FFT, any I = 2^a 3^b 5^c); out[m] m=0..M-1 complex,
+ * out = (1/I) sum_i g_i e^{-2 pi i m i / I}. */
+void oracle_rfft_row(int I, const double *g, int M, double *out);
+
+void oracle_set_threads(int n);
+int oracle_get_threads(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
