@@ -88,6 +88,19 @@ _SIGS = {
                                             ctypes.c_int64, ctypes.c_int, ctypes.c_void_p]),
     "dccm_area_integral_dev": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
                                               ctypes.c_void_p, ctypes.c_void_p]),
+    "dccm_sht_plan_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                            ctypes.c_int, ctypes.c_void_p]),
+    "dccm_sht_plan_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "dccm_sht_axes": (ctypes.c_int, [ctypes.c_void_p] * 5),
+    "dccm_sht_gauss": (ctypes.c_int, [ctypes.c_void_p] * 3),
+    "dccm_sht_pnm": (ctypes.c_int, [ctypes.c_void_p] * 2),
+    "dccm_sht_inverse_dev": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                            ctypes.c_void_p]),
+    "dccm_sht_forward_dev": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                            ctypes.c_void_p]),
+    "dccm_sht_inverse": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
+    "dccm_sht_forward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
+    "dccm_sht_status": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
 }
 
 
@@ -266,3 +279,70 @@ def area_integral_dev(f, area, stream=None):
     _check(load().dccm_area_integral_dev(_p(f), _p(area), f.numel(), ctypes.byref(out), _stream(stream)),
            "dccm_area_integral_dev")
     return out.value
+
+
+# ------------------------------------------------------------------- SHT
+class ShtPlan:
+    """w_Initial(nMax, iMax, jMax) equivalent: a transform plan on the GPU.
+
+    precision SHT_FP64 (CUDA cores) or SHT_MIXED (tcgen05 BF16x3 Legendre,
+    FP32 FFT).  Spectra are complex128 [batch, ncoef] (m-major), grids
+    float64 [batch, jmax, imax]."""
+
+    def __init__(self, nmax, imax, jmax, precision=SHT_FP64, max_batch=1):
+        L = load()
+        self.N, self.I, self.J = int(nmax), int(imax), int(jmax)
+        self.ncoef = (self.N + 1) * (self.N + 2) // 2
+        self.precision = precision
+        self.max_batch = int(max_batch)
+        self.h = ctypes.c_void_p()
+        _check(L.dccm_sht_plan_create(self.N, self.I, self.J, precision, self.max_batch, ctypes.byref(self.h)),
+               "dccm_sht_plan_create")
+
+    def axes(self):
+        """(x_Lon, y_Lat, x_Lon_Weight, y_Lat_Weight) as SPML returns them."""
+        a = [np.zeros(self.I), np.zeros(self.J), np.zeros(self.I), np.zeros(self.J)]
+        _check(load().dccm_sht_axes(self.h, *[_p(x) for x in a]), "dccm_sht_axes")
+        return tuple(a)
+
+    def gauss(self):
+        mu, w = np.zeros(self.J), np.zeros(self.J)
+        _check(load().dccm_sht_gauss(self.h, _p(mu), _p(w)), "dccm_sht_gauss")
+        return mu, w
+
+    def pnm(self):
+        p = np.zeros(self.ncoef * (self.J // 2))
+        _check(load().dccm_sht_pnm(self.h, _p(p)), "dccm_sht_pnm")
+        return p.reshape(self.ncoef, self.J // 2)
+
+    def inverse(self, spec):
+        spec = np.ascontiguousarray(spec, np.complex128)
+        B = spec.shape[0]
+        grid = np.zeros((B, self.J, self.I))
+        _check(load().dccm_sht_inverse(self.h, _p(spec), _p(grid), B), "dccm_sht_inverse")
+        return grid
+
+    def forward(self, grid):
+        grid = np.ascontiguousarray(grid, np.float64)
+        B = grid.shape[0]
+        spec = np.zeros((B, self.ncoef), np.complex128)
+        _check(load().dccm_sht_forward(self.h, _p(grid), _p(spec), B), "dccm_sht_forward")
+        return spec
+
+    def inverse_dev(self, spec, grid, batch, stream=None):
+        _check(load().dccm_sht_inverse_dev(self.h, _p(spec), _p(grid), int(batch), _stream(stream)),
+               "dccm_sht_inverse_dev")
+
+    def forward_dev(self, grid, spec, batch, stream=None):
+        _check(load().dccm_sht_forward_dev(self.h, _p(grid), _p(spec), int(batch), _stream(stream)),
+               "dccm_sht_forward_dev")
+
+    def status(self):
+        e = ctypes.c_int(0)
+        st = load().dccm_sht_status(self.h, ctypes.byref(e))
+        return st, e.value
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.dccm_sht_plan_destroy(self.h)
+            self.h = None

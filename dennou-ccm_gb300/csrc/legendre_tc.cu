@@ -1,0 +1,610 @@
+// Mixed-precision Legendre transforms on the 5th-generation tensor cores
+// (tcgen05, sm_103a): per-zonal-wavenumber batched contractions folded by
+// equatorial symmetry, in split BF16 x 3 with FP32 accumulation in TMEM.
+//
+// A work item is (m, 128 columns c of the batch, up to 128 columns of the
+// N dimension) and computes both parities p (n - m even / odd):
+//   inverse  D_p[c][jj] = sum_k S_p[c][k] Pbar_p[jj][k]   (K = n index)
+//            F(jn) = D_0 + D_1, F(js) = D_0 - D_1
+//   forward  D_p[c][k]  = sum_jj X_p[c][jj] PW_p[k][jj]   (K = latitude pair)
+//            s_{m+p+2k}^m[c] = D_p[c][k],  PW = (w/2) Pbar.
+// Every operand x is split as x = hi + mid + lo (three BF16 numbers, 24
+// significant bits) and the six products hi*hi, hi*mid, mid*hi, hi*lo,
+// lo*hi, mid*mid are accumulated (dropped terms are below 2^-24 relative).
+//
+// Warp roles (288 threads):
+//   warps 0-3  producers: thread t owns row t of the A tile; it reads the
+//              FP64 spectra (inverse) or the FP32 folded Fourier
+//              coefficients (forward), splits them and stores the three
+//              BF16 planes straight into the 128-byte-swizzled K-major
+//              shared-memory layout the MMA reads; thread 0 also issues
+//              the TMA (cp.async.bulk.tensor) loads of the pre-split Pbar
+//              tiles, which the tensor map swizzles the same way;
+//   warps 4-7  epilogue: tcgen05.ld of the accumulators (warp w reads TMEM
+//              lanes 32(w%4)..), parity fold, coalesced stores along c;
+//   warp 8     TMEM allocation and the single MMA-issuing thread.
+// Two shared-memory stages (A and B of one 64-wide K chunk) and two TMEM
+// accumulator sets let the producers, the MMA and the epilogue of
+// consecutive items overlap.  Every mbarrier wait is bounded by a 1 s
+// globaltimer limit; on expiry the kernel records an error code, stops
+// issuing work, and still frees its TMEM.
+#include <cuda_bf16.h>
+
+#include "sht_plan.cuh"
+
+namespace dccm {
+namespace sht {
+
+constexpr int TC_THREADS = 288;
+constexpr int A_SPLIT_BYTES = 128 * 128;     // 128 rows x 64 bf16
+constexpr int B_SPLIT_BYTES = 128 * 128;     // up to 128 rows x 64 bf16
+constexpr int STAGE_BYTES = 3 * A_SPLIT_BYTES + 3 * B_SPLIT_BYTES;  // 96 KB
+constexpr int NSTAGE = 2;
+constexpr int TMEM_COLS = 512;
+constexpr unsigned long long WAIT_LIMIT_NS = 1000000000ull;
+
+struct MInfo {
+  long long base;  // first tile row of (m, p=0)
+  int nr, nq;      // rows per tile (N extent, multiple of 16), K chunks per parity
+  int kv0, kv1;    // valid K per parity
+  int nv0, nv1;    // valid N per parity
+};
+
+struct TcArgs {
+  int dir;  // 0 inverse, 1 forward
+  int N, Jh, batch, nct;
+  long long ncoef;
+  int items_per_ct;
+  const MInfo *mi;
+  const int *pre;  // prefix of n-tiles over m (N+2 entries)
+  const double *spec_in;
+  const float *G;
+  float *F;
+  double *spec_out;
+  int *err;
+};
+
+// ------------------------------------------------------------ PTX helpers
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t *b, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t *b) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_tx(uint64_t *b, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint64_t *b, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ unsigned long long gtimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+// Bounded wait: returns false (and records code) if the phase did not
+// complete within the limit or another role already gave up.
+__device__ __forceinline__ bool mbar_wait(uint64_t *b, uint32_t parity, int *err, volatile int *abort_flag,
+                                          int code) {
+  if (mbar_try(b, parity)) return true;
+  const unsigned long long t0 = gtimer();
+  for (uint32_t it = 1;; ++it) {
+    if (mbar_try(b, parity)) return true;
+    if ((it & 255) == 0) {
+      if (*abort_flag) return false;
+      if (gtimer() - t0 > WAIT_LIMIT_NS) {
+        *abort_flag = 1;
+        atomicCAS(err, 0, code);
+        return false;
+      }
+    }
+  }
+}
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+      "[%4];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+// K-major operand, 128-byte swizzle, 8-row groups 1024 bytes apart.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr >> 4) & 0x3FFF);
+  d |= (uint64_t)1 << 16;                 // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;       // stride byte offset
+  d |= (uint64_t)1 << 46;                 // descriptor version (sm_100 family)
+  d |= (uint64_t)2 << 61;                 // SWIZZLE_128B
+  return d;
+}
+// kind::f16 instruction descriptor: BF16 x BF16 -> F32, both K-major, M = 128.
+__device__ __forceinline__ uint32_t idesc_bf16(int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+}
+__device__ __forceinline__ void mma_bf16(uint32_t dtmem, uint64_t da, uint64_t db, uint32_t idesc, int acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(dtmem),
+      "l"(da), "l"(db), "r"(idesc), "r"(acc)
+      : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint64_t *bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                   smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+      "[%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+        "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void split3(double x, __nv_bfloat16 &h, __nv_bfloat16 &m, __nv_bfloat16 &l) {
+  h = __double2bfloat16(x);
+  double r = x - (double)__bfloat162float(h);
+  m = __double2bfloat16(r);
+  r = r - (double)__bfloat162float(m);
+  l = __double2bfloat16(r);
+}
+
+// Work item decode: items ordered (ct, m, nt), heavy (small m) first within ct.
+__device__ __forceinline__ void decode(const TcArgs &a, int it, int &m, int &ct, int &nt) {
+  ct = it / a.items_per_ct;
+  int r = it % a.items_per_ct;
+  int lo = 0, hi = a.N + 1;  // find m with pre[m] <= r < pre[m+1]
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (a.pre[mid] <= r) lo = mid;
+    else hi = mid;
+  }
+  m = lo;
+  nt = r - a.pre[m];
+}
+
+__global__ void __launch_bounds__(TC_THREADS, 1)
+legendre_tc_kernel(const __grid_constant__ CUtensorMap tmap, TcArgs a) {
+  extern __shared__ __align__(1024) unsigned char smem_dyn[];
+  // 1024-byte aligned stage area (swizzle atoms are address based).
+  unsigned char *sm = reinterpret_cast<unsigned char *>(
+      (reinterpret_cast<uintptr_t>(smem_dyn) + 1023) & ~(uintptr_t)1023);
+  unsigned char *stage = sm;
+  uint64_t *bars = reinterpret_cast<uint64_t *>(sm + NSTAGE * STAGE_BYTES);
+  uint64_t *full = bars, *empty = bars + 2, *accf = bars + 4, *acce = bars + 6;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 8);
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(bars + 9);
+
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < NSTAGE; ++s) {
+      mbar_init(&full[s], 129);
+      mbar_init(&empty[s], 1);
+      mbar_init(&accf[s], 1);
+      mbar_init(&acce[s], 128);
+    }
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 8) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  const int nitems = a.nct * a.items_per_ct;
+  const int C2B = 2 * a.batch;
+
+  if (warp < 4) {
+    // ------------------------------------------------------- producers
+    const int t = threadIdx.x;  // row of the A tile
+    int g = 0;                  // chunk counter
+    bool ok = true;
+    for (int it = blockIdx.x; it < nitems && ok; it += gridDim.x) {
+      int m, ct, nt;
+      decode(a, it, m, ct, nt);
+      const MInfo mi = a.mi[m];
+      const int nrow = min(128, mi.nr - nt * 128);
+      const int c = ct * 128 + t;
+      for (int p = 0; p < 2 && ok; ++p) {
+        const int kv = p ? mi.kv1 : mi.kv0;
+        const int nq = (kv + 63) / 64;
+        for (int q = 0; q < nq; ++q, ++g) {
+          const int s = g % NSTAGE;
+          if (!mbar_wait(&empty[s], ((g / NSTAGE) & 1) ^ 1, a.err, abort_flag, 1)) { ok = false; break; }
+          unsigned char *As = stage + s * STAGE_BYTES;
+          unsigned char *Bs = As + 3 * A_SPLIT_BYTES;
+          if (t == 0) {
+            mbar_arrive_tx(&full[s], (uint32_t)(3 * nrow * 128));
+            for (int sp = 0; sp < 3; ++sp) {
+              const long long row0 = mi.base + ((long long)(p * mi.nq + q) * 3 + sp) * mi.nr + nt * 128;
+              for (int r = 0; r < nrow; r += 16)
+                tma_load_2d(Bs + sp * B_SPLIT_BYTES + r * 128, &tmap, 0, (int)(row0 + r), &full[s]);
+            }
+          }
+          // A row t: 8 groups of 8 bf16 along K, three split planes.
+          const int kbase = q * 64;
+          for (int g8 = 0; g8 < 8; ++g8) {
+            __align__(16) __nv_bfloat16 h[8], md[8], lo[8];
+            const int k0 = kbase + g8 * 8;
+#pragma unroll
+            for (int e = 0; e < 8; ++e) {
+              const int k = k0 + e;
+              double x = 0.0;
+              if (c < C2B && k < kv) {
+                if (a.dir == 0) {
+                  const int n = m + p + 2 * k;
+                  x = a.spec_in[((long long)(c >> 1) * a.ncoef + idx_mn(a.N, m, n)) * 2 + (c & 1)];
+                } else {
+                  x = (double)a.G[(((long long)m * 2 + p) * a.Jh + k) * C2B + c];
+                }
+              }
+              split3(x, h[e], md[e], lo[e]);
+            }
+            const uint32_t off = (t >> 3) * 1024 + (t & 7) * 128 + ((g8 ^ (t & 7)) << 4);
+            *reinterpret_cast<uint4 *>(As + off) = *reinterpret_cast<const uint4 *>(h);
+            *reinterpret_cast<uint4 *>(As + A_SPLIT_BYTES + off) = *reinterpret_cast<const uint4 *>(md);
+            *reinterpret_cast<uint4 *>(As + 2 * A_SPLIT_BYTES + off) = *reinterpret_cast<const uint4 *>(lo);
+          }
+          fence_proxy_async();
+          mbar_arrive(&full[s]);
+        }
+      }
+    }
+  } else if (warp == 8) {
+    // ------------------------------------------------------------- MMA
+    if (lane == 0) {
+      int g = 0, li = 0;
+      bool ok = true;
+      for (int it = blockIdx.x; it < nitems && ok; it += gridDim.x, ++li) {
+        int m, ct, nt;
+        decode(a, it, m, ct, nt);
+        const MInfo mi = a.mi[m];
+        const int nrow = min(128, mi.nr - nt * 128);
+        const uint32_t idesc = idesc_bf16(nrow);
+        const int ab = li & 1;
+        if (!mbar_wait(&acce[ab], ((li >> 1) & 1) ^ 1, a.err, abort_flag, 2)) { ok = false; break; }
+        tc_fence_after();
+        for (int p = 0; p < 2 && ok; ++p) {
+          const int kv = p ? mi.kv1 : mi.kv0;
+          const int nq = (kv + 63) / 64;
+          const uint32_t dt = tmem + ab * 256 + p * 128;
+          int acc = 0;
+          for (int q = 0; q < nq; ++q, ++g) {
+            const int s = g % NSTAGE;
+            if (!mbar_wait(&full[s], (g / NSTAGE) & 1, a.err, abort_flag, 3)) { ok = false; break; }
+            tc_fence_after();
+            const uint32_t As = smem_u32(stage + s * STAGE_BYTES);
+            const uint32_t Bs = As + 3 * A_SPLIT_BYTES;
+            const int ksteps = min(4, (kv - q * 64 + 15) / 16);
+            for (int ks = 0; ks < ksteps; ++ks) {
+              const uint32_t ko = ks * 32;
+              // (A split, B split): hi*hi, hi*mid, mid*hi, hi*lo, lo*hi, mid*mid
+              const int pa[6] = {0, 0, 1, 0, 2, 1};
+              const int pb[6] = {0, 1, 0, 2, 0, 1};
+#pragma unroll
+              for (int u = 0; u < 6; ++u) {
+                mma_bf16(dt, smem_desc(As + pa[u] * A_SPLIT_BYTES + ko),
+                         smem_desc(Bs + pb[u] * B_SPLIT_BYTES + ko), idesc, acc);
+                acc = 1;
+              }
+            }
+            mma_commit(&empty[s]);
+          }
+        }
+        mma_commit(&accf[ab]);
+      }
+    }
+    __syncwarp();
+  } else {
+    // -------------------------------------------------------- epilogue
+    const int quad = warp & 3;
+    const int row = quad * 32 + lane;
+    int li = 0;
+    for (int it = blockIdx.x; it < nitems; it += gridDim.x, ++li) {
+      int m, ct, nt;
+      decode(a, it, m, ct, nt);
+      const MInfo mi = a.mi[m];
+      const int nrow = min(128, mi.nr - nt * 128);
+      const int ab = li & 1;
+      if (!mbar_wait(&accf[ab], (li >> 1) & 1, a.err, abort_flag, 4)) break;
+      tc_fence_after();
+      const int c = ct * 128 + row;
+      const uint32_t tbase = tmem + ((uint32_t)(quad * 32) << 16) + ab * 256;
+      if (a.dir == 0) {
+        const int J = 2 * a.Jh;
+        const bool odd = mi.kv1 > 0;
+        for (int j0 = 0; j0 < nrow; j0 += 16) {
+          float e[16], o[16];
+          tmem_ld16(tbase + j0, e);
+          if (odd) tmem_ld16(tbase + 128 + j0, o);
+          else
+#pragma unroll
+            for (int i = 0; i < 16; ++i) o[i] = 0.f;
+          if (c < C2B) {
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+              const int jj = nt * 128 + j0 + i;
+              if (jj < a.Jh) {
+                a.F[((long long)m * J + (a.Jh + jj)) * C2B + c] = e[i] + o[i];
+                a.F[((long long)m * J + (a.Jh - 1 - jj)) * C2B + c] = e[i] - o[i];
+              }
+            }
+          }
+        }
+      } else {
+        for (int p = 0; p < 2; ++p) {
+          const int nv = p ? mi.nv1 : mi.nv0;
+          for (int k0 = 0; k0 < nrow; k0 += 16) {
+            if (nt * 128 + k0 >= nv) break;  // uniform across the warp
+            float d[16];
+            tmem_ld16(tbase + p * 128 + k0, d);
+            if (c < C2B) {
+#pragma unroll
+              for (int i = 0; i < 16; ++i) {
+                const int k = nt * 128 + k0 + i;
+                if (k < nv) {
+                  const int n = m + p + 2 * k;
+                  const double v = (m == 0 && (c & 1)) ? 0.0 : (double)d[i];
+                  a.spec_out[((long long)(c >> 1) * a.ncoef + idx_mn(a.N, m, n)) * 2 + (c & 1)] = v;
+                }
+              }
+            }
+          }
+        }
+      }
+      tc_fence_before();
+      mbar_arrive(&acce[ab]);
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 8) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS)
+                 : "memory");
+  }
+}
+
+// ------------------------------------------------------------ tile tables
+// Fill the bf16 split tiles of one direction from the FP64 Pbar table.
+// Thread per (tile row of split 0, group of 8 along K).
+__global__ void build_tiles_kernel(int dir, int N, int Jh, const MInfo *__restrict__ mi,
+                                   const long long *__restrict__ rowstart, long long nrows0,
+                                   const double *__restrict__ pnm, const double *__restrict__ w,
+                                   __nv_bfloat16 *__restrict__ out) {
+  const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (tid >= nrows0 * 8) return;
+  const long long r0 = tid >> 3;
+  const int g8 = (int)(tid & 7);
+  // find (m, p, q, r) of this split-0 row: rowstart[m] = first split-0 row index of m
+  int lo = 0, hi = N + 1;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (rowstart[mid] <= r0) lo = mid;
+    else hi = mid;
+  }
+  const int m = lo;
+  const MInfo M = mi[m];
+  long long rr = r0 - rowstart[m];
+  const int r = (int)(rr % M.nr);
+  rr /= M.nr;
+  const int q = (int)(rr % M.nq);
+  const int p = (int)(rr / M.nq);
+  const int kv = p ? M.kv1 : M.kv0;
+  const int nv = p ? M.nv1 : M.nv0;
+  __align__(16) __nv_bfloat16 h[8], md[8], l[8];
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    const int k = q * 64 + g8 * 8 + e;
+    double x = 0.0;
+    if (k < kv && r < nv) {
+      if (dir == 0) {  // rows = latitude pair jj, K = n index
+        const int n = m + p + 2 * k;
+        x = pnm[idx_mn(N, m, n) * Jh + r];
+      } else {  // rows = n index, K = latitude pair
+        const int n = m + p + 2 * r;
+        x = (0.5 * w[Jh + k]) * pnm[idx_mn(N, m, n) * Jh + k];
+      }
+    }
+    split3(x, h[e], md[e], l[e]);
+  }
+  const long long row_s0 = M.base + ((long long)(p * M.nq + q) * 3 + 0) * M.nr + r;
+  uint4 *o0 = reinterpret_cast<uint4 *>(out + (row_s0)*64 + g8 * 8);
+  uint4 *o1 = reinterpret_cast<uint4 *>(out + (row_s0 + M.nr) * 64 + g8 * 8);
+  uint4 *o2 = reinterpret_cast<uint4 *>(out + (row_s0 + 2LL * M.nr) * 64 + g8 * 8);
+  *o0 = *reinterpret_cast<const uint4 *>(h);
+  *o1 = *reinterpret_cast<const uint4 *>(md);
+  *o2 = *reinterpret_cast<const uint4 *>(l);
+}
+
+// Host metadata for one direction's table.
+struct TabMeta {
+  std::vector<MInfo> mi;
+  std::vector<long long> rowstart;  // split-0 rows before m
+  std::vector<int> pre;             // n-tile prefix
+  long long rows = 0, rows0 = 0;
+};
+
+static TabMeta make_meta(int dir, int N, int Jh) {
+  TabMeta t;
+  t.mi.resize(N + 1);
+  t.rowstart.resize(N + 2);
+  t.pre.resize(N + 2);
+  long long base = 0, r0 = 0;
+  int pre = 0;
+  for (int m = 0; m <= N; ++m) {
+    MInfo &M = t.mi[m];
+    const int c0 = count_np(N, m, 0), c1 = count_np(N, m, 1);
+    if (dir == 0) {
+      M.kv0 = c0; M.kv1 = c1;
+      M.nv0 = Jh; M.nv1 = Jh;
+      M.nr = (Jh + 15) / 16 * 16;
+      M.nq = (c0 + 63) / 64;
+    } else {
+      M.kv0 = Jh; M.kv1 = Jh;
+      M.nv0 = c0; M.nv1 = c1;
+      M.nr = (c0 + 15) / 16 * 16;
+      M.nq = (Jh + 63) / 64;
+    }
+    M.base = base;
+    t.rowstart[m] = r0;
+    t.pre[m] = pre;
+    base += 2LL * M.nq * 3 * M.nr;
+    r0 += 2LL * M.nq * M.nr;
+    pre += (M.nr + 127) / 128;
+  }
+  t.rowstart[N + 1] = r0;
+  t.pre[N + 1] = pre;
+  t.rows = base;
+  t.rows0 = r0;
+  return t;
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *,
+                                  CUtensorMapInterleave, CUtensorMapSwizzle, CUtensorMapL2promotion,
+                                  CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn get_encode() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  }
+  return fn;
+}
+
+static int build_one(Plan &P, int dir, TileTable &T) {
+  TabMeta meta = make_meta(dir, P.N, P.Jh);
+  T.rows = meta.rows;
+  T.base.assign(P.N + 1, 0);
+  for (int m = 0; m <= P.N; ++m) T.base[m] = meta.mi[m].base;
+  DCCM_CUDA(cudaMalloc(&T.d, (size_t)meta.rows * 64 * sizeof(uint16_t)));
+  MInfo *dmi;
+  long long *drs;
+  int *dpre;
+  DCCM_CUDA(cudaMalloc(&dmi, meta.mi.size() * sizeof(MInfo)));
+  DCCM_CUDA(cudaMalloc(&drs, meta.rowstart.size() * sizeof(long long)));
+  DCCM_CUDA(cudaMalloc(&dpre, meta.pre.size() * sizeof(int)));
+  DCCM_CUDA(cudaMemcpy(dmi, meta.mi.data(), meta.mi.size() * sizeof(MInfo), cudaMemcpyHostToDevice));
+  DCCM_CUDA(cudaMemcpy(drs, meta.rowstart.data(), meta.rowstart.size() * sizeof(long long),
+                       cudaMemcpyHostToDevice));
+  DCCM_CUDA(cudaMemcpy(dpre, meta.pre.data(), meta.pre.size() * sizeof(int), cudaMemcpyHostToDevice));
+  const long long nthr = meta.rows0 * 8;
+  if (nthr > 0) {
+    build_tiles_kernel<<<(unsigned)((nthr + 255) / 256), 256>>>(dir, P.N, P.Jh, dmi, drs, meta.rows0,
+                                                               P.d_pnm, P.d_w, (__nv_bfloat16 *)T.d);
+    DCCM_LAUNCH_CHECK();
+  }
+  DCCM_CUDA(cudaDeviceSynchronize());
+  cudaFree(drs);
+  EncodeTiledFn enc = get_encode();
+  if (!enc) return DCCM_ERR_UNSUPPORTED;
+  const cuuint64_t gdim[2] = {64, (cuuint64_t)meta.rows};
+  const cuuint64_t gstr[1] = {128};
+  const cuuint32_t box[2] = {64, 16};
+  const cuuint32_t estr[2] = {1, 1};
+  CUresult r = enc(&T.map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, T.d, gdim, gstr, box, estr,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                   CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return DCCM_ERR_UNSUPPORTED;
+  T.map_ok = true;
+  T.d_mi = dmi;
+  T.d_pre = dpre;
+  T.items_per_ct = meta.pre[P.N + 1];
+  return DCCM_OK;
+}
+
+int build_tiles(Plan &P) {
+  DCCM_TRY(build_one(P, 0, P.tinv));
+  DCCM_TRY(build_one(P, 1, P.tfwd));
+  return DCCM_OK;
+}
+
+static size_t tc_smem_bytes() { return 1024 + (size_t)NSTAGE * STAGE_BYTES + 128; }
+
+static int launch_tc(Plan &P, TileTable &T, TcArgs &a, cudaStream_t s) {
+  static bool attr_done = false;
+  if (!attr_done) {
+    DCCM_CUDA(cudaFuncSetAttribute(legendre_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)tc_smem_bytes()));
+    attr_done = true;
+  }
+  a.N = P.N;
+  a.Jh = P.Jh;
+  a.ncoef = P.ncoef;
+  a.nct = (2 * a.batch + 127) / 128;
+  a.items_per_ct = T.items_per_ct;
+  a.mi = (const MInfo *)T.d_mi;
+  a.pre = T.d_pre;
+  a.err = P.d_err;
+  const int items = a.nct * a.items_per_ct;
+  if (items <= 0) return DCCM_OK;
+  const int grid = items < sm_count() ? items : sm_count();
+  legendre_tc_kernel<<<grid, TC_THREADS, tc_smem_bytes(), s>>>(T.map, a);
+  DCCM_LAUNCH_CHECK();
+  return DCCM_OK;
+}
+
+int legendre_inv_tc(Plan &P, int batch, const double *spec, float *F, cudaStream_t s) {
+  if (batch <= 0) return DCCM_OK;
+  if (!P.tinv.map_ok) return DCCM_ERR_UNSUPPORTED;
+  TcArgs a = {};
+  a.dir = 0;
+  a.batch = batch;
+  a.spec_in = spec;
+  a.F = F;
+  return launch_tc(P, P.tinv, a, s);
+}
+
+int legendre_fwd_tc(Plan &P, int batch, const float *G, double *spec, cudaStream_t s) {
+  if (batch <= 0) return DCCM_OK;
+  if (!P.tfwd.map_ok) return DCCM_ERR_UNSUPPORTED;
+  TcArgs a = {};
+  a.dir = 1;
+  a.batch = batch;
+  a.G = G;
+  a.spec_out = spec;
+  return launch_tc(P, P.tfwd, a, s);
+}
+
+}  // namespace sht
+}  // namespace dccm

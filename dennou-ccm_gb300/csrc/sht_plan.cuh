@@ -1,0 +1,94 @@
+// Spherical-harmonic transform plan (internal header).
+//
+// Convention (the reference's SPML library is external and not vendored;
+// this is the library's own, fixed and documented in the public header):
+// latitudes ascending south to north, mu_j = sin(lat_j) the Gauss-Legendre
+// nodes; longitudes 2 pi i / I; Pbar_n^m with integral Pbar^2 dmu = 2 and no
+// Condon-Shortley phase; spectral coefficients complex, m-major,
+// idx(m,n) = m(N+1) - m(m-1)/2 + (n-m); grid[b][j][i] (i fastest).
+//
+// Hemisphere pairing: jj = 0..J/2-1 indexes latitude pairs from the equator
+// outwards, jn = J/2 + jj (north, mu > 0) and js = J/2 - 1 - jj (its mirror).
+//
+// Intermediate Fourier buffers (c = 2 b + {0: re, 1: im}, c fastest):
+//   inverse: F[m][j][c]       Legendre synthesis output, FFT input;
+//   forward: G[m][p][jj][c]   FFT output folded into parity p: p = 0 holds
+//                             E = G(jn) + G(js), p = 1 holds O = G(jn) - G(js),
+//                             already divided by I.
+#pragma once
+#include <cuda.h>
+
+#include <vector>
+
+#include "common.cuh"
+
+namespace dccm {
+namespace sht {
+
+constexpr int MAX_STAGES = 12;
+
+struct FftPlan {
+  int I = 0;
+  int nst = 0;
+  int radix[MAX_STAGES] = {0};
+};
+
+// Layout of one Legendre operand table of bf16 split tiles (tensor path):
+// rows of 64 bf16 (128 bytes) in a 2-D tensor [rows][64]; for (m, p) the
+// tile of chunk q (64 wide along K) and split s starts at row
+// base[m*2+p] + (q*3 + s) * nr[m*2+p], with nr rows (N-dimension extent
+// rounded up to 16).  Entries past the valid K or N range are zero.
+struct TileTable {
+  std::vector<int64_t> base;  // per (m,p)
+  std::vector<int> nr, nq, kval, nval;
+  int64_t rows = 0;
+  uint16_t *d = nullptr;      // device bf16 bits
+  CUtensorMap map;            // TMA descriptor, box {64, 16}
+  bool map_ok = false;
+  void *d_mi = nullptr;       // per-m tile metadata (device)
+  int *d_pre = nullptr;       // prefix of N-tiles over m (device)
+  int items_per_ct = 0;       // work items per 128-column block of the batch
+};
+
+struct Plan {
+  int N = 0, I = 0, J = 0, Jh = 0;
+  int precision = 0;
+  int max_batch = 0;
+  int64_t ncoef = 0;
+  // host copies of the axes
+  std::vector<double> mu, w;
+  // device
+  double *d_mu = nullptr, *d_w = nullptr;
+  double *d_pnm = nullptr;     // FP64 Pbar(m, n, jj): [idx(m,n)][Jh]
+  double2 *d_tw64 = nullptr;   // FFT twiddles e^{-2 pi i t / I}
+  float2 *d_tw32 = nullptr;
+  FftPlan fft;
+  TileTable tinv, tfwd;        // bf16x3 tiles for the tensor path
+  void *d_work = nullptr;      // Fourier buffer (F or G), sized for max_batch
+  size_t work_bytes = 0;
+  int *d_err = nullptr;        // device error flag of bounded waits
+  DevBuf stage;                // host entry point staging
+  cudaStream_t stream = nullptr;
+};
+
+__host__ __device__ inline int64_t idx_mn(int N, int m, int n) {
+  return (int64_t)m * (N + 1) - (int64_t)m * (m - 1) / 2 + (n - m);
+}
+
+// Number of n in parity p (n - m = p mod 2) for zonal wavenumber m.
+__host__ __device__ inline int count_np(int N, int m, int p) {
+  const int first = m + p;
+  return first > N ? 0 : (N - first) / 2 + 1;
+}
+
+// Kernel launchers (defined in the .cu files).
+int fft_inverse(const Plan &P, int batch, bool fp32, const void *F, double *grid, cudaStream_t s);
+int fft_forward(const Plan &P, int batch, bool fp32, const double *grid, void *G, cudaStream_t s);
+int legendre_inv_f64(const Plan &P, int batch, const double *spec, double *F, cudaStream_t s);
+int legendre_fwd_f64(const Plan &P, int batch, const double *G, double *spec, cudaStream_t s);
+int legendre_inv_tc(Plan &P, int batch, const double *spec, float *F, cudaStream_t s);
+int legendre_fwd_tc(Plan &P, int batch, const float *G, double *spec, cudaStream_t s);
+int build_tiles(Plan &P);
+
+}  // namespace sht
+}  // namespace dccm

@@ -177,6 +177,56 @@ int dccm_remap_apply_dev(dccm_remap_plan *plan, const double *src, int64_t ld_sr
 int dccm_area_integral_dev(const double *f, const double *area, int64_t n,
                            double *result, void *stream);
 
+/* =====================================================================
+ * Spherical-harmonic transforms on the Gaussian grid
+ * Replace the SPML transforms that the atmosphere dynamics call through
+ * libdcpam5 (atm/dcpam_main_mod.f90:2173-2180) and SPML's w_Initial(nMax,
+ * iMax, jMax) with its grid axes xy_Lon, xy_Lat, x_Lon_Weight, y_Lat_Weight
+ * (tool/gmapgen/gmapgen_main.f90:262-305).  SPML is external and not
+ * vendored, so the convention is this library's own:
+ *   - latitudes ascending south to north, mu_j = sin(lat_j) the roots of
+ *     P_J, weights w_j with sum 2; longitudes 2 pi i / I;
+ *   - Pbar_n^m with integral_{-1}^{1} Pbar^2 dmu = 2, no Condon-Shortley
+ *     phase, triangular truncation n <= N = nmax;
+ *   - spec[b][k] complex (re, im interleaved doubles), k = idx(m,n) =
+ *     m(N+1) - m(m-1)/2 + (n-m) for m = 0..N, n = m..N (Im s_n^0 = 0);
+ *   - grid[b][j][i] doubles, i fastest (Fortran (0:imax-1, 1:jmax, b));
+ *   - inverse: g = Re F_0 + 2 Re sum_{m>=1} F_m e^{i m lon},
+ *     F_m(mu) = sum_n s_n^m Pbar_n^m(mu);
+ *   - forward: s_n^m = (1/2) sum_j w_j Pbar_n^m(mu_j) (1/I) sum_i g_ij e^{-i m lon_i}.
+ * precision DCCM_SHT_FP64: FP64 throughout (CUDA cores).
+ * precision DCCM_SHT_MIXED: Legendre sums on the tensor cores in split
+ * BF16 x 3 with FP32 accumulation, FFT in FP32; relative L2 error of a
+ * forward(inverse(s)) round trip below 1e-6.  Requires jmax/2 % 16 == 0.
+ * Requirements: jmax even, jmax >= nmax+1, imax > 2 nmax, imax = 2^a 3^b.
+ * ===================================================================== */
+enum { DCCM_SHT_FP64 = 0, DCCM_SHT_MIXED = 1 };
+
+typedef struct dccm_sht_plan dccm_sht_plan;
+
+int dccm_sht_plan_create(int nmax, int imax, int jmax, int precision, int max_batch,
+                         dccm_sht_plan **plan);
+int dccm_sht_plan_destroy(dccm_sht_plan *plan);
+/* Grid axes as SPML returns them (host arrays, any may be NULL). */
+int dccm_sht_axes(const dccm_sht_plan *plan, double *x_Lon, double *y_Lat,
+                  double *x_Lon_Weight, double *y_Lat_Weight);
+/* Gauss-Legendre nodes mu[jmax] and weights w[jmax] computed on the GPU. */
+int dccm_sht_gauss(const dccm_sht_plan *plan, double *mu, double *w);
+/* FP64 Pbar table as computed on the GPU: pnm[idx(m,n)*(jmax/2) + jj] at
+ * mu[jmax/2 + jj] (northern hemisphere), host array. */
+int dccm_sht_pnm(const dccm_sht_plan *plan, double *pnm);
+/* Device arrays, stream-ordered; batch <= max_batch field-levels. */
+int dccm_sht_inverse_dev(dccm_sht_plan *plan, const double *spec, double *grid, int batch,
+                         void *stream);
+int dccm_sht_forward_dev(dccm_sht_plan *plan, const double *grid, double *spec, int batch,
+                         void *stream);
+/* Host arrays; returns after the result is in host memory. */
+int dccm_sht_inverse(dccm_sht_plan *plan, const double *spec, double *grid, int batch);
+int dccm_sht_forward(dccm_sht_plan *plan, const double *grid, double *spec, int batch);
+/* Synchronises the device and reports (then clears) the error flag that
+ * bounded device waits set; DCCM_ERR_TIMEOUT if one gave up. */
+int dccm_sht_status(dccm_sht_plan *plan, int *device_error);
+
 #ifdef __cplusplus
 }
 #endif

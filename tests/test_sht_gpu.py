@@ -1,0 +1,123 @@
+"""GPU parity of the spherical-harmonic transforms against the FP64 oracle,
+through the C ABI.  Tolerances (relative L2 over the whole batch):
+  FP64 plan   1e-13 (inverse grid, forward spectra), nodes 2e-16;
+  mixed plan  1e-6  (BF16 x 3 Legendre on tcgen05, FP32 FFT)."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+TRUNC = [(21, 64, 32), (42, 128, 64), (63, 192, 96), (85, 256, 128)]
+
+
+@pytest.mark.parametrize("N,I,J", TRUNC + [(341, 1024, 512)])
+def test_gauss_and_pnm_match_oracle(dccm, oracle, N, I, J):
+    plan = dccm.ShtPlan(N, I, J, dccm.SHT_FP64, 1)
+    mu, w = plan.gauss()
+    mo, wo = oracle.gauss_nodes(J)
+    assert np.abs(mu - mo).max() <= 2e-16
+    assert np.abs(w - wo).max() <= 1e-15
+    assert abs(w.sum() - 2.0) <= 1e-13
+    lon, lat, lw, yw = plan.axes()
+    assert np.allclose(np.sin(lat), mu, atol=1e-15) and np.all(yw == w)
+    assert np.allclose(lon, 2 * np.pi * np.arange(I) / I) and np.allclose(lw, 2 * np.pi / I)
+    p = plan.pnm()
+    po = oracle.pnm(N, J)[:, J // 2:]
+    assert np.abs(p - po).max() <= 1e-11 * max(1.0, np.abs(po).max())
+
+
+@pytest.mark.parametrize("N,I,J", TRUNC)
+def test_fp64_transforms_match_oracle(dccm, oracle, synth, N, I, J):
+    B = 6
+    s = synth.spectra(N, B, seed=N)
+    plan = dccm.ShtPlan(N, I, J, dccm.SHT_FP64, B)
+    g = plan.inverse(s)
+    go = oracle.sht_inverse(N, I, J, s)
+    assert rel_l2(g, go) <= 1e-13
+    s2 = plan.forward(go)
+    so = oracle.sht_forward(N, I, J, go)
+    assert rel_l2(s2, so) <= 1e-13
+    assert rel_l2(plan.forward(g), s) <= 1e-13
+
+
+@pytest.mark.parametrize("N,I,J", TRUNC)
+def test_mixed_transforms_match_oracle(dccm, oracle, synth, N, I, J):
+    B = 70  # two 128-column blocks of the batch, the second partial
+    s = synth.spectra(N, B, seed=N + 1)
+    plan = dccm.ShtPlan(N, I, J, dccm.SHT_MIXED, B)
+    g = plan.inverse(s)
+    go = oracle.sht_inverse(N, I, J, s)
+    e_inv = rel_l2(g, go)
+    s2 = plan.forward(go)
+    so = oracle.sht_forward(N, I, J, go)
+    e_fwd = rel_l2(s2, so)
+    e_rt = rel_l2(plan.forward(g), s)
+    assert plan.status() == (0, 0)
+    assert e_inv <= 1e-6 and e_fwd <= 1e-6 and e_rt <= 1e-6, (e_inv, e_fwd, e_rt)
+    # per field-level, not only in aggregate
+    for b in range(0, B, 7):
+        assert rel_l2(g[b], go[b]) <= 2e-6
+        assert rel_l2(s2[b], so[b]) <= 2e-6
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_known_answers(dccm, oracle, prec):
+    N, I, J = 21, 64, 32
+    plan = dccm.ShtPlan(N, I, J, prec, 3)
+    mu, w = plan.gauss()
+    lon = 2 * np.pi * np.arange(I) / I
+    s = np.zeros((3, (N + 1) * (N + 2) // 2), complex)
+    s[0, 1] = 1.0          # Y_1^0 = sqrt(3) mu
+    s[1, N + 1] = 1.0      # s_1^1 = 1: 2 sqrt(3/2) cos(lat) cos(lon)
+    s[2, 2] = 1.0          # Y_2^0 = sqrt(5)/2 (3 mu^2 - 1)
+    g = plan.inverse(s)
+    tol = 1e-13 if prec == 0 else 1e-6
+    assert np.abs(g[0] - np.sqrt(3) * mu[:, None]).max() <= tol * 2
+    ref = 2 * np.sqrt(1.5) * np.sqrt(1 - mu ** 2)[:, None] * np.cos(lon)[None, :]
+    assert np.abs(g[1] - ref).max() <= tol * 3
+    assert np.abs(g[2] - (np.sqrt(5) / 2 * (3 * mu ** 2 - 1))[:, None]).max() <= tol * 3
+    back = plan.forward(g)
+    assert np.abs(back - s).max() <= tol * 3
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_golden_fixture(dccm, prec):
+    z = np.load(os.path.join(GOLDEN, "sht_t21.npz"))
+    N, I, J = int(z["N"]), int(z["I"]), int(z["J"])
+    plan = dccm.ShtPlan(N, I, J, prec, 3)
+    tol = 1e-13 if prec == 0 else 1e-6
+    assert rel_l2(plan.inverse(z["spec"]), z["grid"]) <= tol
+    assert rel_l2(plan.forward(z["grid"]), z["fwd"]) <= tol
+
+
+def test_device_entry_points(dccm, oracle, synth, cuda):
+    torch = cuda
+    N, I, J, B = 85, 256, 128, 128
+    s = synth.spectra(N, B, seed=3)
+    for prec, tol in ((0, 1e-13), (1, 1e-6)):
+        plan = dccm.ShtPlan(N, I, J, prec, B)
+        ds = torch.from_numpy(s.view(np.float64).copy()).cuda()
+        dg = torch.empty((B, J, I), dtype=torch.float64, device="cuda")
+        ds2 = torch.empty_like(ds)
+        st = torch.cuda.current_stream()
+        plan.inverse_dev(ds, dg, B, st)
+        plan.forward_dev(dg, ds2, B, st)
+        torch.cuda.synchronize()
+        s2 = ds2.cpu().numpy().view(np.complex128)
+        assert rel_l2(s2, s) <= tol
+        assert plan.status() == (0, 0)
+
+
+def test_batch_limits(dccm):
+    plan = dccm.ShtPlan(21, 64, 32, 0, 2)
+    with pytest.raises(dccm.DccmError) as e:
+        plan.inverse(np.zeros((3, 253), complex))
+    assert e.value.status == -2
+    with pytest.raises(dccm.DccmError):
+        dccm.ShtPlan(21, 40, 32, 0, 1)  # imax <= 2 nmax
+    with pytest.raises(dccm.DccmError):
+        dccm.ShtPlan(21, 70, 32, 0, 1)  # 70 = 2 * 5 * 7 is not 2^a 3^b
