@@ -101,7 +101,25 @@ _SIGS = {
     "dccm_sht_inverse": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
     "dccm_sht_forward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
     "dccm_sht_status": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "dccm_step_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "dccm_step_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "dccm_step_run": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "dccm_step_run_timed": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "dccm_step_run_host": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                          ctypes.c_void_p, ctypes.c_int]),
 }
+
+
+class StepDesc(ctypes.Structure):
+    _fields_ = [("sht", ctypes.c_void_p), ("nfl", ctypes.c_int), ("spec_in", ctypes.c_void_p),
+                ("grid", ctypes.c_void_p), ("spec_out", ctypes.c_void_p), ("remap", ctypes.c_void_p),
+                ("nfields", ctypes.c_int), ("remap_src", ctypes.c_void_p), ("ld_src", ctypes.c_int64),
+                ("remap_dst", ctypes.c_void_p), ("ld_dst", ctypes.c_int64), ("flux", ctypes.c_void_p),
+                ("flux_grid", ctypes.c_void_p)]
+
+
+class HostCopy(ctypes.Structure):
+    _fields_ = [("host", ctypes.c_void_p), ("dev", ctypes.c_void_p), ("bytes", ctypes.c_size_t)]
 
 
 def exported_symbols():
@@ -345,4 +363,60 @@ class ShtPlan:
     def __del__(self):
         if getattr(self, "h", None) and _lib is not None:
             _lib.dccm_sht_plan_destroy(self.h)
+            self.h = None
+
+
+# ----------------------------------------------------------- coupling step
+class Step:
+    """One coupling step as a CUDA graph (dccm_step_create).  Buffers are
+    device tensors that must outlive the step; flux is a dict of device
+    tensors keyed like DSFCM_Util_SfcBulkFlux_Get's arguments."""
+
+    def __init__(self, sht=None, nfl=0, spec_in=None, grid=None, spec_out=None, remap=None, nfields=0,
+                 remap_src=None, ld_src=0, remap_dst=None, ld_dst=0, flux=None, flux_grid=None):
+        L = load()
+        d = StepDesc()
+        d.sht = sht.h.value if sht is not None else None
+        d.nfl = int(nfl)
+        d.spec_in, d.grid, d.spec_out = (_p(x).value if x is not None else None for x in (spec_in, grid, spec_out))
+        d.remap = remap.h.value if remap is not None else None
+        d.nfields = int(nfields)
+        d.remap_src = _p(remap_src).value if remap_src is not None else None
+        d.remap_dst = _p(remap_dst).value if remap_dst is not None else None
+        d.ld_src, d.ld_dst = int(ld_src), int(ld_dst)
+        self._keep = [sht, remap, spec_in, grid, spec_out, remap_src, remap_dst, flux]
+        if flux is not None:
+            fa = FluxArgs()
+            self._sig = np.ascontiguousarray(np.asarray(flux["a_Sig1Info"], np.float64))
+            for n in FLUX_ARGS:
+                setattr(fa, n, self._sig.ctypes.data if n == "a_Sig1Info" else _p(flux[n]).value)
+            self._fa = fa
+            self._fg = SfcGrid(*flux_grid)
+            d.flux = ctypes.addressof(fa)
+            d.flux_grid = ctypes.addressof(self._fg)
+        self.h = ctypes.c_void_p()
+        _check(L.dccm_step_create(ctypes.byref(d), ctypes.byref(self.h)), "dccm_step_create")
+
+    def run(self, stream=None):
+        _check(load().dccm_step_run(self.h, _stream(stream)), "dccm_step_run")
+
+    def run_timed(self, stream=None):
+        ms = (ctypes.c_float * 4)()
+        _check(load().dccm_step_run_timed(self.h, _stream(stream), ms), "dccm_step_run_timed")
+        return list(ms)
+
+    def run_host(self, h2d, d2h, stream=None):
+        """h2d / d2h: lists of (host tensor or array, device tensor) pairs."""
+        def copies(pairs):
+            arr = (HostCopy * max(1, len(pairs)))()
+            for k, (h, dv) in enumerate(pairs):
+                nb = h.numel() * h.element_size() if hasattr(h, "numel") else h.nbytes
+                arr[k] = HostCopy(_p(h).value, _p(dv).value, nb)
+            return arr
+        a, b = copies(h2d), copies(d2h)
+        _check(load().dccm_step_run_host(self.h, _stream(stream), a, len(h2d), b, len(d2h)), "dccm_step_run_host")
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.dccm_step_destroy(self.h)
             self.h = None

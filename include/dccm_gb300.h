@@ -227,6 +227,58 @@ int dccm_sht_forward(dccm_sht_plan *plan, const double *grid, double *spec, int 
  * bounded device waits set; DCCM_ERR_TIMEOUT if one gave up. */
 int dccm_sht_status(dccm_sht_plan *plan, int *device_error);
 
+/* =====================================================================
+ * Coupling step
+ * One coupling step of the hot path on one GPU, as one CUDA graph: the
+ * atmosphere's inverse then forward transforms of nfl field-levels (the
+ * transforms of the dynamics, atm/dcpam_main_mod.f90:2173-2180), and,
+ * concurrently, the remap of nfields surface fields (interpolate_data,
+ * reached from jcup_get_data at sfc/dccm_sfc_mod.f90:865-881) followed by
+ * the bulk flux on the destination grid (sfc/dccm_sfc_mod.f90:886-897).
+ * All pointers in the descriptor are device pointers owned by the caller
+ * (a_Sig1Info excepted: host, read at creation); a stage whose plan is
+ * NULL is left out.  The graph is recorded at creation, so the buffers must
+ * stay valid and at the same addresses for the life of the step.
+ * ===================================================================== */
+typedef struct dccm_step_desc {
+  dccm_sht_plan *sht;          /* transform plan, or NULL */
+  int nfl;                     /* field-levels per step (<= plan's max_batch) */
+  const double *spec_in;       /* [nfl][ncoef] complex */
+  double *grid;                /* [nfl][jmax][imax] */
+  double *spec_out;            /* [nfl][ncoef] complex */
+  dccm_remap_plan *remap;      /* remap plan, or NULL */
+  int nfields;                 /* surface fields to remap */
+  const double *remap_src;     /* field f at remap_src + f*ld_src */
+  int64_t ld_src;
+  double *remap_dst;           /* field f at remap_dst + f*ld_dst */
+  int64_t ld_dst;
+  const dccm_sfc_bulk_flux_args *flux;  /* device arrays, or NULL */
+  const dccm_sfc_grid *flux_grid;
+} dccm_step_desc;
+
+typedef struct dccm_step dccm_step;
+
+/* One host<->device copy of dccm_step_run_host. */
+typedef struct dccm_host_copy {
+  void *host;
+  void *dev;
+  size_t bytes;
+} dccm_host_copy;
+
+int dccm_step_create(const dccm_step_desc *desc, dccm_step **step);
+int dccm_step_destroy(dccm_step *step);
+/* Replays the step's graph on stream (stream-ordered, no synchronisation). */
+int dccm_step_run(dccm_step *step, void *stream);
+/* Runs the four stages one after another on stream with events between
+ * them and returns their device times: ms[0] inverse transform, ms[1]
+ * forward transform, ms[2] remap, ms[3] bulk flux.  Synchronises. */
+int dccm_step_run_timed(dccm_step *step, void *stream, float *ms);
+/* Copies nh2d host buffers to the device, replays the graph, copies nd2h
+ * device buffers back and synchronises: the step for a caller whose data
+ * live in host memory (page-locked memory makes the copies asynchronous). */
+int dccm_step_run_host(dccm_step *step, void *stream, const dccm_host_copy *h2d, int nh2d,
+                       const dccm_host_copy *d2h, int nd2h);
+
 #ifdef __cplusplus
 }
 #endif
