@@ -16,6 +16,7 @@
 // spectra (A_m = (Z_m + conj Z_{I-m})/2, B_m = (Z_m - conj Z_{I-m})/(2i)),
 // folds them into E = (A + B)/I and O = (A - B)/I, stages them, and the CTA
 // writes G[m][p][jj][c] coalesced along c.
+#include "fp_conv.cuh"
 #include "sht_plan.cuh"
 
 namespace dccm {
@@ -25,7 +26,13 @@ template <typename T> struct Cx;
 template <> struct Cx<float> { using t = float2; };
 template <> struct Cx<double> { using t = double2; };
 
-template <typename C> __device__ __forceinline__ C cmk(double x, double y) {
+// Grid values are FP64 in memory; the FP32 transform converts on the integer pipes.
+__device__ __forceinline__ float from_f64(double x, float) { return f64_to_f32_rn(x); }
+__device__ __forceinline__ double from_f64(double x, double) { return x; }
+__device__ __forceinline__ double to_f64(float x) { return f32_to_f64(x); }
+__device__ __forceinline__ double to_f64(double x) { return x; }
+
+template <typename C> __device__ __forceinline__ C cmk(decltype(C::x) x, decltype(C::x) y) {
   C r;
   r.x = x;
   r.y = y;
@@ -147,7 +154,7 @@ fft_inverse_kernel(FftArgs a, int N, int J, int batch, int BB, const T *__restri
   C *x = bufs + (size_t)warp * 2 * I;
   C *y = x + I;
   for (int bl = warp; bl < nb; bl += nw) {
-    for (int k = lane; k < I; k += 32) x[k] = cmk<C>(0.0, 0.0);
+    for (int k = lane; k < I; k += 32) x[k] = cmk<C>(0, 0);
     __syncwarp();
     for (int m = lane; m <= N; m += 32) {
       const T ar = stA[m * cw + 2 * bl], ai = m ? stA[m * cw + 2 * bl + 1] : (T)0;
@@ -161,8 +168,8 @@ fft_inverse_kernel(FftArgs a, int N, int J, int batch, int BB, const T *__restri
     double *gs = grid + ((int64_t)(b0 + bl) * J + js) * I;
     for (int i = lane; i < I; i += 32) {
       const C v = z[i];
-      gn[i] = (double)v.x;
-      gs[i] = (double)v.y;
+      gn[i] = to_f64(v.x);
+      gs[i] = to_f64(v.y);
     }
     __syncwarp();
   }
@@ -200,7 +207,12 @@ fft_forward_kernel(FftArgs a, int N, int J, int batch, int BB, const double *__r
   for (int bl = warp; bl < nb; bl += nw) {
     const double *gn = grid + ((int64_t)(b0 + bl) * J + jn) * I;
     const double *gs = grid + ((int64_t)(b0 + bl) * J + js) * I;
-    for (int i = lane; i < I; i += 32) x[i] = cmk<C>(gn[i], gs[i]);
+    for (int i = lane; i < I; i += 32) {
+      C v;
+      v.x = from_f64(gn[i], T());
+      v.y = from_f64(gs[i], T());
+      x[i] = v;
+    }
     __syncwarp();
     C *Z = warp_fft<C>(x, y, tw, a, -1, lane);
     for (int m = lane; m <= N; m += 32) {

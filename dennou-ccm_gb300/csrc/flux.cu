@@ -51,6 +51,7 @@ struct Geom {
   int IA, IS, JS, NI;
   int64_t ncol;  // NI*NJ
   double sig1;
+  double sig1k;  // sig1^(R/Cp): Exner(p1) = Exner(ps) * sig1k
 };
 
 __device__ __forceinline__ void bulk_coef_l82(double Ri, double z0m, double z0h, double zs,
@@ -99,20 +100,27 @@ __global__ void __launch_bounds__(128) bulk_flux_column(Ptrs p, Geom g) {
     const double z0h = RoughLenHeatFactor * z0m;
     const double humd = 1.0;
 
-    double Frac[2], QSat[2], SVT[2], Tsn[2], Albn[2];
+    // FP64 is the scarce pipe on this GPU: divisions that do not feed a
+    // cancelling difference become products with a shared reciprocal, and
+    // the two Exner functions share one exp/log pair, (ps/P0)^k = exp(k log),
+    // with Exner(sig1 ps) = Exner(ps) sig1^k.  Each rewrite moves a result by
+    // an ulp or two, far inside the 1e-13 agreement with the reference.
+    const double rPs = 1.0 / Ps;
+    double Frac[2], QSat[2], SVT[2], Tsn[2], Albn[2], rTs[2];
     Frac[0] = 1.0 - SIceCon;
     Frac[1] = SIceCon;
 #pragma unroll
     for (int n = 0; n < 2; ++n) {
       Tsn[n] = p.Ts[c + P * n];
       Albn[n] = p.Alb[c + P * n];
-      QSat[n] = EpsV * Es0 / Ps * exp(aL[n] / GasRWet * (1.0 / 273.0 - 1.0 / Tsn[n]));
+      rTs[n] = 1.0 / Tsn[n];
+      QSat[n] = (EpsV * Es0) * rPs * exp(aL[n] / GasRWet * (1.0 / 273.0 - rTs[n]));
       SVT[n] = Tsn[n] * (1.0 + (((1.0 / EpsV) - 1.0) * QSat[n]));
     }
     const double VirTemp = Ta * (1.0 + (((1.0 / EpsV) - 1.0) * q1));
-    const double Press1 = Ps * g.sig1;
-    const double Exner = pow(Press1 / RefPress, GasRDry / CpDry);
-    const double SfcExner = pow(Ps / RefPress, GasRDry / CpDry);
+    const double SfcExner = exp((GasRDry / CpDry) * log(Ps * (1.0 / RefPress)));
+    const double Exner = SfcExner * g.sig1k;
+    const double rExner = 1.0 / Exner;
     const double VelAbs = sqrt(U * U + V * V);
     const double Height = zs + GasRDry / Grav * VirTemp * (1.0 - g.sig1);
 
@@ -122,6 +130,9 @@ __global__ void __launch_bounds__(128) bulk_flux_column(Ptrs p, Geom g) {
     const double cmn = tmp * tmp;
     const double chn = tmp * (FKarm / log((Height - zs + z0h) / z0h));
     const double vmx = fmax(VelAbs, VelMinForRi);
+    const double rvmx2 = 1.0 / (vmx * vmx);
+    const double VT_E = VirTemp / Exner;  // the Richardson number and the sensible heat
+    const double Ta_E = Ta / Exner;       // flux subtract nearly equal terms: true divisions
 
     double CVel[2], CTemp[2], CQ[2], WSX[2], WSY[2], Sen[2], QV[2], LatH[2], LUw[2], SUw[2];
     bool flag[2];
@@ -129,19 +140,20 @@ __global__ void __launch_bounds__(128) bulk_flux_column(Ptrs p, Geom g) {
            Alb3 = 0.0, CVel3 = 0.0, CTemp3 = 0.0, CQ3 = 0.0;
 #pragma unroll
     for (int n = 0; n < 2; ++n) {
-      const double Ri = Grav / (SVT[n] / SfcExner) * (VirTemp / Exner - SVT[n] / SfcExner) /
-                        (vmx * vmx) * (Height - zs);
+      const double SVT_SE = SVT[n] / SfcExner;
+      const double Ri = Grav / SVT_SE * (VT_E - SVT_SE) * rvmx2 * (Height - zs);
       const bool f = (n == 0) ? true : (Frac[n] > 1e-12);
       flag[n] = f;
       double cm, ch, cq;
       bulk_coef_l82(Ri, z0m, z0h, zs, Height, cmn, chn, f, cm, ch, cq);
-      CVel[n] = cm * Ps / (GasRDry * SVT[n]) * fmin(fmax(VelAbs, VelMinForVel), VelMaxForVel);
-      CTemp[n] = ch * Ps / (GasRDry * SVT[n]) * fmin(fmax(VelAbs, VelMinForTemp), VelMaxForTemp);
-      CQ[n] = cq * Ps / (GasRDry * SVT[n]) * fmin(fmax(VelAbs, VelMinForQVap), VelMaxForQVap);
+      const double rho = Ps / (GasRDry * SVT[n]);
+      CVel[n] = cm * rho * fmin(fmax(VelAbs, VelMinForVel), VelMaxForVel);
+      CTemp[n] = ch * rho * fmin(fmax(VelAbs, VelMinForTemp), VelMaxForTemp);
+      CQ[n] = cq * rho * fmin(fmax(VelAbs, VelMinForQVap), VelMaxForQVap);
       if (f) {
         WSX[n] = -CVel[n] * U;
         WSY[n] = -CVel[n] * V;
-        Sen[n] = -CpDry * SfcExner * CTemp[n] * (Ta / Exner - Tsn[n] / SfcExner);
+        Sen[n] = -CpDry * SfcExner * CTemp[n] * (Ta_E - Tsn[n] / SfcExner);
         QV[n] = -humd * CQ[n] * (q1 - QSat[n]);
         LatH[n] = aL[n] * QV[n];
         const double T2 = Tsn[n] * Tsn[n];
@@ -167,7 +179,7 @@ __global__ void __launch_bounds__(128) bulk_flux_column(Ptrs p, Geom g) {
     // Implicit-coupling back-substitution (:355-382).
     const double c11 = p.C1[c], c12 = p.C1[c + P], c13 = p.C1[c + 2 * P], c14 = p.C1[c + 3 * P];
     const double c21 = p.C2[c], c22 = p.C2[c + P], c23 = p.C2[c + 2 * P], c24 = p.C2[c + 3 * P];
-    const double DFsDT1 = -CpDry * SfcExner * CTemp3 / Exner;
+    const double DFsDT1 = -CpDry * SfcExner * CTemp3 * rExner;
     const double f1 = 1.0 / (c11 + CVel3) * (WSX3 + c21);
     const double f2 = 1.0 / (c12 + CVel3) * (WSY3 + c22);
     const double f3 = 1.0 / (c13 - DFsDT1) * (Sen3 + c23);
@@ -177,7 +189,7 @@ __global__ void __launch_bounds__(128) bulk_flux_column(Ptrs p, Geom g) {
     p.DelV[c + 2 * P] = f3;
     p.DelV[c + 3 * P] = f4;
 
-    const double sfac = CpDry * SfcExner / Exner;
+    const double sfac = CpDry * SfcExner * rExner;
     double Lat3 = 0.0;
 #pragma unroll
     for (int n = 0; n < 2; ++n) {
@@ -201,7 +213,7 @@ __global__ void __launch_bounds__(128) bulk_flux_column(Ptrs p, Geom g) {
         fns = +LUw[n] - LDw + LatH[n] + Sen[n];
         fsr = SUw[n] - SDw;
         dfdt = +4.0 * StB * (Tsn[n] * Tsn[n] * Tsn[n]) + CpDry * CTemp[n] +
-               aL[n] * humd * CQ[n] * (aL[n] * QSat[n] / (GasRWet * (Tsn[n] * Tsn[n])));
+               aL[n] * humd * CQ[n] * (aL[n] * QSat[n] * (1.0 / GasRWet) * (rTs[n] * rTs[n]));
       }
       p.Fns[c + P * n] = fns;
       p.Fsr[c + P * n] = fsr;
@@ -276,6 +288,7 @@ int launch(const Ptrs &p, const dccm_sfc_grid *g, double sig1, cudaStream_t s) {
   if (geo.NI <= 0 || NJ <= 0) return DCCM_OK;
   geo.ncol = (int64_t)geo.NI * NJ;
   geo.sig1 = sig1;
+  geo.sig1k = pow(sig1, (GasRUniv / MolWtDry) / CpDry);
   const int threads = 128;
   int64_t blocks = (geo.ncol + threads - 1) / threads;
   const int64_t cap = (int64_t)sm_count() * 16;

@@ -1,0 +1,48 @@
+// FP32 <-> FP64 conversions on the integer pipes.
+//
+// On GB300 the FP64 pipe is a small fraction of the FP32 one, and the
+// hardware conversion instructions between double and float run on it.
+// The mixed-precision kernels convert every grid value and spectral
+// coefficient once, so they use these bit-level IEEE-754 conversions
+// instead (integer ALU and moves only).  Both are exact restatements of
+// the IEEE rules: widening is exact; narrowing rounds to nearest, ties to
+// even.  Operands outside the normal FP32 range (zero excepted), infinities
+// and NaNs take the hardware instruction.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace dccm {
+
+__device__ __forceinline__ double f32_to_f64(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xFFu;
+  if (e == 0u || e == 0xFFu) {
+    if ((u & 0x7FFFFFFFu) == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
+    return (double)f;  // subnormal, inf, nan
+  }
+  const unsigned m = u & 0x7FFFFFu;
+  const unsigned hi = (u & 0x80000000u) | ((e + (1023u - 127u)) << 20) | (m >> 3);
+  const unsigned lo = m << 29;
+  return __hiloint2double((int)hi, (int)lo);
+}
+
+__device__ __forceinline__ float f64_to_f32_rn(double d) {
+  const unsigned hi = (unsigned)__double2hiint(d);
+  const unsigned lo = (unsigned)__double2loint(d);
+  const unsigned sign = hi & 0x80000000u;
+  const int e = (int)((hi >> 20) & 0x7FFu);
+  const int e32 = e - 1023 + 127;
+  if (e32 <= 0 || e32 >= 255) {
+    if ((hi & 0x7FFFFFFFu) == 0u && lo == 0u) return __uint_as_float(sign);
+    return __double2float_rn(d);  // FP32 subnormal, overflow, inf, nan
+  }
+  const unsigned m = ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+  const unsigned rem = lo & 0x1FFFFFFFu;
+  unsigned r = sign | ((unsigned)e32 << 23) | m;
+  // round to nearest, ties to even; a carry out of the mantissa correctly
+  // increments the exponent (and reaches infinity at the top of the range)
+  if (rem > 0x10000000u || (rem == 0x10000000u && (m & 1u))) r += 1u;
+  return __uint_as_float(r);
+}
+
+}  // namespace dccm

@@ -30,6 +30,7 @@
 // issuing work, and still frees its TMEM.
 #include <cuda_bf16.h>
 
+#include "fp_conv.cuh"
 #include "sht_plan.cuh"
 
 namespace dccm {
@@ -53,6 +54,8 @@ struct MInfo {
 struct TcArgs {
   int dir;  // 0 inverse, 1 forward
   int N, Jh, batch, nct;
+  int ntmax;  // TMEM columns per accumulator (64 or 128)
+  int nacc;   // accumulator sets in TMEM (2: double buffered, 1)
   long long ncoef;
   int items_per_ct;
   const MInfo *mi;
@@ -169,12 +172,22 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// FP64 split used once per table entry at plan creation.
 __device__ __forceinline__ void split3(double x, __nv_bfloat16 &h, __nv_bfloat16 &m, __nv_bfloat16 &l) {
   h = __double2bfloat16(x);
   double r = x - (double)__bfloat162float(h);
   m = __double2bfloat16(r);
   r = r - (double)__bfloat162float(m);
   l = __double2bfloat16(r);
+}
+
+// Exact split of an FP32 value into three BF16 numbers (FP32 arithmetic:
+// each residual is exact because it has fewer significant bits than FP32).
+__device__ __forceinline__ void split3f(float x, __nv_bfloat16 &h, __nv_bfloat16 &m, __nv_bfloat16 &l) {
+  h = __float2bfloat16_rn(x);
+  const float r1 = x - __bfloat162float(h);
+  m = __float2bfloat16_rn(r1);
+  l = __float2bfloat16_rn(r1 - __bfloat162float(m));
 }
 
 // Work item decode: items ordered (ct, m, nt), heavy (small m) first within ct.
@@ -263,16 +276,16 @@ legendre_tc_kernel(const __grid_constant__ CUtensorMap tmap, TcArgs a) {
 #pragma unroll
             for (int e = 0; e < 8; ++e) {
               const int k = k0 + e;
-              double x = 0.0;
+              float x = 0.f;
               if (c < C2B && k < kv) {
                 if (a.dir == 0) {
                   const int n = m + p + 2 * k;
-                  x = a.spec_in[((long long)(c >> 1) * a.ncoef + idx_mn(a.N, m, n)) * 2 + (c & 1)];
+                  x = f64_to_f32_rn(a.spec_in[((long long)(c >> 1) * a.ncoef + idx_mn(a.N, m, n)) * 2 + (c & 1)]);
                 } else {
-                  x = (double)a.G[(((long long)m * 2 + p) * a.Jh + k) * C2B + c];
+                  x = a.G[(((long long)m * 2 + p) * a.Jh + k) * C2B + c];
                 }
               }
-              split3(x, h[e], md[e], lo[e]);
+              split3f(x, h[e], md[e], lo[e]);
             }
             const uint32_t off = (t >> 3) * 1024 + (t & 7) * 128 + ((g8 ^ (t & 7)) << 4);
             *reinterpret_cast<uint4 *>(As + off) = *reinterpret_cast<const uint4 *>(h);
@@ -295,14 +308,18 @@ legendre_tc_kernel(const __grid_constant__ CUtensorMap tmap, TcArgs a) {
         const MInfo mi = a.mi[m];
         const int nrow = min(128, mi.nr - nt * 128);
         const uint32_t idesc = idesc_bf16(nrow);
-        const int ab = li & 1;
-        if (!mbar_wait(&acce[ab], ((li >> 1) & 1) ^ 1, a.err, abort_flag, 2)) { ok = false; break; }
+        const int ab = a.nacc == 2 ? (li & 1) : 0;
+        const int ar = a.nacc == 2 ? (li >> 1) : li;  // use count of this accumulator set
+        if (!mbar_wait(&acce[ab], (ar & 1) ^ 1, a.err, abort_flag, 2)) { ok = false; break; }
         tc_fence_after();
         for (int p = 0; p < 2 && ok; ++p) {
           const int kv = p ? mi.kv1 : mi.kv0;
           const int nq = (kv + 63) / 64;
-          const uint32_t dt = tmem + ab * 256 + p * 128;
-          int acc = 0;
+          // hi*hi accumulates apart from the five cross products, so the small
+          // terms do not lose their low bits in an accumulator 2^8 larger.
+          const uint32_t dmain = tmem + ab * 4 * a.ntmax + (p * 2) * a.ntmax;
+          const uint32_t dcross = dmain + a.ntmax;
+          int accm = 0, accx = 0;
           for (int q = 0; q < nq; ++q, ++g) {
             const int s = g % NSTAGE;
             if (!mbar_wait(&full[s], (g / NSTAGE) & 1, a.err, abort_flag, 3)) { ok = false; break; }
@@ -312,14 +329,16 @@ legendre_tc_kernel(const __grid_constant__ CUtensorMap tmap, TcArgs a) {
             const int ksteps = min(4, (kv - q * 64 + 15) / 16);
             for (int ks = 0; ks < ksteps; ++ks) {
               const uint32_t ko = ks * 32;
-              // (A split, B split): hi*hi, hi*mid, mid*hi, hi*lo, lo*hi, mid*mid
-              const int pa[6] = {0, 0, 1, 0, 2, 1};
-              const int pb[6] = {0, 1, 0, 2, 0, 1};
+              mma_bf16(dmain, smem_desc(As + ko), smem_desc(Bs + ko), idesc, accm);
+              accm = 1;
+              // (A split, B split): hi*mid, mid*hi, hi*lo, lo*hi, mid*mid
+              const int pa[5] = {0, 1, 0, 2, 1};
+              const int pb[5] = {1, 0, 2, 0, 1};
 #pragma unroll
-              for (int u = 0; u < 6; ++u) {
-                mma_bf16(dt, smem_desc(As + pa[u] * A_SPLIT_BYTES + ko),
-                         smem_desc(Bs + pb[u] * B_SPLIT_BYTES + ko), idesc, acc);
-                acc = 1;
+              for (int u = 0; u < 5; ++u) {
+                mma_bf16(dcross, smem_desc(As + pa[u] * A_SPLIT_BYTES + ko),
+                         smem_desc(Bs + pb[u] * B_SPLIT_BYTES + ko), idesc, accx);
+                accx = 1;
               }
             }
             mma_commit(&empty[s]);
@@ -339,21 +358,31 @@ legendre_tc_kernel(const __grid_constant__ CUtensorMap tmap, TcArgs a) {
       decode(a, it, m, ct, nt);
       const MInfo mi = a.mi[m];
       const int nrow = min(128, mi.nr - nt * 128);
-      const int ab = li & 1;
-      if (!mbar_wait(&accf[ab], (li >> 1) & 1, a.err, abort_flag, 4)) break;
+      const int ab = a.nacc == 2 ? (li & 1) : 0;
+      const int ar = a.nacc == 2 ? (li >> 1) : li;
+      if (!mbar_wait(&accf[ab], ar & 1, a.err, abort_flag, 4)) break;
       tc_fence_after();
       const int c = ct * 128 + row;
-      const uint32_t tbase = tmem + ((uint32_t)(quad * 32) << 16) + ab * 256;
+      const int NT = a.ntmax;
+      const uint32_t tbase = tmem + ((uint32_t)(quad * 32) << 16) + ab * 4 * NT;
       if (a.dir == 0) {
         const int J = 2 * a.Jh;
         const bool odd = mi.kv1 > 0;
         for (int j0 = 0; j0 < nrow; j0 += 16) {
-          float e[16], o[16];
+          float e[16], o[16], x[16];
           tmem_ld16(tbase + j0, e);
-          if (odd) tmem_ld16(tbase + 128 + j0, o);
-          else
+          tmem_ld16(tbase + NT + j0, x);
+#pragma unroll
+          for (int i = 0; i < 16; ++i) e[i] += x[i];
+          if (odd) {
+            tmem_ld16(tbase + 2 * NT + j0, o);
+            tmem_ld16(tbase + 3 * NT + j0, x);
+#pragma unroll
+            for (int i = 0; i < 16; ++i) o[i] += x[i];
+          } else {
 #pragma unroll
             for (int i = 0; i < 16; ++i) o[i] = 0.f;
+          }
           if (c < C2B) {
 #pragma unroll
             for (int i = 0; i < 16; ++i) {
@@ -370,15 +399,16 @@ legendre_tc_kernel(const __grid_constant__ CUtensorMap tmap, TcArgs a) {
           const int nv = p ? mi.nv1 : mi.nv0;
           for (int k0 = 0; k0 < nrow; k0 += 16) {
             if (nt * 128 + k0 >= nv) break;  // uniform across the warp
-            float d[16];
-            tmem_ld16(tbase + p * 128 + k0, d);
+            float d[16], x[16];
+            tmem_ld16(tbase + (p * 2) * NT + k0, d);
+            tmem_ld16(tbase + (p * 2 + 1) * NT + k0, x);
             if (c < C2B) {
 #pragma unroll
               for (int i = 0; i < 16; ++i) {
                 const int k = nt * 128 + k0 + i;
                 if (k < nv) {
                   const int n = m + p + 2 * k;
-                  const double v = (m == 0 && (c & 1)) ? 0.0 : (double)d[i];
+                  const double v = (m == 0 && (c & 1)) ? 0.0 : f32_to_f64(d[i] + x[i]);
                   a.spec_out[((long long)(c >> 1) * a.ncoef + idx_mn(a.N, m, n)) * 2 + (c & 1)] = v;
                 }
               }
@@ -550,6 +580,9 @@ static int build_one(Plan &P, int dir, TileTable &T) {
   T.d_mi = dmi;
   T.d_pre = dpre;
   T.items_per_ct = meta.pre[P.N + 1];
+  int nrmax = 16;
+  for (const MInfo &M : meta.mi) nrmax = M.nr > nrmax ? M.nr : nrmax;
+  T.ntmax = nrmax <= 64 ? 64 : 128;
   return DCCM_OK;
 }
 
@@ -576,6 +609,8 @@ static int launch_tc(Plan &P, TileTable &T, TcArgs &a, cudaStream_t s) {
   a.mi = (const MInfo *)T.d_mi;
   a.pre = T.d_pre;
   a.err = P.d_err;
+  a.ntmax = T.ntmax;
+  a.nacc = 8 * T.ntmax <= TMEM_COLS ? 2 : 1;
   const int items = a.nct * a.items_per_ct;
   if (items <= 0) return DCCM_OK;
   const int grid = items < sm_count() ? items : sm_count();

@@ -48,6 +48,7 @@ struct TileTable {
   void *d_mi = nullptr;       // per-m tile metadata (device)
   int *d_pre = nullptr;       // prefix of N-tiles over m (device)
   int items_per_ct = 0;       // work items per 128-column block of the batch
+  int ntmax = 64;             // TMEM columns per accumulator (N tile bound)
 };
 
 struct Plan {
