@@ -88,6 +88,8 @@ _SIGS = {
                                             ctypes.c_int64, ctypes.c_int, ctypes.c_void_p]),
     "dccm_area_integral_dev": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
                                               ctypes.c_void_p, ctypes.c_void_p]),
+    "dccm_area_integral_noalloc_dev": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+                                                      ctypes.c_void_p, ctypes.c_void_p]),
     "dccm_sht_plan_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                             ctypes.c_int, ctypes.c_void_p]),
     "dccm_sht_plan_destroy": (ctypes.c_int, [ctypes.c_void_p]),

@@ -177,6 +177,21 @@ int dccm_remap_apply_dev(dccm_remap_plan *plan, const double *src, int64_t ld_sr
 int dccm_area_integral_dev(const double *f, const double *area, int64_t n,
                            double *result, void *stream);
 
+/* The same compensated integral without allocating any device memory.
+ * No counterpart in the reference: this is for callers that cannot call
+ * cudaMalloc (a model that has already reserved the whole GPU for its own
+ * allocator, code that must not synchronise the device, code running while
+ * a stream is captured into a graph).  Its scratch is a fixed 256 KB array
+ * in the library's device image, held by every GPU that loads the library
+ * until the process exits.  Limit: n <= 67,108,864 (2^26) elements, else
+ * DCCM_ERR_SHAPE.  All calls share that array, so calls that overlap on the
+ * GPU race; serialise them.  The first call on each device looks up the
+ * array's device address (with that device current) and should be made
+ * before any stream capture.  Synchronises the stream and writes *result
+ * (host). */
+int dccm_area_integral_noalloc_dev(const double *f, const double *area, int64_t n,
+                                   double *result, void *stream);
+
 /* =====================================================================
  * Spherical-harmonic transforms on the Gaussian grid
  * Replace the SPML transforms that the atmosphere dynamics call through
