@@ -103,6 +103,16 @@ _SIGS = {
     "dccm_sht_inverse": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
     "dccm_sht_forward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
     "dccm_sht_status": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "dccm_sht_ensemble_create": (ctypes.c_int, [ctypes.c_int] + [ctypes.c_void_p] * 4 + [ctypes.c_int,
+                                                                                     ctypes.c_void_p]),
+    "dccm_sht_ensemble_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "dccm_sht_ensemble_inverse_dev": (ctypes.c_int, [ctypes.c_void_p] * 5),
+    "dccm_sht_ensemble_forward_dev": (ctypes.c_int, [ctypes.c_void_p] * 5),
+    "dccm_sht_ensemble_status": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "dccm_sht_ensemble_groups": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "dccm_step_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p]),
+    "dccm_tune_set": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int]),
+    "dccm_tune_get": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_void_p]),
     "dccm_step_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "dccm_step_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "dccm_step_run": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
@@ -112,11 +122,18 @@ _SIGS = {
 }
 
 
+class StepRemap(ctypes.Structure):
+    _fields_ = [("plan", ctypes.c_void_p), ("nfields", ctypes.c_int), ("src", ctypes.c_void_p),
+                ("ld_src", ctypes.c_int64), ("dst", ctypes.c_void_p), ("ld_dst", ctypes.c_int64),
+                ("nsub", ctypes.c_int), ("ld_dst2", ctypes.c_int64)]
+
+
 class StepDesc(ctypes.Structure):
     _fields_ = [("sht", ctypes.c_void_p), ("nfl", ctypes.c_int), ("spec_in", ctypes.c_void_p),
-                ("grid", ctypes.c_void_p), ("spec_out", ctypes.c_void_p), ("remap", ctypes.c_void_p),
-                ("nfields", ctypes.c_int), ("remap_src", ctypes.c_void_p), ("ld_src", ctypes.c_int64),
-                ("remap_dst", ctypes.c_void_p), ("ld_dst", ctypes.c_int64), ("flux", ctypes.c_void_p),
+                ("grid", ctypes.c_void_p), ("spec_out", ctypes.c_void_p), ("ens", ctypes.c_void_p),
+                ("ens_spec_in", ctypes.c_void_p), ("ens_grid", ctypes.c_void_p),
+                ("ens_spec_out", ctypes.c_void_p), ("ens_nfl", ctypes.c_void_p),
+                ("nremap", ctypes.c_int), ("remaps", ctypes.c_void_p), ("flux", ctypes.c_void_p),
                 ("flux_grid", ctypes.c_void_p)]
 
 
@@ -368,25 +385,75 @@ class ShtPlan:
             self.h = None
 
 
+class Ensemble:
+    """Truncation groups of an ensemble (dccm_sht_ensemble_create): one
+    persistent Legendre launch and one FFT launch per direction on the
+    mixed path.  groups: list of (nmax, imax, jmax, max_batch)."""
+
+    def __init__(self, groups, precision=SHT_MIXED):
+        L = load()
+        ng = len(groups)
+        arr = [(ctypes.c_int * ng)(*[int(g[k]) for g in groups]) for k in range(4)]
+        self.groups = list(groups)
+        self.h = ctypes.c_void_p()
+        _check(L.dccm_sht_ensemble_create(ng, *arr, precision, ctypes.byref(self.h)), "dccm_sht_ensemble_create")
+
+    def _call(self, fn, a, b, batch, stream):
+        ng = len(self.groups)
+        pa = (ctypes.c_void_p * ng)(*[_p(x).value for x in a])
+        pb = (ctypes.c_void_p * ng)(*[_p(x).value for x in b])
+        nb = (ctypes.c_int * ng)(*[int(x) for x in batch])
+        _check(fn(self.h, pa, pb, nb, _stream(stream)), fn.__name__)
+
+    def inverse_dev(self, spec, grid, batch, stream=None):
+        self._call(load().dccm_sht_ensemble_inverse_dev, spec, grid, batch, stream)
+
+    def forward_dev(self, grid, spec, batch, stream=None):
+        self._call(load().dccm_sht_ensemble_forward_dev, grid, spec, batch, stream)
+
+    def status(self):
+        e = ctypes.c_int(0)
+        st = load().dccm_sht_ensemble_status(self.h, ctypes.byref(e))
+        return st, e.value
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.dccm_sht_ensemble_destroy(self.h)
+            self.h = None
+
+
 # ----------------------------------------------------------- coupling step
 class Step:
     """One coupling step as a CUDA graph (dccm_step_create).  Buffers are
     device tensors that must outlive the step; flux is a dict of device
     tensors keyed like DSFCM_Util_SfcBulkFlux_Get's arguments."""
 
-    def __init__(self, sht=None, nfl=0, spec_in=None, grid=None, spec_out=None, remap=None, nfields=0,
-                 remap_src=None, ld_src=0, remap_dst=None, ld_dst=0, flux=None, flux_grid=None):
+    def __init__(self, sht=None, nfl=0, spec_in=None, grid=None, spec_out=None, remaps=(), flux=None,
+                 flux_grid=None, ensemble=None, ens_spec_in=None, ens_grid=None, ens_spec_out=None, ens_nfl=None):
+        """remaps: sequence of (RemapPlan, nfields, src, ld_src, dst, ld_dst[, nsub, ld_dst2])."""
         L = load()
         d = StepDesc()
         d.sht = sht.h.value if sht is not None else None
         d.nfl = int(nfl)
         d.spec_in, d.grid, d.spec_out = (_p(x).value if x is not None else None for x in (spec_in, grid, spec_out))
-        d.remap = remap.h.value if remap is not None else None
-        d.nfields = int(nfields)
-        d.remap_src = _p(remap_src).value if remap_src is not None else None
-        d.remap_dst = _p(remap_dst).value if remap_dst is not None else None
-        d.ld_src, d.ld_dst = int(ld_src), int(ld_dst)
-        self._keep = [sht, remap, spec_in, grid, spec_out, remap_src, remap_dst, flux]
+        self._keep = [sht, spec_in, grid, spec_out, flux, remaps, ensemble, ens_spec_in, ens_grid, ens_spec_out]
+        if ensemble is not None:
+            ng = len(ens_nfl)
+            self._ens = [(ctypes.c_void_p * ng)(*[_p(x).value for x in arrs])
+                         for arrs in (ens_spec_in, ens_grid, ens_spec_out)]
+            self._ens_nfl = (ctypes.c_int * ng)(*[int(x) for x in ens_nfl])
+            d.ens = ensemble.h.value
+            d.ens_spec_in, d.ens_grid, d.ens_spec_out = (ctypes.addressof(a) for a in self._ens)
+            d.ens_nfl = ctypes.addressof(self._ens_nfl)
+        nr = len(remaps)
+        self._remaps = (StepRemap * max(1, nr))()
+        for k, rm in enumerate(remaps):
+            plan, nf, src, lds, dst, ldd = rm[:6]
+            nsub, ld2 = (rm[6], rm[7]) if len(rm) > 6 else (0, 0)
+            self._remaps[k] = StepRemap(plan.h.value, int(nf), _p(src).value, int(lds), _p(dst).value, int(ldd),
+                                        int(nsub), int(ld2))
+        d.nremap = nr
+        d.remaps = ctypes.addressof(self._remaps)
         if flux is not None:
             fa = FluxArgs()
             self._sig = np.ascontiguousarray(np.asarray(flux["a_Sig1Info"], np.float64))
@@ -402,8 +469,19 @@ class Step:
     def run(self, stream=None):
         _check(load().dccm_step_run(self.h, _stream(stream)), "dccm_step_run")
 
+    STAGES = ["legendre_inverse", "fft_inverse", "fft_forward", "legendre_forward", "remap", "bulk_flux"]
+    KNOBS = ["tc_ctas", "fft_bb", "flux_threads", "remap_threads"]
+
+    def autotune(self, cache_path=None):
+        """dccm_step_autotune: choose launch shapes, re-record the graph."""
+        out = (ctypes.c_int * 4)()
+        _check(load().dccm_step_autotune(self.h, cache_path.encode() if cache_path else None, out),
+               "dccm_step_autotune")
+        return dict(zip(self.KNOBS, list(out)))
+
     def run_timed(self, stream=None):
-        ms = (ctypes.c_float * 4)()
+        """Device ms of the six stages (names in Step.STAGES), run back to back."""
+        ms = (ctypes.c_float * 6)()
         _check(load().dccm_step_run_timed(self.h, _stream(stream), ms), "dccm_step_run_timed")
         return list(ms)
 

@@ -35,6 +35,17 @@ inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s
 // Number of SMs of the current device (cached per device).
 int sm_count();
 
+// Launch-shape knobs read by the kernel launchers (0 = the launcher's own
+// default).  dccm_step_autotune chooses them per step by timing candidates;
+// dccm_tune_set / dccm_tune_get expose them.
+struct Tunables {
+  int tc_ctas = 0;        // persistent CTAs of the tensor-core Legendre kernel
+  int fft_bb = 0;         // field-levels (warps) per FFT CTA
+  int flux_threads = 0;   // threads per CTA of the bulk-flux kernel
+  int remap_threads = 0;  // threads per CTA of the remap kernel
+};
+Tunables &tunables();
+
 // Device buffer that grows on demand (never shrinks); used for the host
 // entry points' staging copies.
 struct DevBuf {

@@ -1,21 +1,31 @@
-// Longitude FFT of the spherical-harmonic transform (FP32 for the mixed
-// path, FP64 for the plain path).
+// Longitude FFT of the spherical-harmonic transform, FP32 (mixed path), one
+// warp per pair of latitude rows.  The plain FP64 path has its own
+// transform in fft_f64.cu.
 //
 // Two real latitude rows that mirror each other about the equator (jn, js)
-// travel through one complex FFT of length I: z = g(jn) + i g(js).  One warp
-// owns one field-level's pair of rows and runs a self-sorting Stockham FFT
-// (radix 4, 3 and 2 stages; I = 64, 128, 192, 256, 512, 1024, ...) in its own
-// two shared-memory buffers, synchronising with __syncwarp only.  Twiddles
-// come from a table e^{-2 pi i t / I} evaluated in FP64 on the host.
+// travel through one complex FFT of length I = 32 R: z = g(jn) + i g(js).
+// Lane l holds the R samples z[32 r + l] in registers, and the transform is
+// the four-step factorisation I = R x 32:
+//   forward  (1) length-R DFT over r in registers,
+//            (2) twiddle e^{-2 pi i l k1 / I},
+//            (3) length-32 radix-2 decimation-in-frequency across the lanes
+//                with __shfl_xor; lane l ends with Z[k1 + R brev5(l)];
+//   inverse  the same steps mirrored (decimation in time across lanes from
+//            bit-reversed input, conjugate twiddles, register DFT last), so
+//            lane l ends with z[32 r + l] and the row stores are coalesced.
+// Rows are read and written straight from/to global memory (lanes along
+// longitude); shared memory only stages the Fourier coefficients of the
+// CTA's block of field-levels (coalesced along c) and, in the forward
+// direction, the spectrum for separating the two real rows.  Twiddles come
+// from a table e^{-2 pi i t / I} evaluated in FP64 on the host.  Supported
+// lengths: R in {2, 3, 4, 6, 8, 12, 16, 24, 32}, i.e. I = 64 ... 1024.
 //
-// Inverse: the CTA stages the Fourier coefficients m = 0..N of its block of
-// field-levels for rows jn and js (coalesced along c), each warp assembles
-// the Hermitian spectrum of both rows into one complex array and transforms
-// it; Re and Im of the result are the two grid rows.
-// Forward: each warp loads its two rows, transforms, separates the two real
-// spectra (A_m = (Z_m + conj Z_{I-m})/2, B_m = (Z_m - conj Z_{I-m})/(2i)),
-// folds them into E = (A + B)/I and O = (A - B)/I, stages them, and the CTA
-// writes G[m][p][jj][c] coalesced along c.
+// Inverse: Z_m = A_m + i B_m and Z_{I-m} = conj(A_m) + i conj(B_m) from the
+// Fourier coefficients A (row jn) and B (row js); Re z and Im z are the rows.
+// Forward: A_m = (Z_m + conj Z_{I-m})/2, B_m = (Z_m - conj Z_{I-m})/(2i),
+// folded into E = (A + B)/I and O = (A - B)/I and written as G[m][p][jj][c].
+#include <string.h>
+
 #include "fp_conv.cuh"
 #include "sht_plan.cuh"
 
@@ -46,97 +56,123 @@ template <typename C> __device__ __forceinline__ C cmul(C a, C b) {
   r.y = a.x * b.y + a.y * b.x;
   return r;
 }
-// multiply by i*s (s = +1 or -1)
-template <typename C> __device__ __forceinline__ C cmuli(C a, int s) {
-  C r;
-  r.x = -a.y * s;
-  r.y = a.x * s;
-  return r;
+// twiddle tw[t] = e^{-2 pi i t / I}; sign +1 uses its conjugate
+template <typename C> __device__ __forceinline__ C twid(const C *tw, int t, int sign) {
+  C w = tw[t];
+  if (sign > 0) w.y = -w.y;
+  return w;
 }
+template <typename C> __device__ __forceinline__ C shfl_xor_c(C v, int m) {
+  v.x = __shfl_xor_sync(0xffffffffu, v.x, m);
+  v.y = __shfl_xor_sync(0xffffffffu, v.y, m);
+  return v;
+}
+__device__ __forceinline__ int brev5(int l) { return (int)(__brev((unsigned)l) >> 27); }
 
-struct FftArgs {
-  int I, nst;
-  int radix[MAX_STAGES];
-};
-
-// Stockham autosort FFT of one complex row by one warp.  sign = -1 forward,
-// +1 inverse (unnormalised).  Returns the buffer holding the result.
-template <typename C>
-__device__ C *warp_fft(C *x, C *y, const C *__restrict__ tw, const FftArgs &a, int sign, int lane) {
-  const int I = a.I;
-  int Ns = 1;
-  for (int st = 0; st < a.nst; ++st) {
-    const int R = a.radix[st];
-    const int nb = I / R;
-    const int tstep = I / (Ns * R);
-    for (int j = lane; j < nb; j += 32) {
-      const int k = j % Ns;
-      const int base = (j / Ns) * Ns * R + k;
-      C v[4];
+// In-register DFT of length R: v[k] <- sum_r v[r] e^{sign 2 pi i r k / R}.
+// Even lengths split into two halves (decimation in time), 3 is direct.
+template <int R> struct RegDft {
+  template <typename C> __device__ __forceinline__ static void run(C *v, const C *tw, int I, int sign) {
+    if constexpr (R == 1) {
+      return;
+    } else if constexpr (R == 2) {
+      const C a = v[0], b = v[1];
+      v[0] = cadd(a, b);
+      v[1] = csub(a, b);
+    } else if constexpr (R == 3) {
+      using S = decltype(v[0].x);
+      const C t1 = cadd(v[1], v[2]);
+      const C d = csub(v[1], v[2]);
+      const S h = (S)0.86602540378443864676 * (S)sign;  // sign * sqrt(3)/2
+      C mm, q;
+      mm.x = v[0].x - (S)0.5 * t1.x;
+      mm.y = v[0].y - (S)0.5 * t1.y;
+      q.x = -d.y * h;  // i * sign * sqrt(3)/2 * d
+      q.y = d.x * h;
+      v[0] = cadd(v[0], t1);
+      v[1] = cadd(mm, q);
+      v[2] = csub(mm, q);
+    } else {
+      static_assert(R % 2 == 0, "length");
+      constexpr int H = R / 2;
+      C e[H], o[H];
 #pragma unroll
-      for (int r = 0; r < 4; ++r)
-        if (r < R) {
-          C t = x[j + r * nb];
-          if (r > 0 && k > 0) {
-            C w = tw[k * r * tstep];
-            if (sign > 0) w.y = -w.y;
-            t = cmul(t, w);
-          }
-          v[r] = t;
-        }
-      if (R == 4) {
-        const C s0 = cadd(v[0], v[2]), d0 = csub(v[0], v[2]);
-        const C s1 = cadd(v[1], v[3]), d1 = cmuli(csub(v[1], v[3]), sign);
-        y[base] = cadd(s0, s1);
-        y[base + Ns] = cadd(d0, d1);
-        y[base + 2 * Ns] = csub(s0, s1);
-        y[base + 3 * Ns] = csub(d0, d1);
-      } else if (R == 2) {
-        y[base] = cadd(v[0], v[1]);
-        y[base + Ns] = csub(v[0], v[1]);
-      } else {  // R == 3
-        const C t1 = cadd(v[1], v[2]);
-        const C t2 = cmuli(csub(v[1], v[2]), sign);
-        using R_ = decltype(t1.x);
-        const R_ h = (R_)0.86602540378443864676;  // sqrt(3)/2
-        C m;
-        m.x = v[0].x - (R_)0.5 * t1.x;
-        m.y = v[0].y - (R_)0.5 * t1.y;
-        C q;
-        q.x = t2.x * h;
-        q.y = t2.y * h;
-        y[base] = cadd(v[0], t1);
-        y[base + Ns] = cadd(m, q);
-        y[base + 2 * Ns] = csub(m, q);
+      for (int i = 0; i < H; ++i) {
+        e[i] = v[2 * i];
+        o[i] = v[2 * i + 1];
+      }
+      RegDft<H>::run(e, tw, I, sign);
+      RegDft<H>::run(o, tw, I, sign);
+#pragma unroll
+      for (int k = 0; k < H; ++k) {
+        const C t = k == 0 ? o[0] : cmul(o[k], twid(tw, k * (I / R), sign));
+        v[k] = cadd(e[k], t);
+        v[k + H] = csub(e[k], t);
       }
     }
-    __syncwarp();
-    C *t = x;
-    x = y;
-    y = t;
-    Ns *= R;
   }
-  return x;
+};
+
+// Forward complex FFT of one row held as v[r] = z[32 r + lane];
+// on return v[k1] = Z[k1 + R brev5(lane)].
+template <int R, typename C>
+__device__ __forceinline__ void warp_fft_fwd(C (&v)[R], const C *tw, int lane) {
+  constexpr int I = 32 * R;
+  RegDft<R>::run(v, tw, I, -1);
+#pragma unroll
+  for (int k = 1; k < R; ++k)
+    if (lane) v[k] = cmul(v[k], twid(tw, lane * k, -1));
+#pragma unroll
+  for (int h = 16; h >= 1; h >>= 1) {
+    const bool upper = lane & h;
+    const C w = twid(tw, (lane & (h - 1)) * (I / (2 * h)), -1);
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+      const C p = shfl_xor_c(v[k], h);
+      v[k] = upper ? cmul(csub(p, v[k]), w) : cadd(v[k], p);
+    }
+  }
+}
+
+// Inverse (unnormalised) FFT of one row held as v[k1] = Z[k1 + R brev5(lane)];
+// on return v[r] = z[32 r + lane].
+template <int R, typename C>
+__device__ __forceinline__ void warp_fft_inv(C (&v)[R], const C *tw, int lane) {
+  constexpr int I = 32 * R;
+#pragma unroll
+  for (int h = 1; h <= 16; h <<= 1) {
+    const bool upper = lane & h;
+    const C w = twid(tw, (lane & (h - 1)) * (I / (2 * h)), +1);
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+      const C p = shfl_xor_c(v[k], h);
+      // top = a + w b, bottom = a - w b, with a the lower lane's value
+      v[k] = upper ? csub(p, cmul(v[k], w)) : cadd(v[k], cmul(p, w));
+    }
+  }
+#pragma unroll
+  for (int k = 1; k < R; ++k)
+    if (lane) v[k] = cmul(v[k], twid(tw, lane * k, +1));
+  RegDft<R>::run(v, tw, I, +1);
 }
 
 // ------------------------------------------------------------- inverse
-template <typename T>
-__global__ void __launch_bounds__(512)
-fft_inverse_kernel(FftArgs a, int N, int J, int batch, int BB, const T *__restrict__ F,
-                   double *__restrict__ grid, const typename Cx<T>::t *__restrict__ twg) {
+// One CTA: latitude pair jj, field-levels [by*BB, by*BB + BB).
+template <typename T, int R>
+__device__ __forceinline__ void fft_inv_block(int N, int J, int batch, int BB, const T *__restrict__ F,
+                                              double *__restrict__ grid, const typename Cx<T>::t *__restrict__ twg,
+                                              int jj, int by, unsigned char *smem_raw) {
   using C = typename Cx<T>::t;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int I = a.I, Jh = J / 2;
-  const int jj = blockIdx.x;
+  constexpr int I = 32 * R;
+  const int Jh = J / 2;
   const int jn = Jh + jj, js = Jh - 1 - jj;
-  const int b0 = blockIdx.y * BB;
+  const int b0 = by * BB;
   const int nb = min(BB, batch - b0);
   const int64_t C2B = 2LL * batch;
   const int cw = 2 * BB;
-  T *stA = reinterpret_cast<T *>(smem_raw);      // [N+1][2BB] row jn
-  T *stB = stA + (size_t)(N + 1) * cw;           // [N+1][2BB] row js
-  C *tw = reinterpret_cast<C *>(stB + (size_t)(N + 1) * cw);
-  C *bufs = tw + I;
+  C *tw = reinterpret_cast<C *>(smem_raw);
+  T *stA = reinterpret_cast<T *>(tw + I);  // [N+1][2BB] row jn
+  T *stB = stA + (size_t)(N + 1) * cw;     // [N+1][2BB] row js
   for (int t = threadIdx.x; t < I; t += blockDim.x) tw[t] = twg[t];
   for (int t = threadIdx.x; t < (N + 1) * cw; t += blockDim.x) {
     const int m = t / cw, c = t % cw;
@@ -151,73 +187,75 @@ fft_inverse_kernel(FftArgs a, int N, int J, int batch, int BB, const T *__restri
   __syncthreads();
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
   const int nw = blockDim.x / 32;
-  C *x = bufs + (size_t)warp * 2 * I;
-  C *y = x + I;
+  const int k2 = brev5(lane);
   for (int bl = warp; bl < nb; bl += nw) {
-    for (int k = lane; k < I; k += 32) x[k] = cmk<C>(0, 0);
-    __syncwarp();
-    for (int m = lane; m <= N; m += 32) {
-      const T ar = stA[m * cw + 2 * bl], ai = m ? stA[m * cw + 2 * bl + 1] : (T)0;
-      const T br = stB[m * cw + 2 * bl], bi = m ? stB[m * cw + 2 * bl + 1] : (T)0;
-      x[m] = cmk<C>(ar - bi, ai + br);
-      if (m > 0) x[I - m] = cmk<C>(ar + bi, br - ai);
+    C v[R];
+#pragma unroll
+    for (int k1 = 0; k1 < R; ++k1) {
+      const int k = k1 + R * k2;
+      C z = cmk<C>(0, 0);
+      if (k <= N) {
+        const T ar = stA[k * cw + 2 * bl], ai = k ? stA[k * cw + 2 * bl + 1] : (T)0;
+        const T br = stB[k * cw + 2 * bl], bi = k ? stB[k * cw + 2 * bl + 1] : (T)0;
+        z = cmk<C>(ar - bi, ai + br);
+      } else if (k >= I - N) {
+        const int m = I - k;
+        const T ar = stA[m * cw + 2 * bl], ai = stA[m * cw + 2 * bl + 1];
+        const T br = stB[m * cw + 2 * bl], bi = stB[m * cw + 2 * bl + 1];
+        z = cmk<C>(ar + bi, br - ai);
+      }
+      v[k1] = z;
     }
-    __syncwarp();
-    C *z = warp_fft<C>(x, y, tw, a, +1, lane);
+    warp_fft_inv<R>(v, tw, lane);
     double *gn = grid + ((int64_t)(b0 + bl) * J + jn) * I;
     double *gs = grid + ((int64_t)(b0 + bl) * J + js) * I;
-    for (int i = lane; i < I; i += 32) {
-      const C v = z[i];
-      gn[i] = to_f64(v.x);
-      gs[i] = to_f64(v.y);
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      gn[32 * r + lane] = to_f64(v[r].x);
+      gs[32 * r + lane] = to_f64(v[r].y);
     }
-    __syncwarp();
   }
 }
 
 // ------------------------------------------------------------- forward
-template <typename T>
-__global__ void __launch_bounds__(512)
-fft_forward_kernel(FftArgs a, int N, int J, int batch, int BB, const double *__restrict__ grid,
-                   T *__restrict__ G, const typename Cx<T>::t *__restrict__ twg) {
+template <typename T, int R>
+__device__ __forceinline__ void fft_fwd_block(int N, int J, int batch, int BB, const double *__restrict__ grid,
+                                              T *__restrict__ G, const typename Cx<T>::t *__restrict__ twg,
+                                              int jj, int by, unsigned char *smem_raw) {
   using C = typename Cx<T>::t;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int I = a.I, Jh = J / 2;
-  const int jj = blockIdx.x;
+  constexpr int I = 32 * R;
+  const int Jh = J / 2;
   const int jn = Jh + jj, js = Jh - 1 - jj;
-  const int b0 = blockIdx.y * BB;
+  const int b0 = by * BB;
   const int nb = min(BB, batch - b0);
   const int64_t C2B = 2LL * batch;
   const int cw = 2 * BB;
-  T *stE = reinterpret_cast<T *>(smem_raw);  // [N+1][2BB]
+  const int nw = blockDim.x / 32;
+  C *tw = reinterpret_cast<C *>(smem_raw);
+  C *zb = tw + I;                                        // [nw][I] spectra
+  T *stE = reinterpret_cast<T *>(zb + (size_t)nw * I);  // [N+1][2BB]
   T *stO = stE + (size_t)(N + 1) * cw;
-  C *tw = reinterpret_cast<C *>(stO + (size_t)(N + 1) * cw);
-  C *bufs = tw + I;
   for (int t = threadIdx.x; t < I; t += blockDim.x) tw[t] = twg[t];
-  for (int t = threadIdx.x; t < (N + 1) * cw; t += blockDim.x) {
-    stE[t] = 0;
-    stO[t] = 0;
-  }
   __syncthreads();
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-  const int nw = blockDim.x / 32;
-  C *x = bufs + (size_t)warp * 2 * I;
-  C *y = x + I;
-  const T invI = (T)(1.0 / (double)I);
+  C *Z = zb + (size_t)warp * I;
+  const int k2 = brev5(lane);
+  const T invI = (T)1 / (T)I;
   for (int bl = warp; bl < nb; bl += nw) {
     const double *gn = grid + ((int64_t)(b0 + bl) * J + jn) * I;
     const double *gs = grid + ((int64_t)(b0 + bl) * J + js) * I;
-    for (int i = lane; i < I; i += 32) {
-      C v;
-      v.x = from_f64(gn[i], T());
-      v.y = from_f64(gs[i], T());
-      x[i] = v;
+    C v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      v[r].x = from_f64(gn[32 * r + lane], T());
+      v[r].y = from_f64(gs[32 * r + lane], T());
     }
+    warp_fft_fwd<R>(v, tw, lane);
+#pragma unroll
+    for (int k1 = 0; k1 < R; ++k1) Z[k1 + R * k2] = v[k1];
     __syncwarp();
-    C *Z = warp_fft<C>(x, y, tw, a, -1, lane);
     for (int m = lane; m <= N; m += 32) {
       const C zm = Z[m], zc = Z[(I - m) % I];
-      // A = (Z_m + conj Z_{I-m})/2, B = (Z_m - conj Z_{I-m})/(2i)
       const T ar = (T)0.5 * (zm.x + zc.x), ai = (T)0.5 * (zm.y - zc.y);
       const T br = (T)0.5 * (zm.y + zc.y), bi = (T)-0.5 * (zm.x - zc.x);
       stE[m * cw + 2 * bl] = (ar + br) * invI;
@@ -237,68 +275,131 @@ fft_forward_kernel(FftArgs a, int N, int J, int batch, int BB, const double *__r
   }
 }
 
-template <typename T>
-static int pick_bb(const Plan &P, int batch, size_t *smem, int *threads) {
-  using C = typename Cx<T>::t;
-  const size_t budget = 160 * 1024;
-  int BB = 16;
-  for (; BB > 1; BB /= 2) {
-    const size_t st = (size_t)(P.N + 1) * 2 * BB * 2 * sizeof(T);
-    const size_t bu = (size_t)P.I * sizeof(C) * (1 + 2 * (size_t)BB);
-    if (st + bu <= budget) break;
+// ------------------------------------------------------------- kernels
+// Several truncation groups in one launch: CTA blockIdx.x belongs to the
+// group whose block range contains it; the group's length selects the
+// register FFT (cases up to RMAX are compiled in).
+constexpr int FFT_MAXG = 8;
+struct FftGroup {
+  int N, J, batch, BB, R, blk0;
+  const void *in;
+  void *out;
+  const void *tw;
+};
+struct FftLaunch {
+  FftGroup g[FFT_MAXG];
+  int ngroups;
+};
+
+template <typename T, int R, int RMAX, bool FWD>
+__device__ __forceinline__ void dispatch_case(const FftGroup &G, int jj, int by, unsigned char *sm) {
+  if constexpr (R <= RMAX) {
+    using C = typename Cx<T>::t;
+    if (FWD)
+      fft_fwd_block<T, R>(G.N, G.J, G.batch, G.BB, (const double *)G.in, (T *)G.out, (const C *)G.tw, jj, by, sm);
+    else
+      fft_inv_block<T, R>(G.N, G.J, G.batch, G.BB, (const T *)G.in, (double *)G.out, (const C *)G.tw, jj, by, sm);
   }
-  if (BB > batch) BB = batch < 1 ? 1 : batch;
-  *smem = (size_t)(P.N + 1) * 2 * BB * 2 * sizeof(T) + (size_t)P.I * sizeof(C) * (1 + 2 * (size_t)BB);
-  *threads = 32 * BB;
-  return BB;
 }
 
-static FftArgs fft_args(const Plan &P) {
-  FftArgs a;
-  a.I = P.fft.I;
-  a.nst = P.fft.nst;
-  for (int k = 0; k < MAX_STAGES; ++k) a.radix[k] = P.fft.radix[k];
-  return a;
+template <typename T, int RMAX, bool FWD>
+__global__ void __launch_bounds__(256) fft_multi_kernel(const __grid_constant__ FftLaunch L) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  int gi = 0;
+  while (gi + 1 < L.ngroups && (int)blockIdx.x >= L.g[gi + 1].blk0) ++gi;
+  const FftGroup &G = L.g[gi];
+  const int lb = blockIdx.x - G.blk0;
+  const int Jh = G.J / 2;
+  const int jj = lb % Jh, by = lb / Jh;
+  switch (G.R) {
+    case 2: dispatch_case<T, 2, RMAX, FWD>(G, jj, by, smem_raw); break;
+    case 3: dispatch_case<T, 3, RMAX, FWD>(G, jj, by, smem_raw); break;
+    case 4: dispatch_case<T, 4, RMAX, FWD>(G, jj, by, smem_raw); break;
+    case 6: dispatch_case<T, 6, RMAX, FWD>(G, jj, by, smem_raw); break;
+    case 8: dispatch_case<T, 8, RMAX, FWD>(G, jj, by, smem_raw); break;
+    case 12: dispatch_case<T, 12, RMAX, FWD>(G, jj, by, smem_raw); break;
+    case 16: dispatch_case<T, 16, RMAX, FWD>(G, jj, by, smem_raw); break;
+    case 24: dispatch_case<T, 24, RMAX, FWD>(G, jj, by, smem_raw); break;
+    case 32: dispatch_case<T, 32, RMAX, FWD>(G, jj, by, smem_raw); break;
+    default: break;
+  }
 }
 
-template <typename T>
-static int launch_inv(const Plan &P, int batch, const void *F, double *grid, cudaStream_t s) {
-  size_t smem;
-  int threads;
-  const int BB = pick_bb<T>(P, batch, &smem, &threads);
-  DCCM_CUDA(cudaFuncSetAttribute(fft_inverse_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem));
-  dim3 grd(P.Jh, (batch + BB - 1) / BB);
-  const void *tw = std::is_same<T, float>::value ? (const void *)P.d_tw32 : (const void *)P.d_tw64;
-  fft_inverse_kernel<T><<<grd, threads, smem, s>>>(fft_args(P), P.N, P.J, batch, BB, (const T *)F, grid,
-                                                   (const typename Cx<T>::t *)tw);
-  DCCM_LAUNCH_CHECK();
-  return DCCM_OK;
+// Field-levels per CTA (one warp each) that fit a shared-memory budget.
+static size_t fft_smem(int N, int I, int bb, bool fwd) {
+  size_t s = (size_t)I * sizeof(float2) + (size_t)(N + 1) * 2 * bb * 2 * sizeof(float);
+  if (fwd) s += (size_t)bb * I * sizeof(float2);
+  return s;
 }
 
-template <typename T>
-static int launch_fwd(const Plan &P, int batch, const double *grid, void *G, cudaStream_t s) {
-  size_t smem;
-  int threads;
-  const int BB = pick_bb<T>(P, batch, &smem, &threads);
-  DCCM_CUDA(cudaFuncSetAttribute(fft_forward_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem));
-  dim3 grd(P.Jh, (batch + BB - 1) / BB);
-  const void *tw = std::is_same<T, float>::value ? (const void *)P.d_tw32 : (const void *)P.d_tw64;
-  fft_forward_kernel<T><<<grd, threads, smem, s>>>(fft_args(P), P.N, P.J, batch, BB, grid, (T *)G,
-                                                   (const typename Cx<T>::t *)tw);
-  DCCM_LAUNCH_CHECK();
-  return DCCM_OK;
+// One launch over ngroups plans (FP32).  in/out per group as in the single case.
+int fft_multi(Plan *const *plans, const int *batch, const void *const *in, void *const *out, int ngroups, bool fwd,
+              cudaStream_t s) {
+  if (ngroups < 1 || ngroups > FFT_MAXG) return DCCM_ERR_UNSUPPORTED;
+  const size_t budget = 96 * 1024;
+  int BB = tunables().fft_bb > 0 && tunables().fft_bb <= 8 ? tunables().fft_bb : 8, rmax = 2;
+  for (int g = 0; g < ngroups; ++g) {
+    if (!fft_length_supported(plans[g]->I)) return DCCM_ERR_UNSUPPORTED;
+    rmax = plans[g]->I / 32 > rmax ? plans[g]->I / 32 : rmax;
+    while (BB > 1 && fft_smem(plans[g]->N, plans[g]->I, BB, fwd) > budget) BB /= 2;
+  }
+  FftLaunch L;
+  memset(&L, 0, sizeof L);
+  int nblk = 0, ng = 0;
+  size_t smem = 0;
+  for (int g = 0; g < ngroups; ++g) {
+    if (batch[g] <= 0) continue;
+    const Plan &P = *plans[g];
+    FftGroup &G = L.g[ng++];
+    G.N = P.N;
+    G.J = P.J;
+    G.batch = batch[g];
+    G.BB = BB;
+    G.R = P.I / 32;
+    G.blk0 = nblk;
+    G.in = in[g];
+    G.out = out[g];
+    G.tw = P.d_tw32;
+    nblk += P.Jh * ((batch[g] + BB - 1) / BB);
+    const size_t sm = fft_smem(P.N, P.I, BB, fwd);
+    smem = sm > smem ? sm : smem;
+  }
+  L.ngroups = ng;
+  if (nblk == 0) return DCCM_OK;
+  auto go = [&](auto kernel) -> int {
+    DCCM_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kernel<<<nblk, 32 * BB, smem, s>>>(L);
+    DCCM_LAUNCH_CHECK();
+    return DCCM_OK;
+  };
+  if (rmax <= 8) return fwd ? go(fft_multi_kernel<float, 8, true>) : go(fft_multi_kernel<float, 8, false>);
+  return fwd ? go(fft_multi_kernel<float, 32, true>) : go(fft_multi_kernel<float, 32, false>);
 }
 
+bool fft_length_supported(int I) {
+  if (I % 32 != 0) return false;
+  switch (I / 32) {
+    case 2: case 3: case 4: case 6: case 8: case 12: case 16: case 24: case 32: return true;
+    default: return false;
+  }
+}
+
+// The FP64 path uses the shared-memory Stockham transform (fft_f64.cu),
+// which needs fewer FP64 operations than the register/shuffle one.
 int fft_inverse(const Plan &P, int batch, bool fp32, const void *F, double *grid, cudaStream_t s) {
   if (batch <= 0) return DCCM_OK;
-  return fp32 ? launch_inv<float>(P, batch, F, grid, s) : launch_inv<double>(P, batch, F, grid, s);
+  if (!fp32) return fft_inverse_f64(P, batch, (const double *)F, grid, s);
+  Plan *pp = const_cast<Plan *>(&P);
+  void *out = grid;
+  return fft_multi(&pp, &batch, &F, &out, 1, false, s);
 }
 
 int fft_forward(const Plan &P, int batch, bool fp32, const double *grid, void *G, cudaStream_t s) {
   if (batch <= 0) return DCCM_OK;
-  return fp32 ? launch_fwd<float>(P, batch, grid, G, s) : launch_fwd<double>(P, batch, grid, G, s);
+  if (!fp32) return fft_forward_f64(P, batch, grid, (double *)G, s);
+  Plan *pp = const_cast<Plan *>(&P);
+  const void *in = grid;
+  return fft_multi(&pp, &batch, &in, &G, 1, true, s);
 }
 
 }  // namespace sht

@@ -76,7 +76,7 @@ __device__ __forceinline__ void bulk_coef_l82(double Ri, double z0m, double z0h,
   cq = fmax(fmin(th, QVapBulkCoefMax), QVapBulkCoefMin);
 }
 
-__global__ void __launch_bounds__(128) bulk_flux_column(Ptrs p, Geom g) {
+__global__ void __launch_bounds__(256) bulk_flux_column(Ptrs p, Geom g) {
   constexpr double GasRDry = GasRUniv / MolWtDry;
   constexpr double GasRWet = GasRUniv / MolWtWet;
   constexpr double EpsV = MolWtWet / MolWtDry;
@@ -109,10 +109,19 @@ __global__ void __launch_bounds__(128) bulk_flux_column(Ptrs p, Geom g) {
     double Frac[2], QSat[2], SVT[2], Tsn[2], Albn[2], rTs[2];
     Frac[0] = 1.0 - SIceCon;
     Frac[1] = SIceCon;
+    // Sea-ice flag (:269-273, :389-393): with no ice the reference still
+    // evaluates the ice column, but every ice output is then an exact zero
+    // (bulk coefficients clamp to 0); the ice physics is skipped here.  The
+    // results are the same for any positive finite ice temperature.
+    const bool ice = Frac[1] > 1e-12;
 #pragma unroll
     for (int n = 0; n < 2; ++n) {
       Tsn[n] = p.Ts[c + P * n];
       Albn[n] = p.Alb[c + P * n];
+      if (n == 1 && !ice) {
+        rTs[n] = QSat[n] = SVT[n] = 0.0;
+        continue;
+      }
       rTs[n] = 1.0 / Tsn[n];
       QSat[n] = (EpsV * Es0) * rPs * exp(aL[n] / GasRWet * (1.0 / 273.0 - rTs[n]));
       SVT[n] = Tsn[n] * (1.0 + (((1.0 / EpsV) - 1.0) * QSat[n]));
@@ -140,10 +149,15 @@ __global__ void __launch_bounds__(128) bulk_flux_column(Ptrs p, Geom g) {
            Alb3 = 0.0, CVel3 = 0.0, CTemp3 = 0.0, CQ3 = 0.0;
 #pragma unroll
     for (int n = 0; n < 2; ++n) {
+      const bool f = (n == 0) ? true : ice;
+      flag[n] = f;
+      if (!f) {
+        CVel[n] = CTemp[n] = CQ[n] = 0.0;
+        WSX[n] = WSY[n] = Sen[n] = QV[n] = LatH[n] = LUw[n] = SUw[n] = 0.0;
+        continue;
+      }
       const double SVT_SE = SVT[n] / SfcExner;
       const double Ri = Grav / SVT_SE * (VT_E - SVT_SE) * rvmx2 * (Height - zs);
-      const bool f = (n == 0) ? true : (Frac[n] > 1e-12);
-      flag[n] = f;
       double cm, ch, cq;
       bulk_coef_l82(Ri, z0m, z0h, zs, Height, cmn, chn, f, cm, ch, cq);
       const double rho = Ps / (GasRDry * SVT[n]);
@@ -289,7 +303,7 @@ int launch(const Ptrs &p, const dccm_sfc_grid *g, double sig1, cudaStream_t s) {
   geo.ncol = (int64_t)geo.NI * NJ;
   geo.sig1 = sig1;
   geo.sig1k = pow(sig1, (GasRUniv / MolWtDry) / CpDry);
-  const int threads = 128;
+  const int threads = tunables().flux_threads > 0 ? tunables().flux_threads : 128;
   int64_t blocks = (geo.ncol + threads - 1) / threads;
   const int64_t cap = (int64_t)sm_count() * 16;
   if (blocks > cap) blocks = cap;

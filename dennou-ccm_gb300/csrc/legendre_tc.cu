@@ -29,6 +29,7 @@
 // globaltimer limit; on expiry the kernel records an error code, stops
 // issuing work, and still frees its TMEM.
 #include <cuda_bf16.h>
+#include <string.h>
 
 #include "fp_conv.cuh"
 #include "sht_plan.cuh"
@@ -190,7 +191,28 @@ __device__ __forceinline__ void split3f(float x, __nv_bfloat16 &h, __nv_bfloat16
   l = __float2bfloat16_rn(r1 - __bfloat162float(m));
 }
 
-// Work item decode: items ordered (ct, m, nt), heavy (small m) first within ct.
+// One launch covers up to MAXG truncation groups (an ensemble of mixed
+// truncations): their work items are concatenated, each group with its own
+// tables, tensor map and buffers.
+constexpr int MAXG = 8;
+struct TcLaunch {
+  CUtensorMap map[MAXG];
+  TcArgs g[MAXG];
+  int start[MAXG + 1];  // prefix of work items over groups
+  int ngroups;
+};
+
+// Work item decode: groups in order, then items ordered (ct, m, nt) within a
+// group, heavy (small m) first within ct.
+__device__ __forceinline__ void decode(const TcArgs &a, int it, int &m, int &ct, int &nt);
+__device__ __forceinline__ const TcArgs &decode_item(const TcLaunch &L, int it, int &gi, int &m, int &ct,
+                                                     int &nt) {
+  gi = 0;
+  while (gi + 1 < L.ngroups && it >= L.start[gi + 1]) ++gi;
+  decode(L.g[gi], it - L.start[gi], m, ct, nt);
+  return L.g[gi];
+}
+
 __device__ __forceinline__ void decode(const TcArgs &a, int it, int &m, int &ct, int &nt) {
   ct = it / a.items_per_ct;
   int r = it % a.items_per_ct;
@@ -205,7 +227,7 @@ __device__ __forceinline__ void decode(const TcArgs &a, int it, int &m, int &ct,
 }
 
 __global__ void __launch_bounds__(TC_THREADS, 1)
-legendre_tc_kernel(const __grid_constant__ CUtensorMap tmap, TcArgs a) {
+legendre_tc_kernel(const __grid_constant__ TcLaunch L) {
   extern __shared__ __align__(1024) unsigned char smem_dyn[];
   // 1024-byte aligned stage area (swizzle atoms are address based).
   unsigned char *sm = reinterpret_cast<unsigned char *>(
@@ -238,8 +260,7 @@ legendre_tc_kernel(const __grid_constant__ CUtensorMap tmap, TcArgs a) {
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
-  const int nitems = a.nct * a.items_per_ct;
-  const int C2B = 2 * a.batch;
+  const int nitems = L.start[L.ngroups];
 
   if (warp < 4) {
     // ------------------------------------------------------- producers
@@ -247,8 +268,9 @@ legendre_tc_kernel(const __grid_constant__ CUtensorMap tmap, TcArgs a) {
     int g = 0;                  // chunk counter
     bool ok = true;
     for (int it = blockIdx.x; it < nitems && ok; it += gridDim.x) {
-      int m, ct, nt;
-      decode(a, it, m, ct, nt);
+      int gi, m, ct, nt;
+      const TcArgs &a = decode_item(L, it, gi, m, ct, nt);
+      const int C2B = 2 * a.batch;
       const MInfo mi = a.mi[m];
       const int nrow = min(128, mi.nr - nt * 128);
       const int c = ct * 128 + t;
@@ -265,28 +287,37 @@ legendre_tc_kernel(const __grid_constant__ CUtensorMap tmap, TcArgs a) {
             for (int sp = 0; sp < 3; ++sp) {
               const long long row0 = mi.base + ((long long)(p * mi.nq + q) * 3 + sp) * mi.nr + nt * 128;
               for (int r = 0; r < nrow; r += 16)
-                tma_load_2d(Bs + sp * B_SPLIT_BYTES + r * 128, &tmap, 0, (int)(row0 + r), &full[s]);
+                tma_load_2d(Bs + sp * B_SPLIT_BYTES + r * 128, &L.map[gi], 0, (int)(row0 + r), &full[s]);
             }
           }
-          // A row t: 8 groups of 8 bf16 along K, three split planes.
+          // A row t: all 64 values of the chunk are requested before any is
+          // used (one memory latency per chunk), then split into three planes
+          // of 8 groups of 8 bf16 along K.
           const int kbase = q * 64;
+          float xv[64];
+          if (a.dir == 0) {
+            // spec[b][idx(m, m+p+2k)], component c&1: stride 2 complex along k
+            const double *src = a.spec_in + ((long long)(c >> 1) * a.ncoef + idx_mn(a.N, m, m + p)) * 2 + (c & 1);
+#pragma unroll
+            for (int h2 = 0; h2 < 64; h2 += 32) {  // two halves keep the FP64 staging in registers
+              double dv[32];
+#pragma unroll
+              for (int e = 0; e < 32; ++e)
+                dv[e] = (c < C2B && kbase + h2 + e < kv) ? src[4LL * (kbase + h2 + e)] : 0.0;
+#pragma unroll
+              for (int e = 0; e < 32; ++e) xv[h2 + e] = f64_to_f32_rn(dv[e]);
+            }
+          } else {
+            const float *src = a.G + (((long long)m * 2 + p) * a.Jh) * C2B + c;
+#pragma unroll
+            for (int e = 0; e < 64; ++e)
+              xv[e] = (c < C2B && kbase + e < kv) ? src[(long long)(kbase + e) * C2B] : 0.f;
+          }
+#pragma unroll
           for (int g8 = 0; g8 < 8; ++g8) {
             __align__(16) __nv_bfloat16 h[8], md[8], lo[8];
-            const int k0 = kbase + g8 * 8;
 #pragma unroll
-            for (int e = 0; e < 8; ++e) {
-              const int k = k0 + e;
-              float x = 0.f;
-              if (c < C2B && k < kv) {
-                if (a.dir == 0) {
-                  const int n = m + p + 2 * k;
-                  x = f64_to_f32_rn(a.spec_in[((long long)(c >> 1) * a.ncoef + idx_mn(a.N, m, n)) * 2 + (c & 1)]);
-                } else {
-                  x = a.G[(((long long)m * 2 + p) * a.Jh + k) * C2B + c];
-                }
-              }
-              split3f(x, h[e], md[e], lo[e]);
-            }
+            for (int e = 0; e < 8; ++e) split3f(xv[g8 * 8 + e], h[e], md[e], lo[e]);
             const uint32_t off = (t >> 3) * 1024 + (t & 7) * 128 + ((g8 ^ (t & 7)) << 4);
             *reinterpret_cast<uint4 *>(As + off) = *reinterpret_cast<const uint4 *>(h);
             *reinterpret_cast<uint4 *>(As + A_SPLIT_BYTES + off) = *reinterpret_cast<const uint4 *>(md);
@@ -303,8 +334,8 @@ legendre_tc_kernel(const __grid_constant__ CUtensorMap tmap, TcArgs a) {
       int g = 0, li = 0;
       bool ok = true;
       for (int it = blockIdx.x; it < nitems && ok; it += gridDim.x, ++li) {
-        int m, ct, nt;
-        decode(a, it, m, ct, nt);
+        int gi, m, ct, nt;
+        const TcArgs &a = decode_item(L, it, gi, m, ct, nt);
         const MInfo mi = a.mi[m];
         const int nrow = min(128, mi.nr - nt * 128);
         const uint32_t idesc = idesc_bf16(nrow);
@@ -354,8 +385,9 @@ legendre_tc_kernel(const __grid_constant__ CUtensorMap tmap, TcArgs a) {
     const int row = quad * 32 + lane;
     int li = 0;
     for (int it = blockIdx.x; it < nitems; it += gridDim.x, ++li) {
-      int m, ct, nt;
-      decode(a, it, m, ct, nt);
+      int gi, m, ct, nt;
+      const TcArgs &a = decode_item(L, it, gi, m, ct, nt);
+      const int C2B = 2 * a.batch;
       const MInfo mi = a.mi[m];
       const int nrow = min(128, mi.nr - nt * 128);
       const int ab = a.nacc == 2 ? (li & 1) : 0;
@@ -594,51 +626,79 @@ int build_tiles(Plan &P) {
 
 static size_t tc_smem_bytes() { return 1024 + (size_t)NSTAGE * STAGE_BYTES + 128; }
 
-static int launch_tc(Plan &P, TileTable &T, TcArgs &a, cudaStream_t s) {
+// One persistent launch over ngroups plans (truncation groups) of one
+// direction: dir 0 (inverse) reads in[g] = spectra (double) and writes
+// out[g] = F (float); dir 1 reads G (float) and writes spectra (double).
+int legendre_tc_multi(Plan *const *plans, const int *batch, const void *const *in, void *const *out,
+                      int ngroups, int dir, cudaStream_t s) {
   static bool attr_done = false;
+  if (ngroups < 1 || ngroups > MAXG) return DCCM_ERR_UNSUPPORTED;
   if (!attr_done) {
     DCCM_CUDA(cudaFuncSetAttribute(legendre_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)tc_smem_bytes()));
     attr_done = true;
   }
-  a.N = P.N;
-  a.Jh = P.Jh;
-  a.ncoef = P.ncoef;
-  a.nct = (2 * a.batch + 127) / 128;
-  a.items_per_ct = T.items_per_ct;
-  a.mi = (const MInfo *)T.d_mi;
-  a.pre = T.d_pre;
-  a.err = P.d_err;
-  a.ntmax = T.ntmax;
-  a.nacc = 8 * T.ntmax <= TMEM_COLS ? 2 : 1;
-  const int items = a.nct * a.items_per_ct;
+  TcLaunch L;
+  memset(&L, 0, sizeof L);
+  int ntmax = 64, ng = 0, items = 0;
+  for (int g = 0; g < ngroups; ++g) {
+    const TileTable &T = dir == 0 ? plans[g]->tinv : plans[g]->tfwd;
+    if (!T.map_ok) return DCCM_ERR_UNSUPPORTED;
+    ntmax = T.ntmax > ntmax ? T.ntmax : ntmax;
+  }
+  for (int g = 0; g < ngroups; ++g) {
+    if (batch[g] <= 0) continue;
+    Plan &P = *plans[g];
+    const TileTable &T = dir == 0 ? P.tinv : P.tfwd;
+    TcArgs &a = L.g[ng];
+    a.dir = dir;
+    a.batch = batch[g];
+    a.N = P.N;
+    a.Jh = P.Jh;
+    a.ncoef = P.ncoef;
+    a.nct = (2 * a.batch + 127) / 128;
+    a.items_per_ct = T.items_per_ct;
+    a.mi = (const MInfo *)T.d_mi;
+    a.pre = T.d_pre;
+    a.err = plans[0]->d_err;
+    a.ntmax = ntmax;
+    a.nacc = 8 * ntmax <= TMEM_COLS ? 2 : 1;
+    if (dir == 0) {
+      a.spec_in = (const double *)in[g];
+      a.F = (float *)out[g];
+    } else {
+      a.G = (const float *)in[g];
+      a.spec_out = (double *)out[g];
+    }
+    L.map[ng] = T.map;
+    L.start[ng] = items;
+    items += a.nct * a.items_per_ct;
+    ++ng;
+  }
+  L.start[ng] = items;
+  L.ngroups = ng;
   if (items <= 0) return DCCM_OK;
-  const int grid = items < sm_count() ? items : sm_count();
-  legendre_tc_kernel<<<grid, TC_THREADS, tc_smem_bytes(), s>>>(T.map, a);
+  int ctas = tunables().tc_ctas > 0 ? tunables().tc_ctas : sm_count();
+  const int grid = items < ctas ? items : ctas;
+  legendre_tc_kernel<<<grid, TC_THREADS, tc_smem_bytes(), s>>>(L);
   DCCM_LAUNCH_CHECK();
   return DCCM_OK;
 }
 
 int legendre_inv_tc(Plan &P, int batch, const double *spec, float *F, cudaStream_t s) {
   if (batch <= 0) return DCCM_OK;
-  if (!P.tinv.map_ok) return DCCM_ERR_UNSUPPORTED;
-  TcArgs a = {};
-  a.dir = 0;
-  a.batch = batch;
-  a.spec_in = spec;
-  a.F = F;
-  return launch_tc(P, P.tinv, a, s);
+  Plan *pp = &P;
+  const void *in = spec;
+  void *out = F;
+  return legendre_tc_multi(&pp, &batch, &in, &out, 1, 0, s);
 }
 
 int legendre_fwd_tc(Plan &P, int batch, const float *G, double *spec, cudaStream_t s) {
   if (batch <= 0) return DCCM_OK;
-  if (!P.tfwd.map_ok) return DCCM_ERR_UNSUPPORTED;
-  TcArgs a = {};
-  a.dir = 1;
-  a.batch = batch;
-  a.G = G;
-  a.spec_out = spec;
-  return launch_tc(P, P.tfwd, a, s);
+  Plan *pp = &P;
+  const void *in = G;
+  void *out = spec;
+  return legendre_tc_multi(&pp, &batch, &in, &out, 1, 1, s);
 }
 
 }  // namespace sht

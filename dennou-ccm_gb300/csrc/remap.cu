@@ -19,8 +19,8 @@
 //
 // Apply.  The table is grouped by destination, so a stable counting sort
 // turns it into CSR without changing the per-row order.  One thread owns a
-// destination row; each nonzero is one 16-byte record (weight, column)
-// fetched with a single 128-bit load; sums start at zero and add the
+// (destination row, field) pair; each nonzero is one 16-byte record (weight,
+// column) fetched with a single 128-bit load; sums start at zero and add the
 // separately rounded products in table order, which makes the result
 // bit-identical to the reference loop (:293-302).
 #include <math.h>
@@ -56,40 +56,48 @@ constexpr int UNSET = -2147483647;
 __global__ void __launch_bounds__(256)
 csr_apply(const int64_t *__restrict__ rowptr, const double2 *__restrict__ ent,
           const double *__restrict__ src, int64_t ld_src, double *__restrict__ dst,
-          int64_t ld_dst, int64_t nrow, int nfields) {
-  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < nrow;
-       r += (int64_t)gridDim.x * blockDim.x) {
+          int64_t ld_dst, int64_t nrow, int nfields, int nsub, int64_t ld_dst2) {
+  // One thread per (destination row, field), rows fastest: consecutive
+  // threads gather neighbouring source points and store consecutive rows;
+  // the six fields of a row re-read the same records from L1.  Field f is
+  // written at (f % nsub) * ld_dst + (f / nsub) * ld_dst2.
+  const int64_t total = nrow * nfields;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = t % nrow;
+    const int64_t f = t / nrow;
     const int64_t b = rowptr[r], e = rowptr[r + 1];
-    if (e - b == 1) {  // common single-source row: keep the record in registers
-      const double2 q = __ldg(ent + b);
+    const double *s = src + f * ld_src;
+    double acc = 0.0;
+    for (int64_t k = b; k < e; ++k) {
+      const double2 q = __ldg(ent + k);
       const int64_t col = (int64_t)__double_as_longlong(q.y);
-      for (int f = 0; f < nfields; ++f)
-        dst[f * ld_dst + r] = __dadd_rn(0.0, __dmul_rn(__ldg(src + f * ld_src + col), q.x));
-      continue;
+      acc = __dadd_rn(acc, __dmul_rn(__ldg(s + col), q.x));
     }
-    for (int f = 0; f < nfields; ++f) {
-      double acc = 0.0;
-      for (int64_t k = b; k < e; ++k) {
-        const double2 q = __ldg(ent + k);
-        const int64_t col = (int64_t)__double_as_longlong(q.y);
-        acc = __dadd_rn(acc, __dmul_rn(__ldg(src + f * ld_src + col), q.x));
-      }
-      dst[f * ld_dst + r] = acc;
-    }
+    dst[(f % nsub) * ld_dst + (f / nsub) * ld_dst2 + r] = acc;
   }
+}
+
+int apply2(dccm_remap_plan *p, const double *src, int64_t ld_src, double *dst, int64_t ld_dst, int nfields,
+           int nsub, int64_t ld_dst2, cudaStream_t s) {
+  if (p->n_recv == 0 || nfields == 0) return DCCM_OK;
+  if (nsub <= 0) {
+    nsub = nfields;
+    ld_dst2 = 0;
+  }
+  const int threads = tunables().remap_threads > 0 ? tunables().remap_threads : 256;
+  int64_t blocks = (p->n_recv * nfields + threads - 1) / threads;
+  const int64_t cap = (int64_t)sm_count() * 16;
+  if (blocks > cap) blocks = cap;
+  csr_apply<<<(unsigned)blocks, threads, 0, s>>>(p->d_rowptr, p->d_ent, src, ld_src, dst, ld_dst,
+                                                 p->n_recv, nfields, nsub, ld_dst2);
+  DCCM_LAUNCH_CHECK();
+  return DCCM_OK;
 }
 
 int apply(dccm_remap_plan *p, const double *src, int64_t ld_src, double *dst, int64_t ld_dst,
           int nfields, cudaStream_t s) {
-  if (p->n_recv == 0 || nfields == 0) return DCCM_OK;
-  const int threads = 256;
-  int64_t blocks = (p->n_recv + threads - 1) / threads;
-  const int64_t cap = (int64_t)sm_count() * 8;
-  if (blocks > cap) blocks = cap;
-  csr_apply<<<(unsigned)blocks, threads, 0, s>>>(p->d_rowptr, p->d_ent, src, ld_src, dst, ld_dst,
-                                                 p->n_recv, nfields);
-  DCCM_LAUNCH_CHECK();
-  return DCCM_OK;
+  return apply2(p, src, ld_src, dst, ld_dst, nfields, 0, 0, s);
 }
 
 // ------------------------------------------------------------ generator

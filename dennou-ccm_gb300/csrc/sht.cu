@@ -84,16 +84,6 @@ __global__ void pnm_kernel(int N, int Jh, const double *__restrict__ mu, double 
   }
 }
 
-static bool make_fft_plan(int I, FftPlan &f) {
-  f.I = I;
-  f.nst = 0;
-  int n = I;
-  while (n % 4 == 0 && f.nst < MAX_STAGES) { f.radix[f.nst++] = 4; n /= 4; }
-  while (n % 2 == 0 && f.nst < MAX_STAGES) { f.radix[f.nst++] = 2; n /= 2; }
-  while (n % 3 == 0 && f.nst < MAX_STAGES) { f.radix[f.nst++] = 3; n /= 3; }
-  return n == 1;
-}
-
 static void destroy(Plan &P) {
   void *ptrs[] = {P.d_mu, P.d_w, P.d_pnm, P.d_tw64, P.d_tw32, P.tinv.d, P.tfwd.d, P.tinv.d_mi,
                   P.tfwd.d_mi, P.tinv.d_pre, P.tfwd.d_pre, P.d_work, P.d_err};
@@ -111,7 +101,7 @@ static int create(Plan &P, int N, int I, int J, int precision, int max_batch) {
   P.precision = precision;
   P.max_batch = max_batch;
   P.ncoef = (int64_t)(N + 1) * (N + 2) / 2;
-  if (!make_fft_plan(I, P.fft)) return DCCM_ERR_UNSUPPORTED;
+  if (!fft_length_supported(I)) return DCCM_ERR_UNSUPPORTED;
   DCCM_CUDA(cudaMalloc(&P.d_mu, J * sizeof(double)));
   DCCM_CUDA(cudaMalloc(&P.d_w, J * sizeof(double)));
   DCCM_CUDA(cudaMalloc(&P.d_pnm, (size_t)P.ncoef * P.Jh * sizeof(double)));
@@ -296,3 +286,127 @@ extern "C" int dccm_sht_forward(dccm_sht_plan *p, const double *grid, double *sp
   const size_t ns = (size_t)batch * p->P.ncoef * 2, ng = (size_t)batch * p->P.J * p->P.I;
   return host_call(p, grid, ng, spec, ns, batch, false);
 }
+
+// ----------------------------------------------------------------- ensemble
+// Several truncation groups (an ensemble of members with mixed truncations,
+// members of one truncation concatenated into one group).  On the mixed
+// path each direction is one persistent tcgen05 Legendre launch and one FFT
+// launch over all groups; the FP64 path runs the groups one after another.
+struct dccm_sht_ensemble {
+  std::vector<dccm_sht_plan *> plans;
+  int precision = 0;
+};
+
+extern "C" int dccm_sht_ensemble_create(int ngroups, const int *nmax, const int *imax, const int *jmax,
+                                        const int *max_batch, int precision, dccm_sht_ensemble **ens) {
+  if (!ens) return DCCM_ERR_INVALID_ARG;
+  *ens = nullptr;
+  if (ngroups < 1 || ngroups > 8 || !nmax || !imax || !jmax || !max_batch) return DCCM_ERR_INVALID_ARG;
+  dccm_sht_ensemble *e = new (std::nothrow) dccm_sht_ensemble();
+  if (!e) return DCCM_ERR_NOMEM;
+  e->precision = precision;
+  for (int g = 0; g < ngroups; ++g) {
+    dccm_sht_plan *p = nullptr;
+    const int st = dccm_sht_plan_create(nmax[g], imax[g], jmax[g], precision, max_batch[g], &p);
+    if (st != DCCM_OK) {
+      dccm_sht_ensemble_destroy(e);
+      return st;
+    }
+    e->plans.push_back(p);
+  }
+  *ens = e;
+  return DCCM_OK;
+}
+
+extern "C" int dccm_sht_ensemble_destroy(dccm_sht_ensemble *e) {
+  if (!e) return DCCM_OK;
+  for (dccm_sht_plan *p : e->plans) dccm_sht_plan_destroy(p);
+  delete e;
+  return DCCM_OK;
+}
+
+static int ens_check(dccm_sht_ensemble *e, const void *a, const void *b, const int *batch) {
+  if (!e || !a || !b || !batch) return DCCM_ERR_INVALID_ARG;
+  for (size_t g = 0; g < e->plans.size(); ++g)
+    if (batch[g] < 0 || batch[g] > e->plans[g]->P.max_batch) return DCCM_ERR_SHAPE;
+  return DCCM_OK;
+}
+
+namespace dccm {
+namespace sht {
+int ensemble_inverse(dccm_sht_ensemble *e, const double *const *spec, double *const *grid, const int *batch,
+                     cudaStream_t s) {
+  const int ng = (int)e->plans.size();
+  if (e->precision != DCCM_SHT_MIXED) {
+    for (int g = 0; g < ng; ++g)
+      if (batch[g] > 0) DCCM_TRY(inverse(e->plans[g]->P, spec[g], grid[g], batch[g], s));
+    return DCCM_OK;
+  }
+  Plan *pp[8];
+  const void *in[8];
+  void *work[8];
+  for (int g = 0; g < ng; ++g) {
+    pp[g] = &e->plans[g]->P;
+    in[g] = spec[g];
+    work[g] = pp[g]->d_work;
+  }
+  DCCM_TRY(legendre_tc_multi(pp, batch, in, work, ng, 0, s));
+  return fft_multi(pp, batch, (const void *const *)work, (void *const *)grid, ng, false, s);
+}
+
+int ensemble_forward(dccm_sht_ensemble *e, const double *const *grid, double *const *spec, const int *batch,
+                     cudaStream_t s) {
+  const int ng = (int)e->plans.size();
+  if (e->precision != DCCM_SHT_MIXED) {
+    for (int g = 0; g < ng; ++g)
+      if (batch[g] > 0) DCCM_TRY(forward(e->plans[g]->P, grid[g], spec[g], batch[g], s));
+    return DCCM_OK;
+  }
+  Plan *pp[8];
+  void *work[8];
+  for (int g = 0; g < ng; ++g) {
+    pp[g] = &e->plans[g]->P;
+    work[g] = pp[g]->d_work;
+  }
+  DCCM_TRY(fft_multi(pp, batch, (const void *const *)grid, work, ng, true, s));
+  return legendre_tc_multi(pp, batch, (const void *const *)work, (void *const *)spec, ng, 1, s);
+}
+}  // namespace sht
+}  // namespace dccm
+
+extern "C" int dccm_sht_ensemble_inverse_dev(dccm_sht_ensemble *e, const double *const *spec,
+                                             double *const *grid, const int *batch, void *stream) {
+  DCCM_TRY(ens_check(e, spec, grid, batch));
+  return sht::ensemble_inverse(e, spec, grid, batch, as_stream(stream));
+}
+
+extern "C" int dccm_sht_ensemble_forward_dev(dccm_sht_ensemble *e, const double *const *grid,
+                                             double *const *spec, const int *batch, void *stream) {
+  DCCM_TRY(ens_check(e, grid, spec, batch));
+  return sht::ensemble_forward(e, grid, spec, batch, as_stream(stream));
+}
+
+extern "C" int dccm_sht_ensemble_status(dccm_sht_ensemble *e, int *device_error) {
+  if (!e) return DCCM_ERR_INVALID_ARG;
+  int worst = 0, st = DCCM_OK;
+  for (dccm_sht_plan *p : e->plans) {
+    int d = 0;
+    const int s = dccm_sht_status(p, &d);
+    if (d) worst = d;
+    if (s != DCCM_OK) st = s;
+  }
+  if (device_error) *device_error = worst;
+  return st;
+}
+
+extern "C" int dccm_sht_ensemble_groups(const dccm_sht_ensemble *e, int *ngroups) {
+  if (!e || !ngroups) return DCCM_ERR_INVALID_ARG;
+  *ngroups = (int)e->plans.size();
+  return DCCM_OK;
+}
+
+namespace dccm {
+namespace sht {
+Plan *ensemble_plan(dccm_sht_ensemble *e, int g) { return &e->plans[g]->P; }
+}  // namespace sht
+}  // namespace dccm

@@ -25,14 +25,6 @@
 namespace dccm {
 namespace sht {
 
-constexpr int MAX_STAGES = 12;
-
-struct FftPlan {
-  int I = 0;
-  int nst = 0;
-  int radix[MAX_STAGES] = {0};
-};
-
 // Layout of one Legendre operand table of bf16 split tiles (tensor path):
 // rows of 64 bf16 (128 bytes) in a 2-D tensor [rows][64]; for (m, p) the
 // tile of chunk q (64 wide along K) and split s starts at row
@@ -63,7 +55,6 @@ struct Plan {
   double *d_pnm = nullptr;     // FP64 Pbar(m, n, jj): [idx(m,n)][Jh]
   double2 *d_tw64 = nullptr;   // FFT twiddles e^{-2 pi i t / I}
   float2 *d_tw32 = nullptr;
-  FftPlan fft;
   TileTable tinv, tfwd;        // bf16x3 tiles for the tensor path
   void *d_work = nullptr;      // Fourier buffer (F or G), sized for max_batch
   size_t work_bytes = 0;
@@ -83,12 +74,21 @@ __host__ __device__ inline int count_np(int N, int m, int p) {
 }
 
 // Kernel launchers (defined in the .cu files).
+bool fft_length_supported(int I);
+int fft_inverse_f64(const Plan &P, int batch, const double *F, double *grid, cudaStream_t s);
+int fft_forward_f64(const Plan &P, int batch, const double *grid, double *G, cudaStream_t s);
 int fft_inverse(const Plan &P, int batch, bool fp32, const void *F, double *grid, cudaStream_t s);
 int fft_forward(const Plan &P, int batch, bool fp32, const double *grid, void *G, cudaStream_t s);
 int legendre_inv_f64(const Plan &P, int batch, const double *spec, double *F, cudaStream_t s);
 int legendre_fwd_f64(const Plan &P, int batch, const double *G, double *spec, cudaStream_t s);
 int legendre_inv_tc(Plan &P, int batch, const double *spec, float *F, cudaStream_t s);
 int legendre_fwd_tc(Plan &P, int batch, const float *G, double *spec, cudaStream_t s);
+int legendre_tc_multi(Plan *const *plans, const int *batch, const void *const *in, void *const *out,
+                      int ngroups, int dir, cudaStream_t s);
+int fft_multi(Plan *const *plans, const int *batch, const void *const *in, void *const *out, int ngroups, bool fwd,
+              cudaStream_t s);
+int inverse(Plan &P, const double *spec, double *grid, int batch, cudaStream_t s);
+int forward(Plan &P, const double *grid, double *spec, int batch, cudaStream_t s);
 int build_tiles(Plan &P);
 
 }  // namespace sht

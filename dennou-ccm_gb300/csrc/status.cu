@@ -5,6 +5,11 @@ namespace dccm {
 static thread_local int g_last_cuda_error = 0;
 void set_cuda_error(cudaError_t e) { g_last_cuda_error = (int)e; }
 
+Tunables &tunables() {
+  static Tunables t;
+  return t;
+}
+
 int sm_count() {
   static int cached[64] = {0};
   int dev = 0;

@@ -213,7 +213,8 @@ int dccm_area_integral_noalloc_dev(const double *f, const double *area, int64_t 
  * precision DCCM_SHT_MIXED: Legendre sums on the tensor cores in split
  * BF16 x 3 with FP32 accumulation, FFT in FP32; relative L2 error of a
  * forward(inverse(s)) round trip below 1e-6.  Requires jmax/2 % 16 == 0.
- * Requirements: jmax even, jmax >= nmax+1, imax > 2 nmax, imax = 2^a 3^b.
+ * Requirements: jmax even, jmax >= nmax+1, imax > 2 nmax, imax = 32 R with
+ * R in {2, 3, 4, 6, 8, 12, 16, 24, 32} (imax = 64 ... 1024).
  * ===================================================================== */
 enum { DCCM_SHT_FP64 = 0, DCCM_SHT_MIXED = 1 };
 
@@ -242,6 +243,24 @@ int dccm_sht_forward(dccm_sht_plan *plan, const double *grid, double *spec, int 
  * bounded device waits set; DCCM_ERR_TIMEOUT if one gave up. */
 int dccm_sht_status(dccm_sht_plan *plan, int *device_error);
 
+/* Ensemble of mixed truncations: ngroups (<= 8) truncation groups, each a
+ * plan as above holding the field-levels of all members of that truncation
+ * (members of one truncation are concatenated along the batch).  On the
+ * mixed path each direction is ONE persistent tensor-core Legendre launch
+ * and ONE FFT launch over all groups; the FP64 path runs group by group.
+ * spec[g], grid[g] are device pointers of group g; batch[g] <= max_batch[g]. */
+typedef struct dccm_sht_ensemble dccm_sht_ensemble;
+
+int dccm_sht_ensemble_create(int ngroups, const int *nmax, const int *imax, const int *jmax,
+                             const int *max_batch, int precision, dccm_sht_ensemble **ens);
+int dccm_sht_ensemble_destroy(dccm_sht_ensemble *ens);
+int dccm_sht_ensemble_inverse_dev(dccm_sht_ensemble *ens, const double *const *spec,
+                                  double *const *grid, const int *batch, void *stream);
+int dccm_sht_ensemble_forward_dev(dccm_sht_ensemble *ens, const double *const *grid,
+                                  double *const *spec, const int *batch, void *stream);
+int dccm_sht_ensemble_status(dccm_sht_ensemble *ens, int *device_error);
+int dccm_sht_ensemble_groups(const dccm_sht_ensemble *ens, int *ngroups);
+
 /* =====================================================================
  * Coupling step
  * One coupling step of the hot path on one GPU, as one CUDA graph: the
@@ -255,18 +274,35 @@ int dccm_sht_status(dccm_sht_plan *plan, int *device_error);
  * NULL is left out.  The graph is recorded at creation, so the buffers must
  * stay valid and at the same addresses for the life of the step.
  * ===================================================================== */
+/* One remap of a step: nfields fields through one plan.  With nsub > 0 the
+ * destination of field f is dst + (f % nsub)*ld_dst + (f / nsub)*ld_dst2
+ * (e.g. nsub surface fields of consecutive ensemble members, each member's
+ * block ld_dst2 further along the same output arrays); nsub = 0 means
+ * dst + f*ld_dst. */
+typedef struct dccm_step_remap {
+  dccm_remap_plan *plan;
+  int nfields;
+  const double *src;           /* field f at src + f*ld_src */
+  int64_t ld_src;
+  double *dst;
+  int64_t ld_dst;
+  int nsub;
+  int64_t ld_dst2;
+} dccm_step_remap;
+
 typedef struct dccm_step_desc {
   dccm_sht_plan *sht;          /* transform plan, or NULL */
   int nfl;                     /* field-levels per step (<= plan's max_batch) */
   const double *spec_in;       /* [nfl][ncoef] complex */
   double *grid;                /* [nfl][jmax][imax] */
   double *spec_out;            /* [nfl][ncoef] complex */
-  dccm_remap_plan *remap;      /* remap plan, or NULL */
-  int nfields;                 /* surface fields to remap */
-  const double *remap_src;     /* field f at remap_src + f*ld_src */
-  int64_t ld_src;
-  double *remap_dst;           /* field f at remap_dst + f*ld_dst */
-  int64_t ld_dst;
+  dccm_sht_ensemble *ens;      /* ensemble transforms instead of sht, or NULL */
+  const double *const *ens_spec_in;  /* per group, as dccm_sht_ensemble_*_dev */
+  double *const *ens_grid;
+  double *const *ens_spec_out;
+  const int *ens_nfl;
+  int nremap;                  /* remaps, run in order before the flux */
+  const dccm_step_remap *remaps;
   const dccm_sfc_bulk_flux_args *flux;  /* device arrays, or NULL */
   const dccm_sfc_grid *flux_grid;
 } dccm_step_desc;
@@ -284,15 +320,29 @@ int dccm_step_create(const dccm_step_desc *desc, dccm_step **step);
 int dccm_step_destroy(dccm_step *step);
 /* Replays the step's graph on stream (stream-ordered, no synchronisation). */
 int dccm_step_run(dccm_step *step, void *stream);
-/* Runs the four stages one after another on stream with events between
- * them and returns their device times: ms[0] inverse transform, ms[1]
- * forward transform, ms[2] remap, ms[3] bulk flux.  Synchronises. */
+/* Runs the stages one after another on stream with events between them and
+ * returns their device times: ms[0] Legendre synthesis, ms[1] inverse FFT,
+ * ms[2] forward FFT, ms[3] Legendre analysis, ms[4] remaps, ms[5] bulk
+ * flux (six floats).  Synchronises. */
 int dccm_step_run_timed(dccm_step *step, void *stream, float *ms);
 /* Copies nh2d host buffers to the device, replays the graph, copies nd2h
  * device buffers back and synchronises: the step for a caller whose data
  * live in host memory (page-locked memory makes the copies asynchronous). */
 int dccm_step_run_host(dccm_step *step, void *stream, const dccm_host_copy *h2d, int nh2d,
                        const dccm_host_copy *d2h, int nd2h);
+
+/* Autotuner: chooses the launch shapes of the step's kernels by timing
+ * candidates of each knob on the stage it affects ("tc_ctas": persistent
+ * CTAs of the tensor-core Legendre kernel, "fft_bb": field-levels per FFT
+ * CTA, "flux_threads", "remap_threads": CTA sizes), applies the winners
+ * and records the step's graph again.  With cache_path the choice is read
+ * from / appended to that file (one JSON object per line, keyed by the
+ * GPU name and SM count and the step's shapes).  chosen (4 ints, may be
+ * NULL) receives tc_ctas, fft_bb, flux_threads, remap_threads.  The knobs
+ * are process-wide defaults of later launches too. */
+int dccm_step_autotune(dccm_step *step, const char *cache_path, int *chosen);
+int dccm_tune_set(const char *knob, int value);
+int dccm_tune_get(const char *knob, int *value);
 
 #ifdef __cplusplus
 }

@@ -187,16 +187,50 @@ void oracle_rfft_row(int I, const double *g, int M, double *out) {
   free(y);
 }
 
+/* Gauss nodes, weights and Pbar tables, computed once per (N, J) and kept
+ * (as a transform library keeps them from its initialisation, SPML's
+ * w_Initial).  Called outside parallel regions. */
+typedef struct {
+  int N, J;
+  double *mu, *w, *p;
+} tables_t;
+static tables_t g_tab[8];
+static int g_ntab = 0;
+
+static void tables_for(int N, int J, const double **mu, const double **w, const double **p) {
+  for (int k = 0; k < g_ntab; ++k)
+    if (g_tab[k].N == N && g_tab[k].J == J) {
+      *mu = g_tab[k].mu;
+      *w = g_tab[k].w;
+      *p = g_tab[k].p;
+      return;
+    }
+  const int64_t ncoef = (int64_t)(N + 1) * (N + 2) / 2;
+  tables_t t = {N, J, (double *)malloc(sizeof(double) * J), (double *)malloc(sizeof(double) * J),
+                (double *)malloc(sizeof(double) * ncoef * J)};
+  oracle_gauss_nodes(J, t.mu, t.w);
+  oracle_pnm(N, J, t.mu, t.p);
+  if (g_ntab == 8) { /* evict the oldest */
+    free(g_tab[0].mu);
+    free(g_tab[0].w);
+    free(g_tab[0].p);
+    for (int k = 1; k < 8; ++k) g_tab[k - 1] = g_tab[k];
+    g_ntab = 7;
+  }
+  g_tab[g_ntab++] = t;
+  *mu = t.mu;
+  *w = t.w;
+  *p = t.p;
+}
+
 /* ------------------------------------------------------------ transforms */
 void oracle_sht_inverse(int N, int I, int J, int batch, const double *spec,
                         double *grid) {
   const int64_t ncoef = (int64_t)(N + 1) * (N + 2) / 2;
   const int Jh = J / 2;
-  double *mu = (double *)malloc(sizeof(double) * J);
-  double *w = (double *)malloc(sizeof(double) * J);
-  double *p = (double *)malloc(sizeof(double) * ncoef * J);
-  oracle_gauss_nodes(J, mu, w);
-  oracle_pnm(N, J, mu, p);
+  const double *mu, *w, *p;
+  tables_for(N, J, &mu, &w, &p);
+  (void)mu;
   cplx *tw = make_twiddles(I);
 #pragma omp parallel
   {
@@ -254,20 +288,15 @@ void oracle_sht_inverse(int N, int I, int J, int batch, const double *spec,
     free(Fs);
   }
   free(tw);
-  free(mu);
-  free(w);
-  free(p);
 }
 
 void oracle_sht_forward(int N, int I, int J, int batch, const double *grid,
                         double *spec) {
   const int64_t ncoef = (int64_t)(N + 1) * (N + 2) / 2;
   const int Jh = J / 2;
-  double *mu = (double *)malloc(sizeof(double) * J);
-  double *w = (double *)malloc(sizeof(double) * J);
-  double *p = (double *)malloc(sizeof(double) * ncoef * J);
-  oracle_gauss_nodes(J, mu, w);
-  oracle_pnm(N, J, mu, p);
+  const double *mu, *w, *p;
+  tables_for(N, J, &mu, &w, &p);
+  (void)mu;
   cplx *tw = make_twiddles(I);
 #pragma omp parallel
   {
@@ -321,7 +350,4 @@ void oracle_sht_forward(int N, int I, int J, int batch, const double *grid,
     free(O);
   }
   free(tw);
-  free(mu);
-  free(w);
-  free(p);
 }

@@ -1,0 +1,105 @@
+"""GPU tests of the ensemble transforms and the coupling-step graph, against
+the oracle, through the C ABI.  Tolerances as in test_sht_gpu.py (mixed
+1e-6, FP64 1e-13 relative L2); remap bit-exact; flux 1e-13."""
+import importlib
+
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+GROUPS = [(21, 64, 32, 20), (42, 128, 64, 10), (63, 192, 96, 7), (85, 256, 128, 5)]
+
+
+@pytest.mark.parametrize("prec,tol", [(1, 1e-6), (0, 1e-13)])
+def test_ensemble_matches_oracle(dccm, oracle, synth, cuda, prec, tol):
+    torch = cuda
+    ens = dccm.Ensemble([g for g in GROUPS], prec)
+    specs = [synth.spectra(N, B, seed=N + B) for N, I, J, B in GROUPS]
+    ds = [torch.from_numpy(s.view(np.float64).copy()).cuda() for s in specs]
+    dg = [torch.empty((B, J, I), dtype=torch.float64, device="cuda") for N, I, J, B in GROUPS]
+    ds2 = [torch.empty_like(x) for x in ds]
+    batch = [B for *_, B in GROUPS]
+    ens.inverse_dev(ds, dg, batch)
+    ens.forward_dev(dg, ds2, batch)
+    torch.cuda.synchronize()
+    assert ens.status() == (0, 0)
+    for (N, I, J, B), s, g, s2 in zip(GROUPS, specs, dg, ds2):
+        go = oracle.sht_inverse(N, I, J, s)
+        assert rel_l2(g.cpu().numpy(), go) <= tol, N
+        assert rel_l2(s2.cpu().numpy().view(np.complex128), s) <= tol, N
+    # a group with no field-levels this call is skipped
+    ens.inverse_dev(ds, dg, [0, 10, 0, 5])
+    torch.cuda.synchronize()
+    assert rel_l2(dg[1].cpu().numpy(), oracle.sht_inverse(42, 128, 64, specs[1])) <= tol
+
+
+def _small_step(dccm, synth, oracle, torch, prec):
+    """T21L16 x 3 -> T42 ocean (conservative weights), 8192 flux columns."""
+    bench = importlib.import_module("bench")
+    w = dict(bench.WORKLOADS["c1"])
+    inp = bench.build_inputs(w, synth)
+    S = bench.gpu_setup(w, inp, dccm, synth, torch, torch.device("cuda", 0))
+    return bench, w, inp, S
+
+
+def test_step_outputs_match_oracle(dccm, oracle, synth, cuda):
+    torch = cuda
+    bench, w, inp, S = _small_step(dccm, synth, oracle, torch, 1)
+    g = inp["groups"][0]
+    for key, tol in (("mixed", 1e-6), ("fp64", 1e-13)):
+        S["steps"][key].run()
+        torch.cuda.synchronize()
+        go = oracle.sht_inverse(g.N, g.I, g.J, g.spec)
+        assert rel_l2(S["grid"][0].cpu().numpy(), go) <= tol, key
+        assert rel_l2(S["spec_out"][0].cpu().numpy().view(np.complex128), g.spec) <= tol, key
+    # remapped inputs and fluxes on the ocean columns
+    send, recv, coef = S["tables"][0]
+    n1 = len(inp["ocean"])
+    ref = oracle.remap_apply(send, recv, coef, np.asfortranarray(g.src.T), n1)
+    arrs, grid = bench.ocean_columns(inp)
+    arrs.update(synth.flux_outputs(grid[0], grid[1], fill=0.0))
+    for f, name in enumerate(bench.REMAP_FIELDS):
+        got = S["dflux"][name].cpu().numpy().T[1:-1, 1]
+        assert np.array_equal(got, ref[:, f]), name
+        arrs[name][1:-1, 1] = ref[:, f]
+    oracle.sfc_bulk_flux(arrs, *grid)
+    for name in dccm.FLUX_OUT:
+        got = S["dflux"][name].cpu().numpy().T
+        assert rel_l2(got[1:-1, 1], arrs[name][1:-1, 1]) <= 1e-13, name
+
+
+def test_step_timed_and_host_entry(dccm, oracle, synth, cuda):
+    torch = cuda
+    bench, w, inp, S = _small_step(dccm, synth, oracle, torch, 1)
+    ms = S["steps"]["mixed"].run_timed()
+    assert len(ms) == 6 and all(m > 0 for m in ms)
+    g = inp["groups"][0]
+    h_in = torch.from_numpy(g.spec.view(np.float64).copy()).pin_memory()
+    h_out = torch.empty_like(h_in).pin_memory()
+    S["spec_out"][0].zero_()
+    S["steps"]["mixed"].run_host([(h_in, S["spec_in"][0])], [(h_out, S["spec_out"][0])])
+    assert rel_l2(h_out.numpy().view(np.complex128), g.spec) <= 1e-6
+
+
+def test_remap_two_level_destination(dccm, oracle, synth, cuda):
+    """nsub/ld_dst2: member m's field f lands at dst + f*ld_dst + m*ld_dst2."""
+    torch = cuda
+    bench = importlib.import_module("bench")
+    w = dict(bench.WORKLOADS["c4"])
+    w["members"] = 6
+    inp = bench.build_inputs(w, synth)
+    S = bench.gpu_setup(w, inp, dccm, synth, torch, torch.device("cuda", 0))
+    S["steps"]["mixed"].run()
+    torch.cuda.synchronize()
+    n1 = len(inp["ocean"])
+    off = 0
+    for g, (send, recv, coef) in zip(inp["groups"], S["tables"]):
+        for mi in range(len(g.members)):
+            ref = oracle.remap_apply(send, recv, coef, np.asfortranarray(g.src[6 * mi:6 * mi + 6].T), n1)
+            for f, name in enumerate(bench.REMAP_FIELDS):
+                got = S["dflux"][name].cpu().numpy().T[1 + off * n1:1 + (off + 1) * n1, 1]
+                assert np.array_equal(got, ref[:, f]), (g.N, mi, name)
+            off += 1
