@@ -271,6 +271,50 @@ def gpu_setup(w, inp, dccm, synth, torch, dev):
                 tables=tables, nnz=nnz, ncol=IA - 2, remap_plans=plans)
 
 
+# Flux arrays a coupling step exchanges with the host, with the slots that
+# carry data: per-step surface state in, fluxes and coefficients out (slot 3
+# of the net/SW-radiation fluxes and their derivative is left untouched; the
+# merged surface temperature and albedo land in slot 3).
+FLUX_H2D = {"SDwRFlx": (0,), "ImplCplCoef1": (0, 1, 2, 3), "ImplCplCoef2": (0, 1, 2, 3), "SfcTemp": (0, 1),
+            "SfcAlbedo": (0, 1), "SIceCon": (0,), "SfcHeight": (0,)}
+FLUX_D2H_SLOTS = {"DelVarImplCPL": (0, 1, 2, 3), "SfcHFlx_ns": (0, 1), "SfcHFlx_sr": (0, 1),
+                  "DSfcHFlxDTs": (0, 1), "SfcTemp": (2,), "SfcAlbedo": (2,)}
+
+
+def host_copies(S, groups, dccm, torch):
+    """(pinned host, device) pairs of one coupling step's inputs and results:
+    spectra and remap sources in, analysed spectra out, and the interior
+    ocean columns of the surface arrays (one contiguous run per slot).  The
+    surface side lives in one page-locked host allocation per direction
+    (remap sources then surface rows), as a host model keeps it."""
+    h2d = [(torch.from_numpy(g.spec.view(np.float64).copy()).pin_memory(), s) for g, s in zip(groups, S["spec_in"])]
+    d2h = [(torch.empty_like(s, device="cpu").pin_memory(), s) for s in S["spec_out"]]
+    df = S["dflux"]
+
+    def run(name, slot):
+        a = df[name]
+        return a[slot, 1, 1:-1] if a.dim() == 3 else a[1, 1:-1]
+
+    def host_block(devs, fill):
+        """One pinned buffer holding a view per device tensor, in order."""
+        n = sum(d.numel() for d in devs)
+        buf = torch.empty(n, dtype=torch.float64).pin_memory()
+        out, off = [], 0
+        for d in devs:
+            h = buf[off:off + d.numel()].view(d.shape)
+            if fill:
+                h.copy_(d.cpu())
+            out.append((h, d))
+            off += d.numel()
+        return out
+
+    ins = list(S["src"]) + [run(n, k) for n, slots in FLUX_H2D.items() for k in slots]
+    h2d += host_block(ins, True)
+    outs = [run(n, k) for n in dccm.FLUX_OUT + ["SfcTemp", "SfcAlbedo"] for k in FLUX_D2H_SLOTS.get(n, (0, 1, 2))]
+    d2h += host_block(outs, False)
+    return h2d, d2h
+
+
 def gpu_bench(args, w, inp, rank, world):
     import torch
     dccm = importlib.import_module("dennou-ccm_gb300")
@@ -368,10 +412,7 @@ def gpu_bench(args, w, inp, rank, world):
     roof.update({"kernel": dom, "traffic": None, "peak_source": src_peak, "stages": stages})
 
     # end to end through the public API with host buffers (pinned)
-    h2d = [(torch.from_numpy(g.spec.view(np.float64).copy()).pin_memory(), s) for g, s in zip(groups, S["spec_in"])]
-    h2d += [(torch.from_numpy(np.ascontiguousarray(g.src)).pin_memory(), s) for g, s in zip(groups, S["src"])]
-    d2h = [(torch.empty_like(s, device="cpu").pin_memory(), s) for s in S["spec_out"]]
-    d2h += [(torch.empty_like(S["dflux"][n], device="cpu").pin_memory(), S["dflux"][n]) for n in dccm.FLUX_OUT]
+    h2d, d2h = host_copies(S, groups, dccm, torch)
     h2d_bytes = sum(h.numel() * h.element_size() for h, _ in h2d)
     d2h_bytes = sum(h.numel() * h.element_size() for h, _ in d2h)
     for _ in range(max(3, args.warmup)):

@@ -4,26 +4,39 @@
 //
 // Two real latitude rows that mirror each other about the equator (jn, js)
 // travel through one complex FFT of length I = 32 R: z = g(jn) + i g(js).
-// Lane l holds the R samples z[32 r + l] in registers, and the transform is
-// the four-step factorisation I = R x 32:
-//   forward  (1) length-R DFT over r in registers,
-//            (2) twiddle e^{-2 pi i l k1 / I},
-//            (3) length-32 radix-2 decimation-in-frequency across the lanes
+// Lane l holds R samples in registers and the transform is the four-step
+// factorisation I = R x 32:
+//   forward  (1) length-R DFT over r of z[32 r + l] in registers,
+//            (2) twiddle e^{-2 pi i l k1 / I} (per-lane table [k1][l]),
+//            (3) length-32 radix-2 decimation in frequency across the lanes
 //                with __shfl_xor; lane l ends with Z[k1 + R brev5(l)];
 //   inverse  the same steps mirrored (decimation in time across lanes from
 //            bit-reversed input, conjugate twiddles, register DFT last), so
 //            lane l ends with z[32 r + l] and the row stores are coalesced.
-// Rows are read and written straight from/to global memory (lanes along
-// longitude); shared memory only stages the Fourier coefficients of the
-// CTA's block of field-levels (coalesced along c) and, in the forward
-// direction, the spectrum for separating the two real rows.  Twiddles come
-// from a table e^{-2 pi i t / I} evaluated in FP64 on the host.  Supported
-// lengths: R in {2, 3, 4, 6, 8, 12, 16, 24, 32}, i.e. I = 64 ... 1024.
+// Lane butterflies cost 8 instructions per complex value: the lane that
+// owns the twiddled operand multiplies before the exchange (inverse) or
+// after it (forward), the other lane multiplies by 1, and the sum or
+// difference is one FMA with a per-lane sign.  Lane twiddles are loaded
+// once per warp.
+//
+// Shared memory stages, per CTA (latitude pair jj, BB field-levels), the
+// Fourier coefficients of all m in planes of 16 R + 1 floats, one plane per
+// (row or parity, re/im, field-level); coefficient m sits at slot
+// (m mod R) * 16 + m / R.  A lane reads or writes the m = k1 + R k2 it owns
+// at k1 * 16 + k2 (consecutive across lanes), and the CTA-wide copy between
+// shared and global memory walks field-levels fastest (plane stride odd):
+// both sides are free of bank conflicts and the global side is coalesced.
+// Supported lengths: R in {2, 3, 4, 6, 8, 12, 16, 24, 32}, I = 64 ... 1024.
 //
 // Inverse: Z_m = A_m + i B_m and Z_{I-m} = conj(A_m) + i conj(B_m) from the
-// Fourier coefficients A (row jn) and B (row js); Re z and Im z are the rows.
-// Forward: A_m = (Z_m + conj Z_{I-m})/2, B_m = (Z_m - conj Z_{I-m})/(2i),
-// folded into E = (A + B)/I and O = (A - B)/I and written as G[m][p][jj][c].
+// Fourier coefficients A (row jn) and B (row js) in F[m][j][c]; Re z and
+// Im z are the rows, written as FP64.
+// Forward: Z_{I-m} comes from another lane by one shuffle (lane 31 - l,
+// register R - k1; for k1 = 0 lane brev5(32 - k2)); A_m = (Z_m + conj
+// Z_{I-m})/2, B_m = (Z_m - conj Z_{I-m})/(2i), folded into E = (A + B)/I and
+// O = (A - B)/I and written split into three BF16 planes
+// G3[s][(2m + p) Jh + jj][c] (p = 0: E, 1: O), the operand layout of the
+// tensor-core analysis.
 #include <string.h>
 
 #include "fp_conv.cuh"
@@ -32,39 +45,25 @@
 namespace dccm {
 namespace sht {
 
-template <typename T> struct Cx;
-template <> struct Cx<float> { using t = float2; };
-template <> struct Cx<double> { using t = double2; };
-
-// Grid values are FP64 in memory; the FP32 transform converts on the integer pipes.
-__device__ __forceinline__ float from_f64(double x, float) { return f64_to_f32_rn(x); }
-__device__ __forceinline__ double from_f64(double x, double) { return x; }
-__device__ __forceinline__ double to_f64(float x) { return f32_to_f64(x); }
-__device__ __forceinline__ double to_f64(double x) { return x; }
-
-template <typename C> __device__ __forceinline__ C cmk(decltype(C::x) x, decltype(C::x) y) {
-  C r;
-  r.x = x;
-  r.y = y;
-  return r;
-}
-template <typename C> __device__ __forceinline__ C cadd(C a, C b) { a.x += b.x; a.y += b.y; return a; }
-template <typename C> __device__ __forceinline__ C csub(C a, C b) { a.x -= b.x; a.y -= b.y; return a; }
-template <typename C> __device__ __forceinline__ C cmul(C a, C b) {
-  C r;
-  r.x = a.x * b.x - a.y * b.y;
-  r.y = a.x * b.y + a.y * b.x;
-  return r;
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 // twiddle tw[t] = e^{-2 pi i t / I}; sign +1 uses its conjugate
-template <typename C> __device__ __forceinline__ C twid(const C *tw, int t, int sign) {
-  C w = tw[t];
+__device__ __forceinline__ float2 twid(const float2 *tw, int t, int sign) {
+  float2 w = __ldg(tw + t);
   if (sign > 0) w.y = -w.y;
   return w;
 }
-template <typename C> __device__ __forceinline__ C shfl_xor_c(C v, int m) {
+__device__ __forceinline__ float2 shfl_xor_c(float2 v, int m) {
   v.x = __shfl_xor_sync(0xffffffffu, v.x, m);
   v.y = __shfl_xor_sync(0xffffffffu, v.y, m);
+  return v;
+}
+__device__ __forceinline__ float2 shfl_c(float2 v, int src) {
+  v.x = __shfl_sync(0xffffffffu, v.x, src);
+  v.y = __shfl_sync(0xffffffffu, v.y, src);
   return v;
 }
 __device__ __forceinline__ int brev5(int l) { return (int)(__brev((unsigned)l) >> 27); }
@@ -72,21 +71,20 @@ __device__ __forceinline__ int brev5(int l) { return (int)(__brev((unsigned)l) >
 // In-register DFT of length R: v[k] <- sum_r v[r] e^{sign 2 pi i r k / R}.
 // Even lengths split into two halves (decimation in time), 3 is direct.
 template <int R> struct RegDft {
-  template <typename C> __device__ __forceinline__ static void run(C *v, const C *tw, int I, int sign) {
+  __device__ __forceinline__ static void run(float2 *v, const float2 *tw, int I, int sign) {
     if constexpr (R == 1) {
       return;
     } else if constexpr (R == 2) {
-      const C a = v[0], b = v[1];
+      const float2 a = v[0], b = v[1];
       v[0] = cadd(a, b);
       v[1] = csub(a, b);
     } else if constexpr (R == 3) {
-      using S = decltype(v[0].x);
-      const C t1 = cadd(v[1], v[2]);
-      const C d = csub(v[1], v[2]);
-      const S h = (S)0.86602540378443864676 * (S)sign;  // sign * sqrt(3)/2
-      C mm, q;
-      mm.x = v[0].x - (S)0.5 * t1.x;
-      mm.y = v[0].y - (S)0.5 * t1.y;
+      const float2 t1 = cadd(v[1], v[2]);
+      const float2 d = csub(v[1], v[2]);
+      const float h = 0.86602540378443864676f * (float)sign;  // sign * sqrt(3)/2
+      float2 mm, q;
+      mm.x = v[0].x - 0.5f * t1.x;
+      mm.y = v[0].y - 0.5f * t1.y;
       q.x = -d.y * h;  // i * sign * sqrt(3)/2 * d
       q.y = d.x * h;
       v[0] = cadd(v[0], t1);
@@ -95,7 +93,7 @@ template <int R> struct RegDft {
     } else {
       static_assert(R % 2 == 0, "length");
       constexpr int H = R / 2;
-      C e[H], o[H];
+      float2 e[H], o[H];
 #pragma unroll
       for (int i = 0; i < H; ++i) {
         e[i] = v[2 * i];
@@ -105,7 +103,7 @@ template <int R> struct RegDft {
       RegDft<H>::run(o, tw, I, sign);
 #pragma unroll
       for (int k = 0; k < H; ++k) {
-        const C t = k == 0 ? o[0] : cmul(o[k], twid(tw, k * (I / R), sign));
+        const float2 t = k == 0 ? o[0] : cmul(o[k], twid(tw, k * (I / R), sign));
         v[k] = cadd(e[k], t);
         v[k + H] = csub(e[k], t);
       }
@@ -113,164 +111,195 @@ template <int R> struct RegDft {
   }
 };
 
+// Per-lane twiddles of the five lane stages: stage s exchanges with lane
+// l ^ h (forward h = 16 >> s, inverse h = 1 << s); the upper lane (l & h)
+// multiplies by e^{-+2 pi i (l & (h-1)) / (2h)}, the lower one by 1.
+template <int R>
+__device__ __forceinline__ void lane_twiddles(const float2 *tw, int lane, bool inv, float2 (&w)[5]) {
+  constexpr int I = 32 * R;
+#pragma unroll
+  for (int s = 0; s < 5; ++s) {
+    const int h = inv ? (1 << s) : (16 >> s);
+    w[s] = make_float2(1.f, 0.f);
+    if (lane & h) w[s] = twid(tw, (lane & (h - 1)) * (I / (2 * h)), inv ? 1 : -1);
+  }
+}
+
 // Forward complex FFT of one row held as v[r] = z[32 r + lane];
 // on return v[k1] = Z[k1 + R brev5(lane)].
-template <int R, typename C>
-__device__ __forceinline__ void warp_fft_fwd(C (&v)[R], const C *tw, int lane) {
+template <int R>
+__device__ __forceinline__ void warp_fft_fwd(float2 (&v)[R], const float2 *tw, const float2 *twl,
+                                             const float2 (&w)[5], int lane) {
   constexpr int I = 32 * R;
   RegDft<R>::run(v, tw, I, -1);
 #pragma unroll
-  for (int k = 1; k < R; ++k)
-    if (lane) v[k] = cmul(v[k], twid(tw, lane * k, -1));
+  for (int k = 1; k < R; ++k) v[k] = cmul(v[k], __ldg(twl + k * 32 + lane));
 #pragma unroll
-  for (int h = 16; h >= 1; h >>= 1) {
-    const bool upper = lane & h;
-    const C w = twid(tw, (lane & (h - 1)) * (I / (2 * h)), -1);
+  for (int s = 0; s < 5; ++s) {
+    const int h = 16 >> s;
+    const float sg = (lane & h) ? -1.f : 1.f;
 #pragma unroll
     for (int k = 0; k < R; ++k) {
-      const C p = shfl_xor_c(v[k], h);
-      v[k] = upper ? cmul(csub(p, v[k]), w) : cadd(v[k], p);
+      // lower: a + b; upper: (a - b) w  (the lower lane holds a)
+      const float2 p = shfl_xor_c(v[k], h);
+      const float2 t = make_float2(fmaf(sg, v[k].x, p.x), fmaf(sg, v[k].y, p.y));
+      v[k] = cmul(t, w[s]);
     }
   }
 }
 
 // Inverse (unnormalised) FFT of one row held as v[k1] = Z[k1 + R brev5(lane)];
 // on return v[r] = z[32 r + lane].
-template <int R, typename C>
-__device__ __forceinline__ void warp_fft_inv(C (&v)[R], const C *tw, int lane) {
+template <int R>
+__device__ __forceinline__ void warp_fft_inv(float2 (&v)[R], const float2 *tw, const float2 *twl,
+                                             const float2 (&w)[5], int lane) {
   constexpr int I = 32 * R;
 #pragma unroll
-  for (int h = 1; h <= 16; h <<= 1) {
-    const bool upper = lane & h;
-    const C w = twid(tw, (lane & (h - 1)) * (I / (2 * h)), +1);
+  for (int s = 0; s < 5; ++s) {
+    const int h = 1 << s;
+    const float sg = (lane & h) ? -1.f : 1.f;
 #pragma unroll
     for (int k = 0; k < R; ++k) {
-      const C p = shfl_xor_c(v[k], h);
-      // top = a + w b, bottom = a - w b, with a the lower lane's value
-      v[k] = upper ? csub(p, cmul(v[k], w)) : cadd(v[k], cmul(p, w));
+      // lower: a + w b; upper: a - w b  (the upper lane holds b)
+      const float2 x = cmul(v[k], w[s]);
+      const float2 p = shfl_xor_c(x, h);
+      v[k] = make_float2(fmaf(sg, x.x, p.x), fmaf(sg, x.y, p.y));
     }
   }
 #pragma unroll
-  for (int k = 1; k < R; ++k)
-    if (lane) v[k] = cmul(v[k], twid(tw, lane * k, +1));
+  for (int k = 1; k < R; ++k) {
+    float2 t = __ldg(twl + k * 32 + lane);
+    t.y = -t.y;
+    v[k] = cmul(v[k], t);
+  }
   RegDft<R>::run(v, tw, I, +1);
 }
 
+constexpr int FFT_MAXG = 8;
+struct FftGroup {
+  int N, J, batch, BB, lbb, R, blk0, C2Bp;  // lbb = log2(BB)
+  const void *in;
+  void *out;
+  const float2 *tw, *twl;
+};
+struct FftLaunch {
+  FftGroup g[FFT_MAXG];
+  int ngroups;
+};
+
+template <int R> __device__ __forceinline__ int slot_of(int m) { return (m % R) * 16 + m / R; }
+
 // ------------------------------------------------------------- inverse
-// One CTA: latitude pair jj, field-levels [by*BB, by*BB + BB).
-template <typename T, int R>
-__device__ __forceinline__ void fft_inv_block(int N, int J, int batch, int BB, const T *__restrict__ F,
-                                              double *__restrict__ grid, const typename Cx<T>::t *__restrict__ twg,
-                                              int jj, int by, unsigned char *smem_raw) {
-  using C = typename Cx<T>::t;
-  constexpr int I = 32 * R;
-  const int Jh = J / 2;
+// One CTA: latitude pair jj, field-levels [by*BB, by*BB + BB); warp bl
+// transforms field-level b0 + bl.  Planes (row, re/im, field-level).
+template <int R>
+__device__ __forceinline__ void fft_inv_block(const FftGroup &G, int jj, int by, float *st) {
+  constexpr int I = 32 * R, PS = R * 16 + 1;
+  const int N = G.N, J = G.J, Jh = J / 2, lbb = G.lbb, lcw = G.lbb + 1;
   const int jn = Jh + jj, js = Jh - 1 - jj;
-  const int b0 = by * BB;
-  const int nb = min(BB, batch - b0);
-  const int64_t C2B = 2LL * batch;
-  const int cw = 2 * BB;
-  C *tw = reinterpret_cast<C *>(smem_raw);
-  T *stA = reinterpret_cast<T *>(tw + I);  // [N+1][2BB] row jn
-  T *stB = stA + (size_t)(N + 1) * cw;     // [N+1][2BB] row js
-  for (int t = threadIdx.x; t < I; t += blockDim.x) tw[t] = twg[t];
-  for (int t = threadIdx.x; t < (N + 1) * cw; t += blockDim.x) {
-    const int m = t / cw, c = t % cw;
-    T va = 0, vb = 0;
-    if (c < 2 * nb) {
-      va = F[((int64_t)m * J + jn) * C2B + 2LL * b0 + c];
-      vb = F[((int64_t)m * J + js) * C2B + 2LL * b0 + c];
-    }
-    stA[t] = va;
-    stB[t] = vb;
+  const int b0 = by * G.BB;
+  const int nb = min(G.BB, G.batch - b0);
+  const long long C2B = 2LL * G.batch;
+  const float *F = static_cast<const float *>(G.in);
+  const int tot = (N + 1) << (lcw + 1);  // (m, row, c), c fastest
+  for (int t = threadIdx.x; t < tot; t += blockDim.x) {
+    const int c = t & ((1 << lcw) - 1);
+    const int row = (t >> lcw) & 1;
+    const int m = t >> (lcw + 1);
+    float v = 0.f;
+    if (c < 2 * nb) v = F[((long long)m * J + (row ? js : jn)) * C2B + 2LL * b0 + c];
+    st[(((row * 2 + (c & 1)) << lbb) + (c >> 1)) * PS + slot_of<R>(m)] = v;
   }
   __syncthreads();
-  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-  const int nw = blockDim.x / 32;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   const int k2 = brev5(lane);
+  float2 w[5];
+  lane_twiddles<R>(G.tw, lane, true, w);
   for (int bl = warp; bl < nb; bl += nw) {
-    C v[R];
+    const float *Ar = st + ((0 << lbb) + bl) * PS, *Ai = st + ((1 << lbb) + bl) * PS;
+    const float *Br = st + ((2 << lbb) + bl) * PS, *Bi = st + ((3 << lbb) + bl) * PS;
+    float2 v[R];
 #pragma unroll
     for (int k1 = 0; k1 < R; ++k1) {
       const int k = k1 + R * k2;
-      C z = cmk<C>(0, 0);
-      if (k <= N) {
-        const T ar = stA[k * cw + 2 * bl], ai = k ? stA[k * cw + 2 * bl + 1] : (T)0;
-        const T br = stB[k * cw + 2 * bl], bi = k ? stB[k * cw + 2 * bl + 1] : (T)0;
-        z = cmk<C>(ar - bi, ai + br);
-      } else if (k >= I - N) {
-        const int m = I - k;
-        const T ar = stA[m * cw + 2 * bl], ai = stA[m * cw + 2 * bl + 1];
-        const T br = stB[m * cw + 2 * bl], bi = stB[m * cw + 2 * bl + 1];
-        z = cmk<C>(ar + bi, br - ai);
+      float2 z = make_float2(0.f, 0.f);
+      if (k <= N) {  // m = k: k / R = k2, k mod R = k1
+        const int sl = k1 * 16 + k2;
+        const float ar = Ar[sl], br = Br[sl];
+        const float ai = k ? Ai[sl] : 0.f, bi = k ? Bi[sl] : 0.f;
+        z = make_float2(ar - bi, ai + br);
+      } else if (k >= I - N) {  // m = I - k
+        const int sl = k1 ? (R - k1) * 16 + (31 - k2) : 32 - k2;
+        const float ar = Ar[sl], ai = Ai[sl], br = Br[sl], bi = Bi[sl];
+        z = make_float2(ar + bi, br - ai);
       }
       v[k1] = z;
     }
-    warp_fft_inv<R>(v, tw, lane);
-    double *gn = grid + ((int64_t)(b0 + bl) * J + jn) * I;
-    double *gs = grid + ((int64_t)(b0 + bl) * J + js) * I;
+    warp_fft_inv<R>(v, G.tw, G.twl, w, lane);
+    double *gn = static_cast<double *>(G.out) + ((long long)(b0 + bl) * J + jn) * I;
+    double *gs = static_cast<double *>(G.out) + ((long long)(b0 + bl) * J + js) * I;
 #pragma unroll
     for (int r = 0; r < R; ++r) {
-      gn[32 * r + lane] = to_f64(v[r].x);
-      gs[32 * r + lane] = to_f64(v[r].y);
+      gn[32 * r + lane] = f32_to_f64(v[r].x);
+      gs[32 * r + lane] = f32_to_f64(v[r].y);
     }
   }
 }
 
 // ------------------------------------------------------------- forward
-template <typename T, int R>
-__device__ __forceinline__ void fft_fwd_block(int N, int J, int batch, int BB, const double *__restrict__ grid,
-                                              T *__restrict__ G, const typename Cx<T>::t *__restrict__ twg,
-                                              int jj, int by, unsigned char *smem_raw) {
-  using C = typename Cx<T>::t;
-  constexpr int I = 32 * R;
-  const int Jh = J / 2;
+// Planes (parity, c) with c = 2 bl + re/im.
+template <int R>
+__device__ __forceinline__ void fft_fwd_block(const FftGroup &G, int jj, int by, float *st) {
+  constexpr int I = 32 * R, PS = R * 16 + 1;
+  const int N = G.N, J = G.J, Jh = J / 2, lcw = G.lbb + 1;
   const int jn = Jh + jj, js = Jh - 1 - jj;
-  const int b0 = by * BB;
-  const int nb = min(BB, batch - b0);
-  const int64_t C2B = 2LL * batch;
-  const int cw = 2 * BB;
-  const int nw = blockDim.x / 32;
-  C *tw = reinterpret_cast<C *>(smem_raw);
-  C *zb = tw + I;                                        // [nw][I] spectra
-  T *stE = reinterpret_cast<T *>(zb + (size_t)nw * I);  // [N+1][2BB]
-  T *stO = stE + (size_t)(N + 1) * cw;
-  for (int t = threadIdx.x; t < I; t += blockDim.x) tw[t] = twg[t];
-  __syncthreads();
-  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-  C *Z = zb + (size_t)warp * I;
+  const int b0 = by * G.BB;
+  const int nb = min(G.BB, G.batch - b0);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   const int k2 = brev5(lane);
-  const T invI = (T)1 / (T)I;
+  const int src0 = brev5((32 - k2) & 31);
+  float2 w[5];
+  lane_twiddles<R>(G.tw, lane, false, w);
+  const float invI = 1.f / (float)I;
   for (int bl = warp; bl < nb; bl += nw) {
-    const double *gn = grid + ((int64_t)(b0 + bl) * J + jn) * I;
-    const double *gs = grid + ((int64_t)(b0 + bl) * J + js) * I;
-    C v[R];
+    const double *gn = static_cast<const double *>(G.in) + ((long long)(b0 + bl) * J + jn) * I;
+    const double *gs = static_cast<const double *>(G.in) + ((long long)(b0 + bl) * J + js) * I;
+    float2 v[R];
 #pragma unroll
-    for (int r = 0; r < R; ++r) {
-      v[r].x = from_f64(gn[32 * r + lane], T());
-      v[r].y = from_f64(gs[32 * r + lane], T());
-    }
-    warp_fft_fwd<R>(v, tw, lane);
+    for (int r = 0; r < R; ++r) v[r] = make_float2(f64_to_f32_rn(gn[32 * r + lane]), f64_to_f32_rn(gs[32 * r + lane]));
+    warp_fft_fwd<R>(v, G.tw, G.twl, w, lane);
+    float *E = st + ((0 << lcw) + 2 * bl) * PS, *O = st + ((1 << lcw) + 2 * bl) * PS;
 #pragma unroll
-    for (int k1 = 0; k1 < R; ++k1) Z[k1 + R * k2] = v[k1];
-    __syncwarp();
-    for (int m = lane; m <= N; m += 32) {
-      const C zm = Z[m], zc = Z[(I - m) % I];
-      const T ar = (T)0.5 * (zm.x + zc.x), ai = (T)0.5 * (zm.y - zc.y);
-      const T br = (T)0.5 * (zm.y + zc.y), bi = (T)-0.5 * (zm.x - zc.x);
-      stE[m * cw + 2 * bl] = (ar + br) * invI;
-      stE[m * cw + 2 * bl + 1] = m ? (ai + bi) * invI : (T)0;
-      stO[m * cw + 2 * bl] = (ar - br) * invI;
-      stO[m * cw + 2 * bl + 1] = m ? (ai - bi) * invI : (T)0;
+    for (int k1 = 0; k1 < R; ++k1) {
+      const float2 zc = k1 ? shfl_c(v[(R - k1) % R], 31 - lane) : shfl_c(v[0], src0);  // Z[I - m]
+      const int m = k1 + R * k2;
+      if (m <= N) {
+        const float2 zm = v[k1];
+        const float ar = 0.5f * (zm.x + zc.x), ai = 0.5f * (zm.y - zc.y);
+        const float br = 0.5f * (zm.y + zc.y), bi = -0.5f * (zm.x - zc.x);
+        const int sl = k1 * 16 + k2;
+        E[sl] = (ar + br) * invI;
+        E[PS + sl] = m ? (ai + bi) * invI : 0.f;
+        O[sl] = (ar - br) * invI;
+        O[PS + sl] = m ? (ai - bi) * invI : 0.f;
+      }
     }
-    __syncwarp();
   }
   __syncthreads();
-  for (int t = threadIdx.x; t < (N + 1) * cw; t += blockDim.x) {
-    const int m = t / cw, c = t % cw;
+  unsigned short *G3 = static_cast<unsigned short *>(G.out);
+  const size_t plane = (size_t)(N + 1) * 2 * Jh * G.C2Bp;
+  const int tot = (N + 1) << (lcw + 1);  // (m, p, c), c fastest
+  for (int t = threadIdx.x; t < tot; t += blockDim.x) {
+    const int c = t & ((1 << lcw) - 1);
+    const int p = (t >> lcw) & 1;
+    const int m = t >> (lcw + 1);
     if (c < 2 * nb) {
-      G[(((int64_t)m * 2 + 0) * Jh + jj) * C2B + 2LL * b0 + c] = stE[t];
-      G[(((int64_t)m * 2 + 1) * Jh + jj) * C2B + 2LL * b0 + c] = stO[t];
+      unsigned short h, md, lo;
+      split3f_bits(st[((p << lcw) + c) * PS + slot_of<R>(m)], h, md, lo);
+      unsigned short *o = G3 + ((size_t)(2 * m + p) * Jh + jj) * G.C2Bp + 2 * b0 + c;
+      o[0] = h;
+      o[plane] = md;
+      o[2 * plane] = lo;
     }
   }
 }
@@ -279,32 +308,19 @@ __device__ __forceinline__ void fft_fwd_block(int N, int J, int batch, int BB, c
 // Several truncation groups in one launch: CTA blockIdx.x belongs to the
 // group whose block range contains it; the group's length selects the
 // register FFT (cases up to RMAX are compiled in).
-constexpr int FFT_MAXG = 8;
-struct FftGroup {
-  int N, J, batch, BB, R, blk0;
-  const void *in;
-  void *out;
-  const void *tw;
-};
-struct FftLaunch {
-  FftGroup g[FFT_MAXG];
-  int ngroups;
-};
-
-template <typename T, int R, int RMAX, bool FWD>
-__device__ __forceinline__ void dispatch_case(const FftGroup &G, int jj, int by, unsigned char *sm) {
+template <int R, int RMAX, bool FWD>
+__device__ __forceinline__ void dispatch_case(const FftGroup &G, int jj, int by, float *st) {
   if constexpr (R <= RMAX) {
-    using C = typename Cx<T>::t;
-    if (FWD)
-      fft_fwd_block<T, R>(G.N, G.J, G.batch, G.BB, (const double *)G.in, (T *)G.out, (const C *)G.tw, jj, by, sm);
-    else
-      fft_inv_block<T, R>(G.N, G.J, G.batch, G.BB, (const T *)G.in, (double *)G.out, (const C *)G.tw, jj, by, sm);
+    if (FWD) fft_fwd_block<R>(G, jj, by, st);
+    else fft_inv_block<R>(G, jj, by, st);
   }
 }
 
-template <typename T, int RMAX, bool FWD>
-__global__ void __launch_bounds__(256) fft_multi_kernel(const __grid_constant__ FftLaunch L) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+// Up to 16 field-levels (512 threads) per CTA for R <= 8; 8 for longer
+// rows, whose 32-register-pair rows need more than 128 registers a thread.
+template <int RMAX, bool FWD>
+__global__ void __launch_bounds__(RMAX <= 8 ? 512 : 256) fft_multi_kernel(const __grid_constant__ FftLaunch L) {
+  extern __shared__ __align__(16) float st[];
   int gi = 0;
   while (gi + 1 < L.ngroups && (int)blockIdx.x >= L.g[gi + 1].blk0) ++gi;
   const FftGroup &G = L.g[gi];
@@ -312,37 +328,38 @@ __global__ void __launch_bounds__(256) fft_multi_kernel(const __grid_constant__ 
   const int Jh = G.J / 2;
   const int jj = lb % Jh, by = lb / Jh;
   switch (G.R) {
-    case 2: dispatch_case<T, 2, RMAX, FWD>(G, jj, by, smem_raw); break;
-    case 3: dispatch_case<T, 3, RMAX, FWD>(G, jj, by, smem_raw); break;
-    case 4: dispatch_case<T, 4, RMAX, FWD>(G, jj, by, smem_raw); break;
-    case 6: dispatch_case<T, 6, RMAX, FWD>(G, jj, by, smem_raw); break;
-    case 8: dispatch_case<T, 8, RMAX, FWD>(G, jj, by, smem_raw); break;
-    case 12: dispatch_case<T, 12, RMAX, FWD>(G, jj, by, smem_raw); break;
-    case 16: dispatch_case<T, 16, RMAX, FWD>(G, jj, by, smem_raw); break;
-    case 24: dispatch_case<T, 24, RMAX, FWD>(G, jj, by, smem_raw); break;
-    case 32: dispatch_case<T, 32, RMAX, FWD>(G, jj, by, smem_raw); break;
+    case 2: dispatch_case<2, RMAX, FWD>(G, jj, by, st); break;
+    case 3: dispatch_case<3, RMAX, FWD>(G, jj, by, st); break;
+    case 4: dispatch_case<4, RMAX, FWD>(G, jj, by, st); break;
+    case 6: dispatch_case<6, RMAX, FWD>(G, jj, by, st); break;
+    case 8: dispatch_case<8, RMAX, FWD>(G, jj, by, st); break;
+    case 12: dispatch_case<12, RMAX, FWD>(G, jj, by, st); break;
+    case 16: dispatch_case<16, RMAX, FWD>(G, jj, by, st); break;
+    case 24: dispatch_case<24, RMAX, FWD>(G, jj, by, st); break;
+    case 32: dispatch_case<32, RMAX, FWD>(G, jj, by, st); break;
     default: break;
   }
 }
 
-// Field-levels per CTA (one warp each) that fit a shared-memory budget.
-static size_t fft_smem(int N, int I, int bb, bool fwd) {
-  size_t s = (size_t)I * sizeof(float2) + (size_t)(N + 1) * 2 * bb * 2 * sizeof(float);
-  if (fwd) s += (size_t)bb * I * sizeof(float2);
-  return s;
-}
+// Staging of one CTA: four planes of 16 R + 1 floats per field-level.
+static size_t fft_smem(int R, int bb) { return (size_t)4 * bb * (R * 16 + 1) * sizeof(float); }
 
-// One launch over ngroups plans (FP32).  in/out per group as in the single case.
+// One launch over ngroups plans (FP32).  Inverse: in[g] = F, out[g] = grid;
+// forward: in[g] = grid, out[g] = G3 (the plan's Fourier buffer).
 int fft_multi(Plan *const *plans, const int *batch, const void *const *in, void *const *out, int ngroups, bool fwd,
               cudaStream_t s) {
   if (ngroups < 1 || ngroups > FFT_MAXG) return DCCM_ERR_UNSUPPORTED;
-  const size_t budget = 96 * 1024;
-  int BB = tunables().fft_bb > 0 && tunables().fft_bb <= 8 ? tunables().fft_bb : 8, rmax = 2;
+  const size_t budget = 100 * 1024;
+  const int tb = tunables().fft_bb;
+  int BB = (tb == 4 || tb == 8 || tb == 16) ? tb : 8, rmax = 2;
   for (int g = 0; g < ngroups; ++g) {
     if (!fft_length_supported(plans[g]->I)) return DCCM_ERR_UNSUPPORTED;
     rmax = plans[g]->I / 32 > rmax ? plans[g]->I / 32 : rmax;
-    while (BB > 1 && fft_smem(plans[g]->N, plans[g]->I, BB, fwd) > budget) BB /= 2;
+    while (BB > 1 && fft_smem(plans[g]->I / 32, BB) > budget) BB /= 2;
   }
+  if (rmax > 8 && BB > 8) BB = 8;
+  int lbb = 0;
+  while ((1 << lbb) < BB) ++lbb;
   FftLaunch L;
   memset(&L, 0, sizeof L);
   int nblk = 0, ng = 0;
@@ -355,13 +372,16 @@ int fft_multi(Plan *const *plans, const int *batch, const void *const *in, void 
     G.J = P.J;
     G.batch = batch[g];
     G.BB = BB;
+    G.lbb = lbb;
     G.R = P.I / 32;
     G.blk0 = nblk;
+    G.C2Bp = P.C2Bp;
     G.in = in[g];
     G.out = out[g];
     G.tw = P.d_tw32;
+    G.twl = P.d_twl32;
     nblk += P.Jh * ((batch[g] + BB - 1) / BB);
-    const size_t sm = fft_smem(P.N, P.I, BB, fwd);
+    const size_t sm = fft_smem(G.R, BB);
     smem = sm > smem ? sm : smem;
   }
   L.ngroups = ng;
@@ -372,8 +392,8 @@ int fft_multi(Plan *const *plans, const int *batch, const void *const *in, void 
     DCCM_LAUNCH_CHECK();
     return DCCM_OK;
   };
-  if (rmax <= 8) return fwd ? go(fft_multi_kernel<float, 8, true>) : go(fft_multi_kernel<float, 8, false>);
-  return fwd ? go(fft_multi_kernel<float, 32, true>) : go(fft_multi_kernel<float, 32, false>);
+  if (rmax <= 8) return fwd ? go(fft_multi_kernel<8, true>) : go(fft_multi_kernel<8, false>);
+  return fwd ? go(fft_multi_kernel<32, true>) : go(fft_multi_kernel<32, false>);
 }
 
 bool fft_length_supported(int I) {

@@ -9,6 +9,7 @@
 // even.  Operands outside the normal FP32 range (zero excepted), infinities
 // and NaNs take the hardware instruction.
 #pragma once
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 namespace dccm {
@@ -43,6 +44,19 @@ __device__ __forceinline__ float f64_to_f32_rn(double d) {
   // increments the exponent (and reaches infinity at the top of the range)
   if (rem > 0x10000000u || (rem == 0x10000000u && (m & 1u))) r += 1u;
   return __uint_as_float(r);
+}
+
+// Exact split of an FP32 value into three BF16 numbers x = hi + mid + lo
+// (FP32 arithmetic: each residual is exact because it has fewer
+// significant bits than FP32), returned as raw bits.
+__device__ __forceinline__ void split3f_bits(float x, unsigned short &h, unsigned short &m, unsigned short &l) {
+  const __nv_bfloat16 bh = __float2bfloat16_rn(x);
+  const float r1 = x - __bfloat162float(bh);
+  const __nv_bfloat16 bm = __float2bfloat16_rn(r1);
+  const __nv_bfloat16 bl = __float2bfloat16_rn(r1 - __bfloat162float(bm));
+  h = __bfloat16_as_ushort(bh);
+  m = __bfloat16_as_ushort(bm);
+  l = __bfloat16_as_ushort(bl);
 }
 
 }  // namespace dccm

@@ -10,24 +10,24 @@
 //            s_{m+p+2k}^m[c] = D_p[c][k],  PW = (w/2) Pbar.
 // Every operand x is split as x = hi + mid + lo (three BF16 numbers, 24
 // significant bits) and the six products hi*hi, hi*mid, mid*hi, hi*lo,
-// lo*hi, mid*mid are accumulated (dropped terms are below 2^-24 relative).
+// lo*hi, mid*mid are accumulated (dropped terms are below 2^-24 relative);
+// hi*hi has an accumulator of its own so the small terms keep their bits.
 //
-// Warp roles (288 threads):
-//   warps 0-3  producers: thread t owns row t of the A tile; it reads the
-//              FP64 spectra (inverse) or the FP32 folded Fourier
-//              coefficients (forward), splits them and stores the three
-//              BF16 planes straight into the 128-byte-swizzled K-major
-//              shared-memory layout the MMA reads; thread 0 also issues
-//              the TMA (cp.async.bulk.tensor) loads of the pre-split Pbar
-//              tiles, which the tensor map swizzles the same way;
-//   warps 4-7  epilogue: tcgen05.ld of the accumulators (warp w reads TMEM
-//              lanes 32(w%4)..), parity fold, coalesced stores along c;
-//   warp 8     TMEM allocation and the single MMA-issuing thread.
-// Two shared-memory stages (A and B of one 64-wide K chunk) and two TMEM
-// accumulator sets let the producers, the MMA and the epilogue of
-// consecutive items overlap.  Every mbarrier wait is bounded by a 1 s
-// globaltimer limit; on expiry the kernel records an error code, stops
-// issuing work, and still frees its TMEM.
+// Both operands arrive by TMA (cp.async.bulk.tensor) already split into BF16
+// planes and swizzled (128 B) by the tensor maps:
+//   A inverse  Apack[s][c][x], K-major: written by pack_spectra_kernel from
+//              the FP64 spectra (one bandwidth-bound pass, all SMs);
+//   A forward  G3[s][(2m+p) Jh + jj][c], MN-major (c contiguous): written
+//              split by the forward FFT;
+//   B          the pre-split Pbar tiles built at plan creation.
+// Warp roles (192 threads): warp 0 lane 0 issues the TMA loads of a stage
+// (six boxes of A and B per 64-wide K chunk); warp 1 allocates TMEM and its
+// lane 0 issues the MMAs; warps 2-5 are the epilogue (tcgen05.ld of the
+// accumulators, warp w reading TMEM lanes 32 (w % 4) .., parity fold,
+// stores coalesced along c).  Two shared-memory stages and two TMEM
+// accumulator sets overlap loads, MMAs and epilogue of consecutive items.
+// Every mbarrier wait is bounded by a 1 s globaltimer limit; on expiry the
+// kernel records an error code, stops issuing work, and still frees its TMEM.
 #include <cuda_bf16.h>
 #include <string.h>
 
@@ -37,9 +37,9 @@
 namespace dccm {
 namespace sht {
 
-constexpr int TC_THREADS = 288;
-constexpr int A_SPLIT_BYTES = 128 * 128;     // 128 rows x 64 bf16
-constexpr int B_SPLIT_BYTES = 128 * 128;     // up to 128 rows x 64 bf16
+constexpr int TC_THREADS = 192;
+constexpr int A_SPLIT_BYTES = 128 * 128;     // 128 rows (c) x 64 bf16 (K)
+constexpr int B_SPLIT_BYTES = 128 * 128;     // 128 rows (N) x 64 bf16 (K)
 constexpr int STAGE_BYTES = 3 * A_SPLIT_BYTES + 3 * B_SPLIT_BYTES;  // 96 KB
 constexpr int NSTAGE = 2;
 constexpr int TMEM_COLS = 512;
@@ -50,19 +50,17 @@ struct MInfo {
   int nr, nq;      // rows per tile (N extent, multiple of 16), K chunks per parity
   int kv0, kv1;    // valid K per parity
   int nv0, nv1;    // valid N per parity
+  int x0, x1;      // A operand coordinate of (m, p): Apack column / G3 row
 };
 
 struct TcArgs {
   int dir;  // 0 inverse, 1 forward
-  int N, Jh, batch, nct;
+  int N, Jh, batch;
   int ntmax;  // TMEM columns per accumulator (64 or 128)
   int nacc;   // accumulator sets in TMEM (2: double buffered, 1)
   long long ncoef;
-  int items_per_ct;
   const MInfo *mi;
-  const int *pre;  // prefix of n-tiles over m (N+2 entries)
-  const double *spec_in;
-  const float *G;
+  const int4 *items;  // (m, ct, nt, -)
   float *F;
   double *spec_out;
   int *err;
@@ -116,14 +114,19 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *b, uint32_t parity, int *err
     }
   }
 }
-__device__ __forceinline__ void fence_proxy_async() {
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
 __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y, uint64_t *bar) {
   asm volatile(
       "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
       "[%4];" ::"r"(smem_u32(dst)),
       "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int x, int y, int z,
+                                            uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+      "[%5];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
       : "memory");
 }
 __device__ __forceinline__ void tc_fence_before() {
@@ -132,19 +135,24 @@ __device__ __forceinline__ void tc_fence_before() {
 __device__ __forceinline__ void tc_fence_after() {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
-// K-major operand, 128-byte swizzle, 8-row groups 1024 bytes apart.
-__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+// Shared-memory operand descriptor, 128-byte swizzle, 8-row groups 1024
+// bytes apart (stride byte offset).  K-major: the leading byte offset is
+// unused.  MN-major: it is the distance between the 64-element (128-byte)
+// column blocks along M.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo) {
   uint64_t d = 0;
   d |= (uint64_t)((addr >> 4) & 0x3FFF);
-  d |= (uint64_t)1 << 16;                 // leading byte offset (unused for swizzled K-major)
-  d |= (uint64_t)(1024 >> 4) << 32;       // stride byte offset
-  d |= (uint64_t)1 << 46;                 // descriptor version (sm_100 family)
-  d |= (uint64_t)2 << 61;                 // SWIZZLE_128B
+  d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;  // leading byte offset
+  d |= (uint64_t)(1024 >> 4) << 32;            // stride byte offset
+  d |= (uint64_t)1 << 46;                      // descriptor version (sm_100 family)
+  d |= (uint64_t)2 << 61;                      // SWIZZLE_128B
   return d;
 }
-// kind::f16 instruction descriptor: BF16 x BF16 -> F32, both K-major, M = 128.
-__device__ __forceinline__ uint32_t idesc_bf16(int n) {
-  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+// kind::f16 instruction descriptor: BF16 x BF16 -> F32, M = 128, B K-major,
+// A K-major (a_mn = 0) or MN-major (a_mn = 1, bit 15).
+__device__ __forceinline__ uint32_t idesc_bf16(int n, int a_mn) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)a_mn << 15) | ((uint32_t)(n >> 3) << 17) |
+         ((uint32_t)(128 >> 4) << 24);
 }
 __device__ __forceinline__ void mma_bf16(uint32_t dtmem, uint64_t da, uint64_t db, uint32_t idesc, int acc) {
   asm volatile(
@@ -182,48 +190,24 @@ __device__ __forceinline__ void split3(double x, __nv_bfloat16 &h, __nv_bfloat16
   l = __double2bfloat16(r);
 }
 
-// Exact split of an FP32 value into three BF16 numbers (FP32 arithmetic:
-// each residual is exact because it has fewer significant bits than FP32).
-__device__ __forceinline__ void split3f(float x, __nv_bfloat16 &h, __nv_bfloat16 &m, __nv_bfloat16 &l) {
-  h = __float2bfloat16_rn(x);
-  const float r1 = x - __bfloat162float(h);
-  m = __float2bfloat16_rn(r1);
-  l = __float2bfloat16_rn(r1 - __bfloat162float(m));
-}
-
 // One launch covers up to MAXG truncation groups (an ensemble of mixed
 // truncations): their work items are concatenated, each group with its own
-// tables, tensor map and buffers.
+// tables, tensor maps and buffers.
 constexpr int MAXG = 8;
 struct TcLaunch {
-  CUtensorMap map[MAXG];
+  CUtensorMap map[MAXG];   // B tiles
+  CUtensorMap amap[MAXG];  // A operand
   TcArgs g[MAXG];
   int start[MAXG + 1];  // prefix of work items over groups
   int ngroups;
 };
 
-// Work item decode: groups in order, then items ordered (ct, m, nt) within a
-// group, heavy (small m) first within ct.
-__device__ __forceinline__ void decode(const TcArgs &a, int it, int &m, int &ct, int &nt);
-__device__ __forceinline__ const TcArgs &decode_item(const TcLaunch &L, int it, int &gi, int &m, int &ct,
-                                                     int &nt) {
-  gi = 0;
+// Work item it -> group and (m, ct, nt); items of a group are ordered
+// (ct, m, nt), heavy (small m) first within ct.
+__device__ __forceinline__ int group_of(const TcLaunch &L, int it) {
+  int gi = 0;
   while (gi + 1 < L.ngroups && it >= L.start[gi + 1]) ++gi;
-  decode(L.g[gi], it - L.start[gi], m, ct, nt);
-  return L.g[gi];
-}
-
-__device__ __forceinline__ void decode(const TcArgs &a, int it, int &m, int &ct, int &nt) {
-  ct = it / a.items_per_ct;
-  int r = it % a.items_per_ct;
-  int lo = 0, hi = a.N + 1;  // find m with pre[m] <= r < pre[m+1]
-  while (hi - lo > 1) {
-    const int mid = (lo + hi) >> 1;
-    if (a.pre[mid] <= r) lo = mid;
-    else hi = mid;
-  }
-  m = lo;
-  nt = r - a.pre[m];
+  return gi;
 }
 
 __global__ void __launch_bounds__(TC_THREADS, 1)
@@ -241,7 +225,7 @@ legendre_tc_kernel(const __grid_constant__ TcLaunch L) {
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
   if (threadIdx.x == 0) {
     for (int s = 0; s < NSTAGE; ++s) {
-      mbar_init(&full[s], 129);
+      mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
       mbar_init(&accf[s], 1);
       mbar_init(&acce[s], 128);
@@ -249,7 +233,7 @@ legendre_tc_kernel(const __grid_constant__ TcLaunch L) {
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 8) {
+  if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(tmem_slot)),
                  "r"(TMEM_COLS)
@@ -262,83 +246,57 @@ legendre_tc_kernel(const __grid_constant__ TcLaunch L) {
   const uint32_t tmem = *tmem_slot;
   const int nitems = L.start[L.ngroups];
 
-  if (warp < 4) {
-    // ------------------------------------------------------- producers
-    const int t = threadIdx.x;  // row of the A tile
-    int g = 0;                  // chunk counter
-    bool ok = true;
-    for (int it = blockIdx.x; it < nitems && ok; it += gridDim.x) {
-      int gi, m, ct, nt;
-      const TcArgs &a = decode_item(L, it, gi, m, ct, nt);
-      const int C2B = 2 * a.batch;
-      const MInfo mi = a.mi[m];
-      const int nrow = min(128, mi.nr - nt * 128);
-      const int c = ct * 128 + t;
-      for (int p = 0; p < 2 && ok; ++p) {
-        const int kv = p ? mi.kv1 : mi.kv0;
-        const int nq = (kv + 63) / 64;
-        for (int q = 0; q < nq; ++q, ++g) {
-          const int s = g % NSTAGE;
-          if (!mbar_wait(&empty[s], ((g / NSTAGE) & 1) ^ 1, a.err, abort_flag, 1)) { ok = false; break; }
-          unsigned char *As = stage + s * STAGE_BYTES;
-          unsigned char *Bs = As + 3 * A_SPLIT_BYTES;
-          if (t == 0) {
-            mbar_arrive_tx(&full[s], (uint32_t)(3 * nrow * 128));
+  if (warp == 0) {
+    // ---------------------------------------------------------- TMA
+    if (lane == 0) {
+      int g = 0;  // chunk counter
+      bool ok = true;
+      for (int it = blockIdx.x; it < nitems && ok; it += gridDim.x) {
+        const int gi = group_of(L, it);
+        const TcArgs &a = L.g[gi];
+        const int4 w = a.items[it - L.start[gi]];
+        const int m = w.x, ct = w.y, nt = w.z;
+        const MInfo mi = a.mi[m];
+        for (int p = 0; p < 2 && ok; ++p) {
+          const int kv = p ? mi.kv1 : mi.kv0;
+          const int nq = (kv + 63) / 64;
+          const int x0 = p ? mi.x1 : mi.x0;
+          for (int q = 0; q < nq; ++q, ++g) {
+            const int s = g % NSTAGE;
+            if (!mbar_wait(&empty[s], ((g / NSTAGE) & 1) ^ 1, a.err, abort_flag, 1)) { ok = false; break; }
+            unsigned char *As = stage + s * STAGE_BYTES;
+            unsigned char *Bs = As + 3 * A_SPLIT_BYTES;
+            mbar_arrive_tx(&full[s], (uint32_t)STAGE_BYTES);
             for (int sp = 0; sp < 3; ++sp) {
+              unsigned char *Ad = As + sp * A_SPLIT_BYTES;
+              if (a.dir == 0) {
+                tma_load_3d(Ad, &L.amap[gi], x0 + 64 * q, ct * 128, sp, &full[s]);
+              } else {
+                tma_load_3d(Ad, &L.amap[gi], ct * 128, x0 + 64 * q, sp, &full[s]);
+                tma_load_3d(Ad + 8192, &L.amap[gi], ct * 128 + 64, x0 + 64 * q, sp, &full[s]);
+              }
               const long long row0 = mi.base + ((long long)(p * mi.nq + q) * 3 + sp) * mi.nr + nt * 128;
-              for (int r = 0; r < nrow; r += 16)
-                tma_load_2d(Bs + sp * B_SPLIT_BYTES + r * 128, &L.map[gi], 0, (int)(row0 + r), &full[s]);
+              tma_load_2d(Bs + sp * B_SPLIT_BYTES, &L.map[gi], 0, (int)row0, &full[s]);
             }
           }
-          // A row t: all 64 values of the chunk are requested before any is
-          // used (one memory latency per chunk), then split into three planes
-          // of 8 groups of 8 bf16 along K.
-          const int kbase = q * 64;
-          float xv[64];
-          if (a.dir == 0) {
-            // spec[b][idx(m, m+p+2k)], component c&1: stride 2 complex along k
-            const double *src = a.spec_in + ((long long)(c >> 1) * a.ncoef + idx_mn(a.N, m, m + p)) * 2 + (c & 1);
-#pragma unroll
-            for (int h2 = 0; h2 < 64; h2 += 32) {  // two halves keep the FP64 staging in registers
-              double dv[32];
-#pragma unroll
-              for (int e = 0; e < 32; ++e)
-                dv[e] = (c < C2B && kbase + h2 + e < kv) ? src[4LL * (kbase + h2 + e)] : 0.0;
-#pragma unroll
-              for (int e = 0; e < 32; ++e) xv[h2 + e] = f64_to_f32_rn(dv[e]);
-            }
-          } else {
-            const float *src = a.G + (((long long)m * 2 + p) * a.Jh) * C2B + c;
-#pragma unroll
-            for (int e = 0; e < 64; ++e)
-              xv[e] = (c < C2B && kbase + e < kv) ? src[(long long)(kbase + e) * C2B] : 0.f;
-          }
-#pragma unroll
-          for (int g8 = 0; g8 < 8; ++g8) {
-            __align__(16) __nv_bfloat16 h[8], md[8], lo[8];
-#pragma unroll
-            for (int e = 0; e < 8; ++e) split3f(xv[g8 * 8 + e], h[e], md[e], lo[e]);
-            const uint32_t off = (t >> 3) * 1024 + (t & 7) * 128 + ((g8 ^ (t & 7)) << 4);
-            *reinterpret_cast<uint4 *>(As + off) = *reinterpret_cast<const uint4 *>(h);
-            *reinterpret_cast<uint4 *>(As + A_SPLIT_BYTES + off) = *reinterpret_cast<const uint4 *>(md);
-            *reinterpret_cast<uint4 *>(As + 2 * A_SPLIT_BYTES + off) = *reinterpret_cast<const uint4 *>(lo);
-          }
-          fence_proxy_async();
-          mbar_arrive(&full[s]);
         }
       }
     }
-  } else if (warp == 8) {
+    __syncwarp();
+  } else if (warp == 1) {
     // ------------------------------------------------------------- MMA
     if (lane == 0) {
       int g = 0, li = 0;
       bool ok = true;
       for (int it = blockIdx.x; it < nitems && ok; it += gridDim.x, ++li) {
-        int gi, m, ct, nt;
-        const TcArgs &a = decode_item(L, it, gi, m, ct, nt);
+        const int gi = group_of(L, it);
+        const TcArgs &a = L.g[gi];
+        const int4 w = a.items[it - L.start[gi]];
+        const int m = w.x, nt = w.z;
         const MInfo mi = a.mi[m];
         const int nrow = min(128, mi.nr - nt * 128);
-        const uint32_t idesc = idesc_bf16(nrow);
+        const int amn = a.dir;  // forward A is MN-major
+        const uint32_t idesc = idesc_bf16(nrow, amn);
         const int ab = a.nacc == 2 ? (li & 1) : 0;
         const int ar = a.nacc == 2 ? (li >> 1) : li;  // use count of this accumulator set
         if (!mbar_wait(&acce[ab], (ar & 1) ^ 1, a.err, abort_flag, 2)) { ok = false; break; }
@@ -346,8 +304,6 @@ legendre_tc_kernel(const __grid_constant__ TcLaunch L) {
         for (int p = 0; p < 2 && ok; ++p) {
           const int kv = p ? mi.kv1 : mi.kv0;
           const int nq = (kv + 63) / 64;
-          // hi*hi accumulates apart from the five cross products, so the small
-          // terms do not lose their low bits in an accumulator 2^8 larger.
           const uint32_t dmain = tmem + ab * 4 * a.ntmax + (p * 2) * a.ntmax;
           const uint32_t dcross = dmain + a.ntmax;
           int accm = 0, accx = 0;
@@ -359,16 +315,19 @@ legendre_tc_kernel(const __grid_constant__ TcLaunch L) {
             const uint32_t Bs = As + 3 * A_SPLIT_BYTES;
             const int ksteps = min(4, (kv - q * 64 + 15) / 16);
             for (int ks = 0; ks < ksteps; ++ks) {
-              const uint32_t ko = ks * 32;
-              mma_bf16(dmain, smem_desc(As + ko), smem_desc(Bs + ko), idesc, accm);
+              // K step of 16: 32 bytes along a K-major row, 16 rows of an MN-major tile
+              const uint32_t ka = amn ? ks * 2048 : ks * 32;
+              const uint32_t lbo = amn ? 8192 : 16;
+              const uint32_t kb = ks * 32;
+              mma_bf16(dmain, smem_desc(As + ka, lbo), smem_desc(Bs + kb, 16), idesc, accm);
               accm = 1;
               // (A split, B split): hi*mid, mid*hi, hi*lo, lo*hi, mid*mid
               const int pa[5] = {0, 1, 0, 2, 1};
               const int pb[5] = {1, 0, 2, 0, 1};
 #pragma unroll
               for (int u = 0; u < 5; ++u) {
-                mma_bf16(dcross, smem_desc(As + pa[u] * A_SPLIT_BYTES + ko),
-                         smem_desc(Bs + pb[u] * B_SPLIT_BYTES + ko), idesc, accx);
+                mma_bf16(dcross, smem_desc(As + pa[u] * A_SPLIT_BYTES + ka, lbo),
+                         smem_desc(Bs + pb[u] * B_SPLIT_BYTES + kb, 16), idesc, accx);
                 accx = 1;
               }
             }
@@ -385,8 +344,10 @@ legendre_tc_kernel(const __grid_constant__ TcLaunch L) {
     const int row = quad * 32 + lane;
     int li = 0;
     for (int it = blockIdx.x; it < nitems; it += gridDim.x, ++li) {
-      int gi, m, ct, nt;
-      const TcArgs &a = decode_item(L, it, gi, m, ct, nt);
+      const int gi = group_of(L, it);
+      const TcArgs &a = L.g[gi];
+      const int4 w = a.items[it - L.start[gi]];
+      const int m = w.x, ct = w.y, nt = w.z;
       const int C2B = 2 * a.batch;
       const MInfo mi = a.mi[m];
       const int nrow = min(128, mi.nr - nt * 128);
@@ -454,11 +415,83 @@ legendre_tc_kernel(const __grid_constant__ TcLaunch L) {
   }
   tc_fence_before();
   __syncthreads();
-  if (warp == 8) {
+  if (warp == 1) {
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS)
                  : "memory");
   }
+}
+
+// ------------------------------------------------------------ spectra pack
+// Apack[s][2b + comp][xpos[i]] = split s of the FP32 rounding of spectral
+// coefficient i of field b (one thread per coefficient and field; the
+// (m, p) segment padding stays zero from plan creation).
+struct PackGroup {
+  const double2 *spec;
+  const int *xpos;
+  unsigned short *A;
+  long long ncoef, KX;
+  int C2Bp, f0;
+};
+struct PackLaunch {
+  PackGroup g[MAXG];
+  int ngroups;
+};
+
+__global__ void __launch_bounds__(256) pack_spectra_kernel(const __grid_constant__ PackLaunch L) {
+  int gi = 0;
+  while (gi + 1 < L.ngroups && (int)blockIdx.y >= L.g[gi + 1].f0) ++gi;
+  const PackGroup &G = L.g[gi];
+  const int b = blockIdx.y - G.f0;
+  const size_t plane = (size_t)G.C2Bp * G.KX;
+  const double2 *src = G.spec + (size_t)b * G.ncoef;
+  unsigned short *dst = G.A + (size_t)(2 * b) * G.KX;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < G.ncoef;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double2 v = __ldg(src + i);
+    const int x = __ldg(G.xpos + i);
+    unsigned short h0, m0, l0, h1, m1, l1;
+    split3f_bits(f64_to_f32_rn(v.x), h0, m0, l0);
+    split3f_bits(f64_to_f32_rn(v.y), h1, m1, l1);
+    unsigned short *o = dst + x;
+    o[0] = h0;
+    o[G.KX] = h1;
+    o[plane] = m0;
+    o[plane + G.KX] = m1;
+    o[2 * plane] = l0;
+    o[2 * plane + G.KX] = l1;
+  }
+}
+
+int pack_spectra(Plan *const *plans, const int *batch, const double *const *spec, int ngroups, cudaStream_t s) {
+  if (ngroups < 1 || ngroups > MAXG) return DCCM_ERR_UNSUPPORTED;
+  PackLaunch L;
+  memset(&L, 0, sizeof L);
+  int ng = 0, nf = 0;
+  long long maxc = 0;
+  for (int g = 0; g < ngroups; ++g) {
+    if (batch[g] <= 0) continue;
+    const Plan &P = *plans[g];
+    if (!P.d_apack) return DCCM_ERR_UNSUPPORTED;
+    PackGroup &G = L.g[ng++];
+    G.spec = reinterpret_cast<const double2 *>(spec[g]);
+    G.xpos = P.d_xpos;
+    G.A = P.d_apack;
+    G.ncoef = P.ncoef;
+    G.KX = P.KX;
+    G.C2Bp = P.C2Bp;
+    G.f0 = nf;
+    nf += batch[g];
+    maxc = P.ncoef > maxc ? P.ncoef : maxc;
+  }
+  L.ngroups = ng;
+  if (nf == 0) return DCCM_OK;
+  if (nf > 65535) return DCCM_ERR_UNSUPPORTED;
+  long long bx = (maxc + 255) / 256;
+  if (bx > 64) bx = 64;
+  pack_spectra_kernel<<<dim3((unsigned)bx, (unsigned)nf), 256, 0, s>>>(L);
+  DCCM_LAUNCH_CHECK();
+  return DCCM_OK;
 }
 
 // ------------------------------------------------------------ tile tables
@@ -517,17 +550,16 @@ __global__ void build_tiles_kernel(int dir, int N, int Jh, const MInfo *__restri
 struct TabMeta {
   std::vector<MInfo> mi;
   std::vector<long long> rowstart;  // split-0 rows before m
-  std::vector<int> pre;             // n-tile prefix
+  std::vector<int4> items;          // (m, 0, nt, 0) of one 128-column block
   long long rows = 0, rows0 = 0;
 };
 
-static TabMeta make_meta(int dir, int N, int Jh) {
+static TabMeta make_meta(int dir, const Plan &P) {
+  const int N = P.N, Jh = P.Jh;
   TabMeta t;
   t.mi.resize(N + 1);
   t.rowstart.resize(N + 2);
-  t.pre.resize(N + 2);
   long long base = 0, r0 = 0;
-  int pre = 0;
   for (int m = 0; m <= N; ++m) {
     MInfo &M = t.mi[m];
     const int c0 = count_np(N, m, 0), c1 = count_np(N, m, 1);
@@ -536,21 +568,23 @@ static TabMeta make_meta(int dir, int N, int Jh) {
       M.nv0 = Jh; M.nv1 = Jh;
       M.nr = (Jh + 15) / 16 * 16;
       M.nq = (c0 + 63) / 64;
+      M.x0 = P.xoff[2 * m];
+      M.x1 = P.xoff[2 * m + 1];
     } else {
       M.kv0 = Jh; M.kv1 = Jh;
       M.nv0 = c0; M.nv1 = c1;
       M.nr = (c0 + 15) / 16 * 16;
       M.nq = (Jh + 63) / 64;
+      M.x0 = 2 * m * Jh;
+      M.x1 = (2 * m + 1) * Jh;
     }
     M.base = base;
     t.rowstart[m] = r0;
-    t.pre[m] = pre;
     base += 2LL * M.nq * 3 * M.nr;
     r0 += 2LL * M.nq * M.nr;
-    pre += (M.nr + 127) / 128;
+    for (int nt = 0; nt < (M.nr + 127) / 128; ++nt) t.items.push_back(make_int4(m, 0, nt, 0));
   }
   t.rowstart[N + 1] = r0;
-  t.pre[N + 1] = pre;
   t.rows = base;
   t.rows0 = r0;
   return t;
@@ -574,22 +608,40 @@ static EncodeTiledFn get_encode() {
   return fn;
 }
 
+// bf16 tensor map with a 128-byte swizzle; dims/strides/box innermost first.
+static int encode_bf16(CUtensorMap *map, void *base, int rank, const cuuint64_t *dims, const cuuint64_t *strides,
+                       const cuuint32_t *box) {
+  EncodeTiledFn enc = get_encode();
+  if (!enc) return DCCM_ERR_UNSUPPORTED;
+  const cuuint32_t estr[3] = {1, 1, 1};
+  const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, (cuuint32_t)rank, base, dims, strides, box, estr,
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                         CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? DCCM_OK : DCCM_ERR_UNSUPPORTED;
+}
+
 static int build_one(Plan &P, int dir, TileTable &T) {
-  TabMeta meta = make_meta(dir, P.N, P.Jh);
+  TabMeta meta = make_meta(dir, P);
   T.rows = meta.rows;
   T.base.assign(P.N + 1, 0);
   for (int m = 0; m <= P.N; ++m) T.base[m] = meta.mi[m].base;
   DCCM_CUDA(cudaMalloc(&T.d, (size_t)meta.rows * 64 * sizeof(uint16_t)));
   MInfo *dmi;
   long long *drs;
-  int *dpre;
   DCCM_CUDA(cudaMalloc(&dmi, meta.mi.size() * sizeof(MInfo)));
+  T.d_mi = dmi;
   DCCM_CUDA(cudaMalloc(&drs, meta.rowstart.size() * sizeof(long long)));
-  DCCM_CUDA(cudaMalloc(&dpre, meta.pre.size() * sizeof(int)));
   DCCM_CUDA(cudaMemcpy(dmi, meta.mi.data(), meta.mi.size() * sizeof(MInfo), cudaMemcpyHostToDevice));
   DCCM_CUDA(cudaMemcpy(drs, meta.rowstart.data(), meta.rowstart.size() * sizeof(long long),
                        cudaMemcpyHostToDevice));
-  DCCM_CUDA(cudaMemcpy(dpre, meta.pre.data(), meta.pre.size() * sizeof(int), cudaMemcpyHostToDevice));
+  // Work items of every 128-column block of the largest batch, block-major.
+  const int nct = (2 * P.max_batch + 127) / 128;
+  std::vector<int4> items;
+  items.reserve((size_t)nct * meta.items.size());
+  for (int ct = 0; ct < nct; ++ct)
+    for (int4 w : meta.items) items.push_back(make_int4(w.x, ct, w.z, 0));
+  DCCM_CUDA(cudaMalloc(&T.d_items, items.size() * sizeof(int4)));
+  DCCM_CUDA(cudaMemcpy(T.d_items, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice));
   const long long nthr = meta.rows0 * 8;
   if (nthr > 0) {
     build_tiles_kernel<<<(unsigned)((nthr + 255) / 256), 256>>>(dir, P.N, P.Jh, dmi, drs, meta.rows0,
@@ -598,27 +650,63 @@ static int build_one(Plan &P, int dir, TileTable &T) {
   }
   DCCM_CUDA(cudaDeviceSynchronize());
   cudaFree(drs);
-  EncodeTiledFn enc = get_encode();
-  if (!enc) return DCCM_ERR_UNSUPPORTED;
-  const cuuint64_t gdim[2] = {64, (cuuint64_t)meta.rows};
-  const cuuint64_t gstr[1] = {128};
-  const cuuint32_t box[2] = {64, 16};
-  const cuuint32_t estr[2] = {1, 1};
-  CUresult r = enc(&T.map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, T.d, gdim, gstr, box, estr,
-                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
-                   CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  if (r != CUDA_SUCCESS) return DCCM_ERR_UNSUPPORTED;
+  {
+    const cuuint64_t dims[2] = {64, (cuuint64_t)meta.rows};
+    const cuuint64_t str[1] = {128};
+    const cuuint32_t box[2] = {64, 128};
+    DCCM_TRY(encode_bf16(&T.map, T.d, 2, dims, str, box));
+  }
+  if (dir == 0) {  // Apack[3][C2Bp][KX], box 64 (K) x 128 (c)
+    const cuuint64_t dims[3] = {(cuuint64_t)P.KX, (cuuint64_t)P.C2Bp, 3};
+    const cuuint64_t str[2] = {(cuuint64_t)P.KX * 2, (cuuint64_t)P.KX * 2 * P.C2Bp};
+    const cuuint32_t box[3] = {64, 128, 1};
+    DCCM_TRY(encode_bf16(&T.amap, P.d_apack, 3, dims, str, box));
+  } else {  // G3[3][(N+1) 2 Jh][C2Bp], box 64 (c) x 64 (K)
+    const cuuint64_t rows = (cuuint64_t)(P.N + 1) * 2 * P.Jh;
+    const cuuint64_t dims[3] = {(cuuint64_t)P.C2Bp, rows, 3};
+    const cuuint64_t str[2] = {(cuuint64_t)P.C2Bp * 2, (cuuint64_t)P.C2Bp * 2 * rows};
+    const cuuint32_t box[3] = {64, 64, 1};
+    DCCM_TRY(encode_bf16(&T.amap, P.d_work, 3, dims, str, box));
+  }
   T.map_ok = true;
-  T.d_mi = dmi;
-  T.d_pre = dpre;
-  T.items_per_ct = meta.pre[P.N + 1];
+  T.items_per_ct = (int)meta.items.size();
   int nrmax = 16;
   for (const MInfo &M : meta.mi) nrmax = M.nr > nrmax ? M.nr : nrmax;
   T.ntmax = nrmax <= 64 ? 64 : 128;
   return DCCM_OK;
 }
 
+// Apack layout (segments of (m, p) along x, each rounded up to 16) and the
+// column of every coefficient; the buffer is zeroed once so the segment
+// padding contributes nothing.
+static int build_pack(Plan &P) {
+  P.C2Bp = (2 * P.max_batch + 7) / 8 * 8;
+  P.xoff.assign(2 * (P.N + 1), 0);
+  long long x = 0;
+  for (int m = 0; m <= P.N; ++m)
+    for (int p = 0; p < 2; ++p) {
+      P.xoff[2 * m + p] = (int)x;
+      x += (count_np(P.N, m, p) + 15) / 16 * 16;
+    }
+  P.KX = x;
+  if (P.KX >= (1LL << 31)) return DCCM_ERR_UNSUPPORTED;
+  std::vector<int> xpos((size_t)P.ncoef);
+  for (int m = 0; m <= P.N; ++m)
+    for (int n = m; n <= P.N; ++n) {
+      const int p = (n - m) & 1;
+      xpos[(size_t)idx_mn(P.N, m, n)] = P.xoff[2 * m + p] + (n - m - p) / 2;
+    }
+  DCCM_CUDA(cudaMalloc(&P.d_xpos, xpos.size() * sizeof(int)));
+  DCCM_CUDA(cudaMemcpy(P.d_xpos, xpos.data(), xpos.size() * sizeof(int), cudaMemcpyHostToDevice));
+  const size_t bytes = (size_t)3 * P.C2Bp * P.KX * sizeof(uint16_t);
+  DCCM_CUDA(cudaMalloc(&P.d_apack, bytes));
+  DCCM_CUDA(cudaMemset(P.d_apack, 0, bytes));
+  return DCCM_OK;
+}
+
+// Called after d_work exists (the forward A map points into it).
 int build_tiles(Plan &P) {
+  DCCM_TRY(build_pack(P));
   DCCM_TRY(build_one(P, 0, P.tinv));
   DCCM_TRY(build_one(P, 1, P.tfwd));
   return DCCM_OK;
@@ -627,10 +715,13 @@ int build_tiles(Plan &P) {
 static size_t tc_smem_bytes() { return 1024 + (size_t)NSTAGE * STAGE_BYTES + 128; }
 
 // One persistent launch over ngroups plans (truncation groups) of one
-// direction: dir 0 (inverse) reads in[g] = spectra (double) and writes
-// out[g] = F (float); dir 1 reads G (float) and writes spectra (double).
+// direction: dir 0 (inverse) reads the plan's packed spectra (pack_spectra
+// must have run on the same stream) and writes out[g] = F (float); dir 1
+// reads the plan's G3 (written by the forward FFT) and writes out[g] =
+// spectra (double).  in[] is unused (the operands come by TMA).
 int legendre_tc_multi(Plan *const *plans, const int *batch, const void *const *in, void *const *out,
                       int ngroups, int dir, cudaStream_t s) {
+  (void)in;
   static bool attr_done = false;
   if (ngroups < 1 || ngroups > MAXG) return DCCM_ERR_UNSUPPORTED;
   if (!attr_done) {
@@ -656,23 +747,17 @@ int legendre_tc_multi(Plan *const *plans, const int *batch, const void *const *i
     a.N = P.N;
     a.Jh = P.Jh;
     a.ncoef = P.ncoef;
-    a.nct = (2 * a.batch + 127) / 128;
-    a.items_per_ct = T.items_per_ct;
     a.mi = (const MInfo *)T.d_mi;
-    a.pre = T.d_pre;
+    a.items = T.d_items;
     a.err = plans[0]->d_err;
     a.ntmax = ntmax;
     a.nacc = 8 * ntmax <= TMEM_COLS ? 2 : 1;
-    if (dir == 0) {
-      a.spec_in = (const double *)in[g];
-      a.F = (float *)out[g];
-    } else {
-      a.G = (const float *)in[g];
-      a.spec_out = (double *)out[g];
-    }
+    if (dir == 0) a.F = (float *)out[g];
+    else a.spec_out = (double *)out[g];
     L.map[ng] = T.map;
+    L.amap[ng] = T.amap;
     L.start[ng] = items;
-    items += a.nct * a.items_per_ct;
+    items += ((2 * a.batch + 127) / 128) * T.items_per_ct;
     ++ng;
   }
   L.start[ng] = items;
@@ -688,15 +773,16 @@ int legendre_tc_multi(Plan *const *plans, const int *batch, const void *const *i
 int legendre_inv_tc(Plan &P, int batch, const double *spec, float *F, cudaStream_t s) {
   if (batch <= 0) return DCCM_OK;
   Plan *pp = &P;
+  DCCM_TRY(pack_spectra(&pp, &batch, &spec, 1, s));
   const void *in = spec;
   void *out = F;
   return legendre_tc_multi(&pp, &batch, &in, &out, 1, 0, s);
 }
 
-int legendre_fwd_tc(Plan &P, int batch, const float *G, double *spec, cudaStream_t s) {
+int legendre_fwd_tc(Plan &P, int batch, const void *G3, double *spec, cudaStream_t s) {
   if (batch <= 0) return DCCM_OK;
   Plan *pp = &P;
-  const void *in = G;
+  const void *in = G3;
   void *out = spec;
   return legendre_tc_multi(&pp, &batch, &in, &out, 1, 1, s);
 }

@@ -61,26 +61,31 @@ csr_apply(const int64_t *__restrict__ rowptr, const double2 *__restrict__ ent,
   // threads gather neighbouring source points and store consecutive rows;
   // the six fields of a row re-read the same records from L1.  Field f is
   // written at (f % nsub) * ld_dst + (f / nsub) * ld_dst2.
-  const int64_t total = nrow * nfields;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
-       t += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t r = t % nrow;
-    const int64_t f = t / nrow;
+  // Index arithmetic in 32 bits (the launcher guarantees nrow * nfields <
+  // 2^30, so t + stride cannot overflow): 64-bit division is a long
+  // emulated sequence on this GPU.
+  const int total = (int)(nrow * nfields);
+  const int nr = (int)nrow;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+    const int f = t / nr;
+    const int r = t - f * nr;
     const int64_t b = rowptr[r], e = rowptr[r + 1];
-    const double *s = src + f * ld_src;
+    const double *s = src + (int64_t)f * ld_src;
     double acc = 0.0;
     for (int64_t k = b; k < e; ++k) {
       const double2 q = __ldg(ent + k);
       const int64_t col = (int64_t)__double_as_longlong(q.y);
       acc = __dadd_rn(acc, __dmul_rn(__ldg(s + col), q.x));
     }
-    dst[(f % nsub) * ld_dst + (f / nsub) * ld_dst2 + r] = acc;
+    const int fs = f / nsub;
+    dst[(int64_t)(f - fs * nsub) * ld_dst + (int64_t)fs * ld_dst2 + r] = acc;
   }
 }
 
 int apply2(dccm_remap_plan *p, const double *src, int64_t ld_src, double *dst, int64_t ld_dst, int nfields,
            int nsub, int64_t ld_dst2, cudaStream_t s) {
   if (p->n_recv == 0 || nfields == 0) return DCCM_OK;
+  if (p->n_recv * (int64_t)nfields >= (1LL << 30)) return DCCM_ERR_UNSUPPORTED;
   if (nsub <= 0) {
     nsub = nfields;
     ld_dst2 = 0;

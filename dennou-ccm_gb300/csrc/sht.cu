@@ -85,8 +85,9 @@ __global__ void pnm_kernel(int N, int Jh, const double *__restrict__ mu, double 
 }
 
 static void destroy(Plan &P) {
-  void *ptrs[] = {P.d_mu, P.d_w, P.d_pnm, P.d_tw64, P.d_tw32, P.tinv.d, P.tfwd.d, P.tinv.d_mi,
-                  P.tfwd.d_mi, P.tinv.d_pre, P.tfwd.d_pre, P.d_work, P.d_err};
+  void *ptrs[] = {P.d_mu,      P.d_w,        P.d_pnm,       P.d_tw64,  P.d_tw32,  P.d_twl32,
+                  P.tinv.d,    P.tfwd.d,     P.tinv.d_mi,   P.tfwd.d_mi, P.tinv.d_items,
+                  P.tfwd.d_items, P.d_work,  P.d_err,       P.d_apack, P.d_xpos};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   P.stage.release();
@@ -117,22 +118,37 @@ static int create(Plan &P, int N, int I, int J, int precision, int max_batch) {
   DCCM_CUDA(cudaMemcpy(P.mu.data(), P.d_mu, J * sizeof(double), cudaMemcpyDeviceToHost));
   DCCM_CUDA(cudaMemcpy(P.w.data(), P.d_w, J * sizeof(double), cudaMemcpyDeviceToHost));
   // FFT twiddles e^{-2 pi i t / I} in FP64 on the host.
+  // and, for the FP32 warp transform, the per-lane table e^{-2 pi i l k / I}
+  // at [k][l] (l < 32, k < I/32).
   std::vector<double2> tw64(I);
-  std::vector<float2> tw32(I);
+  std::vector<float2> tw32(I), twl32(I);
   const double PI = acos(-1.0);
   for (int t = 0; t < I; ++t) {
     const double ang = 2.0 * PI * (double)t / (double)I;
     tw64[t] = make_double2(cos(ang), -sin(ang));
     tw32[t] = make_float2((float)tw64[t].x, (float)tw64[t].y);
+    const int k = t / 32, l = t % 32;
+    const double al = 2.0 * PI * (double)(l * k) / (double)I;
+    twl32[t] = make_float2((float)cos(al), (float)-sin(al));
   }
   DCCM_CUDA(cudaMalloc(&P.d_tw64, I * sizeof(double2)));
   DCCM_CUDA(cudaMalloc(&P.d_tw32, I * sizeof(float2)));
+  DCCM_CUDA(cudaMalloc(&P.d_twl32, I * sizeof(float2)));
   DCCM_CUDA(cudaMemcpy(P.d_tw64, tw64.data(), I * sizeof(double2), cudaMemcpyHostToDevice));
   DCCM_CUDA(cudaMemcpy(P.d_tw32, tw32.data(), I * sizeof(float2), cudaMemcpyHostToDevice));
-  if (precision == DCCM_SHT_MIXED) DCCM_TRY(build_tiles(P));
-  const size_t elem = precision == DCCM_SHT_MIXED ? sizeof(float) : sizeof(double);
-  P.work_bytes = (size_t)(N + 1) * J * 2 * (size_t)max_batch * elem;
+  DCCM_CUDA(cudaMemcpy(P.d_twl32, twl32.data(), I * sizeof(float2), cudaMemcpyHostToDevice));
+  if (precision == DCCM_SHT_MIXED) {
+    // F (FP32, [m][j][2 max_batch]) and G3 (three BF16 planes, rows of
+    // C2Bp) share the Fourier buffer.
+    const size_t c2bp = (size_t)(2 * max_batch + 7) / 8 * 8;
+    const size_t f_bytes = (size_t)(N + 1) * J * 2 * (size_t)max_batch * sizeof(float);
+    const size_t g3_bytes = 3 * (size_t)(N + 1) * J * c2bp * sizeof(uint16_t);
+    P.work_bytes = f_bytes > g3_bytes ? f_bytes : g3_bytes;
+  } else {
+    P.work_bytes = (size_t)(N + 1) * J * 2 * (size_t)max_batch * sizeof(double);
+  }
   DCCM_CUDA(cudaMalloc(&P.d_work, P.work_bytes));
+  if (precision == DCCM_SHT_MIXED) DCCM_TRY(build_tiles(P));
   DCCM_CUDA(cudaDeviceSynchronize());
   return DCCM_OK;
 }
@@ -149,7 +165,7 @@ int inverse(Plan &P, const double *spec, double *grid, int batch, cudaStream_t s
 int forward(Plan &P, const double *grid, double *spec, int batch, cudaStream_t s) {
   if (P.precision == DCCM_SHT_MIXED) {
     DCCM_TRY(fft_forward(P, batch, true, grid, P.d_work, s));
-    return legendre_fwd_tc(P, batch, (const float *)P.d_work, spec, s);
+    return legendre_fwd_tc(P, batch, P.d_work, spec, s);
   }
   DCCM_TRY(fft_forward(P, batch, false, grid, P.d_work, s));
   return legendre_fwd_f64(P, batch, (const double *)P.d_work, spec, s);
@@ -350,6 +366,7 @@ int ensemble_inverse(dccm_sht_ensemble *e, const double *const *spec, double *co
     in[g] = spec[g];
     work[g] = pp[g]->d_work;
   }
+  DCCM_TRY(pack_spectra(pp, batch, spec, ng, s));
   DCCM_TRY(legendre_tc_multi(pp, batch, in, work, ng, 0, s));
   return fft_multi(pp, batch, (const void *const *)work, (void *const *)grid, ng, false, s);
 }

@@ -15,6 +15,12 @@
 //   forward: G[m][p][jj][c]   FFT output folded into parity p: p = 0 holds
 //                             E = G(jn) + G(js), p = 1 holds O = G(jn) - G(js),
 //                             already divided by I.
+// Mixed precision: F is FP32; G is stored split as three BF16 planes
+// G3[s][(2m + p) Jh + jj][c] (row length C2Bp = 2 max_batch rounded up to 8),
+// the MN-major A operand of the tensor-core analysis; the spectra enter the
+// tensor-core synthesis through Apack[s][c][x], BF16 planes of the split
+// spectra with x = xoff(m, p) + k for n = m + p + 2k (K-major, each (m, p)
+// segment rounded up to 16 with zeros).
 #pragma once
 #include <cuda.h>
 
@@ -35,10 +41,11 @@ struct TileTable {
   std::vector<int> nr, nq, kval, nval;
   int64_t rows = 0;
   uint16_t *d = nullptr;      // device bf16 bits
-  CUtensorMap map;            // TMA descriptor, box {64, 16}
+  CUtensorMap map;            // TMA descriptor of the tiles, box {64, 128}
+  CUtensorMap amap;           // TMA descriptor of the A operand (Apack or G3)
   bool map_ok = false;
   void *d_mi = nullptr;       // per-m tile metadata (device)
-  int *d_pre = nullptr;       // prefix of N-tiles over m (device)
+  int4 *d_items = nullptr;    // work items (m, ct, nt, -) for every 128-column block
   int items_per_ct = 0;       // work items per 128-column block of the batch
   int ntmax = 64;             // TMEM columns per accumulator (N tile bound)
 };
@@ -55,9 +62,15 @@ struct Plan {
   double *d_pnm = nullptr;     // FP64 Pbar(m, n, jj): [idx(m,n)][Jh]
   double2 *d_tw64 = nullptr;   // FFT twiddles e^{-2 pi i t / I}
   float2 *d_tw32 = nullptr;
+  float2 *d_twl32 = nullptr;   // per-lane twiddles e^{-2 pi i l k / I} at [k][l], l < 32, k < I/32
   TileTable tinv, tfwd;        // bf16x3 tiles for the tensor path
-  void *d_work = nullptr;      // Fourier buffer (F or G), sized for max_batch
+  void *d_work = nullptr;      // Fourier buffer (F, G or G3), sized for max_batch
   size_t work_bytes = 0;
+  int C2Bp = 0;                // row length of G3 and Apack (2 max_batch rounded up to 8)
+  int64_t KX = 0;              // row length of Apack
+  std::vector<int> xoff;       // Apack segment offset of (m, p) at [2m + p]
+  uint16_t *d_apack = nullptr; // Apack[3][C2Bp][KX] (bf16 bits)
+  int *d_xpos = nullptr;       // Apack column x of each spectral coefficient
   int *d_err = nullptr;        // device error flag of bounded waits
   DevBuf stage;                // host entry point staging
   cudaStream_t stream = nullptr;
@@ -82,9 +95,10 @@ int fft_forward(const Plan &P, int batch, bool fp32, const double *grid, void *G
 int legendre_inv_f64(const Plan &P, int batch, const double *spec, double *F, cudaStream_t s);
 int legendre_fwd_f64(const Plan &P, int batch, const double *G, double *spec, cudaStream_t s);
 int legendre_inv_tc(Plan &P, int batch, const double *spec, float *F, cudaStream_t s);
-int legendre_fwd_tc(Plan &P, int batch, const float *G, double *spec, cudaStream_t s);
+int legendre_fwd_tc(Plan &P, int batch, const void *G3, double *spec, cudaStream_t s);
 int legendre_tc_multi(Plan *const *plans, const int *batch, const void *const *in, void *const *out,
                       int ngroups, int dir, cudaStream_t s);
+int pack_spectra(Plan *const *plans, const int *batch, const double *const *spec, int ngroups, cudaStream_t s);
 int fft_multi(Plan *const *plans, const int *batch, const void *const *in, void *const *out, int ngroups, bool fwd,
               cudaStream_t s);
 int inverse(Plan &P, const double *spec, double *grid, int batch, cudaStream_t s);

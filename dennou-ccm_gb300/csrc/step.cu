@@ -17,6 +17,7 @@
 // stream with events in between (per-stage device times for roofline
 // reports); dccm_step_run_host adds the host<->device copies of a caller
 // that holds its data in host memory.
+#include <algorithm>
 #include <new>
 #include <vector>
 
@@ -46,11 +47,16 @@ struct dccm_step {
   dccm_sfc_bulk_flux_args flux;
   dccm_sfc_grid fgrid;
   double sig1[2];
-  cudaStream_t s0 = nullptr, s1 = nullptr;
-  cudaEvent_t fork = nullptr, join = nullptr;
+  cudaStream_t s0 = nullptr, s1 = nullptr, s2 = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr, ev_grid = nullptr, ev_copy = nullptr, ev_in = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   cudaEvent_t ev[8] = {};
+  // graph of dccm_step_run_host for the copy lists it was recorded with
+  std::vector<dccm_host_copy> host_h2d, host_d2h;
+  cudaGraph_t hgraph = nullptr;
+  cudaGraphExec_t hexec = nullptr;
+  std::vector<void *> host_tabs;  // device segment tables of that graph
 };
 
 using namespace dccm;
@@ -96,6 +102,7 @@ static int stage_leg_inv(dccm_step *st, cudaStream_t s) {
   if (mixed(G)) {
     void *work[8];
     for (int g = 0; g < G.n; ++g) work[g] = G.P[g]->d_work;
+    DCCM_TRY(sht::pack_spectra(G.P, G.nfl, G.spec_in, G.n, s));
     return sht::legendre_tc_multi(G.P, G.nfl, (const void *const *)G.spec_in, work, G.n, 0, s);
   }
   for (int g = 0; g < G.n; ++g)
@@ -156,6 +163,266 @@ static int stage_flux(dccm_step *st, cudaStream_t s) {
   return dccm_sfc_bulk_flux_get_dev(&st->flux, &st->fgrid, (void *)s);
 }
 
+// Host copies of dccm_step_run_host, sorted by the buffers they touch into
+// the places of the graph where their data are ready or first needed:
+//   pre      H2D before everything (touches what the transforms write, or
+//            both branches)
+//   sht_in   H2D before Legendre synthesis (spectral input only)
+//   sfc_in   H2D at the head of the surface branch (remaps, flux)
+//   grid     D2H after the inverse FFT, on a third stream, overlapping
+//            the analysis transforms (which only read the grid)
+//   spec     D2H after Legendre analysis
+//   sfc_out  D2H at the tail of the surface branch
+//   post     D2H after both branches (touches several of the above, or
+//            memory that one of this call's H2D copies writes)
+struct HostPlan {
+  std::vector<dccm_host_copy> pre, sht_in, sfc_in, grid, spec, sfc_out, post;
+};
+
+// Copies of many small buffers (rows of the surface arrays, a few hundred
+// KB each) would pay a copy engine's fixed cost of a few microseconds per
+// transfer.  They are merged: host-contiguous runs become one staged
+// transfer (below); the other copies of at most SMALL_COPY bytes move in one
+// kernel per group that reads or writes the page-locked host memory through
+// its device mapping.  seg_copy_kernel moves segment y, 16 KB per block, in
+// 16-, 8-, 4- or 1-byte words (the widest that divides both addresses and
+// the length).
+constexpr size_t SMALL_COPY = 1 << 20;
+constexpr unsigned SEG_CHUNK = 16384;
+struct Seg {
+  const unsigned char *src;
+  unsigned char *dst;
+  unsigned long long bytes;
+};
+
+template <typename W>
+__device__ __forceinline__ void seg_words(const unsigned char *src, unsigned char *dst, unsigned long long b0,
+                                          unsigned long long b1) {
+  constexpr int U = 4;
+  const unsigned long long step = (unsigned long long)blockDim.x * sizeof(W);
+  for (unsigned long long i = b0 + threadIdx.x * sizeof(W); i < b1; i += U * step) {
+    W v[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+      if (i + u * step < b1) v[u] = *reinterpret_cast<const W *>(src + i + u * step);
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+      if (i + u * step < b1) *reinterpret_cast<W *>(dst + i + u * step) = v[u];
+  }
+}
+
+__global__ void __launch_bounds__(256) seg_copy_kernel(const Seg *__restrict__ segs) {
+  const Seg sg = segs[blockIdx.y];
+  const unsigned long long b0 = (unsigned long long)blockIdx.x * SEG_CHUNK;
+  if (b0 >= sg.bytes) return;
+  const unsigned long long b1 = b0 + SEG_CHUNK < sg.bytes ? b0 + SEG_CHUNK : sg.bytes;
+  const unsigned long long al = (unsigned long long)(uintptr_t)sg.src | (uintptr_t)sg.dst | sg.bytes;
+  if ((al & 15) == 0) seg_words<uint4>(sg.src, sg.dst, b0, b1);
+  else if ((al & 7) == 0) seg_words<uint2>(sg.src, sg.dst, b0, b1);
+  else if ((al & 3) == 0) seg_words<unsigned>(sg.src, sg.dst, b0, b1);
+  else seg_words<unsigned char>(sg.src, sg.dst, b0, b1);
+}
+
+// A device table of segments for seg_copy_kernel.
+struct SegTab {
+  Seg *tab = nullptr;
+  int nseg = 0;
+  unsigned long long maxb = 0;
+};
+// Copies whose host buffers lie back to back (rows of one host allocation)
+// travel as one copy-engine transfer of the whole host range through a
+// device staging buffer, gathered (D2H) or scattered (H2D) on the device by
+// seg_copy_kernel at HBM speed.
+struct Staged {
+  void *host;
+  unsigned char *stage;
+  size_t bytes;
+  SegTab segs;  // device pieces <-> staging
+};
+// One group of copies as recorded: large single copies (or host memory
+// without a device mapping) as copy-engine transfers, runs of host-
+// contiguous copies staged, the remaining small ones in one kernel through
+// the host mapping.
+struct CopySet {
+  std::vector<dccm_host_copy> big;
+  std::vector<Staged> staged;
+  SegTab mapped;
+};
+struct HostSets {
+  CopySet pre, sht_in, sfc_in, grid, spec, sfc_out, post;
+};
+
+static int upload_segs(dccm_step *st, const std::vector<Seg> &segs, SegTab &t) {
+  if (segs.empty()) return DCCM_OK;
+  if (segs.size() > 65535) return DCCM_ERR_UNSUPPORTED;
+  DCCM_CUDA(cudaMalloc(&t.tab, segs.size() * sizeof(Seg)));
+  st->host_tabs.push_back(t.tab);
+  DCCM_CUDA(cudaMemcpy(t.tab, segs.data(), segs.size() * sizeof(Seg), cudaMemcpyHostToDevice));
+  t.nseg = (int)segs.size();
+  for (const Seg &g : segs) t.maxb = g.bytes > t.maxb ? g.bytes : t.maxb;
+  return DCCM_OK;
+}
+
+static int prepare_set(dccm_step *st, std::vector<dccm_host_copy> v, bool h2d, CopySet &cs) {
+  std::sort(v.begin(), v.end(), [](const dccm_host_copy &a, const dccm_host_copy &b) {
+    return (uintptr_t)a.host < (uintptr_t)b.host;
+  });
+  std::vector<Seg> mapped;
+  size_t k = 0;
+  while (k < v.size()) {
+    // the run of copies whose host ranges follow each other
+    size_t e = k + 1;
+    size_t total = v[k].bytes;
+    while (e < v.size() && (uintptr_t)v[e].host == (uintptr_t)v[e - 1].host + v[e - 1].bytes && v[e].bytes) {
+      total += v[e].bytes;
+      ++e;
+    }
+    if (e - k >= 2 && total > SMALL_COPY) {
+      Staged sg;
+      sg.host = v[k].host;
+      sg.bytes = total;
+      DCCM_CUDA(cudaMalloc(&sg.stage, total));
+      st->host_tabs.push_back(sg.stage);
+      std::vector<Seg> pieces;
+      size_t off = 0;
+      for (size_t i = k; i < e; ++i) {
+        Seg g;
+        g.src = static_cast<const unsigned char *>(h2d ? (const void *)(sg.stage + off) : v[i].dev);
+        g.dst = static_cast<unsigned char *>(h2d ? v[i].dev : (void *)(sg.stage + off));
+        g.bytes = v[i].bytes;
+        pieces.push_back(g);
+        off += v[i].bytes;
+      }
+      DCCM_TRY(upload_segs(st, pieces, sg.segs));
+      cs.staged.push_back(sg);
+    } else {
+      for (size_t i = k; i < e; ++i) {
+        const dccm_host_copy &c = v[i];
+        cudaPointerAttributes a;
+        void *hdev = nullptr;
+        if (c.bytes <= SMALL_COPY && cudaPointerGetAttributes(&a, c.host) == cudaSuccess) hdev = a.devicePointer;
+        cudaGetLastError();
+        if (!hdev || c.bytes == 0) {
+          cs.big.push_back(c);
+          continue;
+        }
+        Seg g;
+        g.src = static_cast<const unsigned char *>(h2d ? hdev : c.dev);
+        g.dst = static_cast<unsigned char *>(h2d ? c.dev : hdev);
+        g.bytes = c.bytes;
+        mapped.push_back(g);
+      }
+    }
+    k = e;
+  }
+  return upload_segs(st, mapped, cs.mapped);
+}
+
+static int prepare_sets(dccm_step *st, const HostPlan &hp, HostSets &hs) {
+  DCCM_TRY(prepare_set(st, hp.pre, true, hs.pre));
+  DCCM_TRY(prepare_set(st, hp.sht_in, true, hs.sht_in));
+  DCCM_TRY(prepare_set(st, hp.sfc_in, true, hs.sfc_in));
+  DCCM_TRY(prepare_set(st, hp.grid, false, hs.grid));
+  DCCM_TRY(prepare_set(st, hp.spec, false, hs.spec));
+  DCCM_TRY(prepare_set(st, hp.sfc_out, false, hs.sfc_out));
+  return prepare_set(st, hp.post, false, hs.post);
+}
+
+static int capture(dccm_step *st, const HostSets *hp, cudaGraph_t *out) {
+  *out = nullptr;
+  DCCM_CUDA(cudaStreamBeginCapture(st->s0, cudaStreamCaptureModeThreadLocal));
+  int rc = DCCM_OK;
+  cudaError_t e = cudaSuccess;
+  auto segs = [&](const SegTab &t, cudaStream_t s) {
+    if (t.nseg > 0 && e == cudaSuccess) {
+      const dim3 grid((unsigned)((t.maxb + SEG_CHUNK - 1) / SEG_CHUNK), (unsigned)t.nseg);
+      seg_copy_kernel<<<grid, 256, 0, s>>>(t.tab);
+      e = cudaGetLastError();
+    }
+  };
+  auto copies = [&](const CopySet &cs, bool h2d, cudaStream_t s) {
+    for (const dccm_host_copy &c : cs.big) {
+      if (e != cudaSuccess) return;
+      e = h2d ? cudaMemcpyAsync(c.dev, c.host, c.bytes, cudaMemcpyHostToDevice, s)
+              : cudaMemcpyAsync(c.host, c.dev, c.bytes, cudaMemcpyDeviceToHost, s);
+    }
+    for (const Staged &g : cs.staged) {
+      if (e != cudaSuccess) return;
+      if (h2d) {
+        e = cudaMemcpyAsync(g.stage, g.host, g.bytes, cudaMemcpyHostToDevice, s);
+        segs(g.segs, s);
+      } else {
+        segs(g.segs, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(g.host, g.stage, g.bytes, cudaMemcpyDeviceToHost, s);
+      }
+    }
+    segs(cs.mapped, s);
+  };
+  auto step = [&](int (*f)(dccm_step *, cudaStream_t), cudaStream_t s) {
+    if (rc == DCCM_OK && e == cudaSuccess) rc = f(st, s);
+  };
+  if (hp) copies(hp->pre, true, st->s0);
+  if (e == cudaSuccess) e = cudaEventRecord(st->fork, st->s0);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(st->s1, st->fork, 0);
+  // transforms on s0
+  if (hp) copies(hp->sht_in, true, st->s0);
+  // The transform chain is the longer branch: its upload goes first on the
+  // host link, the surface uploads follow it.
+  auto any = [](const CopySet &c) { return !c.big.empty() || !c.staged.empty() || c.mapped.nseg > 0; };
+  if (hp && any(hp->sht_in) && any(hp->sfc_in)) {
+    if (e == cudaSuccess) e = cudaEventRecord(st->ev_in, st->s0);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(st->s1, st->ev_in, 0);
+  }
+  step(stage_leg_inv, st->s0);
+  step(stage_fft_inv, st->s0);
+  const bool grid_copies = hp && any(hp->grid);
+  if (grid_copies && rc == DCCM_OK) {
+    if (e == cudaSuccess) e = cudaEventRecord(st->ev_grid, st->s0);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(st->s2, st->ev_grid, 0);
+    copies(hp->grid, false, st->s2);
+    if (e == cudaSuccess) e = cudaEventRecord(st->ev_copy, st->s2);
+  }
+  step(stage_fft_fwd, st->s0);
+  step(stage_leg_fwd, st->s0);
+  if (hp) copies(hp->spec, false, st->s0);
+  // surface branch on s1
+  if (hp) copies(hp->sfc_in, true, st->s1);
+  step(stage_remap, st->s1);
+  step(stage_flux, st->s1);
+  if (hp) copies(hp->sfc_out, false, st->s1);
+  if (e == cudaSuccess) e = cudaEventRecord(st->join, st->s1);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(st->s0, st->join, 0);
+  if (grid_copies && rc == DCCM_OK && e == cudaSuccess) e = cudaStreamWaitEvent(st->s0, st->ev_copy, 0);
+  if (hp) copies(hp->post, false, st->s0);
+  cudaGraph_t g = nullptr;
+  const cudaError_t e2 = cudaStreamEndCapture(st->s0, &g);
+  if (rc == DCCM_OK && e != cudaSuccess) {
+    set_cuda_error(e);
+    rc = DCCM_ERR_CUDA;
+  }
+  if (rc == DCCM_OK && e2 != cudaSuccess) {
+    set_cuda_error(e2);
+    rc = DCCM_ERR_CUDA;
+  }
+  if (rc != DCCM_OK) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  *out = g;
+  return DCCM_OK;
+}
+
+static void drop_host_graph(dccm_step *st) {
+  if (st->hexec) cudaGraphExecDestroy(st->hexec);
+  if (st->hgraph) cudaGraphDestroy(st->hgraph);
+  st->hexec = nullptr;
+  st->hgraph = nullptr;
+  st->host_h2d.clear();
+  st->host_d2h.clear();
+  for (void *p : st->host_tabs) cudaFree(p);
+  st->host_tabs.clear();
+}
+
 static int record(dccm_step *st) {
   // One untimed pass outside capture sets every kernel's attributes.
   DCCM_TRY(stage_sht_inv(st, st->s0));
@@ -163,30 +430,9 @@ static int record(dccm_step *st) {
   DCCM_TRY(stage_remap(st, st->s0));
   DCCM_TRY(stage_flux(st, st->s0));
   DCCM_CUDA(cudaStreamSynchronize(st->s0));
-  DCCM_CUDA(cudaStreamBeginCapture(st->s0, cudaStreamCaptureModeThreadLocal));
-  int rc = DCCM_OK;
-  cudaError_t e = cudaEventRecord(st->fork, st->s0);
-  if (e == cudaSuccess) e = cudaStreamWaitEvent(st->s1, st->fork, 0);
-  if (e != cudaSuccess) rc = DCCM_ERR_CUDA;
-  if (rc == DCCM_OK) rc = stage_sht_inv(st, st->s0);
-  if (rc == DCCM_OK) rc = stage_sht_fwd(st, st->s0);
-  if (rc == DCCM_OK) rc = stage_remap(st, st->s1);
-  if (rc == DCCM_OK) rc = stage_flux(st, st->s1);
-  if (rc == DCCM_OK) {
-    e = cudaEventRecord(st->join, st->s1);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(st->s0, st->join, 0);
-    if (e != cudaSuccess) rc = DCCM_ERR_CUDA;
-  }
+  drop_host_graph(st);
   cudaGraph_t g = nullptr;
-  cudaError_t e2 = cudaStreamEndCapture(st->s0, &g);
-  if (rc != DCCM_OK) {
-    if (g) cudaGraphDestroy(g);
-    return rc;
-  }
-  if (e2 != cudaSuccess) {
-    set_cuda_error(e2);
-    return DCCM_ERR_CUDA;
-  }
+  DCCM_TRY(capture(st, nullptr, &g));
   st->graph = g;
   DCCM_CUDA(cudaGraphInstantiate(&st->exec, g, 0));
   return DCCM_OK;
@@ -225,8 +471,12 @@ extern "C" int dccm_step_create(const dccm_step_desc *d, dccm_step **out) {
   }
   cudaError_t e = cudaStreamCreateWithFlags(&st->s0, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&st->s1, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&st->s2, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&st->fork, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&st->join, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&st->ev_grid, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&st->ev_copy, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&st->ev_in, cudaEventDisableTiming);
   for (int k = 0; k < 8 && e == cudaSuccess; ++k) e = cudaEventCreate(&st->ev[k]);
   int rc = e == cudaSuccess ? DCCM_OK : DCCM_ERR_CUDA;
   if (e != cudaSuccess) set_cuda_error(e);
@@ -241,14 +491,15 @@ extern "C" int dccm_step_create(const dccm_step_desc *d, dccm_step **out) {
 
 extern "C" int dccm_step_destroy(dccm_step *st) {
   if (!st) return DCCM_OK;
+  drop_host_graph(st);
   if (st->exec) cudaGraphExecDestroy(st->exec);
   if (st->graph) cudaGraphDestroy(st->graph);
   for (int k = 0; k < 8; ++k)
     if (st->ev[k]) cudaEventDestroy(st->ev[k]);
-  if (st->fork) cudaEventDestroy(st->fork);
-  if (st->join) cudaEventDestroy(st->join);
-  if (st->s0) cudaStreamDestroy(st->s0);
-  if (st->s1) cudaStreamDestroy(st->s1);
+  for (cudaEvent_t ev : {st->fork, st->join, st->ev_grid, st->ev_copy, st->ev_in})
+    if (ev) cudaEventDestroy(ev);
+  for (cudaStream_t s : {st->s0, st->s1, st->s2})
+    if (s) cudaStreamDestroy(s);
   delete st;
   return DCCM_OK;
 }
@@ -274,15 +525,124 @@ extern "C" int dccm_step_run_timed(dccm_step *st, void *stream, float *ms) {
   return DCCM_OK;
 }
 
+// Byte ranges [a, b) of device memory.
+struct Span {
+  uintptr_t a, b;
+};
+static void add_span(std::vector<Span> &v, const void *p, size_t bytes) {
+  if (p && bytes) v.push_back({(uintptr_t)p, (uintptr_t)p + bytes});
+}
+static bool hits(const std::vector<Span> &v, const void *p, size_t bytes) {
+  const uintptr_t a = (uintptr_t)p, b = a + bytes;
+  for (const Span &s : v)
+    if (a < s.b && s.a < b) return true;
+  return false;
+}
+static bool same_copies(const std::vector<dccm_host_copy> &v, const dccm_host_copy *c, int n) {
+  if ((int)v.size() != n) return false;
+  for (int k = 0; k < n; ++k)
+    if (v[k].host != c[k].host || v[k].dev != c[k].dev || v[k].bytes != c[k].bytes) return false;
+  return true;
+}
+
+static void sort_copies(dccm_step *st, const dccm_host_copy *h2d, int nh2d, const dccm_host_copy *d2h, int nd2h,
+                        HostPlan &hp) {
+  // Device memory the two branches touch.
+  std::vector<Span> sht_in, sht_grid, sht_out, sfc, uploads;
+  const Groups G = groups_of(st);
+  for (int g = 0; g < G.n; ++g) {
+    const sht::Plan &P = *G.P[g];
+    add_span(sht_in, G.spec_in[g], (size_t)G.nfl[g] * P.ncoef * 2 * sizeof(double));
+    add_span(sht_grid, G.grid[g], (size_t)G.nfl[g] * P.J * P.I * sizeof(double));
+    add_span(sht_out, G.spec_out[g], (size_t)G.nfl[g] * P.ncoef * 2 * sizeof(double));
+  }
+  for (const dccm_step_remap &r : st->remaps) {
+    if (!r.plan || r.nfields <= 0) continue;
+    int64_t nnz = 0, ns = 0, nr = 0;
+    dccm_remap_plan_info(r.plan, &nnz, &ns, &nr);
+    add_span(sfc, r.src, (size_t)((r.nfields - 1) * r.ld_src + ns) * sizeof(double));
+    const int nsub = r.nsub > 0 ? r.nsub : r.nfields;
+    const int64_t ld2 = r.nsub > 0 ? r.ld_dst2 : 0;
+    int64_t end = 0;
+    for (int f = 0; f < r.nfields; ++f) {
+      const int64_t e = (f % nsub) * r.ld_dst + (f / nsub) * ld2 + nr;
+      end = e > end ? e : end;
+    }
+    add_span(sfc, r.dst, (size_t)end * sizeof(double));
+  }
+  if (st->d.flux) {
+    const dccm_sfc_bulk_flux_args &f = st->flux;
+    const size_t n = (size_t)st->fgrid.IA * st->fgrid.JA * sizeof(double);
+    for (const void *p : {(const void *)f.WindStressX, (const void *)f.WindStressY, (const void *)f.SenHFlx,
+                          (const void *)f.QVapMFlx, (const void *)f.LatHFlx, (const void *)f.SfcVelTransCoef,
+                          (const void *)f.SfcTempTransCoef, (const void *)f.SfcQVapTransCoef, (const void *)f.SUwRFlx,
+                          (const void *)f.LUwRFlx, (const void *)f.SfcHFlx_ns, (const void *)f.SfcHFlx_sr,
+                          (const void *)f.DSfcHFlxDTs, (const void *)f.SfcTemp, (const void *)f.SfcAlbedo})
+      add_span(sfc, p, 3 * n);
+    for (const void *p : {(const void *)f.DelVarImplCPL, (const void *)f.ImplCplCoef1, (const void *)f.ImplCplCoef2})
+      add_span(sfc, p, 4 * n);
+    for (const void *p : {(const void *)f.WindU, (const void *)f.WindV, (const void *)f.SfcAirTemp,
+                          (const void *)f.QVap1, (const void *)f.SDwRFlx, (const void *)f.LDwRFlx,
+                          (const void *)f.SIceCon, (const void *)f.SfcHeight, (const void *)f.SfcPress})
+      add_span(sfc, p, n);
+  }
+  for (int k = 0; k < nh2d; ++k) {
+    const dccm_host_copy &c = h2d[k];
+    add_span(uploads, c.dev, c.bytes);
+    const bool w = hits(sht_grid, c.dev, c.bytes) || hits(sht_out, c.dev, c.bytes);
+    const bool i = hits(sht_in, c.dev, c.bytes), f = hits(sfc, c.dev, c.bytes);
+    if (w || (i && f)) hp.pre.push_back(c);
+    else if (i) hp.sht_in.push_back(c);
+    else hp.sfc_in.push_back(c);
+  }
+  for (int k = 0; k < nd2h; ++k) {
+    const dccm_host_copy &c = d2h[k];
+    const int g = hits(sht_grid, c.dev, c.bytes), o = hits(sht_out, c.dev, c.bytes);
+    const int f = hits(sfc, c.dev, c.bytes);
+    if (g + o + f > 1 || hits(uploads, c.dev, c.bytes)) hp.post.push_back(c);
+    else if (g) hp.grid.push_back(c);
+    else if (o) hp.spec.push_back(c);
+    else hp.sfc_out.push_back(c);  // surface results, or memory no stage writes
+  }
+}
+
 extern "C" int dccm_step_run_host(dccm_step *st, void *stream, const dccm_host_copy *h2d, int nh2d,
                                   const dccm_host_copy *d2h, int nd2h) {
   if (!st || (nh2d > 0 && !h2d) || (nd2h > 0 && !d2h) || nh2d < 0 || nd2h < 0) return DCCM_ERR_INVALID_ARG;
   cudaStream_t s = as_stream(stream);
-  for (int k = 0; k < nh2d; ++k)
-    DCCM_CUDA(cudaMemcpyAsync(h2d[k].dev, h2d[k].host, h2d[k].bytes, cudaMemcpyHostToDevice, s));
-  DCCM_CUDA(cudaGraphLaunch(st->exec, s));
-  for (int k = 0; k < nd2h; ++k)
-    DCCM_CUDA(cudaMemcpyAsync(d2h[k].host, d2h[k].dev, d2h[k].bytes, cudaMemcpyDeviceToHost, s));
+  // Page-locked host buffers: the copies join the step's graph, each next to
+  // the stage that needs or produces its data.  Otherwise (pageable memory)
+  // copy in, replay, copy out.
+  bool locked = true;
+  for (int k = 0; k < nh2d + nd2h && locked; ++k) {
+    const dccm_host_copy &c = k < nh2d ? h2d[k] : d2h[k - nh2d];
+    cudaPointerAttributes a;
+    locked = cudaPointerGetAttributes(&a, c.host) == cudaSuccess && a.type == cudaMemoryTypeHost;
+  }
+  cudaGetLastError();  // clear a failed attribute query
+  if (!locked) {
+    for (int k = 0; k < nh2d; ++k)
+      DCCM_CUDA(cudaMemcpyAsync(h2d[k].dev, h2d[k].host, h2d[k].bytes, cudaMemcpyHostToDevice, s));
+    DCCM_CUDA(cudaGraphLaunch(st->exec, s));
+    for (int k = 0; k < nd2h; ++k)
+      DCCM_CUDA(cudaMemcpyAsync(d2h[k].host, d2h[k].dev, d2h[k].bytes, cudaMemcpyDeviceToHost, s));
+    DCCM_CUDA(cudaStreamSynchronize(s));
+    return DCCM_OK;
+  }
+  if (!same_copies(st->host_h2d, h2d, nh2d) || !same_copies(st->host_d2h, d2h, nd2h) || !st->hexec) {
+    drop_host_graph(st);
+    HostPlan hp;
+    sort_copies(st, h2d, nh2d, d2h, nd2h, hp);
+    HostSets hs;
+    DCCM_TRY(prepare_sets(st, hp, hs));
+    cudaGraph_t g = nullptr;
+    DCCM_TRY(capture(st, &hs, &g));
+    st->hgraph = g;
+    DCCM_CUDA(cudaGraphInstantiate(&st->hexec, g, 0));
+    st->host_h2d.assign(h2d, h2d + nh2d);
+    st->host_d2h.assign(d2h, d2h + nd2h);
+  }
+  DCCM_CUDA(cudaGraphLaunch(st->hexec, s));
   DCCM_CUDA(cudaStreamSynchronize(s));
   return DCCM_OK;
 }
@@ -387,7 +747,7 @@ extern "C" int dccm_step_autotune(dccm_step *st, const char *cache_path, int *ch
       int k0, k1;
     } knobs[] = {
         {&T.tc_ctas, {sms, sms * 3 / 4, sms / 2, sms / 4}, 0, 4},
-        {&T.fft_bb, {8, 4, 2, 1}, 1, 3},
+        {&T.fft_bb, {16, 8, 4}, 1, 3},
         {&T.flux_threads, {64, 128, 256}, 5, 6},
         {&T.remap_threads, {128, 256}, 4, 5},
     };

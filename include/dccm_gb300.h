@@ -151,7 +151,9 @@ int dccm_remap_table_destroy(dccm_remap_table *table);
  * zeroed and then recv(r,d) += send(s,d)*coef in table order, with the
  * product and the sum rounded separately, so results are bit-identical to
  * the reference loop.  mapping/exchange tags select the plan on the
- * caller's side and are not arguments here.
+ * caller's side and are not arguments here.  One call handles
+ * n_recv_points * num_of_data < 2^30 destination values; larger calls
+ * return DCCM_ERR_UNSUPPORTED (split the fields over several calls).
  * ===================================================================== */
 typedef struct dccm_remap_plan dccm_remap_plan;
 
@@ -325,9 +327,23 @@ int dccm_step_run(dccm_step *step, void *stream);
  * ms[2] forward FFT, ms[3] Legendre analysis, ms[4] remaps, ms[5] bulk
  * flux (six floats).  Synchronises. */
 int dccm_step_run_timed(dccm_step *step, void *stream, float *ms);
-/* Copies nh2d host buffers to the device, replays the graph, copies nd2h
- * device buffers back and synchronises: the step for a caller whose data
- * live in host memory (page-locked memory makes the copies asynchronous). */
+/* Copies nh2d host buffers to the device, runs the step, copies nd2h device
+ * buffers back and synchronises: the step for a caller whose data live in
+ * host memory.  With page-locked host buffers the copies are recorded into
+ * a graph of their own (kept until the copy lists change), each next to the
+ * stage that needs or produces its data, so that they overlap the kernels:
+ * spectral inputs before Legendre synthesis, surface inputs at the head of
+ * the remap/flux branch, grid outputs right after the inverse FFT, spectral
+ * outputs after the analysis, surface outputs after the flux.  A copy that
+ * touches the buffers of both branches, or that reads memory an upload of
+ * the same call writes, is ordered before (H2D) or after (D2H) the whole
+ * step.  Copies whose host buffers lie back to back (e.g. rows of one host
+ * allocation, over 1 MiB in all) move as one copy-engine transfer through a
+ * device staging buffer, gathered or scattered on the device; other copies
+ * of at most 1 MiB go, per group, through one kernel that reads or writes
+ * the host buffers through their device mapping; larger ones are
+ * copy-engine transfers.  With pageable buffers: copies in, graph, copies
+ * out. */
 int dccm_step_run_host(dccm_step *step, void *stream, const dccm_host_copy *h2d, int nh2d,
                        const dccm_host_copy *d2h, int nd2h);
 

@@ -84,6 +84,42 @@ def test_step_timed_and_host_entry(dccm, oracle, synth, cuda):
     assert rel_l2(h_out.numpy().view(np.complex128), g.spec) <= 1e-6
 
 
+@pytest.mark.parametrize("pinned", [True, False])
+def test_host_copies_match_device_run(dccm, oracle, synth, cuda, pinned):
+    """run_host (copies recorded into the graph beside their stages when the
+    host buffers are page-locked; copy-in/graph/copy-out otherwise) returns
+    exactly what the device-side run produces, including a read-back of
+    uploaded memory (ordered after the whole step) and the inverse grid."""
+    torch = cuda
+    bench, w, inp, S = _small_step(dccm, synth, oracle, torch, 1)
+    groups = inp["groups"]
+    step = S["steps"]["mixed"]
+    h2d, d2h = bench.host_copies(S, groups, dccm, torch)
+    d2h.append((torch.empty(S["grid"][0].shape, dtype=torch.float64).pin_memory(), S["grid"][0]))
+    d2h.append((torch.empty(S["spec_in"][0].shape, dtype=torch.float64).pin_memory(), S["spec_in"][0]))
+    if not pinned:
+        h2d = [(h.clone(), d) for h, d in h2d]
+        d2h = [(torch.empty(h.shape, dtype=h.dtype), d) for h, d in d2h]
+        assert not h2d[0][0].is_pinned()
+    for h, d in h2d:
+        d.copy_(h)
+    step.run()
+    torch.cuda.synchronize()
+    want = [d.cpu().clone() for _, d in d2h]
+    for _, d in d2h:
+        if d.data_ptr() != S["spec_in"][0].data_ptr():
+            d.zero_()
+    for h, d in h2d:
+        d.zero_()
+    torch.cuda.synchronize()
+    for _ in range(2):  # the second call replays the cached host graph
+        for h, _ in d2h:
+            h.zero_()
+        step.run_host(h2d, d2h)
+        for (h, _), ref in zip(d2h, want):
+            assert torch.equal(h, ref)
+
+
 def test_remap_two_level_destination(dccm, oracle, synth, cuda):
     """nsub/ld_dst2: member m's field f lands at dst + f*ld_dst + m*ld_dst2."""
     torch = cuda
