@@ -315,6 +315,120 @@ def host_copies(S, groups, dccm, torch):
     return h2d, d2h
 
 
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of
+# each stage's kernels in one ncu capture of `bench.py --profile-steps`,
+# summarised in profiles/stages_c3_ncu.md; null where not captured.
+TRAFFIC = {
+    "c3": {"legendre_inverse": int((7.68384 + 12.144896) * 1e6 + 2304), "fft_inverse": int(11.341056e6 + 1792),
+           "fft_forward": int(33.62304e6 + 309248), "legendre_forward": int(18.947072e6 + 2816),
+           "remap": int(4.06912e6), "bulk_flux": int(7.707904e6 + 256)},
+}
+FP64_PEAK_TFLOPS = 152 * 2 * 2 * 2.070e9 / 1e12  # 2 DFMA lanes per SM and clock at the maximum SM clock
+
+
+def stage_work(S, inp, groups):
+    """Algorithmic bytes (minimal HBM traffic) and flops of each stage.
+    Legendre synthesis: FP64 spectra in, FP32 Fourier coefficients out, the
+    split Legendre table (6 bytes an entry) in; analysis the reverse.  The
+    tensor work (six BF16 products of the split operands) is far below the
+    byte time, so both Legendre stages are bandwidth-bound.  FFT: FP32
+    Fourier coefficients <-> FP64 grid.  Remap: 16 bytes per table entry,
+    row pointers, source fields once and destination rows.  Flux: 504
+    bytes per ocean column (inputs and outputs, FP64)."""
+    spec = sum(g.nfl * (g.N + 1) * (g.N + 2) // 2 * 16 for g in groups)
+    four = sum(g.nfl * g.J * (g.N + 1) * 2 * 4 for g in groups)
+    table = sum((g.N + 1) * (g.N + 2) // 2 * (g.J // 2) * 6 for g in groups)
+    grid = sum(g.nfl * g.J * g.I * 8 for g in groups)
+    flops = sum(2.0 * g.J * (g.N + 1) * (g.N + 2) / 2 * g.nfl for g in groups)
+    n1 = len(inp["ocean"])
+    remap = sum(16 * len(tb[2]) + 8 * (n1 + 1) + 8 * 6 * len(g.members) * (g.I * g.J + n1)
+                for g, tb in zip(groups, S["tables"]))
+    return {"legendre_inverse": (spec + four + table, flops), "fft_inverse": (four + grid, None),
+            "fft_forward": (grid + four, None), "legendre_forward": (four + spec + table, flops),
+            "remap": (remap, None), "bulk_flux": (504 * S["ncol"], None)}
+
+
+def roofline(S, inp, groups, stage_ms, workload):
+    """Per-stage roofline against the measured copy bandwidth; the dominant
+    (longest) stage is the headline.  Legendre stages also report their
+    tensor rate (useful flops over the measured BF16 peak); the flux
+    kernel, bound by the FP64 pipe, reports its FP64 rate as counted by ncu
+    over the FP64 peak (2 DFMA lanes per SM and clock)."""
+    hbm, bf16, src_peak = peaks()
+    names = dccm_stages()
+    work = stage_work(S, inp, groups)
+    traffic = TRAFFIC.get(workload, {})
+    stages = {}
+    for n, ms in zip(names, stage_ms):
+        q, fl = work[n]
+        ach = q / (ms / 1e3) / 1e9
+        st = {"ms": float(ms), "bound": "hbm", "achieved": ach, "unit": "GB/s", "peak": hbm, "frac": ach / hbm,
+              "algorithmic_bytes": q, "traffic": traffic.get(n)}
+        if fl is not None:
+            tf = fl / (ms / 1e3) / 1e12
+            st["tensor"] = {"achieved": tf, "unit": "TFLOP/s", "peak": bf16, "frac": tf / bf16,
+                            "algorithmic_flops": fl}
+        stages[n] = st
+    stages["bulk_flux"]["limiter"] = "FP64 pipe, not HBM"
+    f64 = FP64_FLOPS.get(workload)
+    if f64:
+        tf = f64 / (stages["bulk_flux"]["ms"] / 1e3) / 1e12
+        stages["bulk_flux"]["fp64"] = {"achieved": tf, "unit": "TFLOP/s", "peak": FP64_PEAK_TFLOPS,
+                                       "frac": tf / FP64_PEAK_TFLOPS, "flops_per_launch": f64}
+    dom = names[int(np.argmax(stage_ms))]
+    roof = dict(stages[dom])
+    roof.update({"kernel": dom, "peak_source": src_peak, "stages": stages,
+                 "traffic_source": "profiles/stages_c3_ncu.md" if workload in TRAFFIC else None})
+    return roof
+
+
+# FP64 flops per launch of the flux kernel (DADD + DMUL + 2 DFMA thread
+# instructions, ncu sass counters), summarised in profiles/stages_c3_ncu.md.
+FP64_FLOPS = {"c3": (20.948747 + 41.897494 + 2 * 114.69439) * 86836.697368}
+
+
+def dccm_stages():
+    return ["legendre_inverse", "fft_inverse", "fft_forward", "legendre_forward", "remap", "bulk_flux"]
+
+
+def profile_run(args, w, inp):
+    """Graph replays of the mixed-precision step only (default launch
+    shapes, no autotuning, no host copies): a small, countable launch
+    sequence for ncu.  Each replay launches, in order, the spectra pack,
+    Legendre synthesis, inverse FFT, forward FFT, Legendre analysis, one
+    remap per truncation group and the flux kernel."""
+    import torch
+    dccm = importlib.import_module("dennou-ccm_gb300")
+    synth = importlib.import_module("dennou-ccm_gb300.synth")
+    dev = torch.device("cuda", 0)
+    S = gpu_setup(w, inp, dccm, synth, torch, dev)
+    step = S["steps"]["mixed"]
+    for _ in range(args.profile_steps):
+        step.run()
+    torch.cuda.synchronize()
+    st, derr = S["plans"]["mixed"].status()
+    print(json.dumps({"profile_steps": args.profile_steps, "workload": args.workload, "status": st,
+                      "device_error": derr}))
+
+
+def max_over_ranks(vals, world, dev):
+    """Element-wise maximum of per-rank times over the process group (the
+    job's time is its slowest replica); identity on one rank.  dev is where
+    the reduction tensor lives (a CUDA device for NCCL, "cpu" for gloo)."""
+    if world <= 1:
+        return list(vals)
+    import torch
+    t = torch.tensor(vals, dtype=torch.float64, device=dev)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return [float(x) for x in t.cpu()]
+
+
+def job_throughput(world, nfl, t_step):
+    """Whole-job field-levels/s: every replica transforms nfl field-levels
+    per step (weak scaling), the job's step time is the slowest rank's."""
+    return world * nfl / t_step
+
+
 def gpu_bench(args, w, inp, rank, world):
     import torch
     dccm = importlib.import_module("dennou-ccm_gb300")
@@ -354,12 +468,7 @@ def gpu_bench(args, w, inp, rank, world):
     ms_mixed = timed(S["steps"]["mixed"], args.steps, max(3, args.warmup))
     ck = clocks.stop(dev.index or 0)
     ms_fp64 = timed(S["steps"]["fp64"], args.steps, max(3, args.warmup))
-    t_mixed = float(np.mean(ms_mixed)) / 1e3
-    t_fp64 = float(np.mean(ms_fp64)) / 1e3
-    if world > 1:
-        tt = torch.tensor([t_mixed, t_fp64], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_mixed, t_fp64 = (float(x) for x in tt.cpu())
+    t_mixed, t_fp64 = max_over_ranks([float(np.mean(ms_mixed)) / 1e3, float(np.mean(ms_fp64)) / 1e3], world, dev)
 
     # accuracy of the mixed step against the FP64 step on the same inputs
     S["steps"]["fp64"].run(stream)
@@ -386,30 +495,7 @@ def gpu_bench(args, w, inp, rank, world):
         flush.fill_(float(k))
         stage_ms += np.array(S["steps"]["mixed"].run_timed(stream))
     stage_ms /= nt
-    hbm, bf16, src_peak = peaks()
-    leg_flops = sum(2.0 * g.J * (g.N + 1) * (g.N + 2) / 2 * g.nfl for g in groups)
-    fft_bytes = sum(g.nfl * g.J * g.I * 8 + g.nfl * g.J * (g.N + 1) * 2 * 4 for g in groups)
-    n1 = len(inp["ocean"])
-    remap_bytes = sum(12 * len(tb[2]) + 4 * (n1 + 1) + 8 * 6 * len(g.members) * (g.I * g.J + n1)
-                      for g, tb in zip(groups, S["tables"]))
-    flux_bytes = 504 * S["ncol"]
-    names = dccm.Step.STAGES
-    work = [("tensor", leg_flops), ("hbm", fft_bytes), ("hbm", fft_bytes), ("tensor", leg_flops),
-            ("hbm", remap_bytes), ("hbm", flux_bytes)]
-    stages = {}
-    for n, (bound, q), ms in zip(names, work, stage_ms):
-        if bound == "tensor":
-            ach = q / (ms / 1e3) / 1e12
-            stages[n] = {"ms": float(ms), "bound": "tensor", "achieved": ach, "unit": "TFLOP/s", "peak": bf16,
-                         "frac": ach / bf16, "algorithmic_flops": q}
-        else:
-            ach = q / (ms / 1e3) / 1e9
-            stages[n] = {"ms": float(ms), "bound": "hbm", "achieved": ach, "unit": "GB/s", "peak": hbm,
-                         "frac": ach / hbm, "algorithmic_bytes": q}
-    stages["bulk_flux"]["limiter"] = "FP64 pipe (ncu: FP64 pipe ~84 % active), not HBM"
-    dom = names[int(np.argmax(stage_ms))]
-    roof = dict(stages[dom])
-    roof.update({"kernel": dom, "traffic": None, "peak_source": src_peak, "stages": stages})
+    roof = roofline(S, inp, groups, stage_ms, args.workload)
 
     # end to end through the public API with host buffers (pinned)
     h2d, d2h = host_copies(S, groups, dccm, torch)
@@ -426,12 +512,8 @@ def gpu_bench(args, w, inp, rank, world):
         t0 = time.perf_counter()
         S["steps"]["mixed"].run_host(h2d, d2h, stream)
         te.append(time.perf_counter() - t0)
-    t_e2e = float(np.mean(te))
-    if world > 1:
-        tt = torch.tensor([t_e2e], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_e2e = float(tt.cpu()[0])
-    launches = 4 + len(groups) + 1  # 2 Legendre + 2 FFT + one remap per group + flux
+    t_e2e, = max_over_ranks([float(np.mean(te))], world, dev)
+    launches = 5 + len(groups) + 1  # pack + 2 Legendre + 2 FFT + one remap per group + flux
     return dict(t_mixed=t_mixed, t_fp64=t_fp64, t_e2e=t_e2e, clocks=ck, roof=roof, err=err, h2d=h2d_bytes,
                 d2h=d2h_bytes, nfl=nfl, launches=launches, tables=S["tables"], tuned=tuned)
 
@@ -444,6 +526,8 @@ def main():
     ap.add_argument("--workload", default="c3", choices=sorted(WORKLOADS))
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-steps", type=int, default=0,
+                    help="only replay the mixed step this many times (for ncu) and exit")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -482,6 +566,9 @@ def main():
         print(json.dumps(line))
         return
 
+    if args.profile_steps > 0:
+        profile_run(args, w, inp)
+        return
     if world > 1:
         import torch
         torch.distributed.init_process_group("nccl")
@@ -499,15 +586,15 @@ def main():
                "sample": "3 steps: transforms of %d of %d field-levels (scaled), every remap and the bulk flux; "
                          "C FP64 oracle, OpenMP" % (nsample, nfl)}
     line = {
-        "metric": metric, "value": world * nfl / r["t_mixed"], "unit": "field-levels/s", "n_gpus": world,
+        "metric": metric, "value": job_throughput(world, nfl, r["t_mixed"]), "unit": "field-levels/s", "n_gpus": world,
         "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": r["t_mixed"] * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "bf16x3+f32 (Legendre), f32 (FFT), f64 (remap, flux)",
         "data": "synthetic (seeded PCG64; n^-3 spectra, SST-based surface state)", "config": config,
-        "fp64_gpu": {"value": world * nfl / r["t_fp64"], "ms_per_step": r["t_fp64"] * 1e3,
+        "fp64_gpu": {"value": job_throughput(world, nfl, r["t_fp64"]), "ms_per_step": r["t_fp64"] * 1e3,
                      "mixed_over_fp64": r["t_fp64"] / r["t_mixed"]},
         "accuracy": r["err"],
-        "e2e": {"value": world * nfl / r["t_e2e"], "unit": "field-levels/s", "h2d_bytes_per_step": r["h2d"],
+        "e2e": {"value": job_throughput(world, nfl, r["t_e2e"]), "unit": "field-levels/s", "h2d_bytes_per_step": r["h2d"],
                 "d2h_bytes_per_step": r["d2h"], "ms_per_step": r["t_e2e"] * 1e3},
         "gpu_launches": r["launches"] * args.steps,
         "roofline": r["roof"], "clocks": r["clocks"], "cpu_baseline": cpu,
