@@ -514,8 +514,54 @@ def gpu_bench(args, w, inp, rank, world):
         te.append(time.perf_counter() - t0)
     t_e2e, = max_over_ranks([float(np.mean(te))], world, dev)
     launches = 5 + len(groups) + 1  # pack + 2 Legendre + 2 FFT + one remap per group + flux
+    ic = implcpl_leg(args, groups, dccm, synth, torch, dev, stream, flush)
     return dict(t_mixed=t_mixed, t_fp64=t_fp64, t_e2e=t_e2e, clocks=ck, roof=roof, err=err, h2d=h2d_bytes,
-                d2h=d2h_bytes, nfl=nfl, launches=launches, tables=S["tables"], tuned=tuned)
+                d2h=d2h_bytes, nfl=nfl, launches=launches, tables=S["tables"], tuned=tuned, implcpl=ic)
+
+
+def implcpl_leg(args, groups, dccm, synth, torch, dev, stream, flush):
+    """The implicit surface coupling of the largest truncation group's
+    atmosphere (every Gaussian-grid column, the group's level count, one
+    tracer), reported beside the step: forward sweep (ImplCplCoef1/2 for the
+    bulk flux) and backward sweep, CUDA events, L2 flushed between runs.
+    Algorithmic bytes: 12 input profiles and 4 outputs of kmax+1 levels, the
+    module-state matrices written and read back (3 x 3 x kmax), FP64."""
+    g = max(groups, key=lambda q: q.I * q.J)
+    ncol, kmax = g.I * g.J, max(2, g.nfl // 4 if len(groups) == 1 else 32)
+    d = synth.column_profiles(ncol, kmax, ncmax=1, seed=7)
+    plan = dccm.ImplCplPlan(ncol, kmax, 1, 1, synth.IMPLCPL_CONSTS)
+    dd = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in d.items()}
+    out = {"DUDt": (kmax, ncol), "DVDt": (kmax, ncol), "DTempDt": (kmax, ncol), "DQMixDt": (1, kmax, ncol),
+           "ImplCplCoef1": (4, ncol), "ImplCplCoef2": (4, ncol)}
+    out = {k: torch.empty(v, dtype=torch.float64, device=dev) for k, v in out.items()}
+    tf, tb = [], []
+    for it in range(max(3, args.warmup) + max(3, min(args.steps, 20))):
+        flush.fill_(float(it))
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        e[0].record(stream)
+        plan.forward_dev(dd, out, stream)
+        e[1].record(stream)
+        for k in ("DUDt", "DVDt", "DTempDt"):
+            out[k][0].fill_(1e-3)  # the surface solution at level 1
+        out["DQMixDt"][:, 0].fill_(1e-7)
+        plan.backward_dev(out, stream)
+        e[2].record(stream)
+        torch.cuda.synchronize()
+        if it >= max(3, args.warmup):
+            tf.append(e[0].elapsed_time(e[1]))
+            tb.append(e[1].elapsed_time(e[2]))
+    hbm, _, _ = peaks()
+    fwd_bytes = ncol * 8 * ((kmax + 1) * (9 + 1) + kmax * 2 + kmax * 4 + 8 + 3 * 3 * kmax)
+    bwd_bytes = ncol * 8 * (2 * 4 * kmax + 3 * 2 * kmax)
+    f, b = float(np.mean(tf)), float(np.mean(tb))
+    return {"columns": ncol, "levels": kmax, "tracers": 1, "forward_ms": f, "backward_ms": b,
+            "columns_per_s": ncol / ((f + b) / 1e3),
+            "forward_roofline": {"bound": "hbm", "algorithmic_bytes": fwd_bytes,
+                                 "achieved": fwd_bytes / (f / 1e3) / 1e9, "unit": "GB/s", "peak": hbm,
+                                 "frac": fwd_bytes / (f / 1e3) / 1e9 / hbm},
+            "backward_roofline": {"bound": "hbm", "algorithmic_bytes": bwd_bytes,
+                                  "achieved": bwd_bytes / (b / 1e3) / 1e9, "unit": "GB/s", "peak": hbm,
+                                  "frac": bwd_bytes / (b / 1e3) / 1e9 / hbm}}
 
 
 def main():
@@ -598,6 +644,7 @@ def main():
                 "d2h_bytes_per_step": r["d2h"], "ms_per_step": r["t_e2e"] * 1e3},
         "gpu_launches": r["launches"] * args.steps,
         "roofline": r["roof"], "clocks": r["clocks"], "cpu_baseline": cpu,
+        "implicit_coupling": r["implcpl"],
     }
     print(json.dumps(line))
     if world > 1:

@@ -59,6 +59,20 @@ class SfcGrid(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int) for n in ("IA", "JA", "IS", "IE", "JS", "JE")]
 
 
+IMPLCPL_FWD_ARGS = ["xyr_MomFluxX", "xyr_MomFluxY", "xyr_HeatFlux", "xyrf_QMixFlux", "xyr_Press",
+                    "xyz_Exner", "xyr_Exner", "xyr_VirTemp", "xyz_Height", "xyr_VelDiffCoef",
+                    "xyr_TempDiffCoef", "xyr_QMixDiffCoef", "xyz_DUDt", "xyz_DVDt", "xyz_DTempDt",
+                    "xyzf_DQMixDt", "xya_ImplCplCoef1", "xya_ImplCplCoef2"]
+
+
+class ImplCplConsts(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in ("Grav", "CpDry", "GasRDry", "DelTime")]
+
+
+class ImplCplForwardArgs(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_void_p) for n in IMPLCPL_FWD_ARGS]
+
+
 _lib = None
 _SIGS = {
     "dccm_status_string": (ctypes.c_char_p, [ctypes.c_int]),
@@ -66,6 +80,14 @@ _SIGS = {
     "dccm_last_cuda_error": (ctypes.c_int, []),
     "dccm_sfc_bulk_flux_get": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "dccm_sfc_bulk_flux_get_dev": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "dccm_implcpl_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                           ctypes.c_void_p, ctypes.c_void_p]),
+    "dccm_implcpl_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "dccm_implcpl_forward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "dccm_implcpl_forward_dev": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "dccm_implcpl_backward": (ctypes.c_int, [ctypes.c_void_p] * 5),
+    "dccm_implcpl_backward_dev": (ctypes.c_int, [ctypes.c_void_p] * 6),
+    "dccm_implcpl_matrices": (ctypes.c_int, [ctypes.c_void_p] * 4),
     "dccm_j99_generate": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
                                          ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
@@ -500,3 +522,76 @@ class Step:
         if getattr(self, "h", None) and _lib is not None:
             _lib.dccm_step_destroy(self.h)
             self.h = None
+
+
+# ------------------------------------------------------- implicit coupling
+class ImplCplPlan:
+    """SfcImplicitCoupling_VDiffForward / _VDiffBackward
+    (atm/dcpam_sfc_implicit_coupling_mod.f90:72-378, :25-70) over ncol
+    columns of kmax levels; the plan keeps the eliminated matrices (the
+    reference's module state) between the two sweeps.  Arrays are the
+    reference's with the columns flattened, given row-major as [k][c]
+    (tracers [n][k][c], coefficients [a][c]); numpy arrays for the host
+    entry points, CUDA tensors for the device ones."""
+
+    def __init__(self, ncol, kmax, ncmax=1, index_h2ovap=1, consts=(9.8, 1004.6, 287.04, 1200.0)):
+        self.ncol, self.kmax, self.ncmax = int(ncol), int(kmax), int(ncmax)
+        self.consts = ImplCplConsts(*[float(x) for x in consts])
+        h = ctypes.c_void_p()
+        _check(load().dccm_implcpl_create(self.ncol, self.kmax, self.ncmax, int(index_h2ovap),
+                                          ctypes.byref(self.consts), ctypes.byref(h)), "dccm_implcpl_create")
+        self.h = h
+
+    def _args(self, prof, out):
+        a = ImplCplForwardArgs()
+        names = {"xyr_MomFluxX": "MomFluxX", "xyr_MomFluxY": "MomFluxY", "xyr_HeatFlux": "HeatFlux",
+                 "xyrf_QMixFlux": "QMixFlux", "xyr_Press": "Press", "xyz_Exner": "ExnerFull",
+                 "xyr_Exner": "ExnerHalf", "xyr_VirTemp": "VirTemp", "xyz_Height": "Height",
+                 "xyr_VelDiffCoef": "VelDiffCoef", "xyr_TempDiffCoef": "TempDiffCoef",
+                 "xyr_QMixDiffCoef": "QMixDiffCoef", "xyz_DUDt": "DUDt", "xyz_DVDt": "DVDt",
+                 "xyz_DTempDt": "DTempDt", "xyzf_DQMixDt": "DQMixDt", "xya_ImplCplCoef1": "ImplCplCoef1",
+                 "xya_ImplCplCoef2": "ImplCplCoef2"}
+        for f, n in names.items():
+            x = prof.get(n) if n in prof else out[n]
+            setattr(a, f, _p(x).value)
+        return a
+
+    def forward(self, prof):
+        """Host arrays in (synth.column_profiles layout); returns the
+        tendencies and coupling coefficients as numpy arrays."""
+        K, n, nc = self.kmax, self.ncol, self.ncmax
+        prof = {k: np.ascontiguousarray(v, dtype=np.float64) for k, v in prof.items()}
+        out = {"DUDt": np.empty((K, n)), "DVDt": np.empty((K, n)), "DTempDt": np.empty((K, n)),
+               "DQMixDt": np.empty((nc, K, n)), "ImplCplCoef1": np.empty((4, n)), "ImplCplCoef2": np.empty((4, n))}
+        a = self._args(prof, out)
+        _check(load().dccm_implcpl_forward(self.h, ctypes.byref(a)), "dccm_implcpl_forward")
+        return out
+
+    def forward_dev(self, prof, out, stream=None):
+        """Device tensors in and out (same shapes as forward); stream-ordered."""
+        a = self._args(prof, out)
+        _check(load().dccm_implcpl_forward_dev(self.h, ctypes.byref(a), _stream(stream)), "dccm_implcpl_forward_dev")
+
+    def backward(self, tend):
+        """Host arrays DUDt, DVDt, DTempDt, DQMixDt, updated in place."""
+        for k in ("DUDt", "DVDt", "DTempDt", "DQMixDt"):
+            assert tend[k].dtype == np.float64 and tend[k].flags.c_contiguous
+        _check(load().dccm_implcpl_backward(self.h, *[_p(tend[k]) for k in ("DUDt", "DVDt", "DTempDt", "DQMixDt")]),
+               "dccm_implcpl_backward")
+
+    def backward_dev(self, tend, stream=None):
+        _check(load().dccm_implcpl_backward_dev(self.h, *[_p(tend[k]) for k in ("DUDt", "DVDt", "DTempDt", "DQMixDt")],
+                                                _stream(stream)), "dccm_implcpl_backward_dev")
+
+    def matrices(self):
+        """The module-state matrices (UVMtx, TempMtx, QMixMtx), each [3][kmax][ncol]."""
+        m = {k: np.empty((3, self.kmax, self.ncol)) for k in ("UVMtx", "TempMtx", "QMixMtx")}
+        _check(load().dccm_implcpl_matrices(self.h, _p(m["UVMtx"]), _p(m["TempMtx"]), _p(m["QMixMtx"])),
+               "dccm_implcpl_matrices")
+        return m
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.dccm_implcpl_destroy(self.h)
+            self.h = None
+

@@ -40,7 +40,7 @@ int sm_count();
 // dccm_tune_set / dccm_tune_get expose them.
 struct Tunables {
   int tc_ctas = 0;        // persistent CTAs of the tensor-core Legendre kernel
-  int fft_bb = 0;         // field-levels (warps) per FFT CTA
+  int fft_bb = 0;         // warps per FFT CTA (4, 8, 16)
   int flux_threads = 0;   // threads per CTA of the bulk-flux kernel
   int remap_threads = 0;  // threads per CTA of the remap kernel
 };

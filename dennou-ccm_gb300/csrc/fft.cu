@@ -20,12 +20,13 @@
 // once per warp.
 //
 // Shared memory stages, per CTA (latitude pair jj, BB field-levels), the
-// Fourier coefficients of all m in planes of 16 R + 1 floats, one plane per
+// Fourier coefficients of all m in planes of 17 R + 1 floats, one plane per
 // (row or parity, re/im, field-level); coefficient m sits at slot
-// (m mod R) * 16 + m / R.  A lane reads or writes the m = k1 + R k2 it owns
-// at k1 * 16 + k2 (consecutive across lanes), and the CTA-wide copy between
-// shared and global memory walks field-levels fastest (plane stride odd):
-// both sides are free of bank conflicts and the global side is coalesced.
+// (m mod R) * 17 + m / R.  A lane reads or writes the m = k1 + R k2 it owns
+// at k1 * 17 + k2 (consecutive across lanes), and the CTA-wide copy between
+// shared and global memory walks field-levels fastest over an odd plane
+// stride, consecutive m 17 words apart: both sides are free of bank
+// conflicts and the global side is coalesced.
 // Supported lengths: R in {2, 3, 4, 6, 8, 12, 16, 24, 32}, I = 64 ... 1024.
 //
 // Inverse: Z_m = A_m + i B_m and Z_{I-m} = conj(A_m) + i conj(B_m) from the
@@ -125,6 +126,41 @@ __device__ __forceinline__ void lane_twiddles(const float2 *tw, int lane, bool i
   }
 }
 
+// 32-point DFT across the lanes of every register n < NV, decimation in
+// frequency: lane l ends with the output brev5(l).
+template <int NV>
+__device__ __forceinline__ void lane_dif(float2 (&v)[NV], const float2 (&w)[5], int lane) {
+#pragma unroll
+  for (int s = 0; s < 5; ++s) {
+    const int h = 16 >> s;
+    const float sg = (lane & h) ? -1.f : 1.f;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      // lower: a + b; upper: (a - b) w  (the lower lane holds a)
+      const float2 p = shfl_xor_c(v[k], h);
+      const float2 t = make_float2(fmaf(sg, v[k].x, p.x), fmaf(sg, v[k].y, p.y));
+      v[k] = cmul(t, w[s]);
+    }
+  }
+}
+
+// Its inverse (unnormalised), decimation in time from bit-reversed input.
+template <int NV>
+__device__ __forceinline__ void lane_dit(float2 (&v)[NV], const float2 (&w)[5], int lane) {
+#pragma unroll
+  for (int s = 0; s < 5; ++s) {
+    const int h = 1 << s;
+    const float sg = (lane & h) ? -1.f : 1.f;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      // lower: a + w b; upper: a - w b  (the upper lane holds b)
+      const float2 x = cmul(v[k], w[s]);
+      const float2 p = shfl_xor_c(x, h);
+      v[k] = make_float2(fmaf(sg, x.x, p.x), fmaf(sg, x.y, p.y));
+    }
+  }
+}
+
 // Forward complex FFT of one row held as v[r] = z[32 r + lane];
 // on return v[k1] = Z[k1 + R brev5(lane)].
 template <int R>
@@ -134,18 +170,7 @@ __device__ __forceinline__ void warp_fft_fwd(float2 (&v)[R], const float2 *tw, c
   RegDft<R>::run(v, tw, I, -1);
 #pragma unroll
   for (int k = 1; k < R; ++k) v[k] = cmul(v[k], __ldg(twl + k * 32 + lane));
-#pragma unroll
-  for (int s = 0; s < 5; ++s) {
-    const int h = 16 >> s;
-    const float sg = (lane & h) ? -1.f : 1.f;
-#pragma unroll
-    for (int k = 0; k < R; ++k) {
-      // lower: a + b; upper: (a - b) w  (the lower lane holds a)
-      const float2 p = shfl_xor_c(v[k], h);
-      const float2 t = make_float2(fmaf(sg, v[k].x, p.x), fmaf(sg, v[k].y, p.y));
-      v[k] = cmul(t, w[s]);
-    }
-  }
+  lane_dif<R>(v, w, lane);
 }
 
 // Inverse (unnormalised) FFT of one row held as v[k1] = Z[k1 + R brev5(lane)];
@@ -154,18 +179,7 @@ template <int R>
 __device__ __forceinline__ void warp_fft_inv(float2 (&v)[R], const float2 *tw, const float2 *twl,
                                              const float2 (&w)[5], int lane) {
   constexpr int I = 32 * R;
-#pragma unroll
-  for (int s = 0; s < 5; ++s) {
-    const int h = 1 << s;
-    const float sg = (lane & h) ? -1.f : 1.f;
-#pragma unroll
-    for (int k = 0; k < R; ++k) {
-      // lower: a + w b; upper: a - w b  (the upper lane holds b)
-      const float2 x = cmul(v[k], w[s]);
-      const float2 p = shfl_xor_c(x, h);
-      v[k] = make_float2(fmaf(sg, x.x, p.x), fmaf(sg, x.y, p.y));
-    }
-  }
+  lane_dit<R>(v, w, lane);
 #pragma unroll
   for (int k = 1; k < R; ++k) {
     float2 t = __ldg(twl + k * 32 + lane);
@@ -177,7 +191,7 @@ __device__ __forceinline__ void warp_fft_inv(float2 (&v)[R], const float2 *tw, c
 
 constexpr int FFT_MAXG = 8;
 struct FftGroup {
-  int N, J, batch, BB, lbb, R, blk0, C2Bp;  // lbb = log2(BB)
+  int N, J, batch, BB, lbb, R, W, blk0, C2Bp;  // BB row pairs per CTA, lbb = log2(BB), W warps per row pair
   const void *in;
   void *out;
   const float2 *tw, *twl;
@@ -187,54 +201,69 @@ struct FftLaunch {
   int ngroups;
 };
 
-template <int R> __device__ __forceinline__ int slot_of(int m) { return (m % R) * 16 + m / R; }
+template <int R> __device__ __forceinline__ int slot_of(int m) { return (m % R) * 17 + m / R; }
 
 // ------------------------------------------------------------- inverse
 // One CTA: latitude pair jj, field-levels [by*BB, by*BB + BB); warp bl
 // transforms field-level b0 + bl.  Planes (row, re/im, field-level).
+// Copy F[m][jn|js][2 b0 + c] of the CTA's field-levels into the staging
+// planes (row, re/im, field-level) at slot (m mod R) * 17 + m / R.
 template <int R>
-__device__ __forceinline__ void fft_inv_block(const FftGroup &G, int jj, int by, float *st) {
-  constexpr int I = 32 * R, PS = R * 16 + 1;
-  const int N = G.N, J = G.J, Jh = J / 2, lbb = G.lbb, lcw = G.lbb + 1;
-  const int jn = Jh + jj, js = Jh - 1 - jj;
-  const int b0 = by * G.BB;
-  const int nb = min(G.BB, G.batch - b0);
+__device__ __forceinline__ void stage_fourier(const FftGroup &G, int jn, int js, int b0, int nb, float *st) {
+  constexpr int PS = R * 17 + 1;
+  const int lbb = G.lbb, lcw = G.lbb + 1;
   const long long C2B = 2LL * G.batch;
   const float *F = static_cast<const float *>(G.in);
-  const int tot = (N + 1) << (lcw + 1);  // (m, row, c), c fastest
+  const int tot = (G.N + 1) << (lcw + 1);  // (m, row, c), c fastest
   for (int t = threadIdx.x; t < tot; t += blockDim.x) {
     const int c = t & ((1 << lcw) - 1);
     const int row = (t >> lcw) & 1;
     const int m = t >> (lcw + 1);
     float v = 0.f;
-    if (c < 2 * nb) v = F[((long long)m * J + (row ? js : jn)) * C2B + 2LL * b0 + c];
+    if (c < 2 * nb) v = F[((long long)m * G.J + (row ? js : jn)) * C2B + 2LL * b0 + c];
     st[(((row * 2 + (c & 1)) << lbb) + (c >> 1)) * PS + slot_of<R>(m)] = v;
   }
+}
+
+// Z_k of the inverse from the staged coefficients of field-level bl: q is k
+// mod R (q = k1 + R0 wq), kl = k / R the lane's bit-reversed index.
+template <int R>
+__device__ __forceinline__ float2 inverse_input(const float *st, int lbb, int bl, int N, int q, int kl) {
+  constexpr int I = 32 * R, PS = R * 17 + 1;
+  const float *Ar = st + ((0 << lbb) + bl) * PS, *Ai = st + ((1 << lbb) + bl) * PS;
+  const float *Br = st + ((2 << lbb) + bl) * PS, *Bi = st + ((3 << lbb) + bl) * PS;
+  const int k = q + R * kl;
+  float2 z = make_float2(0.f, 0.f);
+  if (k <= N) {  // m = k
+    const int sl = q * 17 + kl;
+    const float ar = Ar[sl], br = Br[sl];
+    const float ai = k ? Ai[sl] : 0.f, bi = k ? Bi[sl] : 0.f;
+    z = make_float2(ar - bi, ai + br);
+  } else if (k >= I - N) {  // m = I - k
+    const int sl = q ? (R - q) * 17 + (31 - kl) : 32 - kl;
+    const float ar = Ar[sl], ai = Ai[sl], br = Br[sl], bi = Bi[sl];
+    z = make_float2(ar + bi, br - ai);
+  }
+  return z;
+}
+
+template <int R>
+__device__ __forceinline__ void fft_inv_block(const FftGroup &G, int jj, int by, float *st) {
+  constexpr int I = 32 * R;
+  const int N = G.N, J = G.J, Jh = J / 2, lbb = G.lbb;
+  const int jn = Jh + jj, js = Jh - 1 - jj;
+  const int b0 = by * G.BB;
+  const int nb = min(G.BB, G.batch - b0);
+  stage_fourier<R>(G, jn, js, b0, nb, st);
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   const int k2 = brev5(lane);
   float2 w[5];
   lane_twiddles<R>(G.tw, lane, true, w);
   for (int bl = warp; bl < nb; bl += nw) {
-    const float *Ar = st + ((0 << lbb) + bl) * PS, *Ai = st + ((1 << lbb) + bl) * PS;
-    const float *Br = st + ((2 << lbb) + bl) * PS, *Bi = st + ((3 << lbb) + bl) * PS;
     float2 v[R];
 #pragma unroll
-    for (int k1 = 0; k1 < R; ++k1) {
-      const int k = k1 + R * k2;
-      float2 z = make_float2(0.f, 0.f);
-      if (k <= N) {  // m = k: k / R = k2, k mod R = k1
-        const int sl = k1 * 16 + k2;
-        const float ar = Ar[sl], br = Br[sl];
-        const float ai = k ? Ai[sl] : 0.f, bi = k ? Bi[sl] : 0.f;
-        z = make_float2(ar - bi, ai + br);
-      } else if (k >= I - N) {  // m = I - k
-        const int sl = k1 ? (R - k1) * 16 + (31 - k2) : 32 - k2;
-        const float ar = Ar[sl], ai = Ai[sl], br = Br[sl], bi = Bi[sl];
-        z = make_float2(ar + bi, br - ai);
-      }
-      v[k1] = z;
-    }
+    for (int k1 = 0; k1 < R; ++k1) v[k1] = inverse_input<R>(st, lbb, bl, N, k1, k2);
     warp_fft_inv<R>(v, G.tw, G.twl, w, lane);
     double *gn = static_cast<double *>(G.out) + ((long long)(b0 + bl) * J + jn) * I;
     double *gs = static_cast<double *>(G.out) + ((long long)(b0 + bl) * J + js) * I;
@@ -247,45 +276,12 @@ __device__ __forceinline__ void fft_inv_block(const FftGroup &G, int jj, int by,
 }
 
 // ------------------------------------------------------------- forward
-// Planes (parity, c) with c = 2 bl + re/im.
+// Split the staged E/O values (planes (parity, c) with c = 2 bl + re/im, m
+// at slot (m mod R) * 17 + m / R) into G3[s][(2m + p) Jh + jj][2 b0 + c].
 template <int R>
-__device__ __forceinline__ void fft_fwd_block(const FftGroup &G, int jj, int by, float *st) {
-  constexpr int I = 32 * R, PS = R * 16 + 1;
-  const int N = G.N, J = G.J, Jh = J / 2, lcw = G.lbb + 1;
-  const int jn = Jh + jj, js = Jh - 1 - jj;
-  const int b0 = by * G.BB;
-  const int nb = min(G.BB, G.batch - b0);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-  const int k2 = brev5(lane);
-  const int src0 = brev5((32 - k2) & 31);
-  float2 w[5];
-  lane_twiddles<R>(G.tw, lane, false, w);
-  const float invI = 1.f / (float)I;
-  for (int bl = warp; bl < nb; bl += nw) {
-    const double *gn = static_cast<const double *>(G.in) + ((long long)(b0 + bl) * J + jn) * I;
-    const double *gs = static_cast<const double *>(G.in) + ((long long)(b0 + bl) * J + js) * I;
-    float2 v[R];
-#pragma unroll
-    for (int r = 0; r < R; ++r) v[r] = make_float2(f64_to_f32_rn(gn[32 * r + lane]), f64_to_f32_rn(gs[32 * r + lane]));
-    warp_fft_fwd<R>(v, G.tw, G.twl, w, lane);
-    float *E = st + ((0 << lcw) + 2 * bl) * PS, *O = st + ((1 << lcw) + 2 * bl) * PS;
-#pragma unroll
-    for (int k1 = 0; k1 < R; ++k1) {
-      const float2 zc = k1 ? shfl_c(v[(R - k1) % R], 31 - lane) : shfl_c(v[0], src0);  // Z[I - m]
-      const int m = k1 + R * k2;
-      if (m <= N) {
-        const float2 zm = v[k1];
-        const float ar = 0.5f * (zm.x + zc.x), ai = 0.5f * (zm.y - zc.y);
-        const float br = 0.5f * (zm.y + zc.y), bi = -0.5f * (zm.x - zc.x);
-        const int sl = k1 * 16 + k2;
-        E[sl] = (ar + br) * invI;
-        E[PS + sl] = m ? (ai + bi) * invI : 0.f;
-        O[sl] = (ar - br) * invI;
-        O[PS + sl] = m ? (ai - bi) * invI : 0.f;
-      }
-    }
-  }
-  __syncthreads();
+__device__ __forceinline__ void write_g3(const FftGroup &G, int jj, int b0, int nb, const float *st) {
+  constexpr int PS = R * 17 + 1;
+  const int N = G.N, Jh = G.J / 2, lcw = G.lbb + 1;
   unsigned short *G3 = static_cast<unsigned short *>(G.out);
   const size_t plane = (size_t)(N + 1) * 2 * Jh * G.C2Bp;
   const int tot = (N + 1) << (lcw + 1);  // (m, p, c), c fastest
@@ -304,6 +300,195 @@ __device__ __forceinline__ void fft_fwd_block(const FftGroup &G, int jj, int by,
   }
 }
 
+// E_m = (A + B)/I and O_m = (A - B)/I of field-level bl from Z_m and
+// Z_{I-m}, into the staging planes at slot sl (m = 0: imaginary parts 0).
+template <int R>
+__device__ __forceinline__ void store_eo(float *st, int lcw, int bl, int m, int sl, float2 zm, float2 zc,
+                                         float invI) {
+  constexpr int PS = R * 17 + 1;
+  float *E = st + ((0 << lcw) + 2 * bl) * PS, *O = st + ((1 << lcw) + 2 * bl) * PS;
+  const float ar = 0.5f * (zm.x + zc.x), ai = 0.5f * (zm.y - zc.y);
+  const float br = 0.5f * (zm.y + zc.y), bi = -0.5f * (zm.x - zc.x);
+  E[sl] = (ar + br) * invI;
+  E[PS + sl] = m ? (ai + bi) * invI : 0.f;
+  O[sl] = (ar - br) * invI;
+  O[PS + sl] = m ? (ai - bi) * invI : 0.f;
+}
+
+template <int R>
+__device__ __forceinline__ void fft_fwd_block(const FftGroup &G, int jj, int by, float *st) {
+  constexpr int I = 32 * R;
+  const int N = G.N, J = G.J, Jh = J / 2, lcw = G.lbb + 1;
+  const int jn = Jh + jj, js = Jh - 1 - jj;
+  const int b0 = by * G.BB;
+  const int nb = min(G.BB, G.batch - b0);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const int k2 = brev5(lane);
+  const int src0 = brev5((32 - k2) & 31);
+  float2 w[5];
+  lane_twiddles<R>(G.tw, lane, false, w);
+  const float invI = 1.f / (float)I;
+  for (int bl = warp; bl < nb; bl += nw) {
+    const double *gn = static_cast<const double *>(G.in) + ((long long)(b0 + bl) * J + jn) * I;
+    const double *gs = static_cast<const double *>(G.in) + ((long long)(b0 + bl) * J + js) * I;
+    float2 v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = make_float2(f64_to_f32_rn(gn[32 * r + lane]), f64_to_f32_rn(gs[32 * r + lane]));
+    warp_fft_fwd<R>(v, G.tw, G.twl, w, lane);
+#pragma unroll
+    for (int k1 = 0; k1 < R; ++k1) {
+      const float2 zc = k1 ? shfl_c(v[(R - k1) % R], 31 - lane) : shfl_c(v[0], src0);  // Z[I - m]
+      const int m = k1 + R * k2;
+      if (m <= N) store_eo<R>(st, lcw, bl, m, k1 * 17 + k2, v[k1], zc, invI);
+    }
+  }
+  __syncthreads();
+  write_g3<R>(G, jj, b0, nb, st);
+}
+
+// ---------------------------------------------- rows over several warps
+// Long rows, R = 8 W with W = 2, 3, 4 (I = 512, 768, 1024): W warps share a
+// row pair, 8 samples a lane, I = 8 L with L = 32 W and t = 32 wq + l:
+//   forward  thread (wq, l) holds z[L r + t], r < 8; an 8-point DFT in
+//            registers, twiddle e^{-2 pi i t k1 / I}, then the L-point DFT
+//            over t: a W-point DFT across the warps through shared memory
+//            (warp wq keeps output k_w = wq), twiddle e^{-2 pi i l k_w / L},
+//            and the 32-point lane DFT; thread (wq, l) ends with
+//            Z[k1 + 8 (wq + W brev5(l))], i.e. m mod R = k1 + 8 wq and
+//            m / R = brev5(l), as in the one-warp path;
+//   inverse  the mirror image.
+// The partner Z_{I-m} of the forward separation comes through the same
+// exchange buffer, float2 [8][W][32] per row pair.  8 samples a lane keep
+// the register count of the R = 8 rows (the one-warp R = 32 row needs 175).
+constexpr int MW_R0 = 8;
+
+template <int W>
+__device__ __forceinline__ void fft_inv_block_mw(const FftGroup &G, int jj, int by, float *st) {
+  constexpr int R = MW_R0 * W, I = 32 * R, L = 32 * W, PS = R * 17 + 1;
+  const int N = G.N, J = G.J, Jh = J / 2, lbb = G.lbb;
+  const int jn = Jh + jj, js = Jh - 1 - jj;
+  const int b0 = by * G.BB;
+  const int nb = min(G.BB, G.batch - b0);
+  stage_fourier<R>(G, jn, js, b0, nb, st);
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int bl = warp / W, wq = warp % W;
+  const bool own = bl < G.BB;  // this warp has staging planes and an exchange slot
+  const int kl = brev5(lane);
+  float2 *xb = reinterpret_cast<float2 *>(st + 4 * G.BB * PS) + (size_t)(own ? bl : 0) * MW_R0 * W * 32;
+  float2 w[5];
+  lane_twiddles<R>(G.tw, lane, true, w);
+  float2 v[MW_R0];
+#pragma unroll
+  for (int k1 = 0; k1 < MW_R0; ++k1)
+    v[k1] = own ? inverse_input<R>(st, lbb, bl, N, k1 + MW_R0 * wq, kl) : make_float2(0.f, 0.f);
+  lane_dit<MW_R0>(v, w, lane);
+  const float2 tq = twid(G.tw, lane * wq * (I / L), +1);
+#pragma unroll
+  for (int k1 = 0; k1 < MW_R0; ++k1) v[k1] = cmul(v[k1], tq);
+  if (own) {
+#pragma unroll
+    for (int k1 = 0; k1 < MW_R0; ++k1) xb[(k1 * W + wq) * 32 + lane] = v[k1];
+  }
+  __syncthreads();
+  if (own) {
+#pragma unroll
+    for (int k1 = 0; k1 < MW_R0; ++k1) {
+      float2 acc = xb[(k1 * W) * 32 + lane];
+#pragma unroll
+      for (int kw = 1; kw < W; ++kw)
+        acc = cadd(acc, cmul(xb[(k1 * W + kw) * 32 + lane], twid(G.tw, ((wq * kw) % W) * (I / W), +1)));
+      v[k1] = acc;
+    }
+  }
+  const int t = 32 * wq + lane;
+#pragma unroll
+  for (int k1 = 1; k1 < MW_R0; ++k1) v[k1] = cmul(v[k1], twid(G.tw, t * k1, +1));
+  RegDft<MW_R0>::run(v, G.tw, I, +1);
+  if (bl < nb) {
+    double *gn = static_cast<double *>(G.out) + ((long long)(b0 + bl) * J + jn) * I;
+    double *gs = static_cast<double *>(G.out) + ((long long)(b0 + bl) * J + js) * I;
+#pragma unroll
+    for (int r = 0; r < MW_R0; ++r) {
+      gn[L * r + t] = f32_to_f64(v[r].x);
+      gs[L * r + t] = f32_to_f64(v[r].y);
+    }
+  }
+}
+
+template <int W>
+__device__ __forceinline__ void fft_fwd_block_mw(const FftGroup &G, int jj, int by, float *st) {
+  constexpr int R = MW_R0 * W, I = 32 * R, L = 32 * W, PS = R * 17 + 1;
+  const int N = G.N, J = G.J, Jh = J / 2, lcw = G.lbb + 1;
+  const int jn = Jh + jj, js = Jh - 1 - jj;
+  const int b0 = by * G.BB;
+  const int nb = min(G.BB, G.batch - b0);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int bl = warp / W, wq = warp % W;
+  const bool own = bl < G.BB;
+  const int kl = brev5(lane);
+  const int t = 32 * wq + lane;
+  float2 *xb = reinterpret_cast<float2 *>(st + 4 * G.BB * PS) + (size_t)(own ? bl : 0) * MW_R0 * W * 32;
+  float2 w[5];
+  lane_twiddles<R>(G.tw, lane, false, w);
+  float2 v[MW_R0];
+  if (bl < nb) {
+    const double *gn = static_cast<const double *>(G.in) + ((long long)(b0 + bl) * J + jn) * I;
+    const double *gs = static_cast<const double *>(G.in) + ((long long)(b0 + bl) * J + js) * I;
+#pragma unroll
+    for (int r = 0; r < MW_R0; ++r) v[r] = make_float2(f64_to_f32_rn(gn[L * r + t]), f64_to_f32_rn(gs[L * r + t]));
+  } else {
+#pragma unroll
+    for (int r = 0; r < MW_R0; ++r) v[r] = make_float2(0.f, 0.f);
+  }
+  RegDft<MW_R0>::run(v, G.tw, I, -1);
+#pragma unroll
+  for (int k1 = 1; k1 < MW_R0; ++k1) v[k1] = cmul(v[k1], twid(G.tw, t * k1, -1));
+  if (own) {
+#pragma unroll
+    for (int k1 = 0; k1 < MW_R0; ++k1) xb[(k1 * W + wq) * 32 + lane] = v[k1];
+  }
+  __syncthreads();
+  if (own) {
+#pragma unroll
+    for (int k1 = 0; k1 < MW_R0; ++k1) {
+      float2 acc = xb[(k1 * W) * 32 + lane];
+#pragma unroll
+      for (int kw = 1; kw < W; ++kw)
+        acc = cadd(acc, cmul(xb[(k1 * W + kw) * 32 + lane], twid(G.tw, ((wq * kw) % W) * (I / W), -1)));
+      v[k1] = acc;
+    }
+  }
+  const float2 tq = twid(G.tw, lane * wq * (I / L), -1);
+#pragma unroll
+  for (int k1 = 0; k1 < MW_R0; ++k1) v[k1] = cmul(v[k1], tq);
+  lane_dif<MW_R0>(v, w, lane);
+  __syncthreads();  // every warp is done reading the exchange buffer
+  if (own) {
+#pragma unroll
+    for (int k1 = 0; k1 < MW_R0; ++k1) xb[(k1 * W + wq) * 32 + lane] = v[k1];
+  }
+  __syncthreads();
+  if (bl < nb) {
+    const float invI = 1.f / (float)I;
+#pragma unroll
+    for (int k1 = 0; k1 < MW_R0; ++k1) {
+      const int q = k1 + MW_R0 * wq;
+      const int m = q + R * kl;
+      if (m <= N) {
+        // Z[I - m]: residue R - q (register (8 - k1) mod 8 of warp W-1-wq, or
+        // W-wq when k1 = 0) in lane 31 - l; for m = 0 mod R lane brev5(32 - kl)
+        int src;
+        if (q) src = ((((MW_R0 - k1) % MW_R0) * W) + (k1 ? W - 1 - wq : W - wq)) * 32 + (31 - lane);
+        else src = brev5((32 - kl) & 31);
+        store_eo<R>(st, lcw, bl, m, q * 17 + kl, v[k1], xb[src], invI);
+      }
+    }
+  }
+  __syncthreads();
+  write_g3<R>(G, jj, b0, nb, st);
+}
+
 // ------------------------------------------------------------- kernels
 // Several truncation groups in one launch: CTA blockIdx.x belongs to the
 // group whose block range contains it; the group's length selects the
@@ -311,22 +496,32 @@ __device__ __forceinline__ void fft_fwd_block(const FftGroup &G, int jj, int by,
 template <int R, int RMAX, bool FWD>
 __device__ __forceinline__ void dispatch_case(const FftGroup &G, int jj, int by, float *st) {
   if constexpr (R <= RMAX) {
-    if (FWD) fft_fwd_block<R>(G, jj, by, st);
-    else fft_inv_block<R>(G, jj, by, st);
+    if constexpr (R >= 16) {
+      if (FWD) fft_fwd_block_mw<R / MW_R0>(G, jj, by, st);
+      else fft_inv_block_mw<R / MW_R0>(G, jj, by, st);
+    } else {
+      if (FWD) fft_fwd_block<R>(G, jj, by, st);
+      else fft_inv_block<R>(G, jj, by, st);
+    }
   }
 }
 
-// Up to 16 field-levels (512 threads) per CTA for R <= 8; 8 for longer
-// rows, whose 32-register-pair rows need more than 128 registers a thread.
+// Up to 16 warps (512 threads) per CTA.
 template <int RMAX, bool FWD>
-__global__ void __launch_bounds__(RMAX <= 8 ? 512 : 256) fft_multi_kernel(const __grid_constant__ FftLaunch L) {
+__global__ void __launch_bounds__(512) fft_multi_kernel(const __grid_constant__ FftLaunch L) {
   extern __shared__ __align__(16) float st[];
   int gi = 0;
   while (gi + 1 < L.ngroups && (int)blockIdx.x >= L.g[gi + 1].blk0) ++gi;
   const FftGroup &G = L.g[gi];
+  // Forward: field-level blocks fastest, so the CTAs that share the G3 rows
+  // of one latitude pair (each writes 2 BB columns of them) run together and
+  // the 32-byte sectors they split are completed in L2, not written back
+  // partly.  Inverse: latitude pairs fastest, so consecutive CTAs write
+  // neighbouring grid rows of the same field-levels.
   const int lb = blockIdx.x - G.blk0;
+  const int nby = (G.batch + G.BB - 1) / G.BB;
   const int Jh = G.J / 2;
-  const int jj = lb % Jh, by = lb / Jh;
+  const int by = FWD ? lb % nby : lb / Jh, jj = FWD ? lb / nby : lb % Jh;
   switch (G.R) {
     case 2: dispatch_case<2, RMAX, FWD>(G, jj, by, st); break;
     case 3: dispatch_case<3, RMAX, FWD>(G, jj, by, st); break;
@@ -341,25 +536,30 @@ __global__ void __launch_bounds__(RMAX <= 8 ? 512 : 256) fft_multi_kernel(const 
   }
 }
 
-// Staging of one CTA: four planes of 16 R + 1 floats per field-level.
-static size_t fft_smem(int R, int bb) { return (size_t)4 * bb * (R * 16 + 1) * sizeof(float); }
+// Warps per row pair and shared memory of one CTA: four planes of 17 R + 1
+// floats per field-level, and for rows over several warps the exchange
+// buffer of 8 x W x 32 complex values per row pair.
+static int fft_warps_per_row(int R) { return R >= 16 ? R / MW_R0 : 1; }
+static size_t fft_smem(int R, int bb) {
+  const int W = fft_warps_per_row(R);
+  size_t s = (size_t)4 * bb * (R * 17 + 1) * sizeof(float);
+  if (W > 1) s += (size_t)bb * MW_R0 * W * 32 * sizeof(float2);
+  return s;
+}
 
 // One launch over ngroups plans (FP32).  Inverse: in[g] = F, out[g] = grid;
 // forward: in[g] = grid, out[g] = G3 (the plan's Fourier buffer).
 int fft_multi(Plan *const *plans, const int *batch, const void *const *in, void *const *out, int ngroups, bool fwd,
               cudaStream_t s) {
   if (ngroups < 1 || ngroups > FFT_MAXG) return DCCM_ERR_UNSUPPORTED;
+  // Warps per CTA (the fft_bb knob); each group fits as many row pairs as
+  // its warps per row allow (a power of two), within the smem budget.
   const size_t budget = 100 * 1024;
   const int tb = tunables().fft_bb;
-  int BB = (tb == 4 || tb == 8 || tb == 16) ? tb : 8, rmax = 2;
-  for (int g = 0; g < ngroups; ++g) {
+  const int WPC = (tb == 4 || tb == 8 || tb == 16) ? tb : 8;
+  int rmax = 2, warps = 1;
+  for (int g = 0; g < ngroups; ++g)
     if (!fft_length_supported(plans[g]->I)) return DCCM_ERR_UNSUPPORTED;
-    rmax = plans[g]->I / 32 > rmax ? plans[g]->I / 32 : rmax;
-    while (BB > 1 && fft_smem(plans[g]->I / 32, BB) > budget) BB /= 2;
-  }
-  if (rmax > 8 && BB > 8) BB = 8;
-  int lbb = 0;
-  while ((1 << lbb) < BB) ++lbb;
   FftLaunch L;
   memset(&L, 0, sizeof L);
   int nblk = 0, ng = 0;
@@ -367,13 +567,21 @@ int fft_multi(Plan *const *plans, const int *batch, const void *const *in, void 
   for (int g = 0; g < ngroups; ++g) {
     if (batch[g] <= 0) continue;
     const Plan &P = *plans[g];
+    const int R = P.I / 32, W = fft_warps_per_row(R);
+    int BB = 1;
+    while (2 * BB * W <= WPC && fft_smem(R, 2 * BB) <= budget) BB *= 2;
+    int lbb = 0;
+    while ((1 << lbb) < BB) ++lbb;
+    rmax = R > rmax ? R : rmax;
+    warps = BB * W > warps ? BB * W : warps;
     FftGroup &G = L.g[ng++];
     G.N = P.N;
     G.J = P.J;
     G.batch = batch[g];
     G.BB = BB;
     G.lbb = lbb;
-    G.R = P.I / 32;
+    G.W = W;
+    G.R = R;
     G.blk0 = nblk;
     G.C2Bp = P.C2Bp;
     G.in = in[g];
@@ -388,7 +596,7 @@ int fft_multi(Plan *const *plans, const int *batch, const void *const *in, void 
   if (nblk == 0) return DCCM_OK;
   auto go = [&](auto kernel) -> int {
     DCCM_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    kernel<<<nblk, 32 * BB, smem, s>>>(L);
+    kernel<<<nblk, 32 * warps, smem, s>>>(L);
     DCCM_LAUNCH_CHECK();
     return DCCM_OK;
   };

@@ -115,3 +115,52 @@ def land_mask(nx, ny, frac=0.3, seed=0):
     """uint8 (ny, nx) flattened lon-fastest: 1 = ocean, 0 = land."""
     rng = np.random.Generator(np.random.PCG64(seed))
     return (rng.uniform(size=nx * ny) >= frac).astype(np.uint8)
+
+
+# Constants of the implicit-coupling inputs (DCPAM defaults): Grav, CpDry,
+# GasRDry, and the 1200 s step of the T21L16 coupled configuration.
+IMPLCPL_CONSTS = (9.8, 1004.6, 287.04, 1200.0)
+
+
+def column_profiles(ncol, kmax, ncmax=1, seed=0):
+    """Atmosphere columns for the implicit surface coupling: half levels
+    (kmax+1, ncol) k = 0 (surface) .. kmax (top, p = 0), full levels
+    (kmax, ncol), tracer fluxes (ncmax, kmax+1, ncol); row-major [k][c] is
+    the reference's (i, j, k) layout with the columns flattened.  Sigma
+    levels, a dry-adiabat-like temperature, hydrostatic heights, diffusion
+    coefficients decaying over 1 km and surface fluxes decaying likewise
+    (seeded PCG64)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    G, Cp, R, _ = IMPLCPL_CONSTS
+    kappa = R / Cp
+    sh = 1.0 - (np.arange(kmax + 1) / kmax) ** 1.5           # sigma at half levels, 1 -> 0
+    sf = 0.5 * (sh[:-1] + sh[1:])                              # full levels
+    ps = 1.0e5 * (1.0 + rng.uniform(-0.02, 0.02, ncol))
+    ph = sh[:, None] * ps[None, :]
+    pf = sf[:, None] * ps[None, :]
+    tf = 288.0 * sf[:, None] ** 0.19 + rng.uniform(-1.0, 1.0, (kmax, ncol))
+    th = np.empty((kmax + 1, ncol))
+    th[0] = tf[0] + 1.0
+    th[1:kmax] = 0.5 * (tf[:-1] + tf[1:])
+    th[kmax] = tf[-1]
+    zf = R * tf / G * np.log(1.0 / sf[:, None])
+    zh = np.empty((kmax + 1, ncol))
+    zh[0] = 0.0
+    zh[1:kmax] = 0.5 * (zf[:-1] + zf[1:])
+    zh[kmax] = zf[-1] + (zf[-1] - zf[-2])
+    decay = np.exp(-zh / 1000.0)
+    kv = (10.0 * decay + 0.1) * rng.uniform(0.5, 1.5, ncol)[None, :]
+    kv[0] = kv[kmax] = 0.0
+    taux = rng.normal(0.0, 0.1, ncol)
+    tauy = rng.normal(0.0, 0.1, ncol)
+    heat = rng.normal(20.0, 10.0, ncol)
+    qflx = np.abs(rng.normal(3e-5, 1e-5, (ncmax, ncol)))
+    mom_x, mom_y, hflx = taux[None] * decay, tauy[None] * decay, heat[None] * decay
+    for a in (mom_x, mom_y, hflx):
+        a[kmax] = 0.0
+    qf = qflx[:, None, :] * decay[None]
+    qf[:, kmax] = 0.0
+    return {"MomFluxX": mom_x, "MomFluxY": mom_y, "HeatFlux": hflx, "QMixFlux": qf,
+            "Press": ph, "ExnerFull": (pf / 1.0e5) ** kappa, "ExnerHalf": (ph / 1.0e5) ** kappa,
+            "VirTemp": th, "Height": zf, "VelDiffCoef": kv, "TempDiffCoef": 1.2 * kv,
+            "QMixDiffCoef": 1.1 * kv}

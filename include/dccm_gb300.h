@@ -97,6 +97,61 @@ int dccm_sfc_bulk_flux_get_dev(const dccm_sfc_bulk_flux_args *args,
                                const dccm_sfc_grid *grid, void *stream);
 
 /* =====================================================================
+ * Implicit surface coupling of the atmosphere's vertical diffusion: the
+ * producer of the bulk flux's ImplCplCoef1/2 and the consumer of its
+ * DelVarImplCPL.
+ * dccm_implcpl_forward[_dev] replaces SfcImplicitCoupling_VDiffForward
+ * (atm/dcpam_sfc_implicit_coupling_mod.f90:72-378, with
+ * Solve_TriDiagSystem_Forward :380-405); dccm_implcpl_backward[_dev]
+ * replaces SfcImplicitCoupling_VDiffBackward (:25-70, with
+ * Solve_TriDiagSystem_Backward :407-420).  The plan holds what the
+ * reference keeps as module state (xyza_UVMtx, xyza_TempMtx,
+ * xyza_QMixMtx, allocated by dcpam_sfc_implicit_coupling_Init :422-428)
+ * from the forward sweep to the backward one.  Arrays are the reference's,
+ * columns (i, j) flattened to ncol = imax*jmax: xyr_* (ncol, 0:kmax),
+ * xyz_* (ncol, kmax), xyrf_QMixFlux (ncol, 0:kmax, ncmax), xyzf_DQMixDt
+ * (ncol, kmax, ncmax), xya_ImplCplCoef1/2 (ncol, 4), column-major.
+ * Level 1 of the forward sweep's tendencies divides by the zero
+ * sub-diagonal the reference sets at k = 1 and holds its infinities or
+ * NaN; the coupler replaces U, V, T and the vapour tracer there with the
+ * surface solution (DelVarImplCPL) before the backward sweep
+ * (atm/dccm_atm_mod.f90:832-835), as a caller must.  FP64; agrees with
+ * the reference's operation order to rounding.
+ * ===================================================================== */
+typedef struct dccm_implcpl dccm_implcpl;
+/* Constants of the `constants' and `timeset' modules the routines use. */
+typedef struct dccm_implcpl_consts {
+  double Grav, CpDry, GasRDry, DelTime;
+} dccm_implcpl_consts;
+typedef struct dccm_implcpl_forward_args {
+  const double *xyr_MomFluxX, *xyr_MomFluxY, *xyr_HeatFlux; /* in (ncol, 0:kmax) */
+  const double *xyrf_QMixFlux;                              /* in (ncol, 0:kmax, ncmax) */
+  const double *xyr_Press, *xyz_Exner, *xyr_Exner;          /* in */
+  const double *xyr_VirTemp, *xyz_Height;                   /* in */
+  const double *xyr_VelDiffCoef, *xyr_TempDiffCoef, *xyr_QMixDiffCoef; /* in (ncol, 0:kmax) */
+  double *xyz_DUDt, *xyz_DVDt, *xyz_DTempDt;                /* out (ncol, kmax) */
+  double *xyzf_DQMixDt;                                     /* out (ncol, kmax, ncmax) */
+  double *xya_ImplCplCoef1, *xya_ImplCplCoef2;              /* out (ncol, 4) */
+} dccm_implcpl_forward_args;
+
+/* index_h2ovap: IndexH2OVap, 1-based tracer of the vapour (1..ncmax); kmax >= 2. */
+int dccm_implcpl_create(int ncol, int kmax, int ncmax, int index_h2ovap,
+                        const dccm_implcpl_consts *consts, dccm_implcpl **plan);
+int dccm_implcpl_destroy(dccm_implcpl *plan);
+/* Host arrays; returns when the outputs are in host memory. */
+int dccm_implcpl_forward(dccm_implcpl *plan, const dccm_implcpl_forward_args *args);
+/* Device arrays; stream-ordered. */
+int dccm_implcpl_forward_dev(dccm_implcpl *plan, const dccm_implcpl_forward_args *args,
+                             void *stream);
+/* In place on the tendencies (after level 1 has been replaced). */
+int dccm_implcpl_backward(dccm_implcpl *plan, double *xyz_DUDt, double *xyz_DVDt,
+                          double *xyz_DTempDt, double *xyzf_DQMixDt);
+int dccm_implcpl_backward_dev(dccm_implcpl *plan, double *xyz_DUDt, double *xyz_DVDt,
+                              double *xyz_DTempDt, double *xyzf_DQMixDt, void *stream);
+/* Copies the module-state matrices out, each (ncol, kmax, -1:1); NULL skips one. */
+int dccm_implcpl_matrices(dccm_implcpl *plan, double *uv, double *temp, double *qmix);
+
+/* =====================================================================
  * Jones-99 remap table
  * dccm_j99_generate replaces gen_gridmapfile_lonlat2lonlat
  * (common/grid_mapping_util_jones99.f90:35-41, body :78-442); the table is
@@ -349,8 +404,8 @@ int dccm_step_run_host(dccm_step *step, void *stream, const dccm_host_copy *h2d,
 
 /* Autotuner: chooses the launch shapes of the step's kernels by timing
  * candidates of each knob on the stage it affects ("tc_ctas": persistent
- * CTAs of the tensor-core Legendre kernel, "fft_bb": field-levels per FFT
- * CTA, "flux_threads", "remap_threads": CTA sizes), applies the winners
+ * CTAs of the tensor-core Legendre kernel, "fft_bb": warps per FFT CTA
+ * (4, 8 or 16), "flux_threads", "remap_threads": CTA sizes), applies the winners
  * and records the step's graph again.  With cache_path the choice is read
  * from / appended to that file (one JSON object per line, keyed by the
  * GPU name and SM count and the step's shapes).  chosen (4 ints, may be

@@ -52,6 +52,8 @@ def lib():
         L.oracle_sht_inverse.argtypes = [i32, i32, i32, i32, P, P]
         L.oracle_sht_forward.argtypes = [i32, i32, i32, i32, P, P]
         L.oracle_rfft_row.argtypes = [i32, P, i32, P]
+        L.oracle_implcpl_forward.argtypes = [P, P, P, P, P, i64, i32, i32, i32, P]
+        L.oracle_implcpl_backward.argtypes = [P, P, P, P, P, P, P, i64, i32, i32, f64]
         L.oracle_set_threads.argtypes = [i32]
         L.oracle_get_threads.restype = i32
         _lib = L
@@ -171,3 +173,46 @@ def rfft_row(g, M):
     out = np.zeros(M, np.complex128)
     lib().oracle_rfft_row(len(g), _p(g), M, _p(out))
     return out
+
+
+# ------------------------------------------------------ implicit coupling
+IMPLCPL_IN = ["MomFluxX", "MomFluxY", "HeatFlux", "QMixFlux", "Press", "ExnerFull", "ExnerHalf",
+              "VirTemp", "Height", "VelDiffCoef", "TempDiffCoef", "QMixDiffCoef"]
+IMPLCPL_OUT = ["DUDt", "DVDt", "DTempDt", "DQMixDt", "ImplCplCoef1", "ImplCplCoef2"]
+
+
+def implcpl_forward(prof, ih2o, consts):
+    """SfcImplicitCoupling_VDiffForward over the columns of prof (arrays
+    [k][c], tracers [n][k][c], as synth.column_profiles returns them).
+    Returns the outputs (DUDt, DVDt, DTempDt [kmax][c], DQMixDt [n][kmax][c],
+    ImplCplCoef1/2 [4][c]) and the eliminated matrices UVMtx, TempMtx,
+    QMixMtx [3][kmax][c] (sub-, main, super-diagonal)."""
+    arrs = [np.ascontiguousarray(prof[n], dtype=np.float64) for n in IMPLCPL_IN]
+    kmax1, ncol = arrs[0].shape
+    kmax = kmax1 - 1
+    ncmax = arrs[3].shape[0]
+    out = {"DUDt": np.zeros((kmax, ncol)), "DVDt": np.zeros((kmax, ncol)), "DTempDt": np.zeros((kmax, ncol)),
+           "DQMixDt": np.zeros((ncmax, kmax, ncol)), "ImplCplCoef1": np.zeros((4, ncol)),
+           "ImplCplCoef2": np.zeros((4, ncol))}
+    mats = {n: np.zeros((3, kmax, ncol)) for n in ("UVMtx", "TempMtx", "QMixMtx")}
+    pin = (ctypes.c_void_p * len(arrs))(*[a.ctypes.data for a in arrs])
+    pout = (ctypes.c_void_p * len(IMPLCPL_OUT))(*[out[n].ctypes.data for n in IMPLCPL_OUT])
+    c = np.ascontiguousarray(consts, dtype=np.float64)
+    lib().oracle_implcpl_forward(ctypes.cast(pin, ctypes.c_void_p), ctypes.cast(pout, ctypes.c_void_p),
+                                 _p(mats["UVMtx"]), _p(mats["TempMtx"]), _p(mats["QMixMtx"]), ncol, kmax,
+                                 ncmax, int(ih2o), _p(c))
+    out.update(mats)
+    return out
+
+
+def implcpl_backward(mats, tend, DelTime):
+    """SfcImplicitCoupling_VDiffBackward on copies of the tendencies (dict
+    with DUDt, DVDt, DTempDt, DQMixDt) with the matrices of the forward."""
+    t = {n: np.array(tend[n], dtype=np.float64, order="C") for n in ("DUDt", "DVDt", "DTempDt", "DQMixDt")}
+    m = [np.ascontiguousarray(mats[n], dtype=np.float64) for n in ("UVMtx", "TempMtx", "QMixMtx")]
+    kmax, ncol = t["DUDt"].shape
+    ncmax = t["DQMixDt"].shape[0]
+    lib().oracle_implcpl_backward(*[_p(x) for x in m], _p(t["DUDt"]), _p(t["DVDt"]), _p(t["DTempDt"]),
+                                  _p(t["DQMixDt"]), ncol, kmax, ncmax, float(DelTime))
+    return t
+

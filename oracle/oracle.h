@@ -10,6 +10,7 @@
  *   - Jones-99 table:     common/grid_mapping_util_jones99.f90:35-442
  *   - table reader:       common/grid_mapping_util_jones99.f90:446-506
  *   - remap apply:        common/interpolation_data_latlon_mod.f90:274-306
+ *   - implicit coupling:  atm/dcpam_sfc_implicit_coupling_mod.f90:25-420
  *   - spherical-harmonic transform: SPML/ISPACK (external, not vendored);
  *     restated from the mathematics with the convention documented in
  *     oracle_sht.c.
@@ -92,6 +93,25 @@ void oracle_rfft_row(int I, const double *g, int M, double *out);
 
 void oracle_set_threads(int n);
 int oracle_get_threads(void);
+
+/* ------------------------------------------------------ implicit coupling */
+/* SfcImplicitCoupling_VDiffForward (atm/dcpam_sfc_implicit_coupling_mod.f90:
+ * 72-378) and VDiffBackward (:25-70) over ncol columns of kmax levels;
+ * layouts in oracle_implcpl.c.  in[] / out[] indices: */
+enum {
+  OI_MomFluxX = 0, OI_MomFluxY, OI_HeatFlux, OI_QMixFlux, OI_Press, OI_ExnerFull,
+  OI_ExnerHalf, OI_VirTemp, OI_Height, OI_VelDiffCoef, OI_TempDiffCoef,
+  OI_QMixDiffCoef, OI_NIN
+};
+enum { OO_DUDt = 0, OO_DVDt, OO_DTempDt, OO_DQMixDt, OO_ImplCplCoef1, OO_ImplCplCoef2, OO_NOUT };
+/* consts = {Grav, CpDry, GasRDry, DelTime}; ih2o is IndexH2OVap (1-based).
+ * uv, tm, qm receive the eliminated matrices (ncol, kmax, -1:1). */
+void oracle_implcpl_forward(const double *const *in, double *const *out, double *uv, double *tm,
+                            double *qm, int64_t ncol, int kmax, int ncmax, int ih2o,
+                            const double *consts);
+void oracle_implcpl_backward(const double *uv, const double *tm, const double *qm, double *DUDt,
+                             double *DVDt, double *DTempDt, double *DQMixDt, int64_t ncol, int kmax,
+                             int ncmax, double DelTime);
 
 #ifdef __cplusplus
 }

@@ -15,7 +15,10 @@ plain Python, kept deliberately different in structure from the C oracle:
   (common/grid_mapping_util_jones99.f90:156-442);
 * spherical harmonics: Legendre functions from scipy.special.lpmv (not the
   recurrence the oracle uses), Gaussian nodes from numpy.polynomial, and
-  full-latitude sums without the equatorial fold; FFTs from numpy.fft.
+  full-latitude sums without the equatorial fold; FFTs from numpy.fft;
+* implicit surface coupling: whole levels of all columns at a time
+  (atm/dcpam_sfc_implicit_coupling_mod.f90:72-405), the oracle loops per
+  column.
 
 Run from the repository root:  python tests/golden/make_golden.py
 """
@@ -307,6 +310,94 @@ def make_sht():
     fwd[:, m_of == 0] = fwd[:, m_of == 0].real
     np.savez_compressed(os.path.join(OUT, "sht_t21.npz"), N=N, I=I, J=J, mu=mu, w=w, pbar=P,
                         spec=spec, grid=grid, fwd=fwd)
+
+
+def implcpl_numpy(d, ih2o, consts):
+    """SfcImplicitCoupling_VDiffForward (atm/dcpam_sfc_implicit_coupling_mod.f90:
+    72-378) over whole levels at a time, Solve_TriDiagSystem_Forward
+    (:380-405) on (kmax, ncol) arrays; every expression in the Fortran
+    order."""
+    G, Cp, R, DT = consts
+    P, Tv, Z = d["Press"], d["VirTemp"], d["Height"]
+    Ef, Eh = d["ExnerFull"], d["ExnerHalf"]
+    K = P.shape[0] - 1
+    ncol = P.shape[1]
+    VTC = np.zeros((K + 1, ncol)); TTC = np.zeros((K + 1, ncol)); QTC = np.zeros((K + 1, ncol))
+    for k in range(1, K):
+        tmp = P[k] / (R * Tv[k]) / (Z[k] - Z[k - 1])  # Height(k+1) - Height(k), full levels 1-based
+        VTC[k] = d["VelDiffCoef"][k] * tmp
+        TTC[k] = d["TempDiffCoef"][k] * tmp
+        QTC[k] = d["QMixDiffCoef"][k] * tmp
+
+    def mat(TC):
+        m = np.zeros((3, K, ncol))
+        for k in range(1, K + 1):
+            mass = -((P[k] - P[k - 1]) / G / (2.0 * DT))
+            m[0, k - 1] = 0.0 if k == 1 else -TC[k - 1]
+            m[1, k - 1] = mass + TC[k] if k == 1 else (mass + TC[k - 1] + TC[k] if k < K else mass + TC[k - 1])
+            m[2, k - 1] = 0.0 if k == K else -TC[k]
+        return m
+    uv, qm = mat(VTC), mat(QTC)
+    tm = np.zeros((3, K, ncol))
+    for k in range(1, K + 1):
+        mass = -(Cp * (P[k] - P[k - 1]) / G / (2.0 * DT))
+        tm[0, k - 1] = 0.0 if k == 1 else -(Cp * Eh[k - 1] / Ef[k - 2] * TTC[k - 1])
+        if k == 1:
+            tm[1, k - 1] = mass + Cp * Eh[k] / Ef[k - 1] * TTC[k]
+        elif k < K:
+            tm[1, k - 1] = mass + Cp * Eh[k - 1] / Ef[k - 1] * TTC[k - 1] + Cp * Eh[k] / Ef[k - 1] * TTC[k]
+        else:
+            tm[1, k - 1] = mass + Cp * Eh[k - 1] / Ef[k - 1] * TTC[k - 1]
+        tm[2, k - 1] = 0.0 if k == K else -(Cp * Eh[k] / Ef[k] * TTC[k])
+    out = {"DUDt": -(d["MomFluxX"][1:] - d["MomFluxX"][:-1]), "DVDt": -(d["MomFluxY"][1:] - d["MomFluxY"][:-1]),
+           "DTempDt": -(d["HeatFlux"][1:] - d["HeatFlux"][:-1]),
+           "DQMixDt": -(d["QMixFlux"][:, 1:] - d["QMixFlux"][:, :-1])}
+    C2 = np.stack([out["DUDt"][0], out["DVDt"][0], out["DTempDt"][0], out["DQMixDt"][ih2o - 1, 0]])
+
+    def solve(m, r):
+        with np.errstate(divide="ignore", invalid="ignore"):
+            m[1, K - 1] = m[1, K - 1] / m[0, K - 1]
+            r[K - 1] = r[K - 1] / m[0, K - 1]
+            m[0, K - 1] = 1.0
+            for k in range(K - 1, 0, -1):
+                i = k - 1
+                m[1, i] = (m[1, i] * m[1, i + 1] - m[2, i]) / (m[0, i] * m[1, i + 1])
+                r[i] = (r[i] * m[1, i + 1] - m[2, i] * r[i + 1]) / (m[0, i] * m[1, i + 1])
+                m[0, i] = 1.0
+                m[2, i] = 0.0
+    uvs = uv.copy()
+    solve(uv, out["DUDt"])
+    solve(uvs, out["DVDt"])
+    solve(tm, out["DTempDt"])
+    qs = qm.copy()
+    for n in range(out["DQMixDt"].shape[0]):
+        qm = qs.copy()
+        solve(qm, out["DQMixDt"][n])
+    Tmp = -((P[1] - P[0]) / G / (2.0 * DT))
+    C1 = np.zeros((4, ncol))
+    C1[0] = Tmp + VTC[1] - (-VTC[1]) / uv[1, 1]
+    C2[0] = C2[0] - (-VTC[1]) * out["DUDt"][1] / uv[1, 1]
+    C1[1] = Tmp + VTC[1] - (-VTC[1]) / uv[1, 1]
+    C2[1] = C2[1] - (-VTC[1]) * out["DVDt"][1] / uv[1, 1]
+    dt1 = Cp * Eh[1] * TTC[1] / Ef[0]
+    dt2 = -(Cp * Eh[1] * TTC[1] / Ef[1])
+    C1[2] = Cp * Tmp + dt1 - dt2 / tm[1, 1]
+    C2[2] = C2[2] - dt2 * out["DTempDt"][1] / tm[1, 1]
+    C1[3] = Tmp + QTC[1] - (-QTC[1]) / qm[1, 1]
+    C2[3] = C2[3] - (-QTC[1]) * out["DQMixDt"][ih2o - 1, 1] / qm[1, 1]
+    out.update(ImplCplCoef1=C1, ImplCplCoef2=C2, UVMtx=uv, TempMtx=tm, QMixMtx=qm)
+    return out
+
+
+def make_implcpl():
+    import importlib
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.dirname(OUT)))
+    synth = importlib.import_module("dennou-ccm_gb300.synth")
+    d = synth.column_profiles(24, 12, ncmax=2, seed=5)
+    o = implcpl_numpy(d, 1, synth.IMPLCPL_CONSTS)
+    np.savez_compressed(os.path.join(OUT, "implcpl_small.npz"), consts=np.array(synth.IMPLCPL_CONSTS), ih2o=1,
+                        **{"in_" + k: v for k, v in d.items()}, **{"out_" + k: v for k, v in o.items()})
 
 
 if __name__ == "__main__":

@@ -195,3 +195,50 @@ def test_area_integral_compensated(oracle):
     f = np.concatenate([f, -f, [1.0]])
     a = np.ones_like(f)
     assert oracle.area_integral(f, a) == 1.0
+
+
+# ------------------------------------------------------ implicit coupling
+def _same(a, g):
+    """Bit-identical finite values; same infinities (with sign) and NaN."""
+    fin = np.isfinite(g)
+    return (np.array_equal(np.isfinite(a), fin) and np.array_equal(np.isnan(a), np.isnan(g))
+            and np.array_equal(np.signbit(a[~fin]), np.signbit(g[~fin])) and np.array_equal(a[fin], g[fin]))
+
+
+def test_implcpl_forward_matches_golden(oracle):
+    z = np.load(os.path.join(GOLDEN, "implcpl_small.npz"))
+    d = {k[3:]: z[k] for k in z.files if k.startswith("in_")}
+    o = oracle.implcpl_forward(d, int(z["ih2o"]), z["consts"])
+    for k, v in o.items():
+        assert _same(v, z["out_" + k]), k
+    # the reference's level-1 division by its zero sub-diagonal (only there)
+    assert not np.isfinite(o["DUDt"][0]).any() and np.isfinite(o["DUDt"][1:]).all()
+    assert np.isfinite(o["ImplCplCoef1"]).all() and np.isfinite(o["ImplCplCoef2"]).all()
+
+
+def test_implcpl_sweeps_solve_the_column_systems(oracle, synth):
+    """Forward elimination, a surface value at level 1 (as the coupler puts
+    DelVarImplCPL there) and back substitution solve rows 2..kmax of the
+    original momentum system: A x = -(flux divergence), x = 2 dt dU/dt."""
+    ncol = 40
+    d = synth.column_profiles(ncol, 20, ncmax=2, seed=9)
+    G, Cp, R, DT = synth.IMPLCPL_CONSTS
+    o = oracle.implcpl_forward(d, 1, synth.IMPLCPL_CONSTS)
+    rng = np.random.Generator(np.random.PCG64(3))
+    t = {k: o[k].copy() for k in ("DUDt", "DVDt", "DTempDt", "DQMixDt")}
+    for k in ("DUDt", "DVDt", "DTempDt"):
+        t[k][0] = rng.normal(0, 1e-3, ncol)
+    t["DQMixDt"][:, 0] = rng.normal(0, 1e-7, (2, ncol))
+    b = oracle.implcpl_backward(o, t, DT)
+    assert all(np.isfinite(v).all() for v in b.values())
+    K = d["Press"].shape[0] - 1
+    VTC = np.zeros((K + 1, ncol))
+    for k in range(1, K):
+        VTC[k] = d["VelDiffCoef"][k] * (d["Press"][k] / (R * d["VirTemp"][k]) / (d["Height"][k] - d["Height"][k - 1]))
+    rhs = -(d["MomFluxX"][1:] - d["MomFluxX"][:-1])
+    x = b["DUDt"] * (2.0 * DT)
+    for k in range(2, K + 1):
+        mass = -((d["Press"][k] - d["Press"][k - 1]) / G / (2.0 * DT))
+        m0 = mass + VTC[k - 1] + (VTC[k] if k < K else 0.0)
+        lhs = -VTC[k - 1] * x[k - 2] + m0 * x[k - 1] + (-VTC[k] * x[k] if k < K else 0.0)
+        assert np.allclose(lhs, rhs[k - 1], rtol=1e-9, atol=1e-12 * np.abs(rhs).max()), k

@@ -64,6 +64,31 @@ def test_mixed_transforms_match_oracle(dccm, oracle, synth, N, I, J):
         assert rel_l2(s2[b], so[b]) <= 2e-6
 
 
+# Longer rows: I = 32 R with R = 12 (one warp per row pair, 12 samples a
+# lane) and R = 16, 24, 32 (rows shared by 2, 3, 4 warps).  Six field-levels
+# leave the last CTA of field-levels partial for every layout.  The
+# tolerance grows with N (BF16 x 3 Legendre sums over up to N/2 terms,
+# FP32 FFT of length I): 2e-6 over the batch, 4e-6 per field-level.
+LONG = [(127, 384, 192), (170, 512, 256), (255, 768, 384), (341, 1024, 512)]
+
+
+@pytest.mark.parametrize("N,I,J", LONG)
+def test_mixed_long_rows_match_oracle(dccm, oracle, synth, N, I, J):
+    B = 6
+    s = synth.spectra(N, B, seed=N + 3)
+    plan = dccm.ShtPlan(N, I, J, dccm.SHT_MIXED, B)
+    g = plan.inverse(s)
+    go = oracle.sht_inverse(N, I, J, s)
+    s2 = plan.forward(go)
+    so = oracle.sht_forward(N, I, J, go)
+    errs = (rel_l2(g, go), rel_l2(s2, so), rel_l2(plan.forward(g), s))
+    assert plan.status() == (0, 0)
+    assert max(errs) <= 2e-6, errs
+    for b in range(B):
+        assert rel_l2(g[b], go[b]) <= 4e-6
+        assert rel_l2(s2[b], so[b]) <= 4e-6
+
+
 @pytest.mark.parametrize("prec", [0, 1])
 def test_known_answers(dccm, oracle, prec):
     N, I, J = 21, 64, 32
