@@ -80,6 +80,12 @@ _SIGS = {
     "dccm_last_cuda_error": (ctypes.c_int, []),
     "dccm_sfc_bulk_flux_get": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "dccm_sfc_bulk_flux_get_dev": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "dccm_bilinear_generate": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
+                                              ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
+                                              ctypes.c_void_p, ctypes.c_void_p]),
+    "dccm_exchange_grid": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                          ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                          ctypes.c_void_p]),
     "dccm_implcpl_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                            ctypes.c_void_p, ctypes.c_void_p]),
     "dccm_implcpl_destroy": (ctypes.c_int, [ctypes.c_void_p]),
@@ -281,6 +287,48 @@ def gen_gridmapfile_lonlat2lonlat(x_LonS, y_LatS, x_LonD, y_LatD, x_LonIntWtS, y
                                _p(arrs[4]), _p(arrs[5]), _p(arrs[6]), _p(arrs[7]),
                                accuracy_order, weight_mode, _p(m), ctypes.byref(h)), "dccm_j99_generate")
     return RemapTable(h)
+
+
+def bilinear_generate(x_LonS, y_LatS, x_LonR, y_LatR, dst_mask=None):
+    """Bilinear table on the GPU (common/grid_mapping_util.f90:32-182)."""
+    L = load()
+    a = [np.ascontiguousarray(x, np.float64) for x in (x_LonS, y_LatS, x_LonR, y_LatR)]
+    m = None if dst_mask is None else np.ascontiguousarray(dst_mask, np.uint8)
+    h = ctypes.c_void_p()
+    _check(L.dccm_bilinear_generate(_p(a[0]), len(a[0]), _p(a[1]), len(a[1]), _p(a[2]), len(a[2]),
+                                    _p(a[3]), len(a[3]), _p(m), ctypes.byref(h)), "dccm_bilinear_generate")
+    return RemapTable(h)
+
+
+def exchange_grid(y_LatA, y_IntWtLatA, y_LatO, y_IntWtLatO):
+    """Latitudes and sin-latitude widths of the surface exchange grid
+    (tool/gmapgen/gmapgen_main.f90:336-405); longitudes are the atmosphere's."""
+    a = [np.ascontiguousarray(x, np.float64) for x in (y_LatA, y_IntWtLatA, y_LatO, y_IntWtLatO)]
+    n = len(a[0]) + len(a[2])
+    lat, w = np.zeros(n), np.zeros(n)
+    m = ctypes.c_int(0)
+    _check(load().dccm_exchange_grid(_p(a[0]), _p(a[1]), len(a[0]), _p(a[2]), _p(a[3]), len(a[2]), _p(lat),
+                                     _p(w), ctypes.byref(m)), "dccm_exchange_grid")
+    return lat[:m.value], w[:m.value]
+
+
+def gmapgen(A, O, conservative=True, orders=(1, 1, 1, 1, 1, 1), weight_mode=J99_REF):
+    """The six tables of tool/gmapgen/gmapgen_main.f90:100-148 between the
+    atmosphere grid A, the ocean grid O and their surface exchange grid S,
+    each grid given as (x_Lon, y_Lat, x_IntWtLon, y_IntWtLat).  Returns
+    (S, {"AO": table, "OA": ..., "AS", "SA", "OS", "SO"})."""
+    latS, wS = exchange_grid(A[1], A[3], O[1], O[3])
+    S = (np.asarray(A[0], np.float64), latS, np.asarray(A[2], np.float64), wS)
+    grids = {"A": A, "O": O, "S": S}
+    out = {}
+    for k, tag in enumerate(("AO", "OA", "AS", "SA", "OS", "SO")):
+        src, dst = grids[tag[0]], grids[tag[1]]
+        if conservative:
+            out[tag] = gen_gridmapfile_lonlat2lonlat(src[0], src[1], dst[0], dst[1], src[2], src[3], dst[2],
+                                                     dst[3], accuracy_order=orders[k], weight_mode=weight_mode)
+        else:
+            out[tag] = bilinear_generate(src[0], src[1], dst[0], dst[1])
+    return S, out
 
 
 def read_table(path):

@@ -32,12 +32,9 @@
 #include <string>
 #include <vector>
 
+#include "remap_table.cuh"
 #include "common.cuh"
 
-struct dccm_remap_table {
-  std::vector<int32_t> iD, jD, iS, jS;
-  std::vector<double> w;
-};
 
 struct dccm_remap_plan {
   int64_t n_send = 0, n_recv = 0, nnz = 0;

@@ -178,6 +178,29 @@ int dccm_j99_generate(const double *x_LonS, int nxs, const double *y_LatS, int n
                       const double *x_LonIntWtD, const double *y_LatIntWtD,
                       int accuracy_order, int weight_mode, const uint8_t *dst_mask,
                       dccm_remap_table **table);
+/* dccm_bilinear_generate replaces gen_gridmapfile_lonlat2lonlat of
+ * common/grid_mapping_util.f90:32-182 (the bilinear mapping of the
+ * coupler's non-conservative tags, tool/gmapgen/gmapgen_main.f90:100-117):
+ * four rows per destination cell (two per source column, or one outside
+ * the source latitudes, when either grid has a single longitude), in the
+ * reference's order, weights bit-identical to the reference's.  North of
+ * the last source latitude the reference reads past its latitude array;
+ * there the rows extrapolate linearly from the last two source latitudes,
+ * as the reference itself does south of the first.  Longitudes are assumed
+ * uniform and starting at 0, as the reference's index formula does.
+ * dst_mask as for dccm_j99_generate.  Returns DCCM_ERR_UNSUPPORTED for a
+ * single source latitude on a grid that is not axisymmetric. */
+int dccm_bilinear_generate(const double *x_LonS, int nxs, const double *y_LatS, int nys,
+                           const double *x_LonR, int nxr, const double *y_LatR, int nyr,
+                           const uint8_t *dst_mask, dccm_remap_table **table);
+/* generate_surface_exchage_grid (tool/gmapgen/gmapgen_main.f90:336-405):
+ * latitudes (radians) and sin-latitude widths of the surface exchange grid
+ * from the atmosphere's and the ocean's; its longitudes are the
+ * atmosphere's.  y_LatX and y_IntWtLatX hold JMA + JMO values; *JMX
+ * receives the count.  Host arithmetic. */
+int dccm_exchange_grid(const double *y_LatA, const double *y_IntWtLatA, int JMA,
+                       const double *y_LatO, const double *y_IntWtLatO, int JMO,
+                       double *y_LatX, double *y_IntWtLatX, int *JMX);
 /* Number of rows (iD, jD, iS, jS, w). */
 int dccm_remap_table_size(const dccm_remap_table *table, int64_t *nrow);
 /* Copies the rows out (1-based grid indices as in the reference file). */

@@ -54,6 +54,10 @@ def lib():
         L.oracle_rfft_row.argtypes = [i32, P, i32, P]
         L.oracle_implcpl_forward.argtypes = [P, P, P, P, P, i64, i32, i32, i32, P]
         L.oracle_implcpl_backward.argtypes = [P, P, P, P, P, P, P, i64, i32, i32, f64]
+        L.oracle_bilin_gen.argtypes = [P, i32, P, i32, P, i32, P, i32, i64, P, P, P, P, P, P]
+        L.oracle_bilin_gen.restype = i32
+        L.oracle_exchange_grid_lat.argtypes = [P, P, i32, P, P, i32, P, P]
+        L.oracle_exchange_grid_lat.restype = i32
         L.oracle_set_threads.argtypes = [i32]
         L.oracle_get_threads.restype = i32
         _lib = L
@@ -215,4 +219,33 @@ def implcpl_backward(mats, tend, DelTime):
     lib().oracle_implcpl_backward(*[_p(x) for x in m], _p(t["DUDt"]), _p(t["DVDt"]), _p(t["DTempDt"]),
                                   _p(t["DQMixDt"]), ncol, kmax, ncmax, float(DelTime))
     return t
+
+
+# -------------------------------------------- bilinear table, exchange grid
+def bilin_gen(lonS, latS, lonR, latR):
+    """Rows (iR, jR, iS, jS, w) of the bilinear table in the reference's
+    order (north of the last source latitude: linear extrapolation from the
+    last two; ValueError if the source has a single latitude)."""
+    a = [np.ascontiguousarray(x, dtype=np.float64) for x in (lonS, latS, lonR, latR)]
+    cap = 0
+    nrow = ctypes.c_int64(0)
+    while True:
+        bufs = [np.zeros(max(cap, 1), np.int32) for _ in range(4)] + [np.zeros(max(cap, 1), np.float64)]
+        st = lib().oracle_bilin_gen(_p(a[0]), len(a[0]), _p(a[1]), len(a[1]), _p(a[2]), len(a[2]), _p(a[3]),
+                                    len(a[3]), cap, *[_p(b) for b in bufs], ctypes.byref(nrow))
+        if st < 0:
+            raise ValueError("oracle_bilin_gen: no source latitude pair (%d)" % st)
+        if st == 0:
+            return tuple(b[:nrow.value] for b in bufs)
+        cap = nrow.value
+
+
+def exchange_grid_lat(latA, wA, latO, wO):
+    """Latitudes and sin-latitude widths of the surface exchange grid."""
+    a = [np.ascontiguousarray(x, dtype=np.float64) for x in (latA, wA, latO, wO)]
+    n = len(a[0]) + len(a[2])
+    lat, w = np.zeros(n), np.zeros(n)
+    m = lib().oracle_exchange_grid_lat(_p(a[0]), _p(a[1]), len(a[0]), _p(a[2]), _p(a[3]), len(a[2]),
+                                       _p(lat), _p(w))
+    return lat[:m], w[:m]
 

@@ -11,6 +11,8 @@
  *   - table reader:       common/grid_mapping_util_jones99.f90:446-506
  *   - remap apply:        common/interpolation_data_latlon_mod.f90:274-306
  *   - implicit coupling:  atm/dcpam_sfc_implicit_coupling_mod.f90:25-420
+ *   - bilinear table:     common/grid_mapping_util.f90:32-182
+ *   - exchange grid:      tool/gmapgen/gmapgen_main.f90:336-425
  *   - spherical-harmonic transform: SPML/ISPACK (external, not vendored);
  *     restated from the mathematics with the convention documented in
  *     oracle_sht.c.
@@ -112,6 +114,22 @@ void oracle_implcpl_forward(const double *const *in, double *const *out, double 
 void oracle_implcpl_backward(const double *uv, const double *tm, const double *qm, double *DUDt,
                              double *DVDt, double *DTempDt, double *DQMixDt, int64_t ncol, int kmax,
                              int ncmax, double DelTime);
+
+/* ------------------------------------------- bilinear table, exchange grid */
+/* gen_gridmapfile_lonlat2lonlat (common/grid_mapping_util.f90:32-182):
+ * rows (iR, jR, iS, jS, w) in the reference's order.  Returns 1 (and the
+ * needed *nrow) if cap is too small.  North of the last source latitude
+ * (undefined in the reference) the rows extrapolate from the last two
+ * source latitudes; -1 if there is only one. */
+int oracle_bilin_gen(const double *lonS, int nxs, const double *latS, int nys, const double *lonR, int nxr,
+                     const double *latR, int nyr, int64_t cap, int32_t *iR, int32_t *jR, int32_t *iS,
+                     int32_t *jS, double *w, int64_t *nrow);
+/* generate_surface_exchage_grid (tool/gmapgen/gmapgen_main.f90:336-405):
+ * latitudes and sin-latitude widths of the surface exchange grid (its
+ * longitudes are the atmosphere's).  latX, wX hold JMA + JMO entries;
+ * returns JMS. */
+int oracle_exchange_grid_lat(const double *latA, const double *wA, int JMA, const double *latO,
+                             const double *wO, int JMO, double *latX, double *wX);
 
 #ifdef __cplusplus
 }

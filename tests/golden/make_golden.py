@@ -18,7 +18,10 @@ plain Python, kept deliberately different in structure from the C oracle:
   full-latitude sums without the equatorial fold; FFTs from numpy.fft;
 * implicit surface coupling: whole levels of all columns at a time
   (atm/dcpam_sfc_implicit_coupling_mod.f90:72-405), the oracle loops per
-  column.
+  column;
+* bilinear table and exchange grid: the Fortran loops transcribed in
+  Python (common/grid_mapping_util.f90:32-182,
+  tool/gmapgen/gmapgen_main.f90:336-405), Python's sort for the edges.
 
 Run from the repository root:  python tests/golden/make_golden.py
 """
@@ -389,6 +392,106 @@ def implcpl_numpy(d, ih2o, consts):
     return out
 
 
+def bilin_python(lonS, latS, lonR, latR):
+    """gen_gridmapfile_lonlat2lonlat (common/grid_mapping_util.f90:32-182)
+    transcribed line by line; north of the last source latitude (a read
+    past the array in the reference) the last two source rows extrapolate,
+    as the reference does south of the first."""
+    nxs, nys, nxr, nyr = len(lonS), len(latS), len(lonR), len(latR)
+    dlon_r, dlon_s = 360.0 / nxr, 360.0 / nxs
+    rows = []
+    for jr in range(1, nyr + 1):
+        js, extp = None, True
+        for j in range(1, nys):
+            if latS[j - 1] < latR[jr - 1] <= latS[j]:
+                js, extp = j, False
+                break
+        if extp:
+            if latR[jr - 1] <= latS[0]:
+                js = 1
+            if latR[jr - 1] > latS[nys - 1]:
+                js = nys
+        if nxr == 1:
+            if not extp:
+                b1 = (latR[jr - 1] - latS[js - 1]) / (latS[js] - latS[js - 1])
+                c1, c2 = (1.0 - b1) / nxs, b1 / nxs
+                for i in range(1, nxs + 1):
+                    rows += [(1, jr, i, js, c1), (1, jr, i, js % nys + 1, c2)]
+            else:
+                rows += [(1, jr, i, js, 1.0 / nxs) for i in range(1, nxs + 1)]
+        elif nxs == 1:
+            if not extp:
+                b1 = (latR[jr - 1] - latS[js - 1]) / (latS[js] - latS[js - 1])
+                for i in range(1, nxr + 1):
+                    rows += [(i, jr, 1, js, 1.0 - b1), (i, jr, 1, js % nys + 1, b1)]
+            else:
+                rows += [(i, jr, 1, js, 1.0) for i in range(1, nxr + 1)]
+        else:
+            if extp and js == nys:
+                js = nys - 1
+            for ir in range(1, nxr + 1):
+                i = int(dlon_r * (ir - 1) / dlon_s) + 1
+                a1 = (lonR[ir - 1] - lonS[i - 1]) / (lonS[i % nxs] - lonS[i - 1])
+                b1 = (latR[jr - 1] - latS[js - 1]) / (latS[js] - latS[js - 1])
+                a2, b2 = 1.0 - a1, 1.0 - b1
+                rows += [(ir, jr, i, js, a2 * b2), (ir, jr, i % nxs + 1, js, a1 * b2),
+                         (ir, jr, i % nxs + 1, js % nys + 1, a1 * b1), (ir, jr, i, js % nys + 1, a2 * b1)]
+    return rows
+
+
+def xgrid_python(wA, wO):
+    """generate_surface_exchage_grid (tool/gmapgen/gmapgen_main.f90:336-405)
+    for JMA != JMO: merged latitude edges, Python's sorted() instead of the
+    exchange sort."""
+    JMA, JMO = len(wA), len(wO)
+    FJA = [-math.pi / 2]
+    for j in range(1, JMA + 1):
+        FJA.append(math.asin(wA[j - 1] + math.sin(FJA[j - 1])))
+    FJA[JMA] = math.pi / 2
+    FJO = [-math.pi / 2]
+    for j in range(1, JMO):
+        FJO.append(math.asin(wO[j - 1] + math.sin(FJO[j - 1])))
+    FJO.append(math.pi / 2)
+    FJS = sorted(FJA[:JMA] + FJO[1:])
+    lat, w = [], []
+    for j in range(1, len(FJS)):
+        wt = math.sin(FJS[j]) - math.sin(FJS[j - 1])
+        if abs(wt) > 1e-12:
+            lat.append(0.5 * (FJS[j - 1] + FJS[j]))
+            w.append(wt)
+    return np.array(lat), np.array(w)
+
+
+def make_bilin():
+    out = {}
+    cases = {"t21_to_t42": (gaussian(64, 32), gaussian(128, 64)),
+             "t42_to_t21": (gaussian(128, 64), gaussian(64, 32)),
+             "t21_to_reg": (gaussian(64, 32), regular(72, 36)),
+             "axi_dst": (gaussian(64, 32), (np.zeros(1), regular(1, 20)[1])),
+             "axi_src": ((np.zeros(1), regular(1, 16)[1]), gaussian(64, 32))}
+    for name, (S, R) in cases.items():
+        rows = bilin_python(S[0], S[1], R[0], R[1])
+        out[name + "_grid"] = np.array([len(S[0]), len(S[1]), len(R[0]), len(R[1])])
+        out[name + "_lon_lat"] = np.concatenate([S[0], S[1], R[0], R[1]])
+        out[name + "_idx"] = np.array([r[:4] for r in rows], dtype=np.int32)
+        out[name + "_w"] = np.array([r[4] for r in rows], dtype=np.float64)
+    lat, w = xgrid_python(list(gaussian(64, 32)[2]), list(regular_w(64)))
+    out["xgrid_lat"], out["xgrid_w"] = lat, w
+    np.savez_compressed(os.path.join(OUT, "bilin_small.npz"), **out)
+
+
+def regular(nx, ny):
+    """Cell-centred regular grid (lon from 0, lat S to N) in radians."""
+    lon = 2.0 * np.pi * np.arange(nx) / nx
+    e = np.linspace(-np.pi / 2, np.pi / 2, ny + 1)
+    return lon, 0.5 * (e[:-1] + e[1:])
+
+
+def regular_w(ny):
+    e = np.linspace(-np.pi / 2, np.pi / 2, ny + 1)
+    return np.sin(e[1:]) - np.sin(e[:-1])
+
+
 def make_implcpl():
     import importlib
     import sys
@@ -404,6 +507,8 @@ if __name__ == "__main__":
     make_flux()
     make_j99()
     make_sht()
+    make_implcpl()
+    make_bilin()
     for f in sorted(os.listdir(OUT)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(OUT, f)))

@@ -242,3 +242,37 @@ def test_implcpl_sweeps_solve_the_column_systems(oracle, synth):
         m0 = mass + VTC[k - 1] + (VTC[k] if k < K else 0.0)
         lhs = -VTC[k - 1] * x[k - 2] + m0 * x[k - 1] + (-VTC[k] * x[k] if k < K else 0.0)
         assert np.allclose(lhs, rhs[k - 1], rtol=1e-9, atol=1e-12 * np.abs(rhs).max()), k
+
+
+# -------------------------------------------- bilinear table, exchange grid
+BILIN_CASES = ["t21_to_t42", "t42_to_t21", "t21_to_reg", "axi_dst", "axi_src"]
+
+
+def bilin_case(z, name):
+    g = z[name + "_grid"]
+    o = np.cumsum([0] + list(g))
+    ll = z[name + "_lon_lat"]
+    return [ll[o[i]:o[i + 1]] for i in range(4)]
+
+
+@pytest.mark.parametrize("name", BILIN_CASES)
+def test_bilinear_matches_golden(oracle, name):
+    z = np.load(os.path.join(GOLDEN, "bilin_small.npz"))
+    lonS, latS, lonR, latR = bilin_case(z, name)
+    r = oracle.bilin_gen(lonS, latS, lonR, latR)
+    assert np.array_equal(np.stack(r[:4], 1), z[name + "_idx"])
+    assert np.array_equal(r[4], z[name + "_w"])
+    # every destination cell's weights sum to 1 (interpolation, extrapolation)
+    nxr = len(lonR)
+    s = np.zeros(nxr * len(latR))
+    np.add.at(s, (r[0] - 1) + nxr * (r[1] - 1), r[4])
+    assert np.allclose(s, 1.0, atol=1e-13)
+
+
+def test_exchange_grid_matches_golden(oracle):
+    z = np.load(os.path.join(GOLDEN, "bilin_small.npz"))
+    mu, wA = np.polynomial.legendre.leggauss(32)
+    e = np.linspace(-np.pi / 2, np.pi / 2, 65)
+    lat, w = oracle.exchange_grid_lat(np.arcsin(mu), wA, 0.5 * (e[1:] + e[:-1]), np.sin(e[1:]) - np.sin(e[:-1]))
+    assert np.array_equal(lat, z["xgrid_lat"]) and np.array_equal(w, z["xgrid_w"])
+    assert abs(w.sum() - 2.0) < 1e-13 and np.all(np.diff(lat) > 0)
