@@ -1,6 +1,8 @@
 // Shared helpers of the dccm_gb300 library (internal header).
 #pragma once
 #include <cuda_runtime.h>
+
+#include <utility>
 #include <stdint.h>
 #include <stdio.h>
 
@@ -23,6 +25,31 @@ void set_cuda_error(cudaError_t e);
 
 // Check the launch status of the preceding kernel launch.
 #define DCCM_LAUNCH_CHECK() DCCM_CUDA(cudaGetLastError())
+
+// Programmatic dependent launch between the kernels of the transform chain:
+// a kernel launched with launch_pdl may start while the previous kernel in
+// its stream is still running (its prologue overlaps that kernel's tail).
+// It must execute pdl_wait() before it reads anything the previous kernel
+// writes or writes anything the previous kernel reads; pdl_trigger() lets
+// the next kernel start.  Both are no-ops for an ordinary launch.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                              Args &&...args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
 
 #define DCCM_TRY(expr)           \
   do {                           \

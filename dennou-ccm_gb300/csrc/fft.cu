@@ -510,6 +510,8 @@ __device__ __forceinline__ void dispatch_case(const FftGroup &G, int jj, int by,
 template <int RMAX, bool FWD>
 __global__ void __launch_bounds__(512) fft_multi_kernel(const __grid_constant__ FftLaunch L) {
   extern __shared__ __align__(16) float st[];
+  pdl_wait();  // reads the previous kernel's output; the forward FFT overwrites the buffer it read
+  pdl_trigger();
   int gi = 0;
   while (gi + 1 < L.ngroups && (int)blockIdx.x >= L.g[gi + 1].blk0) ++gi;
   const FftGroup &G = L.g[gi];
@@ -596,8 +598,7 @@ int fft_multi(Plan *const *plans, const int *batch, const void *const *in, void 
   if (nblk == 0) return DCCM_OK;
   auto go = [&](auto kernel) -> int {
     DCCM_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    kernel<<<nblk, 32 * warps, smem, s>>>(L);
-    DCCM_LAUNCH_CHECK();
+    DCCM_CUDA(launch_pdl(kernel, dim3(nblk), dim3(32 * warps), smem, s, L));
     return DCCM_OK;
   };
   if (rmax <= 8) return fwd ? go(fft_multi_kernel<8, true>) : go(fft_multi_kernel<8, false>);

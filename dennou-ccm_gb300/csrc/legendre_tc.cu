@@ -245,6 +245,8 @@ legendre_tc_kernel(const __grid_constant__ TcLaunch L) {
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
   const int nitems = L.start[L.ngroups];
+  pdl_wait();  // the operands come from the previous kernel (pack or forward FFT)
+  pdl_trigger();
 
   if (warp == 0) {
     // ---------------------------------------------------------- TMA
@@ -439,6 +441,8 @@ struct PackLaunch {
 };
 
 __global__ void __launch_bounds__(256) pack_spectra_kernel(const __grid_constant__ PackLaunch L) {
+  pdl_wait();  // Apack is read by the previous step's synthesis
+  pdl_trigger();
   int gi = 0;
   while (gi + 1 < L.ngroups && (int)blockIdx.y >= L.g[gi + 1].f0) ++gi;
   const PackGroup &G = L.g[gi];
@@ -489,8 +493,7 @@ int pack_spectra(Plan *const *plans, const int *batch, const double *const *spec
   if (nf > 65535) return DCCM_ERR_UNSUPPORTED;
   long long bx = (maxc + 255) / 256;
   if (bx > 64) bx = 64;
-  pack_spectra_kernel<<<dim3((unsigned)bx, (unsigned)nf), 256, 0, s>>>(L);
-  DCCM_LAUNCH_CHECK();
+  DCCM_CUDA(launch_pdl(pack_spectra_kernel, dim3((unsigned)bx, (unsigned)nf), dim3(256), 0, s, L));
   return DCCM_OK;
 }
 
@@ -765,8 +768,7 @@ int legendre_tc_multi(Plan *const *plans, const int *batch, const void *const *i
   if (items <= 0) return DCCM_OK;
   int ctas = tunables().tc_ctas > 0 ? tunables().tc_ctas : sm_count();
   const int grid = items < ctas ? items : ctas;
-  legendre_tc_kernel<<<grid, TC_THREADS, tc_smem_bytes(), s>>>(L);
-  DCCM_LAUNCH_CHECK();
+  DCCM_CUDA(launch_pdl(legendre_tc_kernel, dim3(grid), dim3(TC_THREADS), tc_smem_bytes(), s, L));
   return DCCM_OK;
 }
 
