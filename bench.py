@@ -407,8 +407,22 @@ def profile_run(args, w, inp):
         step.run()
     torch.cuda.synchronize()
     st, derr = S["plans"]["mixed"].status()
+    # then the implicit surface coupling of the largest group's atmosphere:
+    # forward and backward sweep, profile_steps times each, in that order
+    g = max(inp["groups"], key=lambda q: q.I * q.J)
+    ncol, kmax = g.I * g.J, max(2, g.nfl // 4 if len(inp["groups"]) == 1 else 32)
+    d = synth.column_profiles(ncol, kmax, ncmax=1, seed=7)
+    plan = dccm.ImplCplPlan(ncol, kmax, 1, 1, synth.IMPLCPL_CONSTS)
+    dd = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in d.items()}
+    shapes = {"DUDt": (kmax, ncol), "DVDt": (kmax, ncol), "DTempDt": (kmax, ncol), "DQMixDt": (1, kmax, ncol),
+              "ImplCplCoef1": (4, ncol), "ImplCplCoef2": (4, ncol)}
+    out = {k: torch.empty(v, dtype=torch.float64, device=dev) for k, v in shapes.items()}
+    for _ in range(args.profile_steps):
+        plan.forward_dev(dd, out)
+        plan.backward_dev(out)
+    torch.cuda.synchronize()
     print(json.dumps({"profile_steps": args.profile_steps, "workload": args.workload, "status": st,
-                      "device_error": derr}))
+                      "device_error": derr, "implcpl_columns": ncol, "implcpl_levels": kmax}))
 
 
 def max_over_ranks(vals, world, dev):

@@ -5,12 +5,13 @@
 //             Solve_TriDiagSystem_Forward (:380-405);
 //   backward  SfcImplicitCoupling_VDiffBackward (:25-70) with
 //             Solve_TriDiagSystem_Backward (:407-420).
-// One thread per atmosphere column; every array is the reference's
-// (i, j, k[, n]) layout with the columns flattened, so consecutive threads
-// touch consecutive addresses at every level.  The three tridiagonal
-// systems (momentum, temperature, tracers) are built and eliminated from
-// the model top down in place, in the plan-owned matrices that the
-// reference keeps as module state for the backward sweep.
+// One thread per atmosphere column and system (momentum, temperature, each
+// tracer); every array is the reference's (i, j, k[, n]) layout with the
+// columns flattened, so consecutive threads touch consecutive addresses at
+// every level.  The forward sweep builds each level's row and eliminates it
+// in the same pass from the model top down, so the matrices that the
+// reference keeps as module state for the backward sweep are written once
+// and never re-read.
 //
 // FP64 throughout.  Divisions are the scarce operation on this GPU (the
 // FP64 pipe is 1/64 of FP32), so the elimination computes one reciprocal
@@ -47,129 +48,165 @@ struct Fwd {
   double Grav, CpDry, GasR, inv_g2dt;
 };
 
+// One thread per (column, system): blockIdx.y 0 = momentum (U and V share
+// the matrix), 1 = temperature, 2 + t = tracer t (each tracer thread
+// eliminates the tracer matrix; tracer 0 stores it).  A single pass from
+// the model top down builds each level's row (:188-308) and eliminates it
+// at once (:380-405), carrying the eliminated M(k+1,0) and right-hand sides
+// of the level above; the eliminated matrix and tendencies are written
+// once.  The level inputs are fetched LV levels ahead into registers, so
+// the loads of a chunk overlap while the serial elimination runs.
+constexpr int LV = 4;   // forward sweep: levels fetched ahead
+constexpr int LVB = 8;  // backward sweep
+
+template <int SYS>
+__device__ __forceinline__ void forward_column(const Fwd &a, long long c, int tracer) {
+  constexpr int NR = SYS == 0 ? 2 : 1;
+  const long long n = a.ncol;
+  const int K = a.kmax;
+  const long long mstr = n * K;
+  const double *__restrict__ Kd = SYS == 0 ? a.Kv : (SYS == 1 ? a.Kt : a.Kq);
+  const double *__restrict__ fl[NR];
+  double *__restrict__ out[NR];
+  if constexpr (SYS == 0) {
+    fl[0] = a.MomX;
+    fl[1] = a.MomY;
+    out[0] = a.DU;
+    out[1] = a.DV;
+  } else if constexpr (SYS == 1) {
+    fl[0] = a.Heat;
+    out[0] = a.DT;
+  } else {
+    fl[0] = a.QFlx + n * (long long)(K + 1) * tracer;
+    out[0] = a.DQ + n * (long long)K * tracer;
+  }
+  double *mat = SYS == 0 ? a.uv : (SYS == 1 ? a.tm : a.qm);
+  const bool store_mat = SYS != 2 || tracer == 0;
+  // values at level k carried from the previous (upper) iteration
+  double Pk = a.P[c + n * K], Zk = a.Z[c + n * (K - 1)], Ehk = a.Eh[c + n * K];
+  double flk[NR];
+#pragma unroll
+  for (int r = 0; r < NR; ++r) flk[r] = fl[r][c + n * K];
+  double tck = 0.0, ief_k1 = 0.0, ief_k = 1.0 / a.Ef[c + n * (K - 1)];
+  double m0p = 0.0, rp[NR], m0_2 = 0.0, r_2[NR], c2[NR], tc1 = 0.0, dfadt1 = 0.0, dfadt2 = 0.0;
+  for (int k0 = K; k0 >= 1; k0 -= LV) {
+    // fetch half level k-1 and full level k-1 of the next LV levels
+    double Pm[LV], Tvm[LV], Zm[LV], Kdm[LV], Ehm[LV], Efm[LV], flm[LV][NR];
+#pragma unroll
+    for (int i = 0; i < LV; ++i) {
+      const int k = k0 - i;
+      if (k >= 1) {
+        Pm[i] = a.P[c + n * (k - 1)];
+        if (k > 1) {
+          Tvm[i] = a.Tv[c + n * (k - 1)];
+          Zm[i] = a.Z[c + n * (k - 2)];
+          Kdm[i] = Kd[c + n * (k - 1)];
+          if (SYS == 1) {
+            Ehm[i] = a.Eh[c + n * (k - 1)];
+            Efm[i] = a.Ef[c + n * (k - 2)];
+          }
+        }
+#pragma unroll
+        for (int r = 0; r < NR; ++r) flm[i][r] = fl[r][c + n * (k - 1)];
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < LV; ++i) {
+      const int k = k0 - i;
+      if (k < 1) break;
+      // transfer coefficient at half level k-1 (0 at the surface, :182-195)
+      double tkm = 0.0, ief_km = 0.0;
+      if (k > 1) {
+        const double tmp = Pm[i] / (a.GasR * Tvm[i] * (Zk - Zm[i]));
+        tkm = Kdm[i] * tmp;
+        if (SYS == 1) ief_km = 1.0 / Efm[i];
+      }
+      const double mass = -(Pk - Pm[i]) * a.inv_g2dt;
+      double mm, m0, mp;  // row k; +0 where the reference assigns 0
+      if constexpr (SYS != 1) {
+        mm = k > 1 ? -tkm : 0.0;
+        m0 = mass + tkm + tck;
+        mp = k < K ? -tck : 0.0;
+      } else {
+        const double ehm = k > 1 ? a.CpDry * Ehm[i] * tkm : 0.0;
+        const double ehk = a.CpDry * Ehk * tck;
+        mm = k > 1 ? -(ehm * ief_km) : 0.0;
+        m0 = a.CpDry * mass + ehm * ief_k + ehk * ief_k;
+        mp = k < K ? -(ehk * ief_k1) : 0.0;
+        if (k == 1) {
+          dfadt1 = ehk * ief_k;  // DFADT1 = Cp Exner_h(1) TTC(1) / Exner_f(1)
+          dfadt2 = mp;           // DFADT2 = -Cp Exner_h(1) TTC(1) / Exner_f(2)
+        }
+      }
+      if (k == 1) tc1 = tck;
+      double inv, m0e;
+      if (k == K) {
+        inv = 1.0 / mm;
+        m0e = m0 * inv;
+      } else {
+        inv = 1.0 / (mm * m0p);
+        m0e = (m0 * m0p - mp) * inv;
+      }
+#pragma unroll
+      for (int r = 0; r < NR; ++r) {
+        const double b = -(flk[r] - flm[i][r]);
+        if (k == 1) c2[r] = b;  // ImplCplCoef2 starts from the level-1 divergence (:310-313)
+        const double re = k == K ? b * inv : (b * m0p - mp * rp[r]) * inv;
+        out[r][c + n * (k - 1)] = re;
+        rp[r] = re;
+        if (k == 2) r_2[r] = re;
+        flk[r] = flm[i][r];
+      }
+      if (store_mat) {
+        mat[c + n * (k - 1)] = 1.0;
+        mat[c + n * (k - 1) + mstr] = m0e;
+        mat[c + n * (k - 1) + 2 * mstr] = 0.0;
+      }
+      if (k == 2) m0_2 = m0e;
+      m0p = m0e;
+      tck = tkm;
+      ief_k1 = ief_k;
+      ief_k = ief_km;
+      Pk = Pm[i];
+      if (k > 1) {
+        Zk = Zm[i];
+        if (SYS == 1) Ehk = Ehm[i];
+      }
+    }
+  }
+  // coupling coefficients (:342-375); DFADUV1 = -DFADUV2 = TC(1)
+  const double Tmp = -(a.P[c + n] - a.P[c]) * a.inv_g2dt;
+  const double i2 = 1.0 / m0_2;
+  if constexpr (SYS == 0) {
+    const double cu = Tmp + tc1 + tc1 * i2;
+    a.C1[c + n * 0] = cu;
+    a.C2[c + n * 0] = c2[0] + tc1 * r_2[0] * i2;
+    a.C1[c + n * 1] = cu;
+    a.C2[c + n * 1] = c2[1] + tc1 * r_2[1] * i2;
+  } else if constexpr (SYS == 1) {
+    a.C1[c + n * 2] = a.CpDry * Tmp + dfadt1 - dfadt2 * i2;
+    a.C2[c + n * 2] = c2[0] - dfadt2 * r_2[0] * i2;
+  } else {
+    if (tracer == a.ih2o - 1) {
+      a.C1[c + n * 3] = Tmp + tc1 + tc1 * i2;
+      a.C2[c + n * 3] = c2[0] + tc1 * r_2[0] * i2;
+    }
+  }
+}
+
 __global__ void __launch_bounds__(128) forward_kernel(const Fwd a) {
   const long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (c >= a.ncol) return;
-  const long long n = a.ncol;
-  const int K = a.kmax;
-  const long long mstr = n * K;  // one diagonal
-  auto H = [&](const double *x, int k) { return x[c + n * k]; };                 // half level k = 0..K
-  auto F = [&](auto *x, int k) -> auto & { return x[c + n * (k - 1)]; };          // full level k = 1..K
-  auto M = [&](double *m, int k, int d) -> double & { return m[c + n * (k - 1) + mstr * (d + 1)]; };
-
-  // ---- matrices and right-hand sides (:188-308), level by level, carrying
-  // the transfer coefficients and inverse Exner functions of k-1, k, k+1
-  double vp = 0.0, tp = 0.0, qp = 0.0;  // transfer coefficients at half level k-1
-  double iep = 0.0;                     // 1 / Exner at full level k-1
-  double iec = 1.0 / F(a.Ef, 1);
-  double Pprev = H(a.P, 0);
-  double dfadt1 = 0.0;
-  for (int k = 1; k <= K; ++k) {
-    double vk = 0.0, tk = 0.0, qk = 0.0, ien = 0.0;
-    if (k < K) {
-      const double tmp = H(a.P, k) / (a.GasR * H(a.Tv, k) * (F(a.Z, k + 1) - F(a.Z, k)));
-      vk = H(a.Kv, k) * tmp;
-      tk = H(a.Kt, k) * tmp;
-      qk = H(a.Kq, k) * tmp;
-      ien = 1.0 / F(a.Ef, k + 1);
-    }
-    const double Pk = H(a.P, k);
-    const double mass = -(Pk - Pprev) * a.inv_g2dt;
-    Pprev = Pk;
-    // momentum and tracers
-    // (+0 where the reference assigns 0: the sign of the level-1 division
-    // by the zero sub-diagonal follows it)
-    M(a.uv, k, -1) = k > 1 ? -vp : 0.0;
-    M(a.uv, k, 0) = mass + vp + vk;
-    M(a.uv, k, 1) = k < K ? -vk : 0.0;
-    M(a.qm, k, -1) = k > 1 ? -qp : 0.0;
-    M(a.qm, k, 0) = mass + qp + qk;
-    M(a.qm, k, 1) = k < K ? -qk : 0.0;
-    // temperature: the Exner ratios of the reference's dry static energy form
-    const double ehp = k > 1 ? a.CpDry * H(a.Eh, k - 1) * tp : 0.0;
-    const double ehk = a.CpDry * H(a.Eh, k) * tk;
-    M(a.tm, k, -1) = k > 1 ? -(ehp * iep) : 0.0;
-    M(a.tm, k, 0) = a.CpDry * mass + ehp * iec + ehk * iec;
-    M(a.tm, k, 1) = k < K ? -(ehk * ien) : 0.0;
-    if (k == 1) dfadt1 = ehk * iec;  // DFADT1 = Cp Exner_h(1) TTC(1) / Exner_f(1)
-    // right-hand sides: flux divergences
-    F(a.DU, k) = -(H(a.MomX, k) - H(a.MomX, k - 1));
-    F(a.DV, k) = -(H(a.MomY, k) - H(a.MomY, k - 1));
-    F(a.DT, k) = -(H(a.Heat, k) - H(a.Heat, k - 1));
-    for (int t = 0; t < a.ncmax; ++t) {
-      const double *q = a.QFlx + n * (long long)(K + 1) * t;
-      a.DQ[c + n * ((k - 1) + (long long)K * t)] = -(q[c + n * k] - q[c + n * (k - 1)]);
-    }
-    vp = vk;
-    tp = tk;
-    qp = qk;
-    iep = iec;
-    iec = ien;
-  }
-  const double vt1 = M(a.uv, 1, 1), qt1 = M(a.qm, 1, 1);  // -(transfer coefficient at half level 1)
-  const double tt1 = M(a.tm, 1, 1);  // DFADT2 = -Cp Exner_h(1) TTC(1) / Exner_f(2)
-  a.C2[c + n * 0] = F(a.DU, 1);      // :310-313
-  a.C2[c + n * 1] = F(a.DV, 1);
-  a.C2[c + n * 2] = F(a.DT, 1);
-  a.C2[c + n * 3] = a.DQ[c + n * ((long long)K * (a.ih2o - 1))];
-
-  // ---- elimination from the top (:380-405) for all systems at once
-  {
-    const double iu = 1.0 / M(a.uv, K, -1), it = 1.0 / M(a.tm, K, -1), iq = 1.0 / M(a.qm, K, -1);
-    M(a.uv, K, 0) *= iu;
-    F(a.DU, K) *= iu;
-    F(a.DV, K) *= iu;
-    M(a.uv, K, -1) = 1.0;
-    M(a.tm, K, 0) *= it;
-    F(a.DT, K) *= it;
-    M(a.tm, K, -1) = 1.0;
-    M(a.qm, K, 0) *= iq;
-    for (int t = 0; t < a.ncmax; ++t) a.DQ[c + n * ((K - 1) + (long long)K * t)] *= iq;
-    M(a.qm, K, -1) = 1.0;
-  }
-  double u0 = M(a.uv, K, 0), t0 = M(a.tm, K, 0), q0 = M(a.qm, K, 0);  // M(k+1, 0)
-  for (int k = K - 1; k >= 1; --k) {
-    const double iu = 1.0 / (M(a.uv, k, -1) * u0);
-    const double it = 1.0 / (M(a.tm, k, -1) * t0);
-    const double iq = 1.0 / (M(a.qm, k, -1) * q0);
-    const double pu = M(a.uv, k, 1), pt = M(a.tm, k, 1), pq = M(a.qm, k, 1);
-    F(a.DU, k) = (F(a.DU, k) * u0 - pu * F(a.DU, k + 1)) * iu;
-    F(a.DV, k) = (F(a.DV, k) * u0 - pu * F(a.DV, k + 1)) * iu;
-    F(a.DT, k) = (F(a.DT, k) * t0 - pt * F(a.DT, k + 1)) * it;
-    for (int t = 0; t < a.ncmax; ++t) {
-      double *q = a.DQ + n * (long long)K * t;
-      q[c + n * (k - 1)] = (q[c + n * (k - 1)] * q0 - pq * q[c + n * k]) * iq;
-    }
-    u0 = (M(a.uv, k, 0) * u0 - pu) * iu;
-    t0 = (M(a.tm, k, 0) * t0 - pt) * it;
-    q0 = (M(a.qm, k, 0) * q0 - pq) * iq;
-    M(a.uv, k, 0) = u0;
-    M(a.tm, k, 0) = t0;
-    M(a.qm, k, 0) = q0;
-    M(a.uv, k, -1) = 1.0;
-    M(a.uv, k, 1) = 0.0;
-    M(a.tm, k, -1) = 1.0;
-    M(a.tm, k, 1) = 0.0;
-    M(a.qm, k, -1) = 1.0;
-    M(a.qm, k, 1) = 0.0;
-  }
-
-  // ---- coupling coefficients (:342-375); DFADUV1 = -DFADUV2 = the
-  // transfer coefficient at half level 1 (vt1 is the super-diagonal)
-  const double Tmp = -(H(a.P, 1) - H(a.P, 0)) * a.inv_g2dt;
-  const double iu2 = 1.0 / M(a.uv, 2, 0), it2 = 1.0 / M(a.tm, 2, 0), iq2 = 1.0 / M(a.qm, 2, 0);
-  const double cu = Tmp - vt1 - vt1 * iu2;
-  a.C1[c + n * 0] = cu;
-  a.C2[c + n * 0] = a.C2[c + n * 0] - vt1 * F(a.DU, 2) * iu2;
-  a.C1[c + n * 1] = cu;
-  a.C2[c + n * 1] = a.C2[c + n * 1] - vt1 * F(a.DV, 2) * iu2;
-  a.C1[c + n * 2] = a.CpDry * Tmp + dfadt1 - tt1 * it2;
-  a.C2[c + n * 2] = a.C2[c + n * 2] - tt1 * F(a.DT, 2) * it2;
-  a.C1[c + n * 3] = Tmp - qt1 - qt1 * iq2;
-  a.C2[c + n * 3] = a.C2[c + n * 3] - qt1 * a.DQ[c + n * (1 + (long long)K * (a.ih2o - 1))] * iq2;
+  if (blockIdx.y == 0) forward_column<0>(a, c, 0);
+  else if (blockIdx.y == 1) forward_column<1>(a, c, 0);
+  else forward_column<2>(a, c, blockIdx.y - 2);
 }
 
-// Back substitution (:407-420) and the division by 2 dt (:53-61).
+// Back substitution (:407-420) and the division by 2 dt (:53-61), one
+// thread per (column, matrix): blockIdx.y 0 = momentum (U and V), 1 =
+// temperature, 2 = the tracers; one reciprocal of M(k,0) per level serves
+// every right-hand side of the matrix, and levels are fetched LVB at a time
+// ahead of the serial chains.
 struct Bwd {
   const double *uv, *tm, *qm;
   double *DU, *DV, *DT, *DQ;
@@ -178,35 +215,64 @@ struct Bwd {
   double inv_2dt;
 };
 
+template <int NR>
+__device__ __forceinline__ void backward_chains(const double *__restrict__ mat, double *const *x, long long c,
+                                                long long n, int K, double inv_2dt) {
+  const long long mstr = n * K;
+  double v[NR];
+#pragma unroll
+  for (int r = 0; r < NR; ++r) {
+    v[r] = x[r][c];
+    x[r][c] = v[r] * inv_2dt;
+  }
+  for (int k0 = 2; k0 <= K; k0 += LVB) {
+    double xs[LVB][NR], mm[LVB], m0[LVB];
+#pragma unroll
+    for (int i = 0; i < LVB; ++i) {
+      const int k = k0 + i;
+      if (k <= K) {
+        const long long o = c + n * (k - 1);
+#pragma unroll
+        for (int r = 0; r < NR; ++r) xs[i][r] = x[r][o];
+        mm[i] = mat[o];
+        m0[i] = mat[o + mstr];
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < LVB; ++i) {
+      const int k = k0 + i;
+      if (k > K) break;
+      const double im = 1.0 / m0[i];
+#pragma unroll
+      for (int r = 0; r < NR; ++r) {
+        v[r] = (xs[i][r] - mm[i] * v[r]) * im;
+        x[r][c + n * (k - 1)] = v[r] * inv_2dt;
+      }
+    }
+  }
+}
+
 __global__ void __launch_bounds__(128) backward_kernel(const Bwd a) {
   const long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (c >= a.ncol) return;
   const long long n = a.ncol;
   const int K = a.kmax;
-  const long long mstr = n * K;
-  auto M = [&](const double *m, int k, int d) { return m[c + n * (k - 1) + mstr * (d + 1)]; };
-  double u = a.DU[c], v = a.DV[c], t = a.DT[c];
-  a.DU[c] = u * a.inv_2dt;
-  a.DV[c] = v * a.inv_2dt;
-  a.DT[c] = t * a.inv_2dt;
-  for (int k = 2; k <= K; ++k) {
-    const long long o = c + n * (k - 1);
-    const double iu = 1.0 / M(a.uv, k, 0), it = 1.0 / M(a.tm, k, 0);
-    u = (a.DU[o] - M(a.uv, k, -1) * u) * iu;
-    v = (a.DV[o] - M(a.uv, k, -1) * v) * iu;
-    t = (a.DT[o] - M(a.tm, k, -1) * t) * it;
-    a.DU[o] = u * a.inv_2dt;
-    a.DV[o] = v * a.inv_2dt;
-    a.DT[o] = t * a.inv_2dt;
-  }
-  for (int s = 0; s < a.ncmax; ++s) {
-    double *q = a.DQ + n * (long long)K * s;
-    double x = q[c];
-    q[c] = x * a.inv_2dt;
-    for (int k = 2; k <= K; ++k) {
-      const long long o = c + n * (k - 1);
-      x = (q[o] - M(a.qm, k, -1) * x) / M(a.qm, k, 0);
-      q[o] = x * a.inv_2dt;
+  if (blockIdx.y == 0) {
+    double *x[2] = {a.DU, a.DV};
+    backward_chains<2>(a.uv, x, c, n, K, a.inv_2dt);
+  } else if (blockIdx.y == 1) {
+    double *x[1] = {a.DT};
+    backward_chains<1>(a.tm, x, c, n, K, a.inv_2dt);
+  } else {
+    // tracers in pairs (one reciprocal per level for both)
+    for (int t = 0; t < a.ncmax; t += 2) {
+      if (t + 1 < a.ncmax) {
+        double *x[2] = {a.DQ + n * (long long)K * t, a.DQ + n * (long long)K * (t + 1)};
+        backward_chains<2>(a.qm, x, c, n, K, a.inv_2dt);
+      } else {
+        double *x[1] = {a.DQ + n * (long long)K * t};
+        backward_chains<1>(a.qm, x, c, n, K, a.inv_2dt);
+      }
     }
   }
 }
@@ -289,7 +355,8 @@ extern "C" int dccm_implcpl_forward_dev(dccm_implcpl *p, const dccm_implcpl_forw
   f.GasR = p->k.GasRDry;
   f.inv_g2dt = 1.0 / (p->k.Grav * (2.0 * p->k.DelTime));
   const int threads = 128;
-  implcpl::forward_kernel<<<(unsigned)((p->ncol + threads - 1) / threads), threads, 0, as_stream(stream)>>>(f);
+  implcpl::forward_kernel<<<dim3((unsigned)((p->ncol + threads - 1) / threads), 2 + p->ncmax), threads, 0,
+                            as_stream(stream)>>>(f);
   DCCM_LAUNCH_CHECK();
   return DCCM_OK;
 }
@@ -310,7 +377,8 @@ extern "C" int dccm_implcpl_backward_dev(dccm_implcpl *p, double *xyz_DUDt, doub
   b.ncmax = p->ncmax;
   b.inv_2dt = 1.0 / (2.0 * p->k.DelTime);
   const int threads = 128;
-  implcpl::backward_kernel<<<(unsigned)((p->ncol + threads - 1) / threads), threads, 0, as_stream(stream)>>>(b);
+  implcpl::backward_kernel<<<dim3((unsigned)((p->ncol + threads - 1) / threads), 3), threads, 0,
+                             as_stream(stream)>>>(b);
   DCCM_LAUNCH_CHECK();
   return DCCM_OK;
 }
