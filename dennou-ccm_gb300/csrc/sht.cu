@@ -33,6 +33,7 @@ __global__ void gauss_newton_kernel(int J, double *mu, double *w) {
   const double PI = 3.141592653589793238462643383279502884;
   double x = cos(PI * (k + 0.75) / (J + 0.5));
   double dp = 0.0;
+  bool last = false;
   for (int it = 0; it < 100; ++it) {
     double p0 = 1.0, p1 = x;
     for (int l = 2; l <= J; ++l) {
@@ -43,7 +44,8 @@ __global__ void gauss_newton_kernel(int J, double *mu, double *w) {
     dp = J * (x * p1 - p0) / (x * x - 1.0);
     const double dx = p1 / dp;
     x -= dx;
-    if (fabs(dx) <= 1e-16 * fabs(x) && it > 2) break;
+    if (last) break;  // one more step after |dx| <= 1e-15 |x| (quadratic convergence)
+    if (fabs(dx) <= 1e-15 * fabs(x)) last = true;
   }
   double p0 = 1.0, p1 = x;
   for (int l = 2; l <= J; ++l) {

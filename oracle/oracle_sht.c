@@ -61,6 +61,7 @@ void oracle_gauss_nodes(int J, double *mu, double *w) {
   for (int k = 0; k < J / 2; ++k) {
     double x = cos(PI * (k + 0.75) / (J + 0.5));
     double dp = 0.0;
+    int last = 0;
     for (int it = 0; it < 100; ++it) {
       double p0 = 1.0, p1 = x;
       for (int l = 2; l <= J; ++l) {
@@ -71,7 +72,8 @@ void oracle_gauss_nodes(int J, double *mu, double *w) {
       dp = J * (x * p1 - p0) / (x * x - 1.0);
       const double dx = p1 / dp;
       x -= dx;
-      if (fabs(dx) <= 1e-16 * fabs(x) && it > 2) break;
+      if (last) break; /* one more step after |dx| <= 1e-15 |x| (quadratic convergence) */
+      if (fabs(dx) <= 1e-15 * fabs(x)) last = 1;
     }
     {
       double p0 = 1.0, p1 = x;
