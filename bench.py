@@ -319,9 +319,9 @@ def host_copies(S, groups, dccm, torch):
 # each stage's kernels in one ncu capture of `bench.py --profile-steps`,
 # summarised in profiles/stages_c3_ncu.md; null where not captured.
 TRAFFIC = {
-    "c3": {"legendre_inverse": int((7.68384 + 12.144896) * 1e6 + 2304), "fft_inverse": int(11.341056e6 + 1792),
-           "fft_forward": int(33.62304e6 + 309248), "legendre_forward": int(18.947072e6 + 2816),
-           "remap": int(4.06912e6), "bulk_flux": int(7.707904e6 + 256)},
+    "c3": {"legendre_inverse": int((7.683584 + 12.144896) * 1e6 + 2304), "fft_inverse": int(11.3408e6 + 3584),
+           "fft_forward": int(33.62304e6 + 57344), "legendre_forward": int(18.947072e6 + 1792),
+           "remap": int(4.069376e6), "bulk_flux": int(7.708928e6 + 768)},
 }
 FP64_PEAK_TFLOPS = 152 * 2 * 2 * 2.070e9 / 1e12  # 2 DFMA lanes per SM and clock at the maximum SM clock
 
@@ -385,6 +385,13 @@ def roofline(S, inp, groups, stage_ms, workload):
 # FP64 flops per launch of the flux kernel (DADD + DMUL + 2 DFMA thread
 # instructions, ncu sass counters), summarised in profiles/stages_c3_ncu.md.
 FP64_FLOPS = {"c3": (20.948747 + 41.897494 + 2 * 114.69439) * 86836.697368}
+
+
+# FP64 flops of the implicit-coupling sweeps per column and level, one
+# tracer (DADD + DMUL + 2 DFMA thread instructions per cycle x elapsed
+# cycles, ncu, 32768 columns x 32 levels; profiles/implcpl_c3_ncu.md):
+# 4932 per 32-level column forward, 1430 backward.
+IMPLCPL_FP64_FLOPS = {"forward": 4932 / 32, "backward": 1430 / 32}
 
 
 def dccm_stages():
@@ -512,11 +519,13 @@ def gpu_bench(args, w, inp, rank, world):
     roof = roofline(S, inp, groups, stage_ms, args.workload)
 
     # end to end through the public API with host buffers (pinned)
-    h2d, d2h = host_copies(S, groups, dccm, torch)
-    h2d_bytes = sum(h.numel() * h.element_size() for h, _ in h2d)
-    d2h_bytes = sum(h.numel() * h.element_size() for h, _ in d2h)
+    # (the copy lists are prepared once, as a model with persistent host
+    # buffers would; every call still copies every byte in and out)
+    hc = dccm.HostCopies(*host_copies(S, groups, dccm, torch))
+    h2d_bytes, d2h_bytes = hc.nbytes()
+    host_tuned = S["steps"]["mixed"].autotune_host(hc, stream=stream)
     for _ in range(max(3, args.warmup)):
-        S["steps"]["mixed"].run_host(h2d, d2h, stream)
+        S["steps"]["mixed"].run_host(hc, stream=stream)
     if world > 1:
         torch.distributed.barrier()
     te = []
@@ -524,13 +533,14 @@ def gpu_bench(args, w, inp, rank, world):
         flush.fill_(float(k))
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        S["steps"]["mixed"].run_host(h2d, d2h, stream)
+        S["steps"]["mixed"].run_host(hc, stream=stream)
         te.append(time.perf_counter() - t0)
     t_e2e, = max_over_ranks([float(np.mean(te))], world, dev)
     launches = 5 + len(groups) + 1  # pack + 2 Legendre + 2 FFT + one remap per group + flux
     ic = implcpl_leg(args, groups, dccm, synth, torch, dev, stream, flush)
     return dict(t_mixed=t_mixed, t_fp64=t_fp64, t_e2e=t_e2e, clocks=ck, roof=roof, err=err, h2d=h2d_bytes,
-                d2h=d2h_bytes, nfl=nfl, launches=launches, tables=S["tables"], tuned=tuned, implcpl=ic)
+                d2h=d2h_bytes, nfl=nfl, launches=launches, tables=S["tables"], tuned=dict(tuned, host=host_tuned),
+                implcpl=ic)
 
 
 def implcpl_leg(args, groups, dccm, synth, torch, dev, stream, flush):
@@ -568,14 +578,23 @@ def implcpl_leg(args, groups, dccm, synth, torch, dev, stream, flush):
     fwd_bytes = ncol * 8 * ((kmax + 1) * (9 + 1) + kmax * 2 + kmax * 4 + 8 + 3 * 3 * kmax)
     bwd_bytes = ncol * 8 * (2 * 4 * kmax + 3 * 2 * kmax)
     f, b = float(np.mean(tf)), float(np.mean(tb))
+
+    def fp64(key, ms):
+        fl = IMPLCPL_FP64_FLOPS[key] * ncol * kmax
+        tfl = fl / (ms / 1e3) / 1e12
+        return {"achieved": tfl, "unit": "TFLOP/s", "peak": FP64_PEAK_TFLOPS, "frac": tfl / FP64_PEAK_TFLOPS,
+                "flops_per_launch": fl}
+
     return {"columns": ncol, "levels": kmax, "tracers": 1, "forward_ms": f, "backward_ms": b,
             "columns_per_s": ncol / ((f + b) / 1e3),
             "forward_roofline": {"bound": "hbm", "algorithmic_bytes": fwd_bytes,
                                  "achieved": fwd_bytes / (f / 1e3) / 1e9, "unit": "GB/s", "peak": hbm,
-                                 "frac": fwd_bytes / (f / 1e3) / 1e9 / hbm},
+                                 "frac": fwd_bytes / (f / 1e3) / 1e9 / hbm, "limiter": "FP64 pipe, not HBM",
+                                 "fp64": fp64("forward", f)},
             "backward_roofline": {"bound": "hbm", "algorithmic_bytes": bwd_bytes,
                                   "achieved": bwd_bytes / (b / 1e3) / 1e9, "unit": "GB/s", "peak": hbm,
-                                  "frac": bwd_bytes / (b / 1e3) / 1e9 / hbm}}
+                                  "frac": bwd_bytes / (b / 1e3) / 1e9 / hbm, "limiter": "FP64 pipe, not HBM",
+                                  "fp64": fp64("backward", b)}}
 
 
 def main():

@@ -147,6 +147,9 @@ _SIGS = {
     "dccm_step_run_timed": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "dccm_step_run_host": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                           ctypes.c_void_p, ctypes.c_int]),
+    "dccm_step_host_release": (ctypes.c_int, [ctypes.c_void_p]),
+    "dccm_step_autotune_host": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                               ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
 }
 
 
@@ -211,6 +214,19 @@ def _stream(s):
     if hasattr(s, "cuda_stream"):
         return ctypes.c_void_p(s.cuda_stream)
     return ctypes.c_void_p(int(s))
+
+
+def tune_set(knob, value):
+    """dccm_tune_set: process-wide launch-shape knob (tc_ctas, fft_bb,
+    flux_threads, remap_threads, serial, upload_order, host_path); 0 = the
+    default."""
+    _check(load().dccm_tune_set(knob.encode(), int(value)), "dccm_tune_set")
+
+
+def tune_get(knob):
+    v = ctypes.c_int()
+    _check(load().dccm_tune_get(knob.encode(), ctypes.byref(v)), "dccm_tune_get")
+    return v.value
 
 
 # ------------------------------------------------------------- bulk flux
@@ -493,6 +509,30 @@ class Ensemble:
 
 
 # ----------------------------------------------------------- coupling step
+class HostCopies:
+    """The copy lists of Step.run_host as the C arrays it passes: (host
+    tensor or array, device tensor) pairs for the uploads and the
+    downloads.  The buffers are kept referenced; they must stay allocated
+    (and page-locked, if they were) while the lists are in use."""
+
+    def __init__(self, h2d, d2h):
+        self.pairs = (list(h2d), list(d2h))
+        self.h2d, self.nh2d = self._array(self.pairs[0])
+        self.d2h, self.nd2h = self._array(self.pairs[1])
+
+    @staticmethod
+    def _array(pairs):
+        arr = (HostCopy * max(1, len(pairs)))()
+        for k, (h, dv) in enumerate(pairs):
+            nb = h.numel() * h.element_size() if hasattr(h, "numel") else h.nbytes
+            arr[k] = HostCopy(_p(h).value, _p(dv).value, nb)
+        return arr, len(pairs)
+
+    def nbytes(self):
+        """(bytes uploaded, bytes downloaded) per call."""
+        return tuple(sum(c.bytes for c in arr[:n]) for arr, n in ((self.h2d, self.nh2d), (self.d2h, self.nd2h)))
+
+
 class Step:
     """One coupling step as a CUDA graph (dccm_step_create).  Buffers are
     device tensors that must outlive the step; flux is a dict of device
@@ -547,7 +587,9 @@ class Step:
         out = (ctypes.c_int * 4)()
         _check(load().dccm_step_autotune(self.h, cache_path.encode() if cache_path else None, out),
                "dccm_step_autotune")
-        return dict(zip(self.KNOBS, list(out)))
+        chosen = dict(zip(self.KNOBS, list(out)))
+        chosen["serial"] = tune_get("serial")
+        return chosen
 
     def run_timed(self, stream=None):
         """Device ms of the six stages (names in Step.STAGES), run back to back."""
@@ -555,16 +597,26 @@ class Step:
         _check(load().dccm_step_run_timed(self.h, _stream(stream), ms), "dccm_step_run_timed")
         return list(ms)
 
-    def run_host(self, h2d, d2h, stream=None):
-        """h2d / d2h: lists of (host tensor or array, device tensor) pairs."""
-        def copies(pairs):
-            arr = (HostCopy * max(1, len(pairs)))()
-            for k, (h, dv) in enumerate(pairs):
-                nb = h.numel() * h.element_size() if hasattr(h, "numel") else h.nbytes
-                arr[k] = HostCopy(_p(h).value, _p(dv).value, nb)
-            return arr
-        a, b = copies(h2d), copies(d2h)
-        _check(load().dccm_step_run_host(self.h, _stream(stream), a, len(h2d), b, len(d2h)), "dccm_step_run_host")
+    def run_host(self, h2d, d2h=None, stream=None):
+        """dccm_step_run_host.  h2d / d2h: lists of (host tensor or array,
+        device tensor) pairs, or h2d a HostCopies holding both lists (built
+        once, for a caller that passes the same buffers every step)."""
+        c = h2d if isinstance(h2d, HostCopies) else HostCopies(h2d, d2h or [])
+        _check(load().dccm_step_run_host(self.h, _stream(stream), c.h2d, c.nh2d, c.d2h, c.nd2h),
+               "dccm_step_run_host")
+
+    def autotune_host(self, h2d, d2h=None, stream=None):
+        """dccm_step_autotune_host: upload order and copy path for these
+        copy lists, by timing (the step runs 36 times)."""
+        c = h2d if isinstance(h2d, HostCopies) else HostCopies(h2d, d2h or [])
+        out = (ctypes.c_int * 2)()
+        _check(load().dccm_step_autotune_host(self.h, _stream(stream), c.h2d, c.nh2d, c.d2h, c.nd2h, out),
+               "dccm_step_autotune_host")
+        return {"upload_order": out[0], "host_path": out[1]}
+
+    def host_release(self):
+        """dccm_step_host_release: forget the recorded copy graph."""
+        _check(load().dccm_step_host_release(self.h), "dccm_step_host_release")
 
     def __del__(self):
         if getattr(self, "h", None) and _lib is not None:

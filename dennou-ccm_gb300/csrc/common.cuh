@@ -26,12 +26,28 @@ void set_cuda_error(cudaError_t e);
 // Check the launch status of the preceding kernel launch.
 #define DCCM_LAUNCH_CHECK() DCCM_CUDA(cudaGetLastError())
 
+// Launch-shape knobs read by the kernel launchers (0 = the launcher's own
+// default).  dccm_step_autotune chooses them per step by timing candidates;
+// dccm_tune_set / dccm_tune_get expose them.
+struct Tunables {
+  int tc_ctas = 0;        // persistent CTAs of the tensor-core Legendre kernel
+  int fft_bb = 0;         // warps per FFT CTA (4, 8, 16)
+  int flux_threads = 0;   // threads per CTA of the bulk-flux kernel
+  int remap_threads = 0;  // threads per CTA of the remap kernel
+  int serial = 0;         // 1: launch_pdl makes ordinary launches
+  int upload_order = 0;   // dccm_step_run_host: 1 transforms' inputs first, 2 surface inputs first
+  int host_path = 0;      // dccm_step_run_host: 1 (default) copy engines and staging, 2 kernels through the host mapping
+};
+Tunables &tunables();
+
 // Programmatic dependent launch between the kernels of the transform chain:
 // a kernel launched with launch_pdl may start while the previous kernel in
 // its stream is still running (its prologue overlaps that kernel's tail).
 // It must execute pdl_wait() before it reads anything the previous kernel
 // writes or writes anything the previous kernel reads; pdl_trigger() lets
-// the next kernel start.  Both are no-ops for an ordinary launch.
+// the next kernel start.  Both are no-ops for an ordinary launch (the
+// "serial" knob), which the step autotuner picks where early-resident CTAs
+// of the chain would keep a concurrent branch of the step off the SMs.
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
@@ -47,7 +63,7 @@ inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, s
   attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
-  cfg.numAttrs = 1;
+  cfg.numAttrs = tunables().serial ? 0 : 1;
   return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
 }
 
@@ -61,17 +77,6 @@ inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s
 
 // Number of SMs of the current device (cached per device).
 int sm_count();
-
-// Launch-shape knobs read by the kernel launchers (0 = the launcher's own
-// default).  dccm_step_autotune chooses them per step by timing candidates;
-// dccm_tune_set / dccm_tune_get expose them.
-struct Tunables {
-  int tc_ctas = 0;        // persistent CTAs of the tensor-core Legendre kernel
-  int fft_bb = 0;         // warps per FFT CTA (4, 8, 16)
-  int flux_threads = 0;   // threads per CTA of the bulk-flux kernel
-  int remap_threads = 0;  // threads per CTA of the remap kernel
-};
-Tunables &tunables();
 
 // Device buffer that grows on demand (never shrinks); used for the host
 // entry points' staging copies.

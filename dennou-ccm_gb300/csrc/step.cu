@@ -57,6 +57,12 @@ struct dccm_step {
   cudaGraph_t hgraph = nullptr;
   cudaGraphExec_t hexec = nullptr;
   std::vector<void *> host_tabs;  // device segment tables of that graph
+  bool sfc_first = false;         // that graph uploads the surface inputs first
+  // choices of dccm_step_autotune_host (0: the process-wide knobs)
+  int host_order = 0, host_path = 0;
+  // stage times of the last dccm_step_run_timed (ms), for the upload order
+  float stage_ms[6] = {};
+  bool have_stage_ms = false;
 };
 
 using namespace dccm;
@@ -227,7 +233,7 @@ __global__ void __launch_bounds__(256) seg_copy_kernel(const Seg *__restrict__ s
 struct SegTab {
   Seg *tab = nullptr;
   int nseg = 0;
-  unsigned long long maxb = 0;
+  unsigned long long maxb = 0, total = 0;
 };
 // Copies whose host buffers lie back to back (rows of one host allocation)
 // travel as one copy-engine transfer of the whole host range through a
@@ -259,11 +265,23 @@ static int upload_segs(dccm_step *st, const std::vector<Seg> &segs, SegTab &t) {
   st->host_tabs.push_back(t.tab);
   DCCM_CUDA(cudaMemcpy(t.tab, segs.data(), segs.size() * sizeof(Seg), cudaMemcpyHostToDevice));
   t.nseg = (int)segs.size();
-  for (const Seg &g : segs) t.maxb = g.bytes > t.maxb ? g.bytes : t.maxb;
+  for (const Seg &g : segs) {
+    t.maxb = g.bytes > t.maxb ? g.bytes : t.maxb;
+    t.total += g.bytes;
+  }
   return DCCM_OK;
 }
 
+// Path 2: every copy whose host buffer has a device mapping moves in the
+// set's one kernel (SMs read or write the host memory over the link);
+// path 1: staging and copy engines as described above.
+static int effective_path(const dccm_step *st) {
+  const int p = st->host_path ? st->host_path : tunables().host_path;
+  return p == 2 ? 2 : 1;
+}
+
 static int prepare_set(dccm_step *st, std::vector<dccm_host_copy> v, bool h2d, CopySet &cs) {
+  const bool mapped_all = effective_path(st) == 2;
   std::sort(v.begin(), v.end(), [](const dccm_host_copy &a, const dccm_host_copy &b) {
     return (uintptr_t)a.host < (uintptr_t)b.host;
   });
@@ -277,7 +295,7 @@ static int prepare_set(dccm_step *st, std::vector<dccm_host_copy> v, bool h2d, C
       total += v[e].bytes;
       ++e;
     }
-    if (e - k >= 2 && total > SMALL_COPY) {
+    if (!mapped_all && e - k >= 2 && total > SMALL_COPY) {
       Staged sg;
       sg.host = v[k].host;
       sg.bytes = total;
@@ -300,7 +318,8 @@ static int prepare_set(dccm_step *st, std::vector<dccm_host_copy> v, bool h2d, C
         const dccm_host_copy &c = v[i];
         cudaPointerAttributes a;
         void *hdev = nullptr;
-        if (c.bytes <= SMALL_COPY && cudaPointerGetAttributes(&a, c.host) == cudaSuccess) hdev = a.devicePointer;
+        if ((mapped_all || c.bytes <= SMALL_COPY) && cudaPointerGetAttributes(&a, c.host) == cudaSuccess)
+          hdev = a.devicePointer;
         cudaGetLastError();
         if (!hdev || c.bytes == 0) {
           cs.big.push_back(c);
@@ -328,6 +347,38 @@ static int prepare_sets(dccm_step *st, const HostPlan &hp, HostSets &hs) {
   return prepare_set(st, hp.post, false, hs.post);
 }
 
+// Bytes a copy set moves over the host link.
+static double link_bytes(const CopySet &c) {
+  double b = (double)c.mapped.total;
+  for (const dccm_host_copy &x : c.big) b += (double)x.bytes;
+  for (const Staged &g : c.staged) b += (double)g.bytes;
+  return b;
+}
+
+// Which branch's inputs go first on the host link.  Each branch ends when
+// its inputs are in (after those of the branch before it), its kernels have
+// run and its results are back; the order with the earlier end of the
+// later branch wins.  The link moves about 190 GB/s per direction on a
+// GB300 (Grace C2C, page-locked memory, one copy engine); kernel times are
+// those of the last timed run (dccm_step_run_timed, called by the
+// autotuner), or zero before any, which leaves the bytes to decide.
+static bool surface_first(const dccm_step *st, const HostSets &h) {
+  constexpr double BYTES_PER_US = 190e3;
+  const double in_t = link_bytes(h.sht_in) / BYTES_PER_US, in_f = link_bytes(h.sfc_in) / BYTES_PER_US;
+  const double out_t = (link_bytes(h.grid) + link_bytes(h.spec)) / BYTES_PER_US;
+  const double out_f = link_bytes(h.sfc_out) / BYTES_PER_US;
+  double run_t = 0, run_f = 0;
+  if (st->have_stage_ms) {
+    run_t = 1e3 * (st->stage_ms[0] + st->stage_ms[1] + st->stage_ms[2] + st->stage_ms[3]);
+    run_f = 1e3 * (st->stage_ms[4] + st->stage_ms[5]);
+  }
+  auto end = [](double in1, double run1, double out1, double in2, double run2, double out2) {
+    const double e1 = in1 + run1 + out1, e2 = in1 + in2 + run2 + out2;
+    return e1 > e2 ? e1 : e2;
+  };
+  return end(in_f, run_f, out_f, in_t, run_t, out_t) < end(in_t, run_t, out_t, in_f, run_f, out_f);
+}
+
 static int capture(dccm_step *st, const HostSets *hp, cudaGraph_t *out) {
   *out = nullptr;
   DCCM_CUDA(cudaStreamBeginCapture(st->s0, cudaStreamCaptureModeThreadLocal));
@@ -340,23 +391,27 @@ static int capture(dccm_step *st, const HostSets *hp, cudaGraph_t *out) {
       e = cudaGetLastError();
     }
   };
-  auto copies = [&](const CopySet &cs, bool h2d, cudaStream_t s) {
+  // ev (uploads only): recorded once the set's host-link transfers are
+  // done, before the device-side scatters.
+  auto copies = [&](const CopySet &cs, bool h2d, cudaStream_t s, cudaEvent_t ev = nullptr) {
     for (const dccm_host_copy &c : cs.big) {
       if (e != cudaSuccess) return;
       e = h2d ? cudaMemcpyAsync(c.dev, c.host, c.bytes, cudaMemcpyHostToDevice, s)
               : cudaMemcpyAsync(c.host, c.dev, c.bytes, cudaMemcpyDeviceToHost, s);
     }
-    for (const Staged &g : cs.staged) {
-      if (e != cudaSuccess) return;
-      if (h2d) {
-        e = cudaMemcpyAsync(g.stage, g.host, g.bytes, cudaMemcpyHostToDevice, s);
-        segs(g.segs, s);
-      } else {
+    if (h2d) {
+      for (const Staged &g : cs.staged)
+        if (e == cudaSuccess) e = cudaMemcpyAsync(g.stage, g.host, g.bytes, cudaMemcpyHostToDevice, s);
+      segs(cs.mapped, s);
+      if (ev && e == cudaSuccess) e = cudaEventRecord(ev, s);
+      for (const Staged &g : cs.staged) segs(g.segs, s);
+    } else {
+      for (const Staged &g : cs.staged) {
         segs(g.segs, s);
         if (e == cudaSuccess) e = cudaMemcpyAsync(g.host, g.stage, g.bytes, cudaMemcpyDeviceToHost, s);
       }
+      segs(cs.mapped, s);
     }
-    segs(cs.mapped, s);
   };
   auto step = [&](int (*f)(dccm_step *, cudaStream_t), cudaStream_t s) {
     if (rc == DCCM_OK && e == cudaSuccess) rc = f(st, s);
@@ -364,15 +419,22 @@ static int capture(dccm_step *st, const HostSets *hp, cudaGraph_t *out) {
   if (hp) copies(hp->pre, true, st->s0);
   if (e == cudaSuccess) e = cudaEventRecord(st->fork, st->s0);
   if (e == cudaSuccess) e = cudaStreamWaitEvent(st->s1, st->fork, 0);
-  // transforms on s0
-  if (hp) copies(hp->sht_in, true, st->s0);
-  // The transform chain is the longer branch: its upload goes first on the
-  // host link, the surface uploads follow it.
+  // Uploads: one branch's host-link transfers before the other's
+  // (surface_first), so that the first branch's kernels start early.
   auto any = [](const CopySet &c) { return !c.big.empty() || !c.staged.empty() || c.mapped.nseg > 0; };
-  if (hp && any(hp->sht_in) && any(hp->sfc_in)) {
-    if (e == cudaSuccess) e = cudaEventRecord(st->ev_in, st->s0);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(st->s1, st->ev_in, 0);
+  const bool order = hp && any(hp->sht_in) && any(hp->sfc_in);
+  const int forced = st->host_order ? st->host_order : tunables().upload_order;
+  const bool sfc1 = order && (forced ? forced == 2 : surface_first(st, *hp));
+  if (hp) st->sfc_first = sfc1;
+  if (sfc1) {
+    copies(hp->sfc_in, true, st->s1, st->ev_in);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(st->s0, st->ev_in, 0);
+    copies(hp->sht_in, true, st->s0);
+  } else if (hp) {
+    copies(hp->sht_in, true, st->s0, order ? st->ev_in : nullptr);
+    if (order && e == cudaSuccess) e = cudaStreamWaitEvent(st->s1, st->ev_in, 0);
   }
+  // transforms on s0
   step(stage_leg_inv, st->s0);
   step(stage_fft_inv, st->s0);
   const bool grid_copies = hp && any(hp->grid);
@@ -386,7 +448,7 @@ static int capture(dccm_step *st, const HostSets *hp, cudaGraph_t *out) {
   step(stage_leg_fwd, st->s0);
   if (hp) copies(hp->spec, false, st->s0);
   // surface branch on s1
-  if (hp) copies(hp->sfc_in, true, st->s1);
+  if (hp && !sfc1) copies(hp->sfc_in, true, st->s1);
   step(stage_remap, st->s1);
   step(stage_flux, st->s1);
   if (hp) copies(hp->sfc_out, false, st->s1);
@@ -522,6 +584,8 @@ extern "C" int dccm_step_run_timed(dccm_step *st, void *stream, float *ms) {
   }
   DCCM_CUDA(cudaEventSynchronize(st->ev[6]));
   for (int k = 0; k < 6; ++k) DCCM_CUDA(cudaEventElapsedTime(&ms[k], st->ev[k], st->ev[k + 1]));
+  for (int k = 0; k < 6; ++k) st->stage_ms[k] = ms[k];
+  st->have_stage_ms = true;
   return DCCM_OK;
 }
 
@@ -606,13 +670,24 @@ static void sort_copies(dccm_step *st, const dccm_host_copy *h2d, int nh2d, cons
   }
 }
 
-extern "C" int dccm_step_run_host(dccm_step *st, void *stream, const dccm_host_copy *h2d, int nh2d,
-                                  const dccm_host_copy *d2h, int nd2h) {
-  if (!st || (nh2d > 0 && !h2d) || (nd2h > 0 && !d2h) || nh2d < 0 || nd2h < 0) return DCCM_ERR_INVALID_ARG;
-  cudaStream_t s = as_stream(stream);
-  // Page-locked host buffers: the copies join the step's graph, each next to
-  // the stage that needs or produces its data.  Otherwise (pageable memory)
-  // copy in, replay, copy out.
+// Records the graph of dccm_step_run_host for these (page-locked) copy lists.
+static int build_host_graph(dccm_step *st, const dccm_host_copy *h2d, int nh2d, const dccm_host_copy *d2h,
+                            int nd2h) {
+  drop_host_graph(st);
+  HostPlan hp;
+  sort_copies(st, h2d, nh2d, d2h, nd2h, hp);
+  HostSets hs;
+  DCCM_TRY(prepare_sets(st, hp, hs));
+  cudaGraph_t g = nullptr;
+  DCCM_TRY(capture(st, &hs, &g));
+  st->hgraph = g;
+  DCCM_CUDA(cudaGraphInstantiate(&st->hexec, g, 0));
+  st->host_h2d.assign(h2d, h2d + nh2d);
+  st->host_d2h.assign(d2h, d2h + nd2h);
+  return DCCM_OK;
+}
+
+static bool page_locked(const dccm_host_copy *h2d, int nh2d, const dccm_host_copy *d2h, int nd2h) {
   bool locked = true;
   for (int k = 0; k < nh2d + nd2h && locked; ++k) {
     const dccm_host_copy &c = k < nh2d ? h2d[k] : d2h[k - nh2d];
@@ -620,7 +695,23 @@ extern "C" int dccm_step_run_host(dccm_step *st, void *stream, const dccm_host_c
     locked = cudaPointerGetAttributes(&a, c.host) == cudaSuccess && a.type == cudaMemoryTypeHost;
   }
   cudaGetLastError();  // clear a failed attribute query
-  if (!locked) {
+  return locked;
+}
+
+extern "C" int dccm_step_run_host(dccm_step *st, void *stream, const dccm_host_copy *h2d, int nh2d,
+                                  const dccm_host_copy *d2h, int nd2h) {
+  if (!st || (nh2d > 0 && !h2d) || (nd2h > 0 && !d2h) || nh2d < 0 || nd2h < 0) return DCCM_ERR_INVALID_ARG;
+  cudaStream_t s = as_stream(stream);
+  // The copy lists of the recorded host graph again: replay it.
+  if (st->hexec && same_copies(st->host_h2d, h2d, nh2d) && same_copies(st->host_d2h, d2h, nd2h)) {
+    DCCM_CUDA(cudaGraphLaunch(st->hexec, s));
+    DCCM_CUDA(cudaStreamSynchronize(s));
+    return DCCM_OK;
+  }
+  // Page-locked host buffers: the copies join the step's graph, each next to
+  // the stage that needs or produces its data.  Otherwise (pageable memory)
+  // copy in, replay, copy out.
+  if (!page_locked(h2d, nh2d, d2h, nd2h)) {
     for (int k = 0; k < nh2d; ++k)
       DCCM_CUDA(cudaMemcpyAsync(h2d[k].dev, h2d[k].host, h2d[k].bytes, cudaMemcpyHostToDevice, s));
     DCCM_CUDA(cudaGraphLaunch(st->exec, s));
@@ -629,30 +720,68 @@ extern "C" int dccm_step_run_host(dccm_step *st, void *stream, const dccm_host_c
     DCCM_CUDA(cudaStreamSynchronize(s));
     return DCCM_OK;
   }
-  if (!same_copies(st->host_h2d, h2d, nh2d) || !same_copies(st->host_d2h, d2h, nd2h) || !st->hexec) {
-    drop_host_graph(st);
-    HostPlan hp;
-    sort_copies(st, h2d, nh2d, d2h, nd2h, hp);
-    HostSets hs;
-    DCCM_TRY(prepare_sets(st, hp, hs));
-    cudaGraph_t g = nullptr;
-    DCCM_TRY(capture(st, &hs, &g));
-    st->hgraph = g;
-    DCCM_CUDA(cudaGraphInstantiate(&st->hexec, g, 0));
-    st->host_h2d.assign(h2d, h2d + nh2d);
-    st->host_d2h.assign(d2h, d2h + nd2h);
-  }
+  DCCM_TRY(build_host_graph(st, h2d, nh2d, d2h, nd2h));
   DCCM_CUDA(cudaGraphLaunch(st->hexec, s));
   DCCM_CUDA(cudaStreamSynchronize(s));
   return DCCM_OK;
 }
 
+extern "C" int dccm_step_autotune_host(dccm_step *st, void *stream, const dccm_host_copy *h2d, int nh2d,
+                                       const dccm_host_copy *d2h, int nd2h, int *chosen) {
+  if (!st || (nh2d > 0 && !h2d) || (nd2h > 0 && !d2h) || nh2d < 0 || nd2h < 0) return DCCM_ERR_INVALID_ARG;
+  if (chosen) chosen[0] = chosen[1] = 0;
+  if (!page_locked(h2d, nh2d, d2h, nd2h)) return DCCM_OK;  // pageable: nothing to choose
+  cudaStream_t s = as_stream(stream);
+  int best_o = 1, best_p = 1;
+  float best = 1e30f;
+  for (int o = 1; o <= 2; ++o)
+    for (int p = 1; p <= 2; ++p) {
+      st->host_order = o;
+      st->host_path = p;
+      DCCM_TRY(build_host_graph(st, h2d, nh2d, d2h, nd2h));
+      std::vector<float> v;
+      for (int r = 0; r < 9; ++r) {
+        DCCM_CUDA(cudaEventRecord(st->ev[0], s));
+        DCCM_CUDA(cudaGraphLaunch(st->hexec, s));
+        DCCM_CUDA(cudaEventRecord(st->ev[1], s));
+        DCCM_CUDA(cudaEventSynchronize(st->ev[1]));
+        float ms = 0.f;
+        DCCM_CUDA(cudaEventElapsedTime(&ms, st->ev[0], st->ev[1]));
+        if (r >= 2) v.push_back(ms);
+      }
+      std::sort(v.begin(), v.end());
+      if (v[v.size() / 2] < best) {
+        best = v[v.size() / 2];
+        best_o = o;
+        best_p = p;
+      }
+    }
+  st->host_order = best_o;
+  st->host_path = best_p;
+  DCCM_TRY(build_host_graph(st, h2d, nh2d, d2h, nd2h));
+  if (chosen) {
+    chosen[0] = best_o;
+    chosen[1] = best_p;
+  }
+  return DCCM_OK;
+}
+
+extern "C" int dccm_step_host_release(dccm_step *st) {
+  if (!st) return DCCM_ERR_INVALID_ARG;
+  DCCM_CUDA(cudaDeviceSynchronize());
+  drop_host_graph(st);
+  return DCCM_OK;
+}
+
 // ------------------------------------------------------------- autotuning
-// Launch-shape knobs (common.cuh, Tunables) chosen per step by timing the
-// stage each one affects, candidates one knob at a time, with the other
-// knobs at their current values; the winners are applied and the step's
-// graph is recorded again.  A cache file keeps the choice per step shape
-// and GPU, one JSON object per line.
+// Launch-shape knobs (common.cuh, Tunables) chosen per step in two passes,
+// one knob at a time with the others at their current values: first each
+// knob's candidates timed on the stage it affects, then the knobs whose
+// effect reaches across the step's two concurrent branches (the Legendre
+// CTA count, plain versus programmatic dependent launches) timed on replays
+// of the whole recorded graph.  The winners are applied and the graph is
+// recorded again.  A cache file keeps the choice per step shape and GPU,
+// one JSON object per line.
 #include <stdio.h>
 #include <string.h>
 
@@ -697,6 +826,7 @@ static bool cache_lookup(const char *path, const std::string &key, Tunables &t) 
     if ((p = strstr(line, "\"fft_bb\": "))) v.fft_bb = atoi(p + 10);
     if ((p = strstr(line, "\"flux_threads\": "))) v.flux_threads = atoi(p + 16);
     if ((p = strstr(line, "\"remap_threads\": "))) v.remap_threads = atoi(p + 17);
+    if ((p = strstr(line, "\"serial\": "))) v.serial = atoi(p + 10);
     t = v;
     found = true;
   }
@@ -704,15 +834,16 @@ static bool cache_lookup(const char *path, const std::string &key, Tunables &t) 
   return found;
 }
 
-static void cache_store(const char *path, const std::string &key, const Tunables &t, const float *ms) {
+static void cache_store(const char *path, const std::string &key, const Tunables &t, float step_ms,
+                        const float *ms) {
   if (!path) return;
   FILE *fp = fopen(path, "a");
   if (!fp) return;
   fprintf(fp,
           "{\"key\": \"%s\", \"tc_ctas\": %d, \"fft_bb\": %d, \"flux_threads\": %d, \"remap_threads\": %d, "
-          "\"stage_ms\": [%.4f, %.4f, %.4f, %.4f, %.4f, %.4f]}\n",
-          key.c_str(), t.tc_ctas, t.fft_bb, t.flux_threads, t.remap_threads, ms[0], ms[1], ms[2], ms[3], ms[4],
-          ms[5]);
+          "\"serial\": %d, \"step_ms\": %.4f, \"stage_ms\": [%.4f, %.4f, %.4f, %.4f, %.4f, %.4f]}\n",
+          key.c_str(), t.tc_ctas, t.fft_bb, t.flux_threads, t.remap_threads, t.serial, step_ms, ms[0], ms[1],
+          ms[2], ms[3], ms[4], ms[5]);
   fclose(fp);
 }
 
@@ -731,6 +862,59 @@ static int time_stages(dccm_step *st, cudaStream_t s, int k0, int k1, int reps, 
   return DCCM_OK;
 }
 
+// Drop the recorded graph and record it again with the current knobs.
+static int rerecord(dccm_step *st) {
+  if (st->exec) cudaGraphExecDestroy(st->exec);
+  if (st->graph) cudaGraphDestroy(st->graph);
+  st->exec = nullptr;
+  st->graph = nullptr;
+  return record(st);
+}
+
+// Median over reps of the device time per replay of the whole step graph
+// (recorded again with the current knobs), 16 back-to-back replays a rep.
+static int time_graph(dccm_step *st, cudaStream_t s, int reps, float *out) {
+  DCCM_TRY(rerecord(st));
+  for (int w = 0; w < 3; ++w) DCCM_CUDA(cudaGraphLaunch(st->exec, s));
+  std::vector<float> v;
+  for (int r = 0; r < reps; ++r) {
+    DCCM_CUDA(cudaEventRecord(st->ev[0], s));
+    for (int k = 0; k < 16; ++k) DCCM_CUDA(cudaGraphLaunch(st->exec, s));
+    DCCM_CUDA(cudaEventRecord(st->ev[1], s));
+    DCCM_CUDA(cudaEventSynchronize(st->ev[1]));
+    float ms = 0.f;
+    DCCM_CUDA(cudaEventElapsedTime(&ms, st->ev[0], st->ev[1]));
+    v.push_back(ms / 16.f);
+  }
+  std::sort(v.begin(), v.end());
+  *out = v[v.size() / 2];
+  return DCCM_OK;
+}
+
+struct Knob {
+  int *field;
+  std::vector<int> cand;
+  int k0, k1;  // stages timed; k0 < 0: the whole graph
+};
+
+// Try each candidate of kb, keep the fastest (ties keep the earlier one).
+static int tune_knob(dccm_step *st, cudaStream_t s, Knob &kb, float *best_t) {
+  int bestv = *kb.field;
+  float bt = 1e30f;
+  for (int c : kb.cand) {
+    *kb.field = c;
+    float t;
+    DCCM_TRY(kb.k0 < 0 ? time_graph(st, s, 7, &t) : time_stages(st, s, kb.k0, kb.k1, 7, &t));
+    if (t < bt) {
+      bt = t;
+      bestv = c;
+    }
+  }
+  *kb.field = bestv;
+  if (best_t) *best_t = bt;
+  return DCCM_OK;
+}
+
 extern "C" int dccm_step_autotune(dccm_step *st, const char *cache_path, int *chosen) {
   if (!st) return DCCM_ERR_INVALID_ARG;
   Tunables &T = tunables();
@@ -741,45 +925,46 @@ extern "C" int dccm_step_autotune(dccm_step *st, const char *cache_path, int *ch
   if (!cache_lookup(cache_path, key, best)) {
     cudaStream_t s = st->s0;
     const int sms = sm_count();
-    struct Knob {
-      int *field;
-      std::vector<int> cand;
-      int k0, k1;
-    } knobs[] = {
+    Knob stage_knobs[] = {
         {&T.tc_ctas, {sms, sms * 3 / 4, sms / 2, sms / 4}, 0, 4},
         {&T.fft_bb, {16, 8, 4}, 1, 3},
         {&T.flux_threads, {64, 128, 256}, 5, 6},
         {&T.remap_threads, {128, 256}, 4, 5},
     };
-    for (Knob &kb : knobs) {
-      int bestv = *kb.field;
-      float bt = 1e30f;
-      for (int c : kb.cand) {
-        *kb.field = c;
-        float t;
-        const int rc = time_stages(st, s, kb.k0, kb.k1, 7, &t);
-        if (rc != DCCM_OK) {
-          T = saved;
-          return rc;
-        }
-        if (t < bt) {
-          bt = t;
-          bestv = c;
-        }
+    for (Knob &kb : stage_knobs) {
+      const int rc = tune_knob(st, s, kb, nullptr);
+      if (rc != DCCM_OK) {
+        T = saved;
+        rerecord(st);
+        return rc;
       }
-      *kb.field = bestv;
+    }
+    // Whole-graph pass: the stage pass's Legendre CTA count first, so a
+    // tie keeps it.
+    const int tc0 = T.tc_ctas;
+    std::vector<int> tc_cand = {tc0};
+    for (int c : {sms, sms * 3 / 4, sms / 2, sms / 4})
+      if (c != tc0) tc_cand.push_back(c);
+    Knob graph_knobs[] = {
+        {&T.serial, {0, 1}, -1, -1},
+        {&T.tc_ctas, tc_cand, -1, -1},
+    };
+    float step_ms = 0.f;
+    for (Knob &kb : graph_knobs) {
+      const int rc = tune_knob(st, s, kb, &step_ms);
+      if (rc != DCCM_OK) {
+        T = saved;
+        rerecord(st);
+        return rc;
+      }
     }
     best = T;
     DCCM_TRY(dccm_step_run_timed(st, s, ms));
-    cache_store(cache_path, key, best, ms);
+    cache_store(cache_path, key, best, step_ms, ms);
   }
   T = best;
   // Record the graph again with the chosen launch shapes.
-  if (st->exec) cudaGraphExecDestroy(st->exec);
-  if (st->graph) cudaGraphDestroy(st->graph);
-  st->exec = nullptr;
-  st->graph = nullptr;
-  const int rc = record(st);
+  const int rc = rerecord(st);
   if (chosen) {
     chosen[0] = best.tc_ctas;
     chosen[1] = best.fft_bb;
@@ -796,6 +981,11 @@ extern "C" int dccm_tune_set(const char *knob, int value) {
   else if (!strcmp(knob, "fft_bb")) T.fft_bb = value;
   else if (!strcmp(knob, "flux_threads")) T.flux_threads = value;
   else if (!strcmp(knob, "remap_threads")) T.remap_threads = value;
+  else if (!strcmp(knob, "serial")) T.serial = value ? 1 : 0;
+  else if (!strcmp(knob, "upload_order") || !strcmp(knob, "host_path")) {
+    if (value > 2) return DCCM_ERR_INVALID_ARG;
+    (knob[0] == 'u' ? T.upload_order : T.host_path) = value;
+  }
   else return DCCM_ERR_INVALID_ARG;
   return DCCM_OK;
 }
@@ -807,6 +997,9 @@ extern "C" int dccm_tune_get(const char *knob, int *value) {
   else if (!strcmp(knob, "fft_bb")) *value = T.fft_bb;
   else if (!strcmp(knob, "flux_threads")) *value = T.flux_threads;
   else if (!strcmp(knob, "remap_threads")) *value = T.remap_threads;
+  else if (!strcmp(knob, "serial")) *value = T.serial;
+  else if (!strcmp(knob, "upload_order")) *value = T.upload_order;
+  else if (!strcmp(knob, "host_path")) *value = T.host_path;
   else return DCCM_ERR_INVALID_ARG;
   return DCCM_OK;
 }

@@ -420,20 +420,49 @@ int dccm_step_run_timed(dccm_step *step, void *stream, float *ms);
  * device staging buffer, gathered or scattered on the device; other copies
  * of at most 1 MiB go, per group, through one kernel that reads or writes
  * the host buffers through their device mapping; larger ones are
- * copy-engine transfers.  With pageable buffers: copies in, graph, copies
- * out. */
+ * copy-engine transfers.  The uploads of one branch go on the host link
+ * before the other's: the branch whose inputs, kernels (as last timed by
+ * dccm_step_run_timed or the autotuner) and results would end later goes
+ * first (knob "upload_order": 0 this choice, 1 the transforms' inputs
+ * first, 2 the surface inputs first; knob "host_path": 2 moves every copy
+ * through the host mapping instead; both apply when the graph is recorded,
+ * and dccm_step_autotune_host chooses them per step by timing).  With pageable buffers: copies in, graph, copies out.
+ * A call whose copy lists equal those the graph was recorded with replays
+ * it without examining the buffers again: page-locked host buffers must
+ * stay allocated and page-locked while the same lists are passed (call
+ * dccm_step_host_release after freeing or unpinning one of them). */
 int dccm_step_run_host(dccm_step *step, void *stream, const dccm_host_copy *h2d, int nh2d,
                        const dccm_host_copy *d2h, int nd2h);
+/* Drops the graph and the staging buffers dccm_step_run_host keeps for its
+ * copy lists (the next call records them again). */
+int dccm_step_host_release(dccm_step *step);
+/* Chooses, for these page-locked copy lists, the upload order (1: the
+ * transforms' inputs first, 2: the surface inputs first) and the copy path
+ * (1: copy engines, host-contiguous runs through a staging buffer; 2: every
+ * copy in one kernel per group through the host mapping) by replaying the
+ * step with each of the four combinations (9 times each on stream: the
+ * step's outputs are written as by dccm_step_run_host), keeps the fastest
+ * for this step and leaves its graph recorded.  chosen (2 ints, may be
+ * NULL) receives the order and the path; both 0 with pageable buffers,
+ * for which there is nothing to choose.  The process-wide knobs
+ * "upload_order" and "host_path" (dccm_tune_set) apply to steps that have
+ * not been tuned this way. */
+int dccm_step_autotune_host(dccm_step *step, void *stream, const dccm_host_copy *h2d, int nh2d,
+                            const dccm_host_copy *d2h, int nd2h, int *chosen);
 
 /* Autotuner: chooses the launch shapes of the step's kernels by timing
  * candidates of each knob on the stage it affects ("tc_ctas": persistent
  * CTAs of the tensor-core Legendre kernel, "fft_bb": warps per FFT CTA
- * (4, 8 or 16), "flux_threads", "remap_threads": CTA sizes), applies the winners
+ * (4, 8 or 16), "flux_threads", "remap_threads": CTA sizes), then "serial"
+ * (1: ordinary launches instead of programmatic dependent launches along
+ * the transform chain) and "tc_ctas" again on replays of the whole step
+ * graph, where the two branches run concurrently; applies the winners
  * and records the step's graph again.  With cache_path the choice is read
  * from / appended to that file (one JSON object per line, keyed by the
  * GPU name and SM count and the step's shapes).  chosen (4 ints, may be
- * NULL) receives tc_ctas, fft_bb, flux_threads, remap_threads.  The knobs
- * are process-wide defaults of later launches too. */
+ * NULL) receives tc_ctas, fft_bb, flux_threads, remap_threads (read
+ * "serial" with dccm_tune_get).  The knobs are process-wide defaults of
+ * later launches too. */
 int dccm_step_autotune(dccm_step *step, const char *cache_path, int *chosen);
 int dccm_tune_set(const char *knob, int value);
 int dccm_tune_get(const char *knob, int *value);

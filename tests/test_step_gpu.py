@@ -118,6 +118,35 @@ def test_host_copies_match_device_run(dccm, oracle, synth, cuda, pinned):
         step.run_host(h2d, d2h)
         for (h, _), ref in zip(d2h, want):
             assert torch.equal(h, ref)
+    # both upload orders and both copy paths, copy lists prepared once,
+    # then the per-step choice of the host autotuner
+    saved = {k: dccm.tune_get(k) for k in ("upload_order", "host_path")}
+    hc = dccm.HostCopies(h2d, d2h)
+    assert hc.nbytes()[0] == sum(h.numel() * 8 for h, _ in h2d)
+
+    def check(tag):
+        for _ in range(2):
+            for h, _ in d2h:
+                h.zero_()
+            step.run_host(hc)
+            for (h, _), ref in zip(d2h, want):
+                assert torch.equal(h, ref), tag
+    try:
+        for order in (1, 2, 0):
+            for path in (1, 2):
+                dccm.tune_set("upload_order", order)
+                dccm.tune_set("host_path", path)
+                step.host_release()
+                check((order, path))
+        choice = step.autotune_host(hc)
+        if pinned:
+            assert choice["upload_order"] in (1, 2) and choice["host_path"] in (1, 2)
+        else:
+            assert choice == {"upload_order": 0, "host_path": 0}
+        check(choice)
+    finally:
+        for k, v in saved.items():
+            dccm.tune_set(k, v)
 
 
 def test_remap_two_level_destination(dccm, oracle, synth, cuda):
@@ -139,3 +168,42 @@ def test_remap_two_level_destination(dccm, oracle, synth, cuda):
                 got = S["dflux"][name].cpu().numpy().T[1 + off * n1:1 + (off + 1) * n1, 1]
                 assert np.array_equal(got, ref[:, f]), (g.N, mi, name)
             off += 1
+
+
+def test_autotune_keeps_results_and_caches(dccm, oracle, synth, cuda, tmp_path):
+    """Every launch shape the autotuner can pick (Legendre CTA count, FFT
+    CTA size, flux and remap CTA sizes, plain or programmatic dependent
+    launches) computes each output element the same way, so the step's
+    outputs are bit-identical before and after tuning; the cache file
+    returns the same choice on a second call."""
+    torch = cuda
+    bench, w, inp, S = _small_step(dccm, synth, oracle, torch, 1)
+    step = S["steps"]["mixed"]
+    outs = [S["grid"][0], S["spec_out"][0]] + [S["dflux"][n] for n in dccm.FLUX_OUT]
+
+    def run():
+        for o in outs:
+            o.zero_()
+        step.run()
+        torch.cuda.synchronize()
+        return [o.cpu().clone() for o in outs]
+
+    saved = {k: dccm.tune_get(k) for k in dccm.Step.KNOBS + ["serial"]}
+    try:
+        want = run()
+        cache = str(tmp_path / "tune.jsonl")
+        first = step.autotune(cache)
+        assert set(first) == set(dccm.Step.KNOBS + ["serial"]) and first["serial"] in (0, 1)
+        assert all(torch.equal(a, b) for a, b in zip(run(), want))
+        line = open(cache).read()
+        assert '"serial": ' in line and '"step_ms": ' in line
+        assert step.autotune(cache) == first
+        for serial in (0, 1):  # a step recorded in either launch mode, same bits
+            dccm.tune_set("serial", serial)
+            S = bench.gpu_setup(w, inp, dccm, synth, torch, torch.device("cuda", 0))
+            step = S["steps"]["mixed"]
+            outs = [S["grid"][0], S["spec_out"][0]] + [S["dflux"][n] for n in dccm.FLUX_OUT]
+            assert all(torch.equal(a, b) for a, b in zip(run(), want)), serial
+    finally:
+        for k, v in saved.items():
+            dccm.tune_set(k, v)
