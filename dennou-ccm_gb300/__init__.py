@@ -148,8 +148,13 @@ _SIGS = {
     "dccm_step_run_host": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                           ctypes.c_void_p, ctypes.c_int]),
     "dccm_step_host_release": (ctypes.c_int, [ctypes.c_void_p]),
+    "dccm_fp64_peak": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "dccm_spec_apply": (ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                       ctypes.c_int]),
+    "dccm_spec_apply_dev": (ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                           ctypes.c_int, ctypes.c_void_p]),
     "dccm_step_autotune_host": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
-                                               ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
+                                               ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]),
 }
 
 
@@ -214,6 +219,13 @@ def _stream(s):
     if hasattr(s, "cuda_stream"):
         return ctypes.c_void_p(s.cuda_stream)
     return ctypes.c_void_p(int(s))
+
+
+def fp64_peak(stream=None):
+    """dccm_fp64_peak: measured FP64 FMA throughput of the device, TFLOP/s."""
+    v = ctypes.c_double()
+    _check(load().dccm_fp64_peak(_stream(stream), ctypes.byref(v)), "dccm_fp64_peak")
+    return v.value
 
 
 def tune_set(knob, value):
@@ -402,6 +414,36 @@ def area_integral_dev(f, area, stream=None):
     _check(load().dccm_area_integral_dev(_p(f), _p(area), f.numel(), ctypes.byref(out), _stream(stream)),
            "dccm_area_integral_dev")
     return out.value
+
+
+# ---------------------------------------------------- spectral operators
+SPEC_LAPLACIAN, SPEC_INV_LAPLACIAN, SPEC_HDIFF_TENDENCY, SPEC_HDIFF_IMPLICIT = 0, 1, 2, 3
+
+
+class SpecOp(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int), ("radius", ctypes.c_double), ("order", ctypes.c_int),
+                ("efold_time", ctypes.c_double), ("dt", ctypes.c_double), ("rotation_correction", ctypes.c_int)]
+
+
+def spec_op(kind, radius, order=8, efold_time=1.0, dt=0.0, rotation_correction=False):
+    """A dccm_spec_op: Laplacian, inverse Laplacian, hyperdiffusion tendency
+    or implicit step (HDOrder = order, e-folding time of wavenumber nmax)."""
+    return SpecOp(kind, radius, order, efold_time, dt, int(bool(rotation_correction)))
+
+
+def spec_apply(nmax, op, spec):
+    """dccm_spec_apply on host spectra complex128 [batch, ncoef]."""
+    spec = np.ascontiguousarray(spec, np.complex128)
+    out = np.empty_like(spec)
+    _check(load().dccm_spec_apply(int(nmax), ctypes.byref(op), _p(spec), _p(out), spec.shape[0]),
+           "dccm_spec_apply")
+    return out
+
+
+def spec_apply_dev(nmax, op, spec_in, spec_out, batch, stream=None):
+    """dccm_spec_apply_dev on device spectra (float64 views of complex)."""
+    _check(load().dccm_spec_apply_dev(int(nmax), ctypes.byref(op), _p(spec_in), _p(spec_out), int(batch),
+                                      _stream(stream)), "dccm_spec_apply_dev")
 
 
 # ------------------------------------------------------------------- SHT
@@ -607,12 +649,14 @@ class Step:
 
     def autotune_host(self, h2d, d2h=None, stream=None):
         """dccm_step_autotune_host: upload order and copy path for these
-        copy lists, by timing (the step runs 36 times)."""
+        copy lists, by timing (the step runs 84 times)."""
         c = h2d if isinstance(h2d, HostCopies) else HostCopies(h2d, d2h or [])
         out = (ctypes.c_int * 2)()
-        _check(load().dccm_step_autotune_host(self.h, _stream(stream), c.h2d, c.nh2d, c.d2h, c.nd2h, out),
+        ms = (ctypes.c_float * 4)()
+        _check(load().dccm_step_autotune_host(self.h, _stream(stream), c.h2d, c.nh2d, c.d2h, c.nd2h, out, ms),
                "dccm_step_autotune_host")
-        return {"upload_order": out[0], "host_path": out[1]}
+        return {"upload_order": out[0], "host_path": out[1],
+                "candidates_ms": {"%d,%d" % (1 + k // 2, 1 + k % 2): ms[k] for k in range(4)}}
 
     def host_release(self):
         """dccm_step_host_release: forget the recorded copy graph."""

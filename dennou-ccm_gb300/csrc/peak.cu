@@ -1,0 +1,63 @@
+// FP64 CUDA-core throughput probe: the denominator of the FP64-bound
+// kernels' roofline fractions (flux, remap, implicit coupling).  Every
+// thread runs 8 independent DFMA chains; the result is stored only under
+// a condition the values never meet, so no chain can be removed.
+#include "common.cuh"
+
+namespace dccm {
+namespace peak {
+
+constexpr int CHAINS = 8;
+
+__global__ void __launch_bounds__(256) dfma_kernel(int iters, double b, double c, double *sink) {
+  double a[CHAINS];
+#pragma unroll
+  for (int k = 0; k < CHAINS; ++k) a[k] = 1.0 + 1e-3 * (threadIdx.x + k);
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < CHAINS; ++k) a[k] = fma(a[k], b, c);
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < CHAINS; ++k) s += a[k];
+  if (s == -1.0) sink[blockIdx.x] = s;
+}
+
+}  // namespace peak
+}  // namespace dccm
+
+using namespace dccm;
+
+extern "C" int dccm_fp64_peak(void *stream, double *tflops) {
+  if (!tflops) return DCCM_ERR_INVALID_ARG;
+  cudaStream_t s = as_stream(stream);
+  const int blocks = sm_count() * 8, threads = 256, iters = 4096;
+  double *sink = nullptr;
+  DCCM_CUDA(cudaMalloc(&sink, blocks * sizeof(double)));
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  int rc = DCCM_OK;
+  for (int r = 0; r < 6 && rc == DCCM_OK; ++r) {
+    cudaEventRecord(e0, s);
+    peak::dfma_kernel<<<blocks, threads, 0, s>>>(iters, 0.999999, 1e-7, sink);
+    cudaEventRecord(e1, s);
+    const cudaError_t e = cudaEventSynchronize(e1);
+    if (e != cudaSuccess) {
+      set_cuda_error(e);
+      rc = DCCM_ERR_CUDA;
+      break;
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (r > 0 && ms < best) best = ms;  // the first run warms up
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(sink);
+  if (rc != DCCM_OK) return rc;
+  const double flops = 2.0 * peak::CHAINS * (double)iters * blocks * threads;
+  *tflops = flops / (best * 1e-3) / 1e12;
+  return DCCM_OK;
+}

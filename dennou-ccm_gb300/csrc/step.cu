@@ -727,42 +727,47 @@ extern "C" int dccm_step_run_host(dccm_step *st, void *stream, const dccm_host_c
 }
 
 extern "C" int dccm_step_autotune_host(dccm_step *st, void *stream, const dccm_host_copy *h2d, int nh2d,
-                                       const dccm_host_copy *d2h, int nd2h, int *chosen) {
+                                       const dccm_host_copy *d2h, int nd2h, int *chosen, float *ms) {
   if (!st || (nh2d > 0 && !h2d) || (nd2h > 0 && !d2h) || nh2d < 0 || nd2h < 0) return DCCM_ERR_INVALID_ARG;
   if (chosen) chosen[0] = chosen[1] = 0;
+  if (ms)
+    for (int k = 0; k < 4; ++k) ms[k] = 0.f;
   if (!page_locked(h2d, nh2d, d2h, nd2h)) return DCCM_OK;  // pageable: nothing to choose
   cudaStream_t s = as_stream(stream);
-  int best_o = 1, best_p = 1;
-  float best = 1e30f;
-  for (int o = 1; o <= 2; ++o)
-    for (int p = 1; p <= 2; ++p) {
-      st->host_order = o;
-      st->host_path = p;
+  // Three rounds over the four (order, path) candidates, each the median of
+  // 5 replays after 2; a candidate's time is its best round (rounds
+  // interleave the candidates, so a drift of the clocks hits all of them).
+  float best_t[4] = {1e30f, 1e30f, 1e30f, 1e30f};
+  for (int round = 0; round < 3; ++round)
+    for (int c = 0; c < 4; ++c) {
+      st->host_order = 1 + c / 2;
+      st->host_path = 1 + c % 2;
       DCCM_TRY(build_host_graph(st, h2d, nh2d, d2h, nd2h));
       std::vector<float> v;
-      for (int r = 0; r < 9; ++r) {
+      for (int r = 0; r < 7; ++r) {
         DCCM_CUDA(cudaEventRecord(st->ev[0], s));
         DCCM_CUDA(cudaGraphLaunch(st->hexec, s));
         DCCM_CUDA(cudaEventRecord(st->ev[1], s));
         DCCM_CUDA(cudaEventSynchronize(st->ev[1]));
-        float ms = 0.f;
-        DCCM_CUDA(cudaEventElapsedTime(&ms, st->ev[0], st->ev[1]));
-        if (r >= 2) v.push_back(ms);
+        float t = 0.f;
+        DCCM_CUDA(cudaEventElapsedTime(&t, st->ev[0], st->ev[1]));
+        if (r >= 2) v.push_back(t);
       }
       std::sort(v.begin(), v.end());
-      if (v[v.size() / 2] < best) {
-        best = v[v.size() / 2];
-        best_o = o;
-        best_p = p;
-      }
+      best_t[c] = std::min(best_t[c], v[v.size() / 2]);
     }
-  st->host_order = best_o;
-  st->host_path = best_p;
+  int bc = 0;
+  for (int c = 1; c < 4; ++c)
+    if (best_t[c] < best_t[bc]) bc = c;
+  st->host_order = 1 + bc / 2;
+  st->host_path = 1 + bc % 2;
   DCCM_TRY(build_host_graph(st, h2d, nh2d, d2h, nd2h));
   if (chosen) {
-    chosen[0] = best_o;
-    chosen[1] = best_p;
+    chosen[0] = st->host_order;
+    chosen[1] = st->host_path;
   }
+  if (ms)
+    for (int k = 0; k < 4; ++k) ms[k] = best_t[k];
   return DCCM_OK;
 }
 

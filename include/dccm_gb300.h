@@ -440,15 +440,17 @@ int dccm_step_host_release(dccm_step *step);
  * transforms' inputs first, 2: the surface inputs first) and the copy path
  * (1: copy engines, host-contiguous runs through a staging buffer; 2: every
  * copy in one kernel per group through the host mapping) by replaying the
- * step with each of the four combinations (9 times each on stream: the
- * step's outputs are written as by dccm_step_run_host), keeps the fastest
- * for this step and leaves its graph recorded.  chosen (2 ints, may be
- * NULL) receives the order and the path; both 0 with pageable buffers,
- * for which there is nothing to choose.  The process-wide knobs
+ * step with each of the four combinations (3 interleaved rounds of 7
+ * replays on stream: the step's outputs are written as by
+ * dccm_step_run_host), keeps the fastest for this step and leaves its
+ * graph recorded.  chosen (2 ints, may be NULL) receives the order and the
+ * path; both 0 with pageable buffers, for which there is nothing to
+ * choose.  ms (4 floats, may be NULL) receives each combination's device
+ * time per step, (order, path) = (1,1), (1,2), (2,1), (2,2).  The process-wide knobs
  * "upload_order" and "host_path" (dccm_tune_set) apply to steps that have
  * not been tuned this way. */
 int dccm_step_autotune_host(dccm_step *step, void *stream, const dccm_host_copy *h2d, int nh2d,
-                            const dccm_host_copy *d2h, int nd2h, int *chosen);
+                            const dccm_host_copy *d2h, int nd2h, int *chosen, float *ms);
 
 /* Autotuner: chooses the launch shapes of the step's kernels by timing
  * candidates of each knob on the stage it affects ("tc_ctas": persistent
@@ -466,6 +468,47 @@ int dccm_step_autotune_host(dccm_step *step, void *stream, const dccm_host_copy 
 int dccm_step_autotune(dccm_step *step, const char *cache_path, int *chosen);
 int dccm_tune_set(const char *knob, int value);
 int dccm_tune_get(const char *knob, int *value);
+
+/* ------------------------------------------------------------------
+ * Spectral-space operators around the transform (the reference applies
+ * them inside DynamicsHSplVAS83, atm/dcpam_main_mod.f90:2173-2180, from
+ * the external dcpam5 library; HDOrder and the e-folding time of the
+ * largest wavenumber: exp/APEI07Couple/common/dcpam/
+ * dcpam_APEI07Couple_T21L16.conf:205-227).  Built from the mathematics;
+ * every operator scales coefficient (m, n) of [batch][ncoef] complex
+ * spectra (the SHT layout) by a factor f_n of the total wavenumber:
+ *   DCCM_SPEC_LAPLACIAN        -n(n+1)/a^2
+ *   DCCM_SPEC_INV_LAPLACIAN    -a^2/(n(n+1)), 0 for n = 0
+ *   DCCM_SPEC_HDIFF_TENDENCY   -D_n
+ *   DCCM_SPEC_HDIFF_IMPLICIT   1/(1 + dt D_n)  (backward step over dt)
+ * with D_n = nu (K_n - c), K_n = (n(n+1)/a^2)^(order/2), c = K_1 when
+ * rotation_correction is set (rigid rotation is not damped) else 0,
+ * D_0 = 0 (the global mean is never diffused), and
+ * nu = 1/(efold_time (K_N - c)).  a = radius.  spec_in may equal spec_out.
+ * nmax < 2048 (DCCM_ERR_UNSUPPORTED above).
+ * ------------------------------------------------------------------ */
+#define DCCM_SPEC_LAPLACIAN 0
+#define DCCM_SPEC_INV_LAPLACIAN 1
+#define DCCM_SPEC_HDIFF_TENDENCY 2
+#define DCCM_SPEC_HDIFF_IMPLICIT 3
+typedef struct dccm_spec_op {
+  int kind;                /* DCCM_SPEC_* */
+  double radius;           /* planet radius a (m) */
+  int order;               /* hyperdiffusion order (even, 2..32), e.g. HDOrder = 8 */
+  double efold_time;       /* e-folding time of wavenumber nmax (s) */
+  double dt;               /* time step of the implicit form (s) */
+  int rotation_correction; /* 1: D_1 = 0 */
+} dccm_spec_op;
+/* Device arrays, stream-ordered. */
+int dccm_spec_apply_dev(int nmax, const dccm_spec_op *op, const double *spec_in, double *spec_out, int batch,
+                        void *stream);
+/* Host arrays (staged through the device), synchronises. */
+int dccm_spec_apply(int nmax, const dccm_spec_op *op, const double *spec_in, double *spec_out, int batch);
+
+/* Measures the device's FP64 FMA throughput (TFLOP/s, best of 5 launches
+ * of independent DFMA chains on every SM; synchronises): the denominator
+ * of the FP64-bound kernels' roofline fractions. */
+int dccm_fp64_peak(void *stream, double *tflops);
 
 #ifdef __cplusplus
 }

@@ -58,6 +58,8 @@ def lib():
         L.oracle_bilin_gen.restype = i32
         L.oracle_exchange_grid_lat.argtypes = [P, P, i32, P, P, i32, P, P]
         L.oracle_exchange_grid_lat.restype = i32
+        L.oracle_spec_apply.argtypes = [i32, i32, f64, i32, f64, f64, i32, i32, P, P]
+        L.oracle_spec_apply.restype = i32
         L.oracle_set_threads.argtypes = [i32]
         L.oracle_get_threads.restype = i32
         _lib = L
@@ -249,3 +251,18 @@ def exchange_grid_lat(latA, wA, latO, wO):
                                        _p(lat), _p(w))
     return lat[:m], w[:m]
 
+
+
+# --------------------------------------------------- spectral operators
+SPEC_LAPLACIAN, SPEC_INV_LAPLACIAN, SPEC_HDIFF_TENDENCY, SPEC_HDIFF_IMPLICIT = 0, 1, 2, 3
+
+
+def spec_apply(N, kind, spec, radius, order=8, efold_time=1.0, dt=0.0, rotation_correction=False):
+    """complex128 [batch, ncoef] -> the same scaled per total wavenumber."""
+    spec = np.ascontiguousarray(spec, np.complex128)
+    out = np.zeros_like(spec)
+    rc = lib().oracle_spec_apply(N, kind, radius, order, efold_time, dt, int(bool(rotation_correction)),
+                                 spec.shape[0], _p(spec), _p(out))
+    if rc != 0:
+        raise ValueError("oracle_spec_apply: invalid parameters")
+    return out

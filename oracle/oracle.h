@@ -131,6 +131,14 @@ int oracle_bilin_gen(const double *lonS, int nxs, const double *latS, int nys, c
 int oracle_exchange_grid_lat(const double *latA, const double *wA, int JMA, const double *latO,
                              const double *wO, int JMO, double *latX, double *wX);
 
+/* ------------------------------------------------ spectral-space operators */
+/* Per-wavenumber scalings of [batch][ncoef] complex spectra (m-major):
+ * kind 0 Laplacian, 1 inverse Laplacian, 2 hyperdiffusion tendency,
+ * 3 implicit hyperdiffusion step; formulas in oracle_spec.c.  Returns -1
+ * on invalid parameters.  in may equal out. */
+int oracle_spec_apply(int N, int kind, double radius, int order, double efold_time, double dt,
+                      int rotation_correction, int batch, const double *in, double *out);
+
 #ifdef __cplusplus
 }
 #endif

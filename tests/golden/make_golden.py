@@ -21,7 +21,10 @@ plain Python, kept deliberately different in structure from the C oracle:
   column;
 * bilinear table and exchange grid: the Fortran loops transcribed in
   Python (common/grid_mapping_util.f90:32-182,
-  tool/gmapgen/gmapgen_main.f90:336-405), Python's sort for the edges.
+  tool/gmapgen/gmapgen_main.f90:336-405), Python's sort for the edges;
+* spectral operators (Laplacian, inverse Laplacian, hyperdiffusion; the
+  reference's code is external, so from the mathematics): factors as
+  numpy powers of n(n+1) over a^order, the oracle multiplies per level.
 
 Run from the repository root:  python tests/golden/make_golden.py
 """
@@ -503,7 +506,37 @@ def make_implcpl():
                         **{"in_" + k: v for k, v in d.items()}, **{"out_" + k: v for k, v in o.items()})
 
 
+def spec_numpy(N, kind, spec, a, order, tau, dt, corr):
+    n = np.array([nn for m in range(N + 1) for nn in range(m, N + 1)], dtype=np.float64)
+    nn = n * (n + 1)
+    if kind == 0:
+        f = -nn / a ** 2
+    elif kind == 1:
+        f = np.where(n == 0, 0.0, -(a ** 2) / np.where(n == 0, 1.0, nn))
+    else:
+        p = order // 2
+        K = np.power(nn, p) / a ** (2 * p)
+        c = 2.0 ** p / a ** (2 * p) if corr else 0.0
+        nu = 1.0 / (tau * (np.power(N * (N + 1.0), p) / a ** (2 * p) - c))
+        D = np.where(n == 0, 0.0, nu * (K - c))
+        f = -D if kind == 2 else 1.0 / (1.0 + dt * D)
+    return spec * f[None, :]
+
+
+def make_spec():
+    N, a, order, tau, dt = 21, 6.371e6, 8, 3 * 3600.0, 1200.0
+    rng = np.random.Generator(np.random.PCG64(11))
+    nc = (N + 1) * (N + 2) // 2
+    spec = rng.standard_normal((3, nc)) + 1j * rng.standard_normal((3, nc))
+    out = {"N": N, "a": a, "order": order, "tau": tau, "dt": dt, "spec": spec}
+    for kind in range(4):
+        for corr in (0, 1):
+            out["out_%d_%d" % (kind, corr)] = spec_numpy(N, kind, spec, a, order, tau, dt, corr)
+    np.savez_compressed(os.path.join(OUT, "spec_ops_t21.npz"), **out)
+
+
 if __name__ == "__main__":
+    make_spec()
     make_flux()
     make_j99()
     make_sht()

@@ -139,10 +139,12 @@ def test_host_copies_match_device_run(dccm, oracle, synth, cuda, pinned):
                 step.host_release()
                 check((order, path))
         choice = step.autotune_host(hc)
+        ms = choice.pop("candidates_ms")
         if pinned:
             assert choice["upload_order"] in (1, 2) and choice["host_path"] in (1, 2)
+            assert min(ms.values()) == ms["%d,%d" % (choice["upload_order"], choice["host_path"])] > 0
         else:
-            assert choice == {"upload_order": 0, "host_path": 0}
+            assert choice == {"upload_order": 0, "host_path": 0} and set(ms.values()) == {0.0}
         check(choice)
     finally:
         for k, v in saved.items():
@@ -207,3 +209,11 @@ def test_autotune_keeps_results_and_caches(dccm, oracle, synth, cuda, tmp_path):
     finally:
         for k, v in saved.items():
             dccm.tune_set(k, v)
+
+
+def test_fp64_peak_probe(dccm, cuda):
+    """The measured FP64 FMA rate is that of the CUDA cores: well below the
+    FP32 rate, near the nominal 2 DFMA lanes per SM and clock."""
+    import bench
+    t = dccm.fp64_peak()
+    assert 0.25 * bench.FP64_NOMINAL_TFLOPS < t < 1.5 * bench.FP64_NOMINAL_TFLOPS, t
