@@ -530,6 +530,10 @@ def gpu_bench(args, w, inp, rank, world):
     hc = dccm.HostCopies(*host_copies(S, groups, dccm, torch))
     h2d_bytes, d2h_bytes = hc.nbytes()
     host_tuned = S["steps"]["mixed"].autotune_host(hc, stream=stream)
+    cand = host_tuned.pop("candidates_ms")
+    host_tuned.update({"ms": cand.get("%d,%d" % (host_tuned["upload_order"], host_tuned["host_path"])),
+                       "ms_copy_engines": [cand.get("1,1"), cand.get("2,1")],
+                       "ms_all_mapped": [cand.get("1,16"), cand.get("2,16")]})
     for _ in range(max(3, args.warmup)):
         S["steps"]["mixed"].run_host(hc, stream=stream)
     if world > 1:

@@ -649,14 +649,15 @@ class Step:
 
     def autotune_host(self, h2d, d2h=None, stream=None):
         """dccm_step_autotune_host: upload order and copy path for these
-        copy lists, by timing (the step runs 84 times)."""
+        copy lists, by timing (the step runs 384 times); host_path is
+        1 + the mask of copy groups moved through the host mapping."""
         c = h2d if isinstance(h2d, HostCopies) else HostCopies(h2d, d2h or [])
         out = (ctypes.c_int * 2)()
-        ms = (ctypes.c_float * 4)()
+        ms = (ctypes.c_float * 32)()
         _check(load().dccm_step_autotune_host(self.h, _stream(stream), c.h2d, c.nh2d, c.d2h, c.nd2h, out, ms),
                "dccm_step_autotune_host")
         return {"upload_order": out[0], "host_path": out[1],
-                "candidates_ms": {"%d,%d" % (1 + k // 2, 1 + k % 2): ms[k] for k in range(4)}}
+                "candidates_ms": {"%d,%d" % (1 + k // 16, 1 + k % 16): ms[k] for k in range(32)}}
 
     def host_release(self):
         """dccm_step_host_release: forget the recorded copy graph."""

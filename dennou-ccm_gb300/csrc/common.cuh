@@ -36,7 +36,7 @@ struct Tunables {
   int remap_threads = 0;  // threads per CTA of the remap kernel
   int serial = 0;         // 1: launch_pdl makes ordinary launches
   int upload_order = 0;   // dccm_step_run_host: 1 transforms' inputs first, 2 surface inputs first
-  int host_path = 0;      // dccm_step_run_host: 1 (default) copy engines and staging, 2 kernels through the host mapping
+  int host_path = 0;      // dccm_step_run_host: 1 + mask of the copy groups moved through the host mapping (0: 1)
 };
 Tunables &tunables();
 

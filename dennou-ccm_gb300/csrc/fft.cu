@@ -69,6 +69,44 @@ __device__ __forceinline__ float2 shfl_c(float2 v, int src) {
 }
 __device__ __forceinline__ int brev5(int l) { return (int)(__brev((unsigned)l) >> 27); }
 
+// e^{-2 pi i a / 24} (a multiple of 15 degrees) as literal constants: the
+// in-register DFT lengths (2, 3, 4, 6, 8, 12) all divide 24, so their
+// twiddles fold into the instructions instead of being loaded.  The values
+// are the correctly rounded cos / sin of those angles, the same floats as
+// the twiddle table built on the host.
+__device__ __forceinline__ float2 unit24(int a) {
+  constexpr float C15 = 0.96592582628906829f, S15 = 0.25881904510252076f;
+  constexpr float C30 = 0.86602540378443865f, C45 = 0.70710678118654752f;
+  float c, sn;  // cos and sin of 15 a degrees
+  switch (((a % 24) + 24) % 24) {
+    case 0: c = 1.f; sn = 0.f; break;
+    case 1: c = C15; sn = S15; break;
+    case 2: c = C30; sn = 0.5f; break;
+    case 3: c = C45; sn = C45; break;
+    case 4: c = 0.5f; sn = C30; break;
+    case 5: c = S15; sn = C15; break;
+    case 6: c = 0.f; sn = 1.f; break;
+    case 7: c = -S15; sn = C15; break;
+    case 8: c = -0.5f; sn = C30; break;
+    case 9: c = -C45; sn = C45; break;
+    case 10: c = -C30; sn = 0.5f; break;
+    case 11: c = -C15; sn = S15; break;
+    case 12: c = -1.f; sn = 0.f; break;
+    case 13: c = -C15; sn = -S15; break;
+    case 14: c = -C30; sn = -0.5f; break;
+    case 15: c = -C45; sn = -C45; break;
+    case 16: c = -0.5f; sn = -C30; break;
+    case 17: c = -S15; sn = -C15; break;
+    case 18: c = 0.f; sn = -1.f; break;
+    case 19: c = S15; sn = -C15; break;
+    case 20: c = 0.5f; sn = -C30; break;
+    case 21: c = C45; sn = -C45; break;
+    case 22: c = C30; sn = -0.5f; break;
+    default: c = C15; sn = -S15; break;
+  }
+  return make_float2(c, -sn);
+}
+
 // In-register DFT of length R: v[k] <- sum_r v[r] e^{sign 2 pi i r k / R}.
 // Even lengths split into two halves (decimation in time), 3 is direct.
 template <int R> struct RegDft {
@@ -92,7 +130,7 @@ template <int R> struct RegDft {
       v[1] = cadd(mm, q);
       v[2] = csub(mm, q);
     } else {
-      static_assert(R % 2 == 0, "length");
+      static_assert(R % 2 == 0 && 24 % R == 0, "length");
       constexpr int H = R / 2;
       float2 e[H], o[H];
 #pragma unroll
@@ -104,7 +142,9 @@ template <int R> struct RegDft {
       RegDft<H>::run(o, tw, I, sign);
 #pragma unroll
       for (int k = 0; k < H; ++k) {
-        const float2 t = k == 0 ? o[0] : cmul(o[k], twid(tw, k * (I / R), sign));
+        float2 w = unit24(k * (24 / R));
+        if (sign > 0) w.y = -w.y;
+        const float2 t = k == 0 ? o[0] : cmul(o[k], w);
         v[k] = cadd(e[k], t);
         v[k + H] = csub(e[k], t);
       }

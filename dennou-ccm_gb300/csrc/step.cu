@@ -272,16 +272,19 @@ static int upload_segs(dccm_step *st, const std::vector<Seg> &segs, SegTab &t) {
   return DCCM_OK;
 }
 
-// Path 2: every copy whose host buffer has a device mapping moves in the
-// set's one kernel (SMs read or write the host memory over the link);
-// path 1: staging and copy engines as described above.
-static int effective_path(const dccm_step *st) {
+// Copy path per group, host_path = 1 + mask: mask bit 0 the transforms'
+// uploads, bit 1 the surface uploads, bit 2 the transforms' downloads (grid,
+// spectra), bit 3 the surface downloads; a set bit moves every copy of the
+// group whose host buffer has a device mapping in the group's one kernel
+// (SMs read or write the host memory over the link), a clear bit uses
+// staging and copy engines as described above.
+constexpr int PATH_SHT_IN = 1, PATH_SFC_IN = 2, PATH_SHT_OUT = 4, PATH_SFC_OUT = 8;
+static int path_mask(const dccm_step *st) {
   const int p = st->host_path ? st->host_path : tunables().host_path;
-  return p == 2 ? 2 : 1;
+  return p >= 1 && p <= 16 ? p - 1 : 0;
 }
 
-static int prepare_set(dccm_step *st, std::vector<dccm_host_copy> v, bool h2d, CopySet &cs) {
-  const bool mapped_all = effective_path(st) == 2;
+static int prepare_set(dccm_step *st, std::vector<dccm_host_copy> v, bool h2d, CopySet &cs, bool mapped_all) {
   std::sort(v.begin(), v.end(), [](const dccm_host_copy &a, const dccm_host_copy &b) {
     return (uintptr_t)a.host < (uintptr_t)b.host;
   });
@@ -338,13 +341,14 @@ static int prepare_set(dccm_step *st, std::vector<dccm_host_copy> v, bool h2d, C
 }
 
 static int prepare_sets(dccm_step *st, const HostPlan &hp, HostSets &hs) {
-  DCCM_TRY(prepare_set(st, hp.pre, true, hs.pre));
-  DCCM_TRY(prepare_set(st, hp.sht_in, true, hs.sht_in));
-  DCCM_TRY(prepare_set(st, hp.sfc_in, true, hs.sfc_in));
-  DCCM_TRY(prepare_set(st, hp.grid, false, hs.grid));
-  DCCM_TRY(prepare_set(st, hp.spec, false, hs.spec));
-  DCCM_TRY(prepare_set(st, hp.sfc_out, false, hs.sfc_out));
-  return prepare_set(st, hp.post, false, hs.post);
+  const int m = path_mask(st);
+  DCCM_TRY(prepare_set(st, hp.pre, true, hs.pre, m & PATH_SHT_IN));
+  DCCM_TRY(prepare_set(st, hp.sht_in, true, hs.sht_in, m & PATH_SHT_IN));
+  DCCM_TRY(prepare_set(st, hp.sfc_in, true, hs.sfc_in, m & PATH_SFC_IN));
+  DCCM_TRY(prepare_set(st, hp.grid, false, hs.grid, m & PATH_SHT_OUT));
+  DCCM_TRY(prepare_set(st, hp.spec, false, hs.spec, m & PATH_SHT_OUT));
+  DCCM_TRY(prepare_set(st, hp.sfc_out, false, hs.sfc_out, m & PATH_SFC_OUT));
+  return prepare_set(st, hp.post, false, hs.post, m & PATH_SFC_OUT);
 }
 
 // Bytes a copy set moves over the host link.
@@ -728,23 +732,25 @@ extern "C" int dccm_step_run_host(dccm_step *st, void *stream, const dccm_host_c
 
 extern "C" int dccm_step_autotune_host(dccm_step *st, void *stream, const dccm_host_copy *h2d, int nh2d,
                                        const dccm_host_copy *d2h, int nd2h, int *chosen, float *ms) {
+  constexpr int NC = 32;  // (order 1..2) x (path mask 0..15)
   if (!st || (nh2d > 0 && !h2d) || (nd2h > 0 && !d2h) || nh2d < 0 || nd2h < 0) return DCCM_ERR_INVALID_ARG;
   if (chosen) chosen[0] = chosen[1] = 0;
   if (ms)
-    for (int k = 0; k < 4; ++k) ms[k] = 0.f;
+    for (int k = 0; k < NC; ++k) ms[k] = 0.f;
   if (!page_locked(h2d, nh2d, d2h, nd2h)) return DCCM_OK;  // pageable: nothing to choose
   cudaStream_t s = as_stream(stream);
-  // Three rounds over the four (order, path) candidates, each the median of
-  // 5 replays after 2; a candidate's time is its best round (rounds
-  // interleave the candidates, so a drift of the clocks hits all of them).
-  float best_t[4] = {1e30f, 1e30f, 1e30f, 1e30f};
-  for (int round = 0; round < 3; ++round)
-    for (int c = 0; c < 4; ++c) {
-      st->host_order = 1 + c / 2;
-      st->host_path = 1 + c % 2;
+  // Two rounds over the candidates, each the median of 4 replays after 2;
+  // a candidate's time is its better round (rounds interleave the
+  // candidates, so a drift of the clocks hits all of them).
+  float best_t[NC];
+  for (int c = 0; c < NC; ++c) best_t[c] = 1e30f;
+  for (int round = 0; round < 2; ++round)
+    for (int c = 0; c < NC; ++c) {
+      st->host_order = 1 + c / 16;
+      st->host_path = 1 + c % 16;
       DCCM_TRY(build_host_graph(st, h2d, nh2d, d2h, nd2h));
       std::vector<float> v;
-      for (int r = 0; r < 7; ++r) {
+      for (int r = 0; r < 6; ++r) {
         DCCM_CUDA(cudaEventRecord(st->ev[0], s));
         DCCM_CUDA(cudaGraphLaunch(st->hexec, s));
         DCCM_CUDA(cudaEventRecord(st->ev[1], s));
@@ -754,20 +760,20 @@ extern "C" int dccm_step_autotune_host(dccm_step *st, void *stream, const dccm_h
         if (r >= 2) v.push_back(t);
       }
       std::sort(v.begin(), v.end());
-      best_t[c] = std::min(best_t[c], v[v.size() / 2]);
+      best_t[c] = std::min(best_t[c], 0.5f * (v[1] + v[2]));
     }
   int bc = 0;
-  for (int c = 1; c < 4; ++c)
+  for (int c = 1; c < NC; ++c)
     if (best_t[c] < best_t[bc]) bc = c;
-  st->host_order = 1 + bc / 2;
-  st->host_path = 1 + bc % 2;
+  st->host_order = 1 + bc / 16;
+  st->host_path = 1 + bc % 16;
   DCCM_TRY(build_host_graph(st, h2d, nh2d, d2h, nd2h));
   if (chosen) {
     chosen[0] = st->host_order;
     chosen[1] = st->host_path;
   }
   if (ms)
-    for (int k = 0; k < 4; ++k) ms[k] = best_t[k];
+    for (int k = 0; k < NC; ++k) ms[k] = best_t[k];
   return DCCM_OK;
 }
 
@@ -987,9 +993,12 @@ extern "C" int dccm_tune_set(const char *knob, int value) {
   else if (!strcmp(knob, "flux_threads")) T.flux_threads = value;
   else if (!strcmp(knob, "remap_threads")) T.remap_threads = value;
   else if (!strcmp(knob, "serial")) T.serial = value ? 1 : 0;
-  else if (!strcmp(knob, "upload_order") || !strcmp(knob, "host_path")) {
+  else if (!strcmp(knob, "upload_order")) {
     if (value > 2) return DCCM_ERR_INVALID_ARG;
-    (knob[0] == 'u' ? T.upload_order : T.host_path) = value;
+    T.upload_order = value;
+  } else if (!strcmp(knob, "host_path")) {
+    if (value > 16) return DCCM_ERR_INVALID_ARG;
+    T.host_path = value;
   }
   else return DCCM_ERR_INVALID_ARG;
   return DCCM_OK;

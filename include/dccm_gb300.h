@@ -424,9 +424,10 @@ int dccm_step_run_timed(dccm_step *step, void *stream, float *ms);
  * before the other's: the branch whose inputs, kernels (as last timed by
  * dccm_step_run_timed or the autotuner) and results would end later goes
  * first (knob "upload_order": 0 this choice, 1 the transforms' inputs
- * first, 2 the surface inputs first; knob "host_path": 2 moves every copy
- * through the host mapping instead; both apply when the graph is recorded,
- * and dccm_step_autotune_host chooses them per step by timing).  With pageable buffers: copies in, graph, copies out.
+ * first, 2 the surface inputs first; knob "host_path": 1 + a mask of the
+ * copy groups moved through the host mapping instead, see
+ * dccm_step_autotune_host; both apply when the graph is recorded, and
+ * dccm_step_autotune_host chooses them per step by timing).  With pageable buffers: copies in, graph, copies out.
  * A call whose copy lists equal those the graph was recorded with replays
  * it without examining the buffers again: page-locked host buffers must
  * stay allocated and page-locked while the same lists are passed (call
@@ -438,15 +439,18 @@ int dccm_step_run_host(dccm_step *step, void *stream, const dccm_host_copy *h2d,
 int dccm_step_host_release(dccm_step *step);
 /* Chooses, for these page-locked copy lists, the upload order (1: the
  * transforms' inputs first, 2: the surface inputs first) and the copy path
- * (1: copy engines, host-contiguous runs through a staging buffer; 2: every
- * copy in one kernel per group through the host mapping) by replaying the
- * step with each of the four combinations (3 interleaved rounds of 7
+ * of each group of copies, host_path = 1 + mask with mask bit 0 the
+ * transforms' uploads, bit 1 the surface uploads, bit 2 the transforms'
+ * downloads (grid, spectra), bit 3 the surface downloads: a set bit moves
+ * the group in one kernel through the host mapping, a clear bit by copy
+ * engines with host-contiguous runs through a staging buffer.  It replays
+ * the step with each of the 32 combinations (2 interleaved rounds of 6
  * replays on stream: the step's outputs are written as by
  * dccm_step_run_host), keeps the fastest for this step and leaves its
- * graph recorded.  chosen (2 ints, may be NULL) receives the order and the
- * path; both 0 with pageable buffers, for which there is nothing to
- * choose.  ms (4 floats, may be NULL) receives each combination's device
- * time per step, (order, path) = (1,1), (1,2), (2,1), (2,2).  The process-wide knobs
+ * graph recorded.  chosen (2 ints, may be NULL) receives the order and
+ * host_path; both 0 with pageable buffers, for which there is nothing to
+ * choose.  ms (32 floats, may be NULL) receives each combination's device
+ * time per step at index 16 (order - 1) + mask.  The process-wide knobs
  * "upload_order" and "host_path" (dccm_tune_set) apply to steps that have
  * not been tuned this way. */
 int dccm_step_autotune_host(dccm_step *step, void *stream, const dccm_host_copy *h2d, int nh2d,

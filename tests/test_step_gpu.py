@@ -133,7 +133,7 @@ def test_host_copies_match_device_run(dccm, oracle, synth, cuda, pinned):
                 assert torch.equal(h, ref), tag
     try:
         for order in (1, 2, 0):
-            for path in (1, 2):
+            for path in (1, 16, 1 + 2, 1 + 4 + 8):
                 dccm.tune_set("upload_order", order)
                 dccm.tune_set("host_path", path)
                 step.host_release()
@@ -141,7 +141,7 @@ def test_host_copies_match_device_run(dccm, oracle, synth, cuda, pinned):
         choice = step.autotune_host(hc)
         ms = choice.pop("candidates_ms")
         if pinned:
-            assert choice["upload_order"] in (1, 2) and choice["host_path"] in (1, 2)
+            assert choice["upload_order"] in (1, 2) and 1 <= choice["host_path"] <= 16 and len(ms) == 32
             assert min(ms.values()) == ms["%d,%d" % (choice["upload_order"], choice["host_path"])] > 0
         else:
             assert choice == {"upload_order": 0, "host_path": 0} and set(ms.values()) == {0.0}
