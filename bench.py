@@ -436,6 +436,33 @@ def profile_run(args, w, inp):
                       "device_error": derr, "implcpl_columns": ncol, "implcpl_levels": kmax}))
 
 
+GAUSSIAN_GRIDS = {21: (64, 32), 42: (128, 64), 63: (192, 96), 85: (256, 128), 170: (512, 256), 341: (1024, 512)}
+
+
+def profile_sht(spec):
+    """Mixed-precision transforms only, for ncu on a small case: "N:B"
+    (truncation, field-levels) on the truncation's Gaussian grid; three
+    inverse + forward round trips on the device (each: the spectra pack,
+    Legendre synthesis, inverse FFT, forward FFT, Legendre analysis)."""
+    import torch
+    dccm = importlib.import_module("dennou-ccm_gb300")
+    synth = importlib.import_module("dennou-ccm_gb300.synth")
+    N, B = (int(x) for x in spec.split(":"))
+    I, J = GAUSSIAN_GRIDS[N]
+    plan = dccm.ShtPlan(N, I, J, dccm.SHT_MIXED, max_batch=B)
+    s = torch.from_numpy(synth.spectra(N, B, seed=1).view(np.float64).copy()).cuda()
+    g = torch.empty((B, J, I), dtype=torch.float64, device="cuda")
+    s2 = torch.empty_like(s)
+    for _ in range(3):
+        plan.inverse_dev(s, g, B)
+        plan.forward_dev(g, s2, B)
+    torch.cuda.synchronize()
+    err = float((s2 - s).norm() / s.norm())
+    st = plan.status()
+    print(json.dumps({"profile_sht": spec, "grid": [I, J], "round_trip": err, "status": list(st)}))
+    assert err < 1e-5 and st == (0, 0)
+
+
 def max_over_ranks(vals, world, dev):
     """Element-wise maximum of per-rank times over the process group (the
     job's time is its slowest replica); identity on one rank.  dev is where
@@ -649,7 +676,12 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-steps", type=int, default=0,
                     help="only replay the mixed step this many times (for ncu) and exit")
+    ap.add_argument("--profile-sht", default=None, metavar="N:B",
+                    help="only run 3 mixed SHT round trips of B field-levels at truncation N (for ncu) and exit")
     args = ap.parse_args()
+    if args.profile_sht:
+        profile_sht(args.profile_sht)
+        return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     w = WORKLOADS[args.workload]
