@@ -256,7 +256,7 @@ def gpu_setup(w, inp, dccm, synth, torch, dev):
         off += len(g.members)
     steps = {}
     keep = {}
-    for prec, key in ((dccm.SHT_MIXED, "mixed"), (dccm.SHT_FP64, "fp64")):
+    for prec, key in ((dccm.SHT_MIXED, "mixed"), (dccm.SHT_MIXED_FP16, "fp16"), (dccm.SHT_FP64, "fp64")):
         if len(groups) == 1:
             sp = dccm.ShtPlan(groups[0].N, groups[0].I, groups[0].J, prec, groups[0].nfl)
             steps[key] = dccm.Step(sht=sp, nfl=groups[0].nfl, spec_in=spec_in[0], grid=grid[0],
@@ -491,7 +491,7 @@ def gpu_bench(args, w, inp, rank, world):
     S = gpu_setup(w, inp, dccm, synth, torch, dev)
     # launch shapes from the autotuner (cached per GPU and step shape)
     cache = os.environ.get("DCCM_TUNE_CACHE", os.path.join(ROOT, "dennou-ccm_gb300", "tune_cache.jsonl"))
-    tuned = {k: S["steps"][k].autotune(cache) for k in ("fp64", "mixed")}
+    tuned = {k: S["steps"][k].autotune(cache) for k in ("fp64", "fp16", "mixed")}
     groups = inp["groups"]
     nfl = inp["nfl"]
     stream = torch.cuda.current_stream(dev)
@@ -520,25 +520,37 @@ def gpu_bench(args, w, inp, rank, world):
     ms_mixed = timed(S["steps"]["mixed"], args.steps, max(3, args.warmup))
     ck = clocks.stop(dev.index or 0)
     ms_fp64 = timed(S["steps"]["fp64"], args.steps, max(3, args.warmup))
-    t_mixed, t_fp64 = max_over_ranks([float(np.mean(ms_mixed)) / 1e3, float(np.mean(ms_fp64)) / 1e3], world, dev)
+    ms_fp16 = timed(S["steps"]["fp16"], args.steps, max(3, args.warmup))
+    t_mixed, t_fp64, t_fp16 = max_over_ranks([float(np.mean(ms_mixed)) / 1e3, float(np.mean(ms_fp64)) / 1e3,
+                                              float(np.mean(ms_fp16)) / 1e3], world, dev)
 
-    # accuracy of the mixed step against the FP64 step on the same inputs
+    # accuracy of the mixed steps against the FP64 step on the same inputs
     S["steps"]["fp64"].run(stream)
     torch.cuda.synchronize()
     ref_spec = [s.clone() for s in S["spec_out"]]
     ref_grid = [g.clone() for g in S["grid"]]
-    S["steps"]["mixed"].run(stream)
-    torch.cuda.synchronize()
 
     def rel(a, b):
         num = sum(float(torch.linalg.norm(x - y)) ** 2 for x, y in zip(a, b))
         den = sum(float(torch.linalg.norm(y)) ** 2 for y in b)
         return (num / den) ** 0.5
 
-    err = {"spec_vs_fp64": rel(S["spec_out"], ref_spec), "grid_vs_fp64": rel(S["grid"], ref_grid),
-           "round_trip": rel(S["spec_out"], S["spec_in"])}
-    st, derr = S["plans"]["mixed"].status()
-    assert st == 0 and derr == 0, ("device error", st, derr)
+    def max_field(a, b):  # the worst field-level's relative L2 error
+        return max(float((torch.linalg.norm((x - y).reshape(x.shape[0], -1), dim=1) /
+                          torch.linalg.norm(y.reshape(y.shape[0], -1), dim=1)).max()) for x, y in zip(a, b))
+
+    def accuracy(key):
+        S["steps"][key].run(stream)
+        torch.cuda.synchronize()
+        st, derr = S["plans"][key].status()
+        assert st == 0 and derr == 0, ("device error", key, st, derr)
+        return {"spec_vs_fp64": rel(S["spec_out"], ref_spec), "grid_vs_fp64": rel(S["grid"], ref_grid),
+                "round_trip": rel(S["spec_out"], S["spec_in"]),
+                "max_field_spec_vs_fp64": max_field(S["spec_out"], ref_spec),
+                "max_field_grid_vs_fp64": max_field(S["grid"], ref_grid)}
+
+    err_fp16 = accuracy("fp16")
+    err = accuracy("mixed")  # last, so the mixed step's outputs are the ones left in place
 
     # per-kernel device times (stages launched back to back with events)
     stage_ms = np.zeros(6)
@@ -576,7 +588,7 @@ def gpu_bench(args, w, inp, rank, world):
     launches = 5 + len(groups) + 1  # pack + 2 Legendre + 2 FFT + one remap per group + flux
     ic = implcpl_leg(args, groups, dccm, synth, torch, dev, stream, flush, fp64_peak)
     so = spec_ops_leg(args, groups, S, dccm, torch, stream, flush)
-    return dict(t_mixed=t_mixed, t_fp64=t_fp64, t_e2e=t_e2e, clocks=ck, roof=roof, err=err, h2d=h2d_bytes,
+    return dict(t_mixed=t_mixed, t_fp64=t_fp64, t_fp16=t_fp16, err_fp16=err_fp16, t_e2e=t_e2e, clocks=ck, roof=roof, err=err, h2d=h2d_bytes,
                 d2h=d2h_bytes, nfl=nfl, launches=launches, tables=S["tables"], tuned=dict(tuned, host=host_tuned),
                 implcpl=ic, spec_ops=so)
 
@@ -746,6 +758,10 @@ def main():
         "data": "synthetic (seeded PCG64; n^-3 spectra, SST-based surface state)", "config": config,
         "fp64_gpu": {"value": job_throughput(world, nfl, r["t_fp64"]), "ms_per_step": r["t_fp64"] * 1e3,
                      "mixed_over_fp64": r["t_fp64"] / r["t_mixed"]},
+        "fp16_variant": {"value": job_throughput(world, nfl, r["t_fp16"]), "ms_per_step": r["t_fp16"] * 1e3,
+                         "over_fp64": r["t_fp64"] / r["t_fp16"],
+                         "legendre": "FP16 hi + lo, per-m and per-field-level power-of-two scales",
+                         "accuracy": r["err_fp16"]},
         "accuracy": r["err"],
         "e2e": {"value": job_throughput(world, nfl, r["t_e2e"]), "unit": "field-levels/s", "h2d_bytes_per_step": r["h2d"],
                 "d2h_bytes_per_step": r["d2h"], "ms_per_step": r["t_e2e"] * 1e3},

@@ -40,7 +40,7 @@ FLUX_SLOTS.update({"DelVarImplCPL": 4, "ImplCplCoef1": 4, "ImplCplCoef2": 4,
                    "SfcTemp": 3, "SfcAlbedo": 3})
 
 J99_REF, J99_CONSERVE = 0, 1
-SHT_FP64, SHT_MIXED = 0, 1
+SHT_FP64, SHT_MIXED, SHT_MIXED_FP16 = 0, 1, 2
 
 
 class DccmError(RuntimeError):

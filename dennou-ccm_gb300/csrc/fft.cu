@@ -235,6 +235,8 @@ struct FftGroup {
   const void *in;
   void *out;
   const float2 *tw, *twl;
+  int nsplit;        // forward output planes: 3 BF16, or 2 FP16 scaled by 2^(13 - cexp[b])
+  const int *cexp;   // FP16: exponent of each field-level's largest |grid value|
 };
 struct FftLaunch {
   FftGroup g[FFT_MAXG];
@@ -330,12 +332,20 @@ __device__ __forceinline__ void write_g3(const FftGroup &G, int jj, int b0, int 
     const int p = (t >> lcw) & 1;
     const int m = t >> (lcw + 1);
     if (c < 2 * nb) {
-      unsigned short h, md, lo;
-      split3f_bits(st[((p << lcw) + c) * PS + slot_of<R>(m)], h, md, lo);
+      const float v = st[((p << lcw) + c) * PS + slot_of<R>(m)];
       unsigned short *o = G3 + ((size_t)(2 * m + p) * Jh + jj) * G.C2Bp + 2 * b0 + c;
-      o[0] = h;
-      o[plane] = md;
-      o[2 * plane] = lo;
+      if (G.nsplit == 2) {
+        unsigned short h, lo;
+        split2h_bits(v * pow2f(13 - G.cexp[b0 + (c >> 1)]), h, lo);
+        o[0] = h;
+        o[plane] = lo;
+      } else {
+        unsigned short h, md, lo;
+        split3f_bits(v, h, md, lo);
+        o[0] = h;
+        o[plane] = md;
+        o[2 * plane] = lo;
+      }
     }
   }
 }
@@ -630,6 +640,10 @@ int fft_multi(Plan *const *plans, const int *batch, const void *const *in, void 
     G.out = out[g];
     G.tw = P.d_tw32;
     G.twl = P.d_twl32;
+    G.nsplit = P.nsplit;
+    G.cexp = P.d_cexp ? P.d_cexp + P.max_batch : nullptr;
+    if (fwd && P.nsplit == 2)
+      DCCM_TRY(field_exponents(static_cast<const double *>(in[g]), (long long)P.J * P.I, batch[g], P.d_cexp + P.max_batch, s));
     nblk += P.Jh * ((batch[g] + BB - 1) / BB);
     const size_t sm = fft_smem(G.R, BB);
     smem = sm > smem ? sm : smem;

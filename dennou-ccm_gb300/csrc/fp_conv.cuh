@@ -10,6 +10,7 @@
 // and NaNs take the hardware instruction.
 #pragma once
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 namespace dccm {
@@ -57,6 +58,40 @@ __device__ __forceinline__ void split3f_bits(float x, unsigned short &h, unsigne
   h = __bfloat16_as_ushort(bh);
   m = __bfloat16_as_ushort(bm);
   l = __bfloat16_as_ushort(bl);
+}
+
+// Split of an FP32 value into two FP16 numbers x ~ hi + lo (22 significant
+// bits; the caller scales x by a power of two into FP16's range first),
+// returned as raw bits.  The residual x - hi is exact in FP32.
+__device__ __forceinline__ void split2h_bits(float x, unsigned short &h, unsigned short &l) {
+  const __half hh = __float2half_rn(x);
+  const __half hl = __float2half_rn(x - __half2float(hh));
+  h = __half_as_ushort(hh);
+  l = __half_as_ushort(hl);
+}
+
+// 2^k as an FP32 number, for exponents of normal numbers (-126 <= k <= 127;
+// clamped outside).
+__device__ __forceinline__ float pow2f(int k) {
+  k = k < -126 ? -126 : (k > 127 ? 127 : k);
+  return __int_as_float((k + 127) << 23);
+}
+
+// x * 2^s for a normal double whose result stays normal, by exponent
+// arithmetic on the integer pipes (exact); zero and subnormal x give 0.
+__device__ __forceinline__ double scale_pow2(double x, int s) {
+  const long long b = __double_as_longlong(x);
+  const int e = (int)((b >> 52) & 0x7ff);
+  if (e == 0) return 0.0;
+  int ne = e + s;
+  ne = ne < 1 ? 1 : (ne > 2046 ? 2046 : ne);
+  return __longlong_as_double((b & ~(0x7ffLL << 52)) | ((long long)ne << 52));
+}
+
+// Unbiased binary exponent of the largest |x| contributing to a power-of-two
+// scale: floor(log2|x|) for normal doubles, -1023 for zero and subnormals.
+__device__ __forceinline__ int f64_exponent(double x) {
+  return (int)((__double_as_longlong(x) >> 52) & 0x7ff) - 1023;
 }
 
 }  // namespace dccm

@@ -51,6 +51,7 @@ struct MInfo {
   int kv0, kv1;    // valid K per parity
   int nv0, nv1;    // valid N per parity
   int x0, x1;      // A operand coordinate of (m, p): Apack column / G3 row
+  int eb;          // FP16 tables: the tiles of m hold the values times 2^eb
 };
 
 struct TcArgs {
@@ -64,6 +65,8 @@ struct TcArgs {
   float *F;
   double *spec_out;
   int *err;
+  int nsplit;         // operand splits: 3 (BF16 x 3) or 2 (FP16 hi + lo)
+  const int *cexp;    // FP16: per field-level exponent of the A operand's scale
 };
 
 // ------------------------------------------------------------ PTX helpers
@@ -119,10 +122,12 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo) {
   d |= (uint64_t)2 << 61;                      // SWIZZLE_128B
   return d;
 }
-// kind::f16 instruction descriptor: BF16 x BF16 -> F32, M = 128, B K-major,
-// A K-major (a_mn = 0) or MN-major (a_mn = 1, bit 15).
-__device__ __forceinline__ uint32_t idesc_bf16(int n, int a_mn) {
-  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)a_mn << 15) | ((uint32_t)(n >> 3) << 17) |
+// kind::f16 instruction descriptor: BF16 x BF16 (bf16 = 1) or FP16 x FP16
+// (bf16 = 0; A and B always of one type) -> F32, M = 128, B K-major, A
+// K-major (a_mn = 0) or MN-major (a_mn = 1, bit 15).
+__device__ __forceinline__ uint32_t idesc_f16kind(int n, int a_mn, int bf16) {
+  const uint32_t t = bf16 ? 1u : 0u;
+  return (1u << 4) | (t << 7) | (t << 10) | ((uint32_t)a_mn << 15) | ((uint32_t)(n >> 3) << 17) |
          ((uint32_t)(128 >> 4) << 24);
 }
 __device__ __forceinline__ void mma_bf16(uint32_t dtmem, uint64_t da, uint64_t db, uint32_t idesc, int acc) {
@@ -239,8 +244,8 @@ legendre_tc_kernel(const __grid_constant__ TcLaunch L) {
             if (!mbar_wait(&empty[s], ((g / NSTAGE) & 1) ^ 1, a.err, abort_flag, 1)) { ok = false; break; }
             unsigned char *As = stage + s * STAGE_BYTES;
             unsigned char *Bs = As + 3 * A_SPLIT_BYTES;
-            mbar_arrive_tx(&full[s], (uint32_t)STAGE_BYTES);
-            for (int sp = 0; sp < 3; ++sp) {
+            mbar_arrive_tx(&full[s], (uint32_t)(a.nsplit * (A_SPLIT_BYTES + B_SPLIT_BYTES)));
+            for (int sp = 0; sp < a.nsplit; ++sp) {
               unsigned char *Ad = As + sp * A_SPLIT_BYTES;
               if (a.dir == 0) {
                 tma_load_3d(Ad, &L.amap[gi], x0 + 64 * q, ct * 128, sp, &full[s]);
@@ -248,7 +253,7 @@ legendre_tc_kernel(const __grid_constant__ TcLaunch L) {
                 tma_load_3d(Ad, &L.amap[gi], ct * 128, x0 + 64 * q, sp, &full[s]);
                 tma_load_3d(Ad + 8192, &L.amap[gi], ct * 128 + 64, x0 + 64 * q, sp, &full[s]);
               }
-              const long long row0 = mi.base + ((long long)(p * mi.nq + q) * 3 + sp) * mi.nr + nt * 128;
+              const long long row0 = mi.base + ((long long)(p * mi.nq + q) * a.nsplit + sp) * mi.nr + nt * 128;
               tma_load_2d(Bs + sp * B_SPLIT_BYTES, &L.map[gi], 0, (int)row0, &full[s]);
             }
           }
@@ -269,7 +274,8 @@ legendre_tc_kernel(const __grid_constant__ TcLaunch L) {
         const MInfo mi = a.mi[m];
         const int nrow = min(128, mi.nr - nt * 128);
         const int amn = a.dir;  // forward A is MN-major
-        const uint32_t idesc = idesc_bf16(nrow, amn);
+        const uint32_t idesc = idesc_f16kind(nrow, amn, a.nsplit == 3);
+        const int ncross = a.nsplit == 3 ? 5 : 2;
         const int ab = a.nacc == 2 ? (li & 1) : 0;
         const int ar = a.nacc == 2 ? (li >> 1) : li;  // use count of this accumulator set
         if (!mbar_wait(&acce[ab], (ar & 1) ^ 1, a.err, abort_flag, 2)) { ok = false; break; }
@@ -294,14 +300,17 @@ legendre_tc_kernel(const __grid_constant__ TcLaunch L) {
               const uint32_t kb = ks * 32;
               mma_bf16(dmain, smem_desc(As + ka, lbo), smem_desc(Bs + kb, 16), idesc, accm);
               accm = 1;
-              // (A split, B split): hi*mid, mid*hi, hi*lo, lo*hi, mid*mid
+              // (A split, B split): BF16 x 3 hi*mid, mid*hi, hi*lo, lo*hi,
+              // mid*mid; FP16 hi + lo: hi*lo, lo*hi
               const int pa[5] = {0, 1, 0, 2, 1};
               const int pb[5] = {1, 0, 2, 0, 1};
 #pragma unroll
               for (int u = 0; u < 5; ++u) {
-                mma_bf16(dcross, smem_desc(As + pa[u] * A_SPLIT_BYTES + ka, lbo),
-                         smem_desc(Bs + pb[u] * B_SPLIT_BYTES + kb, 16), idesc, accx);
-                accx = 1;
+                if (u < ncross) {
+                  mma_bf16(dcross, smem_desc(As + pa[u] * A_SPLIT_BYTES + ka, lbo),
+                           smem_desc(Bs + pb[u] * B_SPLIT_BYTES + kb, 16), idesc, accx);
+                  accx = 1;
+                }
               }
             }
             mma_commit(&empty[s]);
@@ -331,6 +340,10 @@ legendre_tc_kernel(const __grid_constant__ TcLaunch L) {
       const int c = ct * 128 + row;
       const int NT = a.ntmax;
       const uint32_t tbase = tmem + ((uint32_t)(quad * 32) << 16) + ab * 4 * NT;
+      // FP16 operands were scaled by 2^(14 - cexp) (spectra) or 2^(13 - cexp)
+      // (Fourier coefficients) and 2^eb (tables): undo both (exact)
+      float us = 1.f;
+      if (a.nsplit == 2 && c < C2B) us = pow2f((a.dir ? 13 : 14) * -1 + a.cexp[c >> 1] - mi.eb);
       if (a.dir == 0) {
         const int J = 2 * a.Jh;
         const bool odd = mi.kv1 > 0;
@@ -354,8 +367,8 @@ legendre_tc_kernel(const __grid_constant__ TcLaunch L) {
             for (int i = 0; i < 16; ++i) {
               const int jj = nt * 128 + j0 + i;
               if (jj < a.Jh) {
-                a.F[((long long)m * J + (a.Jh + jj)) * C2B + c] = e[i] + o[i];
-                a.F[((long long)m * J + (a.Jh - 1 - jj)) * C2B + c] = e[i] - o[i];
+                a.F[((long long)m * J + (a.Jh + jj)) * C2B + c] = (e[i] + o[i]) * us;
+                a.F[((long long)m * J + (a.Jh - 1 - jj)) * C2B + c] = (e[i] - o[i]) * us;
               }
             }
           }
@@ -374,7 +387,7 @@ legendre_tc_kernel(const __grid_constant__ TcLaunch L) {
                 const int k = nt * 128 + k0 + i;
                 if (k < nv) {
                   const int n = m + p + 2 * k;
-                  const double v = (m == 0 && (c & 1)) ? 0.0 : f32_to_f64(d[i] + x[i]);
+                  const double v = (m == 0 && (c & 1)) ? 0.0 : f32_to_f64((d[i] + x[i]) * us);
                   a.spec_out[((long long)(c >> 1) * a.ncoef + idx_mn(a.N, m, n)) * 2 + (c & 1)] = v;
                 }
               }
@@ -405,6 +418,8 @@ struct PackGroup {
   unsigned short *A;
   long long ncoef, KX;
   int C2Bp, f0;
+  int nsplit;        // 3: BF16 x 3; 2: FP16 hi + lo scaled by 2^(14 - cexp[b])
+  const int *cexp;   // FP16: exponent of the field-level's largest |coefficient|
 };
 struct PackLaunch {
   PackGroup g[MAXG];
@@ -421,6 +436,23 @@ __global__ void __launch_bounds__(256) pack_spectra_kernel(const __grid_constant
   const size_t plane = (size_t)G.C2Bp * G.KX;
   const double2 *src = G.spec + (size_t)b * G.ncoef;
   unsigned short *dst = G.A + (size_t)(2 * b) * G.KX;
+  if (G.nsplit == 2) {
+    const int sc = 14 - G.cexp[b];
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < G.ncoef;
+         i += (long long)gridDim.x * blockDim.x) {
+      const double2 v = __ldg(src + i);
+      const int x = __ldg(G.xpos + i);
+      unsigned short h0, l0, h1, l1;
+      split2h_bits(f64_to_f32_rn(scale_pow2(v.x, sc)), h0, l0);
+      split2h_bits(f64_to_f32_rn(scale_pow2(v.y, sc)), h1, l1);
+      unsigned short *o = dst + x;
+      o[0] = h0;
+      o[G.KX] = h1;
+      o[plane] = l0;
+      o[plane + G.KX] = l1;
+    }
+    return;
+  }
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < G.ncoef;
        i += (long long)gridDim.x * blockDim.x) {
     const double2 v = __ldg(src + i);
@@ -436,6 +468,36 @@ __global__ void __launch_bounds__(256) pack_spectra_kernel(const __grid_constant
     o[2 * plane] = l0;
     o[2 * plane + G.KX] = l1;
   }
+}
+
+// Per field-level exponent of the largest |value| (FP16 operand scales):
+// cexp[b] = max over the field-level's count doubles of floor(log2|x|),
+// accumulated with atomicMax (the caller sets cexp to a very negative value
+// first).  Block (x: chunk, y: field-level).
+__global__ void __launch_bounds__(256) field_exponent_kernel(const double *__restrict__ src, long long count,
+                                                             int *cexp) {
+  pdl_wait();
+  pdl_trigger();
+  const int b = blockIdx.y;
+  const double *p = src + (long long)b * count;
+  int e = -1023;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count;
+       i += (long long)gridDim.x * blockDim.x)
+    e = max(e, f64_exponent(__ldg(p + i)));
+  e = __reduce_max_sync(0xffffffffu, e);
+  if ((threadIdx.x & 31) == 0) atomicMax(cexp + b, e);
+}
+
+int field_exponents(const double *src, long long count, int batch, int *cexp, cudaStream_t s) {
+  if (batch <= 0) return DCCM_OK;
+  if (batch > 65535) return DCCM_ERR_UNSUPPORTED;
+  DCCM_CUDA(cudaMemsetAsync(cexp, 0x80, (size_t)batch * sizeof(int), s));  // 0x80808080: below any exponent
+  long long bx = (count + 255) / 256;
+  const long long want = (4LL * sm_count() + batch - 1) / batch;  // a few waves in all
+  if (bx > want) bx = want < 1 ? 1 : want;
+  DCCM_CUDA(launch_pdl(field_exponent_kernel, dim3((unsigned)bx, (unsigned)batch), dim3(256), 0, s, src, count,
+                       cexp));
+  return DCCM_OK;
 }
 
 int pack_spectra(Plan *const *plans, const int *batch, const double *const *spec, int ngroups, cudaStream_t s) {
@@ -456,6 +518,9 @@ int pack_spectra(Plan *const *plans, const int *batch, const double *const *spec
     G.KX = P.KX;
     G.C2Bp = P.C2Bp;
     G.f0 = nf;
+    G.nsplit = P.nsplit;
+    G.cexp = P.d_cexp;
+    if (P.nsplit == 2) DCCM_TRY(field_exponents(spec[g], 2 * P.ncoef, batch[g], P.d_cexp, s));
     nf += batch[g];
     maxc = P.ncoef > maxc ? P.ncoef : maxc;
   }
@@ -469,12 +534,32 @@ int pack_spectra(Plan *const *plans, const int *batch, const double *const *spec
 }
 
 // ------------------------------------------------------------ tile tables
-// Fill the bf16 split tiles of one direction from the FP64 Pbar table.
-// Thread per (tile row of split 0, group of 8 along K).
-__global__ void build_tiles_kernel(int dir, int N, int Jh, const MInfo *__restrict__ mi,
+// Largest binary exponent of the table entries of each m (FP16 tables):
+// dir 0 Pbar, dir 1 (w/2) Pbar, over every n >= m and latitude pair.
+__global__ void table_exponent_kernel(int dir, int N, int Jh, const double *__restrict__ pnm,
+                                      const double *__restrict__ w, int *emax) {
+  const int m = blockIdx.y;  // block (x: entries of m, y: m)
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= (long long)(N + 1 - m) * Jh) return;
+  const int jj = (int)(t % Jh);
+  double x = pnm[idx_mn(N, m, m) * Jh + t];
+  if (dir) x *= 0.5 * w[Jh + jj];
+  atomicMax(emax + m, f64_exponent(x));
+}
+
+// FP64 split into two FP16 numbers x = hi + lo (+ dropped), once per table entry.
+__device__ __forceinline__ void split2h(double x, __half &h, __half &l) {
+  h = __double2half(x);
+  l = __double2half(x - (double)__half2float(h));
+}
+
+// Fill the split tiles of one direction from the FP64 Pbar table: BF16 x 3,
+// or FP16 hi + lo of the values times 2^eb(m).  Thread per (tile row of
+// split 0, group of 8 along K).
+__global__ void build_tiles_kernel(int dir, int N, int Jh, int ns, const MInfo *__restrict__ mi,
                                    const long long *__restrict__ rowstart, long long nrows0,
                                    const double *__restrict__ pnm, const double *__restrict__ w,
-                                   __nv_bfloat16 *__restrict__ out) {
+                                   uint16_t *__restrict__ out) {
   const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (tid >= nrows0 * 8) return;
   const long long r0 = tid >> 3;
@@ -495,7 +580,7 @@ __global__ void build_tiles_kernel(int dir, int N, int Jh, const MInfo *__restri
   const int p = (int)(rr / M.nq);
   const int kv = p ? M.kv1 : M.kv0;
   const int nv = p ? M.nv1 : M.nv0;
-  __align__(16) __nv_bfloat16 h[8], md[8], l[8];
+  __align__(16) uint16_t h[8], md[8], l[8];
 #pragma unroll
   for (int e = 0; e < 8; ++e) {
     const int k = q * 64 + g8 * 8 + e;
@@ -509,15 +594,24 @@ __global__ void build_tiles_kernel(int dir, int N, int Jh, const MInfo *__restri
         x = (0.5 * w[Jh + k]) * pnm[idx_mn(N, m, n) * Jh + k];
       }
     }
-    split3(x, h[e], md[e], l[e]);
+    if (ns == 3) {
+      __nv_bfloat16 bh, bm, bl;
+      split3(x, bh, bm, bl);
+      h[e] = __bfloat16_as_ushort(bh);
+      md[e] = __bfloat16_as_ushort(bm);
+      l[e] = __bfloat16_as_ushort(bl);
+    } else {
+      __half hh, hl;
+      split2h(ldexp(x, M.eb), hh, hl);
+      h[e] = __half_as_ushort(hh);
+      md[e] = __half_as_ushort(hl);
+    }
   }
-  const long long row_s0 = M.base + ((long long)(p * M.nq + q) * 3 + 0) * M.nr + r;
-  uint4 *o0 = reinterpret_cast<uint4 *>(out + (row_s0)*64 + g8 * 8);
-  uint4 *o1 = reinterpret_cast<uint4 *>(out + (row_s0 + M.nr) * 64 + g8 * 8);
-  uint4 *o2 = reinterpret_cast<uint4 *>(out + (row_s0 + 2LL * M.nr) * 64 + g8 * 8);
-  *o0 = *reinterpret_cast<const uint4 *>(h);
-  *o1 = *reinterpret_cast<const uint4 *>(md);
-  *o2 = *reinterpret_cast<const uint4 *>(l);
+  const long long row_s0 = M.base + ((long long)(p * M.nq + q) * ns + 0) * M.nr + r;
+  *reinterpret_cast<uint4 *>(out + row_s0 * 64 + g8 * 8) = *reinterpret_cast<const uint4 *>(h);
+  *reinterpret_cast<uint4 *>(out + (row_s0 + M.nr) * 64 + g8 * 8) = *reinterpret_cast<const uint4 *>(md);
+  if (ns == 3)
+    *reinterpret_cast<uint4 *>(out + (row_s0 + 2LL * M.nr) * 64 + g8 * 8) = *reinterpret_cast<const uint4 *>(l);
 }
 
 // Host metadata for one direction's table.
@@ -528,7 +622,7 @@ struct TabMeta {
   long long rows = 0, rows0 = 0;
 };
 
-static TabMeta make_meta(int dir, const Plan &P) {
+static TabMeta make_meta(int dir, const Plan &P, const std::vector<int> &emax) {
   const int N = P.N, Jh = P.Jh;
   TabMeta t;
   t.mi.resize(N + 1);
@@ -553,8 +647,9 @@ static TabMeta make_meta(int dir, const Plan &P) {
       M.x1 = (2 * m + 1) * Jh;
     }
     M.base = base;
+    M.eb = P.nsplit == 2 ? 14 - emax[m] : 0;
     t.rowstart[m] = r0;
-    base += 2LL * M.nq * 3 * M.nr;
+    base += 2LL * M.nq * P.nsplit * M.nr;
     r0 += 2LL * M.nq * M.nr;
     for (int nt = 0; nt < (M.nr + 127) / 128; ++nt) t.items.push_back(make_int4(m, 0, nt, 0));
   }
@@ -582,20 +677,35 @@ static EncodeTiledFn get_encode() {
   return fn;
 }
 
-// bf16 tensor map with a 128-byte swizzle; dims/strides/box innermost first.
+// bf16 (or fp16) tensor map with a 128-byte swizzle; dims/strides/box
+// innermost first.
 static int encode_bf16(CUtensorMap *map, void *base, int rank, const cuuint64_t *dims, const cuuint64_t *strides,
-                       const cuuint32_t *box) {
+                       const cuuint32_t *box, bool fp16 = false) {
   EncodeTiledFn enc = get_encode();
   if (!enc) return DCCM_ERR_UNSUPPORTED;
   const cuuint32_t estr[3] = {1, 1, 1};
-  const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, (cuuint32_t)rank, base, dims, strides, box, estr,
+  const CUresult r = enc(map, fp16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16,
+                         (cuuint32_t)rank, base, dims, strides, box, estr,
                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                          CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS ? DCCM_OK : DCCM_ERR_UNSUPPORTED;
 }
 
 static int build_one(Plan &P, int dir, TileTable &T) {
-  TabMeta meta = make_meta(dir, P);
+  std::vector<int> emax(P.N + 1, 0);
+  if (P.nsplit == 2) {  // per-m scale exponents of the FP16 tables
+    int *de;
+    DCCM_CUDA(cudaMalloc(&de, (P.N + 1) * sizeof(int)));
+    DCCM_CUDA(cudaMemset(de, 0x80, (P.N + 1) * sizeof(int)));
+    const long long nt = (long long)(P.N + 1) * P.Jh;
+    table_exponent_kernel<<<dim3((unsigned)((nt + 255) / 256), (unsigned)(P.N + 1)), 256>>>(dir, P.N, P.Jh,
+                                                                                        P.d_pnm, P.d_w, de);
+    DCCM_LAUNCH_CHECK();
+    DCCM_CUDA(cudaMemcpy(emax.data(), de, (P.N + 1) * sizeof(int), cudaMemcpyDeviceToHost));
+    cudaFree(de);
+    for (int &e : emax) e = e < -1000 ? -1000 : e;  // an all-zero m: any scale
+  }
+  TabMeta meta = make_meta(dir, P, emax);
   T.rows = meta.rows;
   T.base.assign(P.N + 1, 0);
   for (int m = 0; m <= P.N; ++m) T.base[m] = meta.mi[m].base;
@@ -618,8 +728,8 @@ static int build_one(Plan &P, int dir, TileTable &T) {
   DCCM_CUDA(cudaMemcpy(T.d_items, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice));
   const long long nthr = meta.rows0 * 8;
   if (nthr > 0) {
-    build_tiles_kernel<<<(unsigned)((nthr + 255) / 256), 256>>>(dir, P.N, P.Jh, dmi, drs, meta.rows0,
-                                                               P.d_pnm, P.d_w, (__nv_bfloat16 *)T.d);
+    build_tiles_kernel<<<(unsigned)((nthr + 255) / 256), 256>>>(dir, P.N, P.Jh, P.nsplit, dmi, drs, meta.rows0,
+                                                               P.d_pnm, P.d_w, T.d);
     DCCM_LAUNCH_CHECK();
   }
   DCCM_CUDA(cudaDeviceSynchronize());
@@ -628,19 +738,20 @@ static int build_one(Plan &P, int dir, TileTable &T) {
     const cuuint64_t dims[2] = {64, (cuuint64_t)meta.rows};
     const cuuint64_t str[1] = {128};
     const cuuint32_t box[2] = {64, 128};
-    DCCM_TRY(encode_bf16(&T.map, T.d, 2, dims, str, box));
+    DCCM_TRY(encode_bf16(&T.map, T.d, 2, dims, str, box, P.nsplit == 2));
   }
-  if (dir == 0) {  // Apack[3][C2Bp][KX], box 64 (K) x 128 (c)
-    const cuuint64_t dims[3] = {(cuuint64_t)P.KX, (cuuint64_t)P.C2Bp, 3};
+  const cuuint64_t ns = (cuuint64_t)P.nsplit;
+  if (dir == 0) {  // Apack[ns][C2Bp][KX], box 64 (K) x 128 (c)
+    const cuuint64_t dims[3] = {(cuuint64_t)P.KX, (cuuint64_t)P.C2Bp, ns};
     const cuuint64_t str[2] = {(cuuint64_t)P.KX * 2, (cuuint64_t)P.KX * 2 * P.C2Bp};
     const cuuint32_t box[3] = {64, 128, 1};
-    DCCM_TRY(encode_bf16(&T.amap, P.d_apack, 3, dims, str, box));
-  } else {  // G3[3][(N+1) 2 Jh][C2Bp], box 64 (c) x 64 (K)
+    DCCM_TRY(encode_bf16(&T.amap, P.d_apack, 3, dims, str, box, P.nsplit == 2));
+  } else {  // G3[ns][(N+1) 2 Jh][C2Bp], box 64 (c) x 64 (K)
     const cuuint64_t rows = (cuuint64_t)(P.N + 1) * 2 * P.Jh;
-    const cuuint64_t dims[3] = {(cuuint64_t)P.C2Bp, rows, 3};
+    const cuuint64_t dims[3] = {(cuuint64_t)P.C2Bp, rows, ns};
     const cuuint64_t str[2] = {(cuuint64_t)P.C2Bp * 2, (cuuint64_t)P.C2Bp * 2 * rows};
     const cuuint32_t box[3] = {64, 64, 1};
-    DCCM_TRY(encode_bf16(&T.amap, P.d_work, 3, dims, str, box));
+    DCCM_TRY(encode_bf16(&T.amap, P.d_work, 3, dims, str, box, P.nsplit == 2));
   }
   T.map_ok = true;
   T.items_per_ct = (int)meta.items.size();
@@ -672,7 +783,7 @@ static int build_pack(Plan &P) {
     }
   DCCM_CUDA(cudaMalloc(&P.d_xpos, xpos.size() * sizeof(int)));
   DCCM_CUDA(cudaMemcpy(P.d_xpos, xpos.data(), xpos.size() * sizeof(int), cudaMemcpyHostToDevice));
-  const size_t bytes = (size_t)3 * P.C2Bp * P.KX * sizeof(uint16_t);
+  const size_t bytes = (size_t)P.nsplit * P.C2Bp * P.KX * sizeof(uint16_t);
   DCCM_CUDA(cudaMalloc(&P.d_apack, bytes));
   DCCM_CUDA(cudaMemset(P.d_apack, 0, bytes));
   return DCCM_OK;
@@ -726,6 +837,8 @@ int legendre_tc_multi(Plan *const *plans, const int *batch, const void *const *i
     a.err = plans[0]->d_err;
     a.ntmax = ntmax;
     a.nacc = 8 * ntmax <= TMEM_COLS ? 2 : 1;
+    a.nsplit = P.nsplit;
+    a.cexp = dir == 0 ? P.d_cexp : P.d_cexp + P.max_batch;
     if (dir == 0) a.F = (float *)out[g];
     else a.spec_out = (double *)out[g];
     L.map[ng] = T.map;

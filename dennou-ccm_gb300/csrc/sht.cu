@@ -11,7 +11,11 @@
 // Transform paths (precision chosen at plan creation):
 //   DCCM_SHT_FP64   Legendre on the FP64 CUDA cores, FP64 FFT;
 //   DCCM_SHT_MIXED  Legendre on tcgen05 tensor cores (BF16 x 3, FP32
-//                   accumulation), FP32 FFT; spectra and grids stay FP64.
+//                   accumulation), FP32 FFT; spectra and grids stay FP64;
+//   DCCM_SHT_MIXED_FP16  the same with FP16 hi + lo operands (3 products
+//                   instead of 6): tables scaled by a power of two per
+//                   zonal wavenumber m, spectra and Fourier coefficients
+//                   per field-level, so that both fit FP16's range.
 #include <math.h>
 #include <string.h>
 
@@ -89,7 +93,7 @@ __global__ void pnm_kernel(int N, int Jh, const double *__restrict__ mu, double 
 static void destroy(Plan &P) {
   void *ptrs[] = {P.d_mu,      P.d_w,        P.d_pnm,       P.d_tw64,  P.d_tw32,  P.d_twl32,
                   P.tinv.d,    P.tfwd.d,     P.tinv.d_mi,   P.tfwd.d_mi, P.tinv.d_items,
-                  P.tfwd.d_items, P.d_work,  P.d_err,       P.d_apack, P.d_xpos};
+                  P.tfwd.d_items, P.d_work,  P.d_err,       P.d_apack, P.d_xpos,   P.d_cexp};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   P.stage.release();
@@ -102,6 +106,7 @@ static int create(Plan &P, int N, int I, int J, int precision, int max_batch) {
   P.J = J;
   P.Jh = J / 2;
   P.precision = precision;
+  P.nsplit = precision == DCCM_SHT_MIXED_FP16 ? 2 : 3;
   P.max_batch = max_batch;
   P.ncoef = (int64_t)(N + 1) * (N + 2) / 2;
   if (!fft_length_supported(I)) return DCCM_ERR_UNSUPPORTED;
@@ -139,9 +144,9 @@ static int create(Plan &P, int N, int I, int J, int precision, int max_batch) {
   DCCM_CUDA(cudaMemcpy(P.d_tw64, tw64.data(), I * sizeof(double2), cudaMemcpyHostToDevice));
   DCCM_CUDA(cudaMemcpy(P.d_tw32, tw32.data(), I * sizeof(float2), cudaMemcpyHostToDevice));
   DCCM_CUDA(cudaMemcpy(P.d_twl32, twl32.data(), I * sizeof(float2), cudaMemcpyHostToDevice));
-  if (precision == DCCM_SHT_MIXED) {
-    // F (FP32, [m][j][2 max_batch]) and G3 (three BF16 planes, rows of
-    // C2Bp) share the Fourier buffer.
+  if (precision != DCCM_SHT_FP64) {
+    // F (FP32, [m][j][2 max_batch]) and G3 (three BF16 or two FP16 planes,
+    // rows of C2Bp) share the Fourier buffer.
     const size_t c2bp = (size_t)(2 * max_batch + 7) / 8 * 8;
     const size_t f_bytes = (size_t)(N + 1) * J * 2 * (size_t)max_batch * sizeof(float);
     const size_t g3_bytes = 3 * (size_t)(N + 1) * J * c2bp * sizeof(uint16_t);
@@ -150,13 +155,14 @@ static int create(Plan &P, int N, int I, int J, int precision, int max_batch) {
     P.work_bytes = (size_t)(N + 1) * J * 2 * (size_t)max_batch * sizeof(double);
   }
   DCCM_CUDA(cudaMalloc(&P.d_work, P.work_bytes));
-  if (precision == DCCM_SHT_MIXED) DCCM_TRY(build_tiles(P));
+  if (precision == DCCM_SHT_MIXED_FP16) DCCM_CUDA(cudaMalloc(&P.d_cexp, 2 * (size_t)max_batch * sizeof(int)));
+  if (precision != DCCM_SHT_FP64) DCCM_TRY(build_tiles(P));
   DCCM_CUDA(cudaDeviceSynchronize());
   return DCCM_OK;
 }
 
 int inverse(Plan &P, const double *spec, double *grid, int batch, cudaStream_t s) {
-  if (P.precision == DCCM_SHT_MIXED) {
+  if (P.precision != DCCM_SHT_FP64) {
     DCCM_TRY(legendre_inv_tc(P, batch, spec, (float *)P.d_work, s));
     return fft_inverse(P, batch, true, P.d_work, grid, s);
   }
@@ -165,7 +171,7 @@ int inverse(Plan &P, const double *spec, double *grid, int batch, cudaStream_t s
 }
 
 int forward(Plan &P, const double *grid, double *spec, int batch, cudaStream_t s) {
-  if (P.precision == DCCM_SHT_MIXED) {
+  if (P.precision != DCCM_SHT_FP64) {
     DCCM_TRY(fft_forward(P, batch, true, grid, P.d_work, s));
     return legendre_fwd_tc(P, batch, P.d_work, spec, s);
   }
@@ -182,10 +188,11 @@ extern "C" int dccm_sht_plan_create(int nmax, int imax, int jmax, int precision,
                                     dccm_sht_plan **plan) {
   if (!plan) return DCCM_ERR_INVALID_ARG;
   *plan = nullptr;
-  if (precision != DCCM_SHT_FP64 && precision != DCCM_SHT_MIXED) return DCCM_ERR_INVALID_ARG;
+  if (precision != DCCM_SHT_FP64 && precision != DCCM_SHT_MIXED && precision != DCCM_SHT_MIXED_FP16)
+    return DCCM_ERR_INVALID_ARG;
   if (nmax < 1 || imax < 1 || jmax < 2 || max_batch < 1) return DCCM_ERR_INVALID_ARG;
   if (jmax % 2 != 0 || jmax < nmax + 1 || imax <= 2 * nmax) return DCCM_ERR_UNSUPPORTED;
-  if (precision == DCCM_SHT_MIXED && (jmax / 2) % 16 != 0) return DCCM_ERR_UNSUPPORTED;
+  if (precision != DCCM_SHT_FP64 && (jmax / 2) % 16 != 0) return DCCM_ERR_UNSUPPORTED;
   dccm_sht_plan *p = new (std::nothrow) dccm_sht_plan();
   if (!p) return DCCM_ERR_NOMEM;
   int st = sht::create(p->P, nmax, imax, jmax, precision, max_batch);
@@ -355,7 +362,7 @@ namespace sht {
 int ensemble_inverse(dccm_sht_ensemble *e, const double *const *spec, double *const *grid, const int *batch,
                      cudaStream_t s) {
   const int ng = (int)e->plans.size();
-  if (e->precision != DCCM_SHT_MIXED) {
+  if (e->precision == DCCM_SHT_FP64) {
     for (int g = 0; g < ng; ++g)
       if (batch[g] > 0) DCCM_TRY(inverse(e->plans[g]->P, spec[g], grid[g], batch[g], s));
     return DCCM_OK;
@@ -376,7 +383,7 @@ int ensemble_inverse(dccm_sht_ensemble *e, const double *const *spec, double *co
 int ensemble_forward(dccm_sht_ensemble *e, const double *const *grid, double *const *spec, const int *batch,
                      cudaStream_t s) {
   const int ng = (int)e->plans.size();
-  if (e->precision != DCCM_SHT_MIXED) {
+  if (e->precision == DCCM_SHT_FP64) {
     for (int g = 0; g < ng; ++g)
       if (batch[g] > 0) DCCM_TRY(forward(e->plans[g]->P, grid[g], spec[g], batch[g], s));
     return DCCM_OK;

@@ -15,7 +15,8 @@
 //   forward: G[m][p][jj][c]   FFT output folded into parity p: p = 0 holds
 //                             E = G(jn) + G(js), p = 1 holds O = G(jn) - G(js),
 //                             already divided by I.
-// Mixed precision: F is FP32; G is stored split as three BF16 planes
+// Mixed precision: F is FP32; G is stored split as three BF16 planes (two
+// FP16 planes, scaled per field-level, for DCCM_SHT_MIXED_FP16)
 // G3[s][(2m + p) Jh + jj][c] (row length C2Bp = 2 max_batch rounded up to 8),
 // the MN-major A operand of the tensor-core analysis; the spectra enter the
 // tensor-core synthesis through Apack[s][c][x], BF16 planes of the split
@@ -72,6 +73,8 @@ struct Plan {
   uint16_t *d_apack = nullptr; // Apack[3][C2Bp][KX] (bf16 bits)
   int *d_xpos = nullptr;       // Apack column x of each spectral coefficient
   int *d_err = nullptr;        // device error flag of bounded waits
+  int nsplit = 3;              // tensor-path operand splits: 3 (BF16 x 3) or 2 (FP16 hi + lo)
+  int *d_cexp = nullptr;       // FP16: per field-level scale exponents, [inverse | forward][max_batch]
   DevBuf stage;                // host entry point staging
   cudaStream_t stream = nullptr;
 };
@@ -99,6 +102,7 @@ int legendre_fwd_tc(Plan &P, int batch, const void *G3, double *spec, cudaStream
 int legendre_tc_multi(Plan *const *plans, const int *batch, const void *const *in, void *const *out,
                       int ngroups, int dir, cudaStream_t s);
 int pack_spectra(Plan *const *plans, const int *batch, const double *const *spec, int ngroups, cudaStream_t s);
+int field_exponents(const double *src, long long count, int batch, int *cexp, cudaStream_t s);
 int fft_multi(Plan *const *plans, const int *batch, const void *const *in, void *const *out, int ngroups, bool fwd,
               cudaStream_t s);
 int inverse(Plan &P, const double *spec, double *grid, int batch, cudaStream_t s);

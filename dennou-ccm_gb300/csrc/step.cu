@@ -100,7 +100,7 @@ static Groups groups_of(dccm_step *st) {
   }
   return G;
 }
-static bool mixed(const Groups &G) { return G.n > 0 && G.P[0]->precision == DCCM_SHT_MIXED; }
+static bool mixed(const Groups &G) { return G.n > 0 && G.P[0]->precision != DCCM_SHT_FP64; }
 
 static int stage_leg_inv(dccm_step *st, cudaStream_t s) {
   Groups G = groups_of(st);

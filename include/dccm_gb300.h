@@ -293,10 +293,17 @@ int dccm_area_integral_noalloc_dev(const double *f, const double *area, int64_t 
  * precision DCCM_SHT_MIXED: Legendre sums on the tensor cores in split
  * BF16 x 3 with FP32 accumulation, FFT in FP32; relative L2 error of a
  * forward(inverse(s)) round trip below 1e-6.  Requires jmax/2 % 16 == 0.
+ * precision DCCM_SHT_MIXED_FP16: the same with FP16 operands, each split
+ * into hi + lo (22 bits, 3 products instead of 6): the Legendre tables are
+ * scaled by a power of two per zonal wavenumber m, the spectra (inverse)
+ * and the Fourier coefficients (forward) by a power of two per field-level
+ * from the field-level's largest value, so both fit FP16's range; the
+ * scales are undone exactly in FP32.  Mixed paths take values within FP32's
+ * range.
  * Requirements: jmax even, jmax >= nmax+1, imax > 2 nmax, imax = 32 R with
  * R in {2, 3, 4, 6, 8, 12, 16, 24, 32} (imax = 64 ... 1024).
  * ===================================================================== */
-enum { DCCM_SHT_FP64 = 0, DCCM_SHT_MIXED = 1 };
+enum { DCCM_SHT_FP64 = 0, DCCM_SHT_MIXED = 1, DCCM_SHT_MIXED_FP16 = 2 };
 
 typedef struct dccm_sht_plan dccm_sht_plan;
 

@@ -1,7 +1,9 @@
 """GPU parity of the spherical-harmonic transforms against the FP64 oracle,
 through the C ABI.  Tolerances (relative L2 over the whole batch):
   FP64 plan   1e-13 (inverse grid, forward spectra), nodes 2e-16;
-  mixed plan  1e-6  (BF16 x 3 Legendre on tcgen05, FP32 FFT)."""
+  mixed plan  1e-6  (BF16 x 3 Legendre on tcgen05, FP32 FFT);
+  FP16 plan   1e-6  (FP16 hi + lo Legendre with per-m and per-field-level
+              power-of-two scales, FP32 FFT)."""
 import os
 
 import numpy as np
@@ -44,11 +46,15 @@ def test_fp64_transforms_match_oracle(dccm, oracle, synth, N, I, J):
     assert rel_l2(plan.forward(g), s) <= 1e-13
 
 
+MIXED = [1, 2]  # SHT_MIXED (BF16 x 3), SHT_MIXED_FP16
+
+
+@pytest.mark.parametrize("prec", MIXED)
 @pytest.mark.parametrize("N,I,J", TRUNC)
-def test_mixed_transforms_match_oracle(dccm, oracle, synth, N, I, J):
+def test_mixed_transforms_match_oracle(dccm, oracle, synth, N, I, J, prec):
     B = 70  # two 128-column blocks of the batch, the second partial
     s = synth.spectra(N, B, seed=N + 1)
-    plan = dccm.ShtPlan(N, I, J, dccm.SHT_MIXED, B)
+    plan = dccm.ShtPlan(N, I, J, prec, B)
     g = plan.inverse(s)
     go = oracle.sht_inverse(N, I, J, s)
     e_inv = rel_l2(g, go)
@@ -72,11 +78,12 @@ def test_mixed_transforms_match_oracle(dccm, oracle, synth, N, I, J):
 LONG = [(127, 384, 192), (170, 512, 256), (255, 768, 384), (341, 1024, 512)]
 
 
+@pytest.mark.parametrize("prec", MIXED)
 @pytest.mark.parametrize("N,I,J", LONG)
-def test_mixed_long_rows_match_oracle(dccm, oracle, synth, N, I, J):
+def test_mixed_long_rows_match_oracle(dccm, oracle, synth, N, I, J, prec):
     B = 6
     s = synth.spectra(N, B, seed=N + 3)
-    plan = dccm.ShtPlan(N, I, J, dccm.SHT_MIXED, B)
+    plan = dccm.ShtPlan(N, I, J, prec, B)
     g = plan.inverse(s)
     go = oracle.sht_inverse(N, I, J, s)
     s2 = plan.forward(go)
@@ -89,7 +96,7 @@ def test_mixed_long_rows_match_oracle(dccm, oracle, synth, N, I, J):
         assert rel_l2(s2[b], so[b]) <= 4e-6
 
 
-@pytest.mark.parametrize("prec", [0, 1])
+@pytest.mark.parametrize("prec", [0, 1, 2])
 def test_known_answers(dccm, oracle, prec):
     N, I, J = 21, 64, 32
     plan = dccm.ShtPlan(N, I, J, prec, 3)
@@ -109,7 +116,7 @@ def test_known_answers(dccm, oracle, prec):
     assert np.abs(back - s).max() <= tol * 3
 
 
-@pytest.mark.parametrize("prec", [0, 1])
+@pytest.mark.parametrize("prec", [0, 1, 2])
 def test_golden_fixture(dccm, prec):
     z = np.load(os.path.join(GOLDEN, "sht_t21.npz"))
     N, I, J = int(z["N"]), int(z["I"]), int(z["J"])
@@ -146,3 +153,24 @@ def test_batch_limits(dccm):
         dccm.ShtPlan(21, 40, 32, 0, 1)  # imax <= 2 nmax
     with pytest.raises(dccm.DccmError):
         dccm.ShtPlan(21, 70, 32, 0, 1)  # 70 = 2 * 5 * 7 is not 2^a 3^b
+
+
+@pytest.mark.parametrize("prec", MIXED)
+def test_mixed_field_magnitudes(dccm, oracle, synth, prec):
+    """Field-levels of very different magnitude in one batch (a vorticity
+    of 1e-5, a temperature of 300, a pressure of 1e5, and 1e-12): every
+    field-level keeps its relative accuracy (the FP16 plan scales each
+    field-level into FP16's range on its own)."""
+    N, I, J, B = 85, 256, 128, 8
+    s = synth.spectra(N, B, seed=11)
+    mags = np.array([1e-5, 300.0, 1e5, 1e-12, 1.0, 3e-3, 7e2, 2e-8])
+    s = s * mags[:, None]
+    plan = dccm.ShtPlan(N, I, J, prec, B)
+    g = plan.inverse(s)
+    go = oracle.sht_inverse(N, I, J, s)
+    s2 = plan.forward(go)
+    so = oracle.sht_forward(N, I, J, go)
+    assert plan.status() == (0, 0)
+    for b in range(B):
+        assert rel_l2(g[b], go[b]) <= 2e-6, (b, rel_l2(g[b], go[b]))
+        assert rel_l2(s2[b], so[b]) <= 2e-6, (b, rel_l2(s2[b], so[b]))

@@ -13,7 +13,7 @@ pytestmark = pytest.mark.gpu
 GROUPS = [(21, 64, 32, 20), (42, 128, 64, 10), (63, 192, 96, 7), (85, 256, 128, 5)]
 
 
-@pytest.mark.parametrize("prec,tol", [(1, 1e-6), (0, 1e-13)])
+@pytest.mark.parametrize("prec,tol", [(1, 1e-6), (2, 1e-6), (0, 1e-13)])
 def test_ensemble_matches_oracle(dccm, oracle, synth, cuda, prec, tol):
     torch = cuda
     ens = dccm.Ensemble([g for g in GROUPS], prec)
