@@ -174,3 +174,24 @@ def test_mixed_field_magnitudes(dccm, oracle, synth, prec):
     for b in range(B):
         assert rel_l2(g[b], go[b]) <= 2e-6, (b, rel_l2(g[b], go[b]))
         assert rel_l2(s2[b], so[b]) <= 2e-6, (b, rel_l2(s2[b], so[b]))
+
+
+@pytest.mark.parametrize("prec", [0, 1, 2])
+def test_zero_and_single_field_level(dccm, oracle, synth, cuda, prec):
+    """batch 0 is a no-op that leaves the output untouched; batch 1 uses one
+    ragged column block (1 of 128 columns) of every tensor-core item."""
+    torch = cuda
+    N, I, J = 42, 128, 64
+    plan = dccm.ShtPlan(N, I, J, prec, 4)
+    s = synth.spectra(N, 1, seed=21)
+    ds = torch.from_numpy(s.view(np.float64).copy()).cuda()
+    dg = torch.full((1, J, I), 7.0, dtype=torch.float64, device="cuda")
+    plan.inverse_dev(ds, dg, 0)
+    torch.cuda.synchronize()
+    assert bool((dg == 7.0).all())
+    tol = 1e-13 if prec == 0 else 1e-6
+    g = plan.inverse(s)
+    go = oracle.sht_inverse(N, I, J, s)
+    assert rel_l2(g, go) <= tol
+    assert rel_l2(plan.forward(go), oracle.sht_forward(N, I, J, go)) <= tol
+    assert plan.status() == (0, 0)
