@@ -94,6 +94,7 @@ _SIGS = {
     "dccm_implcpl_backward": (ctypes.c_int, [ctypes.c_void_p] * 5),
     "dccm_implcpl_backward_dev": (ctypes.c_int, [ctypes.c_void_p] * 6),
     "dccm_implcpl_matrices": (ctypes.c_int, [ctypes.c_void_p] * 4),
+    "dccm_implcpl_info": (ctypes.c_int, [ctypes.c_void_p] * 4),
     "dccm_j99_generate": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
                                          ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
@@ -170,7 +171,8 @@ class StepDesc(ctypes.Structure):
                 ("ens_spec_in", ctypes.c_void_p), ("ens_grid", ctypes.c_void_p),
                 ("ens_spec_out", ctypes.c_void_p), ("ens_nfl", ctypes.c_void_p),
                 ("nremap", ctypes.c_int), ("remaps", ctypes.c_void_p), ("flux", ctypes.c_void_p),
-                ("flux_grid", ctypes.c_void_p)]
+                ("flux_grid", ctypes.c_void_p), ("implcpl", ctypes.c_void_p), ("implcpl_fwd", ctypes.c_void_p),
+                ("nremap_post", ctypes.c_int), ("remaps_post", ctypes.c_void_p)]
 
 
 class HostCopy(ctypes.Structure):
@@ -581,8 +583,13 @@ class Step:
     tensors keyed like DSFCM_Util_SfcBulkFlux_Get's arguments."""
 
     def __init__(self, sht=None, nfl=0, spec_in=None, grid=None, spec_out=None, remaps=(), flux=None,
-                 flux_grid=None, ensemble=None, ens_spec_in=None, ens_grid=None, ens_spec_out=None, ens_nfl=None):
-        """remaps: sequence of (RemapPlan, nfields, src, ld_src, dst, ld_dst[, nsub, ld_dst2])."""
+                 flux_grid=None, ensemble=None, ens_spec_in=None, ens_grid=None, ens_spec_out=None, ens_nfl=None,
+                 implcpl=None, implcpl_prof=None, implcpl_out=None, remaps_post=()):
+        """remaps, remaps_post: sequences of (RemapPlan, nfields, src, ld_src,
+        dst, ld_dst[, nsub, ld_dst2]).  implcpl: an ImplCplPlan whose forward
+        sweep (profiles implcpl_prof, outputs implcpl_out: dicts of device
+        tensors as ImplCplPlan.forward_dev takes) runs before the remaps and
+        whose backward sweep runs after the flux and remaps_post."""
         L = load()
         d = StepDesc()
         d.sht = sht.h.value if sht is not None else None
@@ -597,15 +604,25 @@ class Step:
             d.ens = ensemble.h.value
             d.ens_spec_in, d.ens_grid, d.ens_spec_out = (ctypes.addressof(a) for a in self._ens)
             d.ens_nfl = ctypes.addressof(self._ens_nfl)
-        nr = len(remaps)
-        self._remaps = (StepRemap * max(1, nr))()
-        for k, rm in enumerate(remaps):
-            plan, nf, src, lds, dst, ldd = rm[:6]
-            nsub, ld2 = (rm[6], rm[7]) if len(rm) > 6 else (0, 0)
-            self._remaps[k] = StepRemap(plan.h.value, int(nf), _p(src).value, int(lds), _p(dst).value, int(ldd),
-                                        int(nsub), int(ld2))
-        d.nremap = nr
+        def remap_array(lst):
+            arr = (StepRemap * max(1, len(lst)))()
+            for k, rm in enumerate(lst):
+                plan, nf, src, lds, dst, ldd = rm[:6]
+                nsub, ld2 = (rm[6], rm[7]) if len(rm) > 6 else (0, 0)
+                arr[k] = StepRemap(plan.h.value, int(nf), _p(src).value, int(lds), _p(dst).value, int(ldd),
+                                   int(nsub), int(ld2))
+            return arr
+        self._remaps = remap_array(remaps)
+        d.nremap = len(remaps)
         d.remaps = ctypes.addressof(self._remaps)
+        self._remaps_post = remap_array(remaps_post)
+        d.nremap_post = len(remaps_post)
+        d.remaps_post = ctypes.addressof(self._remaps_post)
+        if implcpl is not None:
+            self._icf = implcpl._args(implcpl_prof, implcpl_out)
+            d.implcpl = implcpl.h.value
+            d.implcpl_fwd = ctypes.addressof(self._icf)
+            self._keep += [implcpl, implcpl_prof, implcpl_out, remaps_post]
         if flux is not None:
             fa = FluxArgs()
             self._sig = np.ascontiguousarray(np.asarray(flux["a_Sig1Info"], np.float64))
@@ -727,6 +744,12 @@ class ImplCplPlan:
     def backward_dev(self, tend, stream=None):
         _check(load().dccm_implcpl_backward_dev(self.h, *[_p(tend[k]) for k in ("DUDt", "DVDt", "DTempDt", "DQMixDt")],
                                                 _stream(stream)), "dccm_implcpl_backward_dev")
+
+    def info(self):
+        """dccm_implcpl_info: (ncol, kmax, ncmax)."""
+        v = [ctypes.c_int() for _ in range(3)]
+        _check(load().dccm_implcpl_info(self.h, *[ctypes.byref(x) for x in v]), "dccm_implcpl_info")
+        return tuple(x.value for x in v)
 
     def matrices(self):
         """The module-state matrices (UVMtx, TempMtx, QMixMtx), each [3][kmax][ncol]."""

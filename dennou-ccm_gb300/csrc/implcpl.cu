@@ -43,6 +43,7 @@ struct Fwd {
   const double *MomX, *MomY, *Heat, *QFlx, *P, *Ef, *Eh, *Tv, *Z, *Kv, *Kt, *Kq;
   double *DU, *DV, *DT, *DQ, *C1, *C2;
   double *uv, *tm, *qm;
+  double *G, *IEF;  // per (level, column) factors shared by the systems (geo_kernel)
   long long ncol;
   int kmax, ncmax, ih2o;
   double Grav, CpDry, GasR, inv_g2dt;
@@ -58,6 +59,21 @@ struct Fwd {
 // the loads of a chunk overlap while the serial elimination runs.
 constexpr int LV = 4;   // forward sweep: levels fetched ahead
 constexpr int LVB = 8;  // backward sweep
+
+// The factors every system's row uses, once per (level, column) instead of
+// once per system: G(j) = P_h(j) / (R Tv_h(j) (z(j+1) - z(j))) at half level
+// j = 1..kmax-1 (the transfer coefficient of :182-195 is K(j) G(j)), and the
+// reciprocal Exner function 1 / Exner_f(j) at full level j (0-based index,
+// the temperature rows of :222-260).  Same expressions, same rounding.
+__global__ void __launch_bounds__(256) geo_kernel(const Fwd a) {
+  const long long n = a.ncol;
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= n * a.kmax) return;
+  const int j = (int)(t / n);
+  const long long c = t - j * n;
+  a.IEF[t] = 1.0 / a.Ef[c + n * j];
+  if (j >= 1) a.G[t] = a.P[c + n * j] / (a.GasR * a.Tv[c + n * j] * (a.Z[c + n * j] - a.Z[c + n * (j - 1)]));
+}
 
 template <int SYS>
 __device__ __forceinline__ void forward_column(const Fwd &a, long long c, int tracer) {
@@ -83,27 +99,26 @@ __device__ __forceinline__ void forward_column(const Fwd &a, long long c, int tr
   double *mat = SYS == 0 ? a.uv : (SYS == 1 ? a.tm : a.qm);
   const bool store_mat = SYS != 2 || tracer == 0;
   // values at level k carried from the previous (upper) iteration
-  double Pk = a.P[c + n * K], Zk = a.Z[c + n * (K - 1)], Ehk = a.Eh[c + n * K];
+  double Pk = a.P[c + n * K], Ehk = a.Eh[c + n * K];
   double flk[NR];
 #pragma unroll
   for (int r = 0; r < NR; ++r) flk[r] = fl[r][c + n * K];
-  double tck = 0.0, ief_k1 = 0.0, ief_k = 1.0 / a.Ef[c + n * (K - 1)];
+  double tck = 0.0, ief_k1 = 0.0, ief_k = a.IEF[c + n * (K - 1)];
   double m0p = 0.0, rp[NR], m0_2 = 0.0, r_2[NR], c2[NR], tc1 = 0.0, dfadt1 = 0.0, dfadt2 = 0.0;
   for (int k0 = K; k0 >= 1; k0 -= LV) {
     // fetch half level k-1 and full level k-1 of the next LV levels
-    double Pm[LV], Tvm[LV], Zm[LV], Kdm[LV], Ehm[LV], Efm[LV], flm[LV][NR];
+    double Pm[LV], Gm[LV], Kdm[LV], Ehm[LV], Iefm[LV], flm[LV][NR];
 #pragma unroll
     for (int i = 0; i < LV; ++i) {
       const int k = k0 - i;
       if (k >= 1) {
         Pm[i] = a.P[c + n * (k - 1)];
         if (k > 1) {
-          Tvm[i] = a.Tv[c + n * (k - 1)];
-          Zm[i] = a.Z[c + n * (k - 2)];
+          Gm[i] = a.G[c + n * (k - 1)];
           Kdm[i] = Kd[c + n * (k - 1)];
           if (SYS == 1) {
             Ehm[i] = a.Eh[c + n * (k - 1)];
-            Efm[i] = a.Ef[c + n * (k - 2)];
+            Iefm[i] = a.IEF[c + n * (k - 2)];
           }
         }
 #pragma unroll
@@ -117,9 +132,8 @@ __device__ __forceinline__ void forward_column(const Fwd &a, long long c, int tr
       // transfer coefficient at half level k-1 (0 at the surface, :182-195)
       double tkm = 0.0, ief_km = 0.0;
       if (k > 1) {
-        const double tmp = Pm[i] / (a.GasR * Tvm[i] * (Zk - Zm[i]));
-        tkm = Kdm[i] * tmp;
-        if (SYS == 1) ief_km = 1.0 / Efm[i];
+        tkm = Kdm[i] * Gm[i];
+        if (SYS == 1) ief_km = Iefm[i];
       }
       const double mass = -(Pk - Pm[i]) * a.inv_g2dt;
       double mm, m0, mp;  // row k; +0 where the reference assigns 0
@@ -168,10 +182,7 @@ __device__ __forceinline__ void forward_column(const Fwd &a, long long c, int tr
       ief_k1 = ief_k;
       ief_k = ief_km;
       Pk = Pm[i];
-      if (k > 1) {
-        Zk = Zm[i];
-        if (SYS == 1) Ehk = Ehm[i];
-      }
+      if (SYS == 1 && k > 1) Ehk = Ehm[i];
     }
   }
   // coupling coefficients (:342-375); DFADUV1 = -DFADUV2 = TC(1)
@@ -295,7 +306,9 @@ extern "C" int dccm_implcpl_create(int ncol, int kmax, int ncmax, int index_h2ov
   p->ncmax = ncmax;
   p->ih2o = index_h2ovap;
   p->k = *consts;
-  const cudaError_t e = cudaMalloc(&p->d_mtx, (size_t)3 * 3 * kmax * ncol * sizeof(double));
+  // the three matrices (3 diagonals each), then the forward sweep's shared
+  // factors G and 1/Exner_f (kmax x ncol each)
+  const cudaError_t e = cudaMalloc(&p->d_mtx, (size_t)(3 * 3 + 2) * kmax * ncol * sizeof(double));
   if (e != cudaSuccess) {
     set_cuda_error(e);
     delete p;
@@ -354,6 +367,11 @@ extern "C" int dccm_implcpl_forward_dev(dccm_implcpl *p, const dccm_implcpl_forw
   f.CpDry = p->k.CpDry;
   f.GasR = p->k.GasRDry;
   f.inv_g2dt = 1.0 / (p->k.Grav * (2.0 * p->k.DelTime));
+  f.G = p->d_mtx + 3 * mstride(p);
+  f.IEF = f.G + (size_t)p->kmax * p->ncol;
+  const long long nk = (long long)p->ncol * p->kmax;
+  implcpl::geo_kernel<<<(unsigned)((nk + 255) / 256), 256, 0, as_stream(stream)>>>(f);
+  DCCM_LAUNCH_CHECK();
   const int threads = 128;
   implcpl::forward_kernel<<<dim3((unsigned)((p->ncol + threads - 1) / threads), 2 + p->ncmax), threads, 0,
                             as_stream(stream)>>>(f);
@@ -380,6 +398,14 @@ extern "C" int dccm_implcpl_backward_dev(dccm_implcpl *p, double *xyz_DUDt, doub
   implcpl::backward_kernel<<<dim3((unsigned)((p->ncol + threads - 1) / threads), 3), threads, 0,
                              as_stream(stream)>>>(b);
   DCCM_LAUNCH_CHECK();
+  return DCCM_OK;
+}
+
+extern "C" int dccm_implcpl_info(const dccm_implcpl *p, int *ncol, int *kmax, int *ncmax) {
+  if (!p) return DCCM_ERR_INVALID_ARG;
+  if (ncol) *ncol = (int)p->ncol;
+  if (kmax) *kmax = p->kmax;
+  if (ncmax) *ncmax = p->ncmax;
   return DCCM_OK;
 }
 

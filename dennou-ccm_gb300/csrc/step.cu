@@ -43,7 +43,8 @@ struct dccm_step {
   std::vector<const double *> ens_spec_in;
   std::vector<double *> ens_grid, ens_spec_out;
   std::vector<int> ens_nfl;
-  std::vector<dccm_step_remap> remaps;
+  std::vector<dccm_step_remap> remaps, remaps_post;
+  dccm_implcpl_forward_args icf;  // the implicit coupling's arrays (d.implcpl non-NULL)
   dccm_sfc_bulk_flux_args flux;
   dccm_sfc_grid fgrid;
   double sig1[2];
@@ -157,16 +158,27 @@ static int stage_sht_fwd(dccm_step *st, cudaStream_t s) {
   DCCM_TRY(stage_fft_fwd(st, s));
   return stage_leg_fwd(st, s);
 }
-static int stage_remap(dccm_step *st, cudaStream_t s) {
-  for (const dccm_step_remap &r : st->remaps)
+static int run_remaps(const std::vector<dccm_step_remap> &v, cudaStream_t s) {
+  for (const dccm_step_remap &r : v)
     if (r.plan && r.nfields > 0)
       DCCM_TRY(remap::apply2(r.plan, r.src, r.ld_src, r.dst, r.ld_dst, r.nfields, r.nsub, r.ld_dst2, s));
   return DCCM_OK;
 }
+// The surface branch: [implicit coupling forward sweep], remaps, flux,
+// [remaps after the flux, backward sweep].  Stage "remap" holds the first
+// two, stage "flux" the rest.
+static int stage_remap(dccm_step *st, cudaStream_t s) {
+  if (st->d.implcpl) DCCM_TRY(dccm_implcpl_forward_dev(st->d.implcpl, &st->icf, (void *)s));
+  return run_remaps(st->remaps, s);
+}
 extern "C" int dccm_sfc_bulk_flux_get_dev(const dccm_sfc_bulk_flux_args *, const dccm_sfc_grid *, void *);
 static int stage_flux(dccm_step *st, cudaStream_t s) {
-  if (!st->d.flux) return DCCM_OK;
-  return dccm_sfc_bulk_flux_get_dev(&st->flux, &st->fgrid, (void *)s);
+  if (st->d.flux) DCCM_TRY(dccm_sfc_bulk_flux_get_dev(&st->flux, &st->fgrid, (void *)s));
+  DCCM_TRY(run_remaps(st->remaps_post, s));
+  if (st->d.implcpl)
+    DCCM_TRY(dccm_implcpl_backward_dev(st->d.implcpl, st->icf.xyz_DUDt, st->icf.xyz_DVDt, st->icf.xyz_DTempDt,
+                                       st->icf.xyzf_DQMixDt, (void *)s));
+  return DCCM_OK;
 }
 
 // Host copies of dccm_step_run_host, sorted by the buffers they touch into
@@ -515,6 +527,11 @@ extern "C" int dccm_step_create(const dccm_step_desc *d, dccm_step **out) {
     if (d->remaps[k].plan && d->remaps[k].nfields > 0 && (!d->remaps[k].src || !d->remaps[k].dst))
       return DCCM_ERR_INVALID_ARG;
   if (d->flux && (!d->flux_grid || !d->flux->a_Sig1Info)) return DCCM_ERR_INVALID_ARG;
+  if (d->implcpl && !d->implcpl_fwd) return DCCM_ERR_INVALID_ARG;
+  if (d->nremap_post < 0 || (d->nremap_post > 0 && !d->remaps_post)) return DCCM_ERR_INVALID_ARG;
+  for (int k = 0; k < d->nremap_post; ++k)
+    if (d->remaps_post[k].plan && d->remaps_post[k].nfields > 0 && (!d->remaps_post[k].src || !d->remaps_post[k].dst))
+      return DCCM_ERR_INVALID_ARG;
   dccm_step *st = new (std::nothrow) dccm_step();
   if (!st) return DCCM_ERR_NOMEM;
   st->d = *d;
@@ -528,6 +545,10 @@ extern "C" int dccm_step_create(const dccm_step_desc *d, dccm_step **out) {
   }
   st->remaps.assign(d->remaps, d->remaps + d->nremap);
   st->d.remaps = nullptr;
+  if (d->nremap_post > 0) st->remaps_post.assign(d->remaps_post, d->remaps_post + d->nremap_post);
+  st->d.remaps_post = nullptr;
+  if (d->implcpl) st->icf = *d->implcpl_fwd;
+  st->d.implcpl_fwd = nullptr;
   if (d->flux) {
     st->flux = *d->flux;
     st->fgrid = *d->flux_grid;
@@ -624,7 +645,9 @@ static void sort_copies(dccm_step *st, const dccm_host_copy *h2d, int nh2d, cons
     add_span(sht_grid, G.grid[g], (size_t)G.nfl[g] * P.J * P.I * sizeof(double));
     add_span(sht_out, G.spec_out[g], (size_t)G.nfl[g] * P.ncoef * 2 * sizeof(double));
   }
-  for (const dccm_step_remap &r : st->remaps) {
+  std::vector<dccm_step_remap> all_remaps(st->remaps);
+  all_remaps.insert(all_remaps.end(), st->remaps_post.begin(), st->remaps_post.end());
+  for (const dccm_step_remap &r : all_remaps) {
     if (!r.plan || r.nfields <= 0) continue;
     int64_t nnz = 0, ns = 0, nr = 0;
     dccm_remap_plan_info(r.plan, &nnz, &ns, &nr);
@@ -653,6 +676,24 @@ static void sort_copies(dccm_step *st, const dccm_host_copy *h2d, int nh2d, cons
                           (const void *)f.QVap1, (const void *)f.SDwRFlx, (const void *)f.LDwRFlx,
                           (const void *)f.SIceCon, (const void *)f.SfcHeight, (const void *)f.SfcPress})
       add_span(sfc, p, n);
+  }
+  if (st->d.implcpl) {  // the implicit coupling's arrays belong to the surface branch
+    int nc = 0, K = 0, ncm = 0;
+    dccm_implcpl_info(st->d.implcpl, &nc, &K, &ncm);
+    const dccm_implcpl_forward_args &a = st->icf;
+    const size_t h = (size_t)(K + 1) * nc * sizeof(double), f = (size_t)K * nc * sizeof(double);
+    for (const void *p : {(const void *)a.xyr_MomFluxX, (const void *)a.xyr_MomFluxY, (const void *)a.xyr_HeatFlux,
+                          (const void *)a.xyr_Press, (const void *)a.xyr_Exner, (const void *)a.xyr_VirTemp,
+                          (const void *)a.xyr_VelDiffCoef, (const void *)a.xyr_TempDiffCoef,
+                          (const void *)a.xyr_QMixDiffCoef})
+      add_span(sfc, p, h);
+    add_span(sfc, a.xyrf_QMixFlux, ncm * h);
+    for (const void *p : {(const void *)a.xyz_Exner, (const void *)a.xyz_Height, (const void *)a.xyz_DUDt,
+                          (const void *)a.xyz_DVDt, (const void *)a.xyz_DTempDt})
+      add_span(sfc, p, f);
+    add_span(sfc, a.xyzf_DQMixDt, ncm * f);
+    add_span(sfc, a.xya_ImplCplCoef1, 4 * (size_t)nc * sizeof(double));
+    add_span(sfc, a.xya_ImplCplCoef2, 4 * (size_t)nc * sizeof(double));
   }
   for (int k = 0; k < nh2d; ++k) {
     const dccm_host_copy &c = h2d[k];
@@ -817,6 +858,16 @@ static std::string step_key(dccm_step *st) {
   }
   if (st->d.flux) {
     snprintf(buf, sizeof buf, "|f%dx%d", st->fgrid.IE - st->fgrid.IS + 1, st->fgrid.JE - st->fgrid.JS + 1);
+    k += buf;
+  }
+  for (const dccm_step_remap &r : st->remaps_post) {
+    snprintf(buf, sizeof buf, "|q%d", r.nfields);
+    k += buf;
+  }
+  if (st->d.implcpl) {
+    int nc = 0, K = 0, ncm = 0;
+    dccm_implcpl_info(st->d.implcpl, &nc, &K, &ncm);
+    snprintf(buf, sizeof buf, "|i%dx%dx%d", nc, K, ncm);
     k += buf;
   }
   return k;

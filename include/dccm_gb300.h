@@ -150,6 +150,8 @@ int dccm_implcpl_backward_dev(dccm_implcpl *plan, double *xyz_DUDt, double *xyz_
                               double *xyz_DTempDt, double *xyzf_DQMixDt, void *stream);
 /* Copies the module-state matrices out, each (ncol, kmax, -1:1); NULL skips one. */
 int dccm_implcpl_matrices(dccm_implcpl *plan, double *uv, double *temp, double *qmix);
+/* The plan's shape (any pointer may be NULL). */
+int dccm_implcpl_info(const dccm_implcpl *plan, int *ncol, int *kmax, int *ncmax);
 
 /* =====================================================================
  * Jones-99 remap table
@@ -392,6 +394,17 @@ typedef struct dccm_step_desc {
   const dccm_step_remap *remaps;
   const dccm_sfc_bulk_flux_args *flux;  /* device arrays, or NULL */
   const dccm_sfc_grid *flux_grid;
+  /* Implicit surface coupling around the flux (NULL: none).  The surface
+   * branch then runs: the forward sweep (implcpl_fwd's arrays; it writes
+   * ImplCplCoef1/2, which `remaps` carry to the flux grid), the remaps,
+   * the flux, the remaps_post (e.g. DelVarImplCPL back to level 1 of the
+   * tendencies, as the coupler does at atm/dccm_atm_mod.f90:832-835), and
+   * the backward sweep on implcpl_fwd's tendencies.  Append-only fields: a
+   * caller that zero-initialises the descriptor keeps the plain step. */
+  dccm_implcpl *implcpl;
+  const dccm_implcpl_forward_args *implcpl_fwd;  /* device arrays */
+  int nremap_post;
+  const dccm_step_remap *remaps_post;
 } dccm_step_desc;
 
 typedef struct dccm_step dccm_step;

@@ -217,3 +217,40 @@ def test_fp64_peak_probe(dccm, cuda):
     import bench
     t = dccm.fp64_peak()
     assert 0.25 * bench.FP64_NOMINAL_TFLOPS < t < 1.5 * bench.FP64_NOMINAL_TFLOPS, t
+
+
+def test_coupled_step_matches_pieces(dccm, oracle, synth, cuda):
+    """The step with the implicit coupling around the flux (forward sweep,
+    remaps including ImplCplCoef1/2, flux, DelVarImplCPL back onto level 1
+    of the tendencies, backward sweep) gives bit for bit what the same
+    calls give one by one."""
+    torch = cuda
+    bench, w, inp, S = _small_step(dccm, synth, oracle, torch, 1)
+    C = bench.coupled_setup(S, w, inp, dccm, synth, torch, torch.device("cuda", 0))
+    df, out = S["dflux"], C["out"]
+    names = list(dccm.FLUX_OUT) + ["ImplCplCoef1", "ImplCplCoef2"]
+    C["step"].run()
+    torch.cuda.synchronize()
+    want = {k: v.clone() for k, v in out.items()}
+    want_f = {n: df[n].clone() for n in names}
+    want_s = S["spec_out"][0].clone()
+    assert float(df["DelVarImplCPL"].abs().max()) > 0 and bool(torch.isfinite(want["DTempDt"][1:]).all())
+    # one by one
+    for v in out.values():
+        v.zero_()
+    for n in names:
+        df[n].zero_()
+    torch.cuda.synchronize()
+    C["plan"].forward_dev(C["prof"], out)
+    for plan, nf, src, lds, dst, ldd in C["coef"]:
+        plan.apply_dev(src, lds, dst, ldd, nf)
+    S["steps"]["mixed"].run()
+    for plan, nf, src, lds, dst, ldd in C["post"]:
+        plan.apply_dev(src, lds, dst, ldd, nf)
+    C["plan"].backward_dev(out)
+    torch.cuda.synchronize()
+    for k in out:
+        assert torch.equal(out[k], want[k]), k
+    for n in names:
+        assert torch.equal(df[n], want_f[n]), n
+    assert torch.equal(S["spec_out"][0], want_s)
