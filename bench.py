@@ -446,8 +446,9 @@ FP64_FLOPS = {"c3": (20.948747 + 41.897494 + 2 * 114.69439) * 86836.697368}
 # FP64 flops of the implicit-coupling sweeps per column and level, one
 # tracer (DADD + DMUL + 2 DFMA thread instructions per cycle x elapsed
 # cycles, ncu, 32768 columns x 32 levels; profiles/implcpl_c3_ncu.md):
-# 4932 per 32-level column forward, 1430 backward.
-IMPLCPL_FP64_FLOPS = {"forward": 4932 / 32, "backward": 1430 / 32}
+# per 32-level column forward 3915 (shared factors 878 + elimination 3037),
+# backward 1430.
+IMPLCPL_FP64_FLOPS = {"forward": 3915 / 32, "backward": 1430 / 32}
 
 
 def dccm_stages():
