@@ -423,7 +423,9 @@ int dccm_step_run(dccm_step *step, void *stream);
 /* Runs the stages one after another on stream with events between them and
  * returns their device times: ms[0] Legendre synthesis, ms[1] inverse FFT,
  * ms[2] forward FFT, ms[3] Legendre analysis, ms[4] remaps, ms[5] bulk
- * flux (six floats).  Synchronises. */
+ * flux (six floats; with the implicit coupling, ms[4] includes its
+ * forward sweep and ms[5] the remaps after the flux and the backward
+ * sweep).  Synchronises. */
 int dccm_step_run_timed(dccm_step *step, void *stream, float *ms);
 /* Copies nh2d host buffers to the device, runs the step, copies nd2h device
  * buffers back and synchronises: the step for a caller whose data live in
