@@ -425,12 +425,20 @@ def roofline(S, inp, groups, stage_ms, workload, fp64_peak):
                             "algorithmic_flops": fl}
         stages[n] = st
     stages["bulk_flux"]["limiter"] = "FP64 pipe, not HBM"
-    f64 = FP64_FLOPS.get(workload)
+    f64 = FLUX_FP64_FLOPS_PER_COLUMN * S["ncol"]
     if f64:
         tf = f64 / (stages["bulk_flux"]["ms"] / 1e3) / 1e12
         stages["bulk_flux"]["fp64"] = {"achieved": tf, "unit": "TFLOP/s", "peak": fp64_peak,
                                        "peak_source": "measured (dccm_fp64_peak)", "frac": tf / fp64_peak,
                                        "flops_per_launch": f64}
+    # the remap keeps the reference's separately rounded products and sums
+    # (bit-exact): one DMUL and one DADD per table entry and field
+    rf = sum(2.0 * len(t[2]) * 6 * len(g.members) for g, t in zip(groups, S["tables"]))
+    tf = rf / (stages["remap"]["ms"] / 1e3) / 1e12
+    stages["remap"]["fp64"] = {"achieved": tf, "unit": "TFLOP/s", "peak": fp64_peak,
+                               "peak_source": "measured (dccm_fp64_peak)", "frac": tf / fp64_peak,
+                               "flops_per_launch": rf}
+    stages["remap"]["limiter"] = "FP64 pipe (unfused products and sums), not HBM"
     dom = names[int(np.argmax(stage_ms))]
     roof = dict(stages[dom])
     roof.update({"kernel": dom, "peak_source": src_peak, "stages": stages,
@@ -438,9 +446,12 @@ def roofline(S, inp, groups, stage_ms, workload, fp64_peak):
     return roof
 
 
-# FP64 flops per launch of the flux kernel (DADD + DMUL + 2 DFMA thread
-# instructions, ncu sass counters), summarised in profiles/stages_c3_ncu.md.
-FP64_FLOPS = {"c3": (20.948747 + 41.897494 + 2 * 114.69439) * 86836.697368}
+# FP64 flops of the flux kernel per ocean column (DADD + DMUL + 2 DFMA
+# thread instructions per cycle x elapsed cycles, ncu sass counters, c3:
+# 25.4 M flops for 45,478 columns, profiles/stages_c3_ncu.md).  Every
+# column does the same work when there is no sea ice (all workloads here:
+# the ice physics is skipped where SIceCon = 0).
+FLUX_FP64_FLOPS_PER_COLUMN = (20.948747 + 41.897494 + 2 * 114.69439) * 86836.697368 / 45478
 
 
 # FP64 flops of the implicit-coupling sweeps per column and level, one

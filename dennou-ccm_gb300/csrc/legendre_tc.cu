@@ -40,7 +40,8 @@ namespace sht {
 
 constexpr int TC_THREADS = 192;
 constexpr int A_SPLIT_BYTES = 128 * 128;     // 128 rows (c) x 64 bf16 (K)
-constexpr int B_SPLIT_BYTES = 128 * 128;     // 128 rows (N) x 64 bf16 (K)
+constexpr int B_SPLIT_BYTES = 128 * 128;     // 128 rows (N) x 64 bf16 (K); a table whose N tiles all fit
+                                              // 64 rows loads boxes of 64 rows (half) into the same slot
 constexpr int STAGE_BYTES = 3 * A_SPLIT_BYTES + 3 * B_SPLIT_BYTES;  // 96 KB
 constexpr int NSTAGE = 2;
 constexpr int TMEM_COLS = 512;
@@ -58,6 +59,7 @@ struct TcArgs {
   int dir;  // 0 inverse, 1 forward
   int N, Jh, batch;
   int ntmax;  // TMEM columns per accumulator (64 or 128)
+  int brows;  // rows of this group's B boxes (64 or 128)
   int nacc;   // accumulator sets in TMEM (2: double buffered, 1)
   long long ncoef;
   const MInfo *mi;
@@ -244,7 +246,7 @@ legendre_tc_kernel(const __grid_constant__ TcLaunch L) {
             if (!mbar_wait(&empty[s], ((g / NSTAGE) & 1) ^ 1, a.err, abort_flag, 1)) { ok = false; break; }
             unsigned char *As = stage + s * STAGE_BYTES;
             unsigned char *Bs = As + 3 * A_SPLIT_BYTES;
-            mbar_arrive_tx(&full[s], (uint32_t)(a.nsplit * (A_SPLIT_BYTES + B_SPLIT_BYTES)));
+            mbar_arrive_tx(&full[s], (uint32_t)(a.nsplit * (A_SPLIT_BYTES + a.brows * 128)));
             for (int sp = 0; sp < a.nsplit; ++sp) {
               unsigned char *Ad = As + sp * A_SPLIT_BYTES;
               if (a.dir == 0) {
@@ -734,10 +736,13 @@ static int build_one(Plan &P, int dir, TileTable &T) {
   }
   DCCM_CUDA(cudaDeviceSynchronize());
   cudaFree(drs);
-  {
+  int nrmax = 16;
+  for (const MInfo &M : meta.mi) nrmax = M.nr > nrmax ? M.nr : nrmax;
+  T.ntmax = nrmax <= 64 ? 64 : 128;
+  {  // B boxes of ntmax rows: every N tile of an ntmax = 64 table fits 64
     const cuuint64_t dims[2] = {64, (cuuint64_t)meta.rows};
     const cuuint64_t str[1] = {128};
-    const cuuint32_t box[2] = {64, 128};
+    const cuuint32_t box[2] = {64, (cuuint32_t)T.ntmax};
     DCCM_TRY(encode_bf16(&T.map, T.d, 2, dims, str, box, P.nsplit == 2));
   }
   const cuuint64_t ns = (cuuint64_t)P.nsplit;
@@ -755,9 +760,6 @@ static int build_one(Plan &P, int dir, TileTable &T) {
   }
   T.map_ok = true;
   T.items_per_ct = (int)meta.items.size();
-  int nrmax = 16;
-  for (const MInfo &M : meta.mi) nrmax = M.nr > nrmax ? M.nr : nrmax;
-  T.ntmax = nrmax <= 64 ? 64 : 128;
   return DCCM_OK;
 }
 
@@ -836,6 +838,7 @@ int legendre_tc_multi(Plan *const *plans, const int *batch, const void *const *i
     a.items = T.d_items;
     a.err = plans[0]->d_err;
     a.ntmax = ntmax;
+    a.brows = T.ntmax;
     a.nacc = 8 * ntmax <= TMEM_COLS ? 2 : 1;
     a.nsplit = P.nsplit;
     a.cexp = dir == 0 ? P.d_cexp : P.d_cexp + P.max_batch;
