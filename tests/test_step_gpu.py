@@ -49,7 +49,7 @@ def test_step_outputs_match_oracle(dccm, oracle, synth, cuda):
     torch = cuda
     bench, w, inp, S = _small_step(dccm, synth, oracle, torch, 1)
     g = inp["groups"][0]
-    for key, tol in (("mixed", 1e-6), ("fp64", 1e-13)):
+    for key, tol in (("mixed", 1e-6), ("fp16", 1e-6), ("fp64", 1e-13)):
         S["steps"][key].run()
         torch.cuda.synchronize()
         go = oracle.sht_inverse(g.N, g.I, g.J, g.spec)
@@ -254,3 +254,22 @@ def test_coupled_step_matches_pieces(dccm, oracle, synth, cuda):
     for n in names:
         assert torch.equal(df[n], want_f[n]), n
     assert torch.equal(S["spec_out"][0], want_s)
+    # through run_host: the atmosphere's profiles in and the tendencies and
+    # coefficients out go with the surface branch (page-locked buffers)
+    step = C["step"]
+    h2d = [(v.cpu().pin_memory(), v) for v in C["prof"].values()]
+    d2h = [(torch.empty(v.shape, dtype=v.dtype).pin_memory(), v) for v in out.values()]
+    for v in out.values():
+        v.zero_()
+    for _, d in h2d:
+        d.zero_()
+    torch.cuda.synchronize()
+    for order in (1, 2):
+        dccm.tune_set("upload_order", order)
+        try:
+            step.host_release()
+            step.run_host(h2d, d2h)
+        finally:
+            dccm.tune_set("upload_order", 0)
+        for (h, _), k in zip(d2h, out):
+            assert torch.equal(h, want[k].cpu()), (order, k)
