@@ -145,8 +145,9 @@ __device__ __forceinline__ void mma_commit(uint64_t *bar) {
                    smem_u32(bar))
                : "memory");
 }
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
-  uint32_t r[16];
+// 16 consecutive TMEM columns of this thread's lane into registers, without
+// waiting: several loads are issued, then one tmem_wait_ld before use.
+__device__ __forceinline__ void tmem_ld16_nw(uint32_t taddr, uint32_t (&r)[16]) {
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
       "[%16];"
@@ -154,10 +155,8 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
         "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
         "=r"(r[15])
       : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 // FP64 split used once per table entry at plan creation.
 __device__ __forceinline__ void split3(double x, __nv_bfloat16 &h, __nv_bfloat16 &m, __nv_bfloat16 &l) {
@@ -350,19 +349,20 @@ legendre_tc_kernel(const __grid_constant__ TcLaunch L) {
         const int J = 2 * a.Jh;
         const bool odd = mi.kv1 > 0;
         for (int j0 = 0; j0 < nrow; j0 += 16) {
-          float e[16], o[16], x[16];
-          tmem_ld16(tbase + j0, e);
-          tmem_ld16(tbase + NT + j0, x);
-#pragma unroll
-          for (int i = 0; i < 16; ++i) e[i] += x[i];
+          // the four accumulators' columns j0..j0+15, one wait for all
+          uint32_t re[16], rx[16], ro[16], ry[16];
+          tmem_ld16_nw(tbase + j0, re);
+          tmem_ld16_nw(tbase + NT + j0, rx);
           if (odd) {
-            tmem_ld16(tbase + 2 * NT + j0, o);
-            tmem_ld16(tbase + 3 * NT + j0, x);
+            tmem_ld16_nw(tbase + 2 * NT + j0, ro);
+            tmem_ld16_nw(tbase + 3 * NT + j0, ry);
+          }
+          tmem_wait_ld();
+          float e[16], o[16];
 #pragma unroll
-            for (int i = 0; i < 16; ++i) o[i] += x[i];
-          } else {
-#pragma unroll
-            for (int i = 0; i < 16; ++i) o[i] = 0.f;
+          for (int i = 0; i < 16; ++i) {
+            e[i] = __uint_as_float(re[i]) + __uint_as_float(rx[i]);
+            o[i] = odd ? __uint_as_float(ro[i]) + __uint_as_float(ry[i]) : 0.f;
           }
           if (c < C2B) {
 #pragma unroll
@@ -380,9 +380,16 @@ legendre_tc_kernel(const __grid_constant__ TcLaunch L) {
           const int nv = p ? mi.nv1 : mi.nv0;
           for (int k0 = 0; k0 < nrow; k0 += 16) {
             if (nt * 128 + k0 >= nv) break;  // uniform across the warp
+            uint32_t rd[16], rx[16];
+            tmem_ld16_nw(tbase + (p * 2) * NT + k0, rd);
+            tmem_ld16_nw(tbase + (p * 2 + 1) * NT + k0, rx);
+            tmem_wait_ld();
             float d[16], x[16];
-            tmem_ld16(tbase + (p * 2) * NT + k0, d);
-            tmem_ld16(tbase + (p * 2 + 1) * NT + k0, x);
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+              d[i] = __uint_as_float(rd[i]);
+              x[i] = __uint_as_float(rx[i]);
+            }
             if (c < C2B) {
 #pragma unroll
               for (int i = 0; i < 16; ++i) {
