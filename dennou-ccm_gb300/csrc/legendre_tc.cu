@@ -60,6 +60,7 @@ struct TcArgs {
   int N, Jh, batch;
   int ntmax;  // TMEM columns per accumulator (64 or 128)
   int brows;  // rows of this group's B boxes (64 or 128)
+  int nct;    // 128-column tiles of this launch's batch
   int nacc;   // accumulator sets in TMEM (2: double buffered, 1)
   long long ncoef;
   const MInfo *mi;
@@ -180,7 +181,16 @@ struct TcLaunch {
 };
 
 // Work item it -> group and (m, ct, nt); items of a group are ordered
-// (ct, m, nt), heavy (small m) first within ct.
+// (m, nt, ct), heavy (small m) first, the column tiles ct of one (m, nt)
+// consecutive: CTAs that run at the same time share the (m, nt) table tile
+// (and the (ct, m) operand tile) in L2 instead of each fetching it from
+// DRAM (a T341 table is larger than L2).
+__device__ __forceinline__ void item_of(const TcArgs &a, int li, int &m, int &ct, int &nt) {
+  const int4 w = a.items[li / a.nct];
+  m = w.x;
+  nt = w.z;
+  ct = li % a.nct;
+}
 __device__ __forceinline__ int group_of(const TcLaunch &L, int it) {
   int gi = 0;
   while (gi + 1 < L.ngroups && it >= L.start[gi + 1]) ++gi;
@@ -233,8 +243,8 @@ legendre_tc_kernel(const __grid_constant__ TcLaunch L) {
       for (int it = blockIdx.x; it < nitems && ok; it += gridDim.x) {
         const int gi = group_of(L, it);
         const TcArgs &a = L.g[gi];
-        const int4 w = a.items[it - L.start[gi]];
-        const int m = w.x, ct = w.y, nt = w.z;
+        int m, ct, nt;
+        item_of(a, it - L.start[gi], m, ct, nt);
         const MInfo mi = a.mi[m];
         for (int p = 0; p < 2 && ok; ++p) {
           const int kv = p ? mi.kv1 : mi.kv0;
@@ -270,8 +280,8 @@ legendre_tc_kernel(const __grid_constant__ TcLaunch L) {
       for (int it = blockIdx.x; it < nitems && ok; it += gridDim.x, ++li) {
         const int gi = group_of(L, it);
         const TcArgs &a = L.g[gi];
-        const int4 w = a.items[it - L.start[gi]];
-        const int m = w.x, nt = w.z;
+        int m, ct, nt;
+        item_of(a, it - L.start[gi], m, ct, nt);
         const MInfo mi = a.mi[m];
         const int nrow = min(128, mi.nr - nt * 128);
         const int amn = a.dir;  // forward A is MN-major
@@ -329,8 +339,8 @@ legendre_tc_kernel(const __grid_constant__ TcLaunch L) {
     for (int it = blockIdx.x; it < nitems; it += gridDim.x, ++li) {
       const int gi = group_of(L, it);
       const TcArgs &a = L.g[gi];
-      const int4 w = a.items[it - L.start[gi]];
-      const int m = w.x, ct = w.y, nt = w.z;
+      int m, ct, nt;
+      item_of(a, it - L.start[gi], m, ct, nt);
       const int C2B = 2 * a.batch;
       const MInfo mi = a.mi[m];
       const int nrow = min(128, mi.nr - nt * 128);
@@ -727,12 +737,9 @@ static int build_one(Plan &P, int dir, TileTable &T) {
   DCCM_CUDA(cudaMemcpy(dmi, meta.mi.data(), meta.mi.size() * sizeof(MInfo), cudaMemcpyHostToDevice));
   DCCM_CUDA(cudaMemcpy(drs, meta.rowstart.data(), meta.rowstart.size() * sizeof(long long),
                        cudaMemcpyHostToDevice));
-  // Work items of every 128-column block of the largest batch, block-major.
-  const int nct = (2 * P.max_batch + 127) / 128;
-  std::vector<int4> items;
-  items.reserve((size_t)nct * meta.items.size());
-  for (int ct = 0; ct < nct; ++ct)
-    for (int4 w : meta.items) items.push_back(make_int4(w.x, ct, w.z, 0));
+  // Work items (m, -, nt) of one 128-column block, heavy (small m) first;
+  // a launch runs each of them for every column block of its batch.
+  const std::vector<int4> &items = meta.items;
   DCCM_CUDA(cudaMalloc(&T.d_items, items.size() * sizeof(int4)));
   DCCM_CUDA(cudaMemcpy(T.d_items, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice));
   const long long nthr = meta.rows0 * 8;
@@ -854,7 +861,8 @@ int legendre_tc_multi(Plan *const *plans, const int *batch, const void *const *i
     L.map[ng] = T.map;
     L.amap[ng] = T.amap;
     L.start[ng] = items;
-    items += ((2 * a.batch + 127) / 128) * T.items_per_ct;
+    a.nct = (2 * a.batch + 127) / 128;
+    items += a.nct * T.items_per_ct;
     ++ng;
   }
   L.start[ng] = items;
