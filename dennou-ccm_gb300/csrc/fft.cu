@@ -257,13 +257,30 @@ __device__ __forceinline__ void stage_fourier(const FftGroup &G, int jn, int js,
   const long long C2B = 2LL * G.batch;
   const float *F = static_cast<const float *>(G.in);
   const int tot = (G.N + 1) << (lcw + 1);  // (m, row, c), c fastest
-  for (int t = threadIdx.x; t < tot; t += blockDim.x) {
-    const int c = t & ((1 << lcw) - 1);
-    const int row = (t >> lcw) & 1;
-    const int m = t >> (lcw + 1);
-    float v = 0.f;
-    if (c < 2 * nb) v = F[((long long)m * G.J + (row ? js : jn)) * C2B + 2LL * b0 + c];
-    st[(((row * 2 + (c & 1)) << lbb) + (c >> 1)) * PS + slot_of<R>(m)] = v;
+  // four elements a thread per round: their global loads are all in flight
+  // before the first shared store
+  constexpr int U = 4;
+  for (int t0 = threadIdx.x; t0 < tot; t0 += U * blockDim.x) {
+    float v[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int t = t0 + u * blockDim.x;
+      const int c = t & ((1 << lcw) - 1);
+      const int row = (t >> lcw) & 1;
+      const int m = t >> (lcw + 1);
+      v[u] = 0.f;
+      if (t < tot && c < 2 * nb) v[u] = F[((long long)m * G.J + (row ? js : jn)) * C2B + 2LL * b0 + c];
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int t = t0 + u * blockDim.x;
+      if (t < tot) {
+        const int c = t & ((1 << lcw) - 1);
+        const int row = (t >> lcw) & 1;
+        const int m = t >> (lcw + 1);
+        st[(((row * 2 + (c & 1)) << lbb) + (c >> 1)) * PS + slot_of<R>(m)] = v[u];
+      }
+    }
   }
 }
 
@@ -381,9 +398,16 @@ __device__ __forceinline__ void fft_fwd_block(const FftGroup &G, int jj, int by,
   for (int bl = warp; bl < nb; bl += nw) {
     const double *gn = static_cast<const double *>(G.in) + ((long long)(b0 + bl) * J + jn) * I;
     const double *gs = static_cast<const double *>(G.in) + ((long long)(b0 + bl) * J + js) * I;
+    // all 2R loads of the row pair first, then the conversions
+    double xn[R], xs[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      xn[r] = gn[32 * r + lane];
+      xs[r] = gs[32 * r + lane];
+    }
     float2 v[R];
 #pragma unroll
-    for (int r = 0; r < R; ++r) v[r] = make_float2(f64_to_f32_rn(gn[32 * r + lane]), f64_to_f32_rn(gs[32 * r + lane]));
+    for (int r = 0; r < R; ++r) v[r] = make_float2(f64_to_f32_rn(xn[r]), f64_to_f32_rn(xs[r]));
     warp_fft_fwd<R>(v, G.tw, G.twl, w, lane);
 #pragma unroll
     for (int k1 = 0; k1 < R; ++k1) {
@@ -485,8 +509,14 @@ __device__ __forceinline__ void fft_fwd_block_mw(const FftGroup &G, int jj, int 
   if (bl < nb) {
     const double *gn = static_cast<const double *>(G.in) + ((long long)(b0 + bl) * J + jn) * I;
     const double *gs = static_cast<const double *>(G.in) + ((long long)(b0 + bl) * J + js) * I;
+    double xn[MW_R0], xs[MW_R0];  // all loads first, then the conversions
 #pragma unroll
-    for (int r = 0; r < MW_R0; ++r) v[r] = make_float2(f64_to_f32_rn(gn[L * r + t]), f64_to_f32_rn(gs[L * r + t]));
+    for (int r = 0; r < MW_R0; ++r) {
+      xn[r] = gn[L * r + t];
+      xs[r] = gs[L * r + t];
+    }
+#pragma unroll
+    for (int r = 0; r < MW_R0; ++r) v[r] = make_float2(f64_to_f32_rn(xn[r]), f64_to_f32_rn(xs[r]));
   } else {
 #pragma unroll
     for (int r = 0; r < MW_R0; ++r) v[r] = make_float2(0.f, 0.f);
@@ -558,7 +588,7 @@ __device__ __forceinline__ void dispatch_case(const FftGroup &G, int jj, int by,
 
 // Up to 16 warps (512 threads) per CTA.
 template <int RMAX, bool FWD>
-__global__ void __launch_bounds__(512) fft_multi_kernel(const __grid_constant__ FftLaunch L) {
+__global__ void __launch_bounds__(512, 2) fft_multi_kernel(const __grid_constant__ FftLaunch L) {
   extern __shared__ __align__(16) float st[];
   pdl_wait();  // reads the previous kernel's output; the forward FFT overwrites the buffer it read
   pdl_trigger();
