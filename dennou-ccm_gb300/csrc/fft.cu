@@ -258,7 +258,7 @@ __device__ __forceinline__ void stage_fourier(const FftGroup &G, int jn, int js,
   const float *F = static_cast<const float *>(G.in);
   const int tot = (G.N + 1) << (lcw + 1);  // (m, row, c), c fastest
   // four elements a thread per round: their global loads are all in flight
-  // before the first shared store
+  // before the first shared store (eight measured slower at T341)
   constexpr int U = 4;
   for (int t0 = threadIdx.x; t0 < tot; t0 += U * blockDim.x) {
     float v[U];

@@ -472,20 +472,33 @@ __global__ void __launch_bounds__(256) pack_spectra_kernel(const __grid_constant
     }
     return;
   }
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < G.ncoef;
-       i += (long long)gridDim.x * blockDim.x) {
-    const double2 v = __ldg(src + i);
-    const int x = __ldg(G.xpos + i);
-    unsigned short h0, m0, l0, h1, m1, l1;
-    split3f_bits(f64_to_f32_rn(v.x), h0, m0, l0);
-    split3f_bits(f64_to_f32_rn(v.y), h1, m1, l1);
-    unsigned short *o = dst + x;
-    o[0] = h0;
-    o[G.KX] = h1;
-    o[plane] = m0;
-    o[plane + G.KX] = m1;
-    o[2 * plane] = l0;
-    o[2 * plane + G.KX] = l1;
+  // two coefficients a thread per round, both loads in flight together
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i0 = blockIdx.x * (long long)blockDim.x + threadIdx.x; i0 < G.ncoef; i0 += 2 * stride) {
+    double2 v[2];
+    int x[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const long long i = i0 + u * stride;
+      if (i < G.ncoef) {
+        v[u] = __ldg(src + i);
+        x[u] = __ldg(G.xpos + i);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      if (i0 + u * stride >= G.ncoef) break;
+      unsigned short h0, m0, l0, h1, m1, l1;
+      split3f_bits(f64_to_f32_rn(v[u].x), h0, m0, l0);
+      split3f_bits(f64_to_f32_rn(v[u].y), h1, m1, l1);
+      unsigned short *o = dst + x[u];
+      o[0] = h0;
+      o[G.KX] = h1;
+      o[plane] = m0;
+      o[plane + G.KX] = m1;
+      o[2 * plane] = l0;
+      o[2 * plane + G.KX] = l1;
+    }
   }
 }
 
@@ -546,7 +559,7 @@ int pack_spectra(Plan *const *plans, const int *batch, const double *const *spec
   L.ngroups = ng;
   if (nf == 0) return DCCM_OK;
   if (nf > 65535) return DCCM_ERR_UNSUPPORTED;
-  long long bx = (maxc + 255) / 256;
+  long long bx = (maxc + 511) / 512;  // two coefficients a thread
   if (bx > 64) bx = 64;
   DCCM_CUDA(launch_pdl(pack_spectra_kernel, dim3((unsigned)bx, (unsigned)nf), dim3(256), 0, s, L));
   return DCCM_OK;
