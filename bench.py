@@ -432,13 +432,14 @@ def roofline(S, inp, groups, stage_ms, workload, fp64_peak):
                                        "peak_source": "measured (dccm_fp64_peak)", "frac": tf / fp64_peak,
                                        "flops_per_launch": f64}
     # the remap keeps the reference's separately rounded products and sums
-    # (bit-exact): one DMUL and one DADD per table entry and field
+    # (bit-exact): one DMUL and one DADD per table entry and field, reported
+    # beside its bytes
     rf = sum(2.0 * len(t[2]) * 6 * len(g.members) for g, t in zip(groups, S["tables"]))
     tf = rf / (stages["remap"]["ms"] / 1e3) / 1e12
     stages["remap"]["fp64"] = {"achieved": tf, "unit": "TFLOP/s", "peak": fp64_peak,
                                "peak_source": "measured (dccm_fp64_peak)", "frac": tf / fp64_peak,
                                "flops_per_launch": rf}
-    stages["remap"]["limiter"] = "FP64 pipe (unfused products and sums), not HBM"
+    stages["remap"]["limiter"] = "latency of the dependent gathers (record, then source value), not HBM"
     dom = names[int(np.argmax(stage_ms))]
     roof = dict(stages[dom])
     roof.update({"kernel": dom, "peak_source": src_peak, "stages": stages,

@@ -69,10 +69,21 @@ csr_apply(const int64_t *__restrict__ rowptr, const double2 *__restrict__ ent,
     const int64_t b = rowptr[r], e = rowptr[r + 1];
     const double *s = src + (int64_t)f * ld_src;
     double acc = 0.0;
-    for (int64_t k = b; k < e; ++k) {
-      const double2 q = __ldg(ent + k);
-      const int64_t col = (int64_t)__double_as_longlong(q.y);
-      acc = __dadd_rn(acc, __dmul_rn(__ldg(s + col), q.x));
+    // four entries per round: their records, then their source values, are
+    // all in flight before the sums, which stay in table order (bit-exact)
+    constexpr int U = 4;
+    for (int64_t k0 = b; k0 < e; k0 += U) {
+      double2 q[U];
+      double x[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+        if (k0 + u < e) q[u] = __ldg(ent + k0 + u);
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+        if (k0 + u < e) x[u] = __ldg(s + (int64_t)__double_as_longlong(q[u].y));
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+        if (k0 + u < e) acc = __dadd_rn(acc, __dmul_rn(x[u], q[u].x));
     }
     const int fs = f / nsub;
     dst[(int64_t)(f - fs * nsub) * ld_dst + (int64_t)fs * ld_dst2 + r] = acc;
