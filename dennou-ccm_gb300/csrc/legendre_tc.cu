@@ -232,6 +232,10 @@ legendre_tc_kernel(const __grid_constant__ TcLaunch L) {
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
   const int nitems = L.start[L.ngroups];
+  if (warp == 0 && lane < 2 * L.ngroups) {  // descriptors into the TMA unit's cache, behind the previous kernel
+    const CUtensorMap *mp = (lane & 1) ? &L.amap[lane >> 1] : &L.map[lane >> 1];
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(mp)) : "memory");
+  }
   pdl_wait();  // the operands come from the previous kernel (pack or forward FFT)
   pdl_trigger();
 
