@@ -369,7 +369,7 @@ def host_copies(S, groups, dccm, torch):
 
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of
 # each stage's kernels in one ncu capture of `bench.py --profile-steps`,
-# summarised in profiles/stages_c3_ncu.md; null where not captured.
+# kept with the profiles of the c3 step; null where not captured.
 TRAFFIC = {
     "c3": {"legendre_inverse": int((7.683584 + 12.144896) * 1e6 + 2304), "fft_inverse": int(11.3408e6 + 3584),
            "fft_forward": int(33.62304e6 + 57344), "legendre_forward": int(18.947072e6 + 1792),
@@ -443,13 +443,14 @@ def roofline(S, inp, groups, stage_ms, workload, fp64_peak):
     dom = names[int(np.argmax(stage_ms))]
     roof = dict(stages[dom])
     roof.update({"kernel": dom, "peak_source": src_peak, "stages": stages,
-                 "traffic_source": "profiles/stages_c3_ncu.md" if workload in TRAFFIC else None})
+                 "traffic_source": ("ncu --set full of bench.py --workload c3 --profile-steps 3"
+                                    if workload in TRAFFIC else None)})
     return roof
 
 
 # FP64 flops of the flux kernel per ocean column (DADD + DMUL + 2 DFMA
 # thread instructions per cycle x elapsed cycles, ncu sass counters, c3:
-# 25.4 M flops for 45,478 columns, profiles/stages_c3_ncu.md).  Every
+# 25.4 M flops for 45,478 columns).  Every
 # column does the same work when there is no sea ice (all workloads here:
 # the ice physics is skipped where SIceCon = 0).
 FLUX_FP64_FLOPS_PER_COLUMN = (20.948747 + 41.897494 + 2 * 114.69439) * 86836.697368 / 45478
@@ -457,7 +458,7 @@ FLUX_FP64_FLOPS_PER_COLUMN = (20.948747 + 41.897494 + 2 * 114.69439) * 86836.697
 
 # FP64 flops of the implicit-coupling sweeps per column and level, one
 # tracer (DADD + DMUL + 2 DFMA thread instructions per cycle x elapsed
-# cycles, ncu, 32768 columns x 32 levels; profiles/implcpl_c3_ncu.md):
+# cycles, ncu, 32768 columns x 32 levels):
 # per 32-level column forward 3915 (shared factors 878 + elimination 3037),
 # backward 1430.
 IMPLCPL_FP64_FLOPS = {"forward": 3915 / 32, "backward": 1430 / 32}

@@ -42,7 +42,7 @@ enum dccm_status {
   DCCM_ERR_IO = -6,           /* table file could not be read or written */
   DCCM_ERR_NOMEM = -7,        /* host or device allocation failed */
   DCCM_ERR_TIMEOUT = -8,      /* a bounded device wait gave up */
-  DCCM_ERR_UNSUPPORTED = -9   /* size or mode this build does not handle */
+  DCCM_ERR_UNSUPPORTED = -9   /* size or mode the library does not handle */
 };
 
 /* Message for a status code (static storage). */

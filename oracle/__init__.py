@@ -1,7 +1,8 @@
 """ctypes bindings of the CPU oracle (test infrastructure only).
 
-The oracle is the checker: tests, ``__graft_entry__.smoke()`` and the CPU
-baseline of ``bench.py`` call it; the product library never does.  See
+The oracle is what the GPU results are compared against: tests,
+``__graft_entry__.smoke()`` and the CPU baseline of ``bench.py`` call it;
+the product library never does.  See
 ``oracle.h`` for what each function restates and why parity is unpinned.
 """
 import ctypes

@@ -1,9 +1,9 @@
 /*
  * CPU oracle for the Dennou-CCM coupling-step hot path.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker that the CUDA
- * library is compared against, and the timed CPU baseline of bench.py.  No
- * product code path loads it.
+ * TEST INFRASTRUCTURE ONLY.  This library is what the CUDA library's
+ * results are compared against, and the timed CPU baseline of bench.py.
+ * No product code path loads it.
  *
  * It is a plain-C FP64 restatement of the reference algorithms:
  *   - surface bulk flux:  sfc/DSFCM_Util_SfcBulkFlux_mod.f90:35-58,108-591

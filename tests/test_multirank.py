@@ -66,8 +66,8 @@ def test_single_rank_is_identity():
 
 
 def test_reference_arm_under_torchrun_two_ranks():
-    """`bench.py --impl reference` launched as the driver launches N>1: only
-    rank 0 runs the CPU step and prints one JSON line."""
+    """`bench.py --impl reference` launched by torch.distributed.run with two
+    ranks: only rank 0 runs the CPU step and prints one JSON line."""
     oracle = pytest.importorskip("oracle")
     try:
         oracle.lib()
