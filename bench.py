@@ -137,24 +137,88 @@ def remap_index(w, inp, g, gen):
 
 
 # --------------------------------------------------------------- clocks
+# NVML poller run as its own process (so that it takes no time from the
+# launching thread): SM clock and clock-event reason bits every 2 ms until its
+# standard input closes, then one JSON summary line.  argv[1]: the PCI bus id
+# of the GPU in use, or "" when NVML sees one GPU.  Read-only NVML queries.
+_NVML_POLL = r"""
+import ctypes, json, select, sys
+lib = ctypes.CDLL("libnvidia-ml.so.1")
+assert lib.nvmlInit_v2() == 0
+h = ctypes.c_void_p()
+n = ctypes.c_uint()
+lib.nvmlDeviceGetCount_v2(ctypes.byref(n))
+if n.value == 1 or not sys.argv[1]:
+    assert lib.nvmlDeviceGetHandleByIndex_v2(0, ctypes.byref(h)) == 0
+else:
+    assert lib.nvmlDeviceGetHandleByPciBusId_v2(sys.argv[1].encode(), ctypes.byref(h)) == 0
+get_rs = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or lib.nvmlDeviceGetCurrentClocksThrottleReasons
+clk, cmax, rs = ctypes.c_uint(), ctypes.c_uint(), ctypes.c_ulonglong()
+lib.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(cmax))
+sm, bits = [], 0
+print("ready", flush=True)
+while not select.select([sys.stdin], [], [], 0.002)[0]:
+    if lib.nvmlDeviceGetClockInfo(h, 1, ctypes.byref(clk)) == 0 and get_rs(h, ctypes.byref(rs)) == 0:
+        sm.append(clk.value)
+        bits |= rs.value
+sm.sort()
+print(json.dumps({"n": len(sm), "median": sm[len(sm) // 2] if sm else None, "max": cmax.value, "bits": bits}), flush=True)
+"""
+
+
 class Clocks:
-    def __init__(self):
+    """SM clock and clock-event reasons sampled during the timed region: an
+    NVML poller process (every 2 ms), or nvidia-smi -lms 20 where NVML cannot
+    be loaded."""
+
+    # NVML clocks event (throttle) reason bits
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown"}
+
+    def __init__(self, dev=0):
         self.p = None
+        self.poll = None
+        self.dev = dev
 
     def start(self):
+        try:
+            import torch
+            bus = ""
+            if torch.cuda.device_count() >= 1:
+                pr = torch.cuda.get_device_properties(self.dev)
+                bus = "%08x:%02x:%02x.0" % (pr.pci_domain_id, pr.pci_bus_id, pr.pci_device_id)
+            self.poll = subprocess.Popen([sys.executable, "-c", _NVML_POLL, bus], stdin=subprocess.PIPE,
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            if self.poll.stdout.readline().strip() == "ready":
+                return
+            self.poll.wait(timeout=10)
+        except Exception:
+            pass
+        self.poll = None
         q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
         try:
             self.p = subprocess.Popen(["nvidia-smi", "--query-gpu=" + q, "--format=csv,noheader,nounits",
-                                       "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                                       "-lms", "20"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            time.sleep(0.3)  # nvidia-smi up before the region starts
         except Exception:
             self.p = None
 
     def stop(self, dev=0):
+        if self.poll is not None:
+            try:
+                out, _ = self.poll.communicate(input="", timeout=10)
+                r = json.loads(out.strip().splitlines()[-1])
+            except Exception as e:  # noqa: BLE001
+                self.poll.kill()
+                return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvml poller failed: %s" % e]}
+            if not r["n"]:
+                return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "source": "nvml"}
+            return {"sm_mhz": float(r["median"]), "sm_max_mhz": float(r["max"]),
+                    "reasons": sorted(nm for bit, nm in self.REASONS.items() if r["bits"] & bit),
+                    "samples": r["n"], "source": "nvml, 2 ms"}
         if self.p is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        time.sleep(0.25)
         self.p.terminate()
         out, _ = self.p.communicate(timeout=10)
         sm, smax, reasons = [], [], set()
@@ -174,7 +238,7 @@ class Clocks:
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)), "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "source": "nvidia-smi, 20 ms"}
 
 
 # -------------------------------------------------------------- CPU step
@@ -581,7 +645,7 @@ def gpu_bench(args, w, inp, rank, world):
             torch.distributed.barrier()
         return [a.elapsed_time(b) for a, b in evs]
 
-    clocks = Clocks()
+    clocks = Clocks(dev.index or 0)
     clocks.start()
     ms_mixed = timed(S["steps"]["mixed"], args.steps, max(3, args.warmup))
     ck = clocks.stop(dev.index or 0)
