@@ -23,8 +23,9 @@
 // Warp roles (192 threads): warp 0 lane 0 issues the TMA loads of a stage
 // (six boxes of A and B per 64-wide K chunk); warp 1 allocates TMEM and its
 // lane 0 issues the MMAs; warps 2-5 are the epilogue (tcgen05.ld of the
-// accumulators, warp w reading TMEM lanes 32 (w % 4) .., parity fold,
-// stores coalesced along c).  Two shared-memory stages and two TMEM
+// accumulators, warp w reading TMEM lanes 32 (w % 4) ..; inverse: parity
+// fold, stores coalesced along c; forward: both parities through shared
+// memory, stores coalesced along n).  Two shared-memory stages and two TMEM
 // accumulator sets overlap loads, MMAs and epilogue of consecutive items.
 // Every mbarrier wait is bounded by a 1 s globaltimer limit; on expiry the
 // kernel records an error code, stops issuing work, and still frees its TMEM.
@@ -45,6 +46,10 @@ constexpr int B_SPLIT_BYTES = 128 * 128;     // 128 rows (N) x 64 bf16 (K); a ta
 constexpr int STAGE_BYTES = 3 * A_SPLIT_BYTES + 3 * B_SPLIT_BYTES;  // 96 KB
 constexpr int NSTAGE = 2;
 constexpr int TMEM_COLS = 512;
+// Analysis epilogue staging: 128 rows (c) x 32 floats (16 k of both
+// parities), rows padded to 33 floats (conflict-free row and column access).
+constexpr int EP_LD = 33;
+constexpr int EP_BYTES = 128 * EP_LD * 4;
 
 struct MInfo {
   long long base;  // first tile row of (m, p=0)
@@ -158,6 +163,8 @@ __device__ __forceinline__ void tmem_ld16_nw(uint32_t taddr, uint32_t (&r)[16]) 
       : "r"(taddr));
 }
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+// Named barrier of the four epilogue warps (threads 64..191).
+__device__ __forceinline__ void epi_sync() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
 
 // FP64 split used once per table entry at plan creation.
 __device__ __forceinline__ void split3(double x, __nv_bfloat16 &h, __nv_bfloat16 &m, __nv_bfloat16 &l) {
@@ -190,6 +197,14 @@ __device__ __forceinline__ void item_of(const TcArgs &a, int li, int &m, int &ct
   m = w.x;
   nt = w.z;
   ct = li % a.nct;
+}
+// The k-th work item of this CTA: rounds of gridDim.x items taken in
+// alternating directions (CTA b: b, 2G-1-b, 2G+b, ...), so that with items
+// heavy first the CTAs that get one item more get light ones.  Strictly
+// increasing in k.
+__device__ __forceinline__ int cta_item(int k) {
+  const int G = (int)gridDim.x, b = (int)blockIdx.x;
+  return (k & 1) ? (k + 1) * G - 1 - b : k * G + b;
 }
 __device__ __forceinline__ int group_of(const TcLaunch &L, int it) {
   int gi = 0;
@@ -236,6 +251,20 @@ legendre_tc_kernel(const __grid_constant__ TcLaunch L) {
     const CUtensorMap *mp = (lane & 1) ? &L.amap[lane >> 1] : &L.map[lane >> 1];
     asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(mp)) : "memory");
   }
+  if (warp == 2 && lane < 2) {
+    // The item list and MInfo of this CTA's first two items (plan constants,
+    // not written by the previous kernel) into L1 while the previous kernel
+    // finishes: every role reads them right after the dependency wait.
+    const int it = cta_item(lane);
+    if (it < nitems) {
+      const int gi = group_of(L, it);
+      int m, ct, nt;
+      item_of(L.g[gi], it - L.start[gi], m, ct, nt);
+      const char *q = reinterpret_cast<const char *>(L.g[gi].mi + m);
+      asm volatile("prefetch.global.L1 [%0];" ::"l"(q));
+      asm volatile("prefetch.global.L1 [%0];" ::"l"(q + sizeof(MInfo) - 1));
+    }
+  }
   pdl_wait();  // the operands come from the previous kernel (pack or forward FFT)
   pdl_trigger();
 
@@ -244,7 +273,7 @@ legendre_tc_kernel(const __grid_constant__ TcLaunch L) {
     if (lane == 0) {
       int g = 0;  // chunk counter
       bool ok = true;
-      for (int it = blockIdx.x; it < nitems && ok; it += gridDim.x) {
+      for (int k = 0, it = cta_item(0); it < nitems && ok; it = cta_item(++k)) {
         const int gi = group_of(L, it);
         const TcArgs &a = L.g[gi];
         int m, ct, nt;
@@ -281,7 +310,7 @@ legendre_tc_kernel(const __grid_constant__ TcLaunch L) {
     if (lane == 0) {
       int g = 0, li = 0;
       bool ok = true;
-      for (int it = blockIdx.x; it < nitems && ok; it += gridDim.x, ++li) {
+      for (int it = cta_item(0); it < nitems && ok; it = cta_item(++li)) {
         const int gi = group_of(L, it);
         const TcArgs &a = L.g[gi];
         int m, ct, nt;
@@ -339,8 +368,13 @@ legendre_tc_kernel(const __grid_constant__ TcLaunch L) {
     // -------------------------------------------------------- epilogue
     const int quad = warp & 3;
     const int row = quad * 32 + lane;
+    float *ep = reinterpret_cast<float *>(sm + NSTAGE * STAGE_BYTES + 128);  // [128][EP_LD]
     int li = 0;
-    for (int it = blockIdx.x; it < nitems; it += gridDim.x, ++li) {
+    // A failed wait ends the inverse epilogue; the forward epilogue's warps
+    // keep passing their shared barriers (without TMEM loads or stores) so
+    // that none of them waits on a warp that left.
+    bool dead = false;
+    for (int it = cta_item(0); it < nitems; it = cta_item(++li)) {
       const int gi = group_of(L, it);
       const TcArgs &a = L.g[gi];
       int m, ct, nt;
@@ -350,7 +384,10 @@ legendre_tc_kernel(const __grid_constant__ TcLaunch L) {
       const int nrow = min(128, mi.nr - nt * 128);
       const int ab = a.nacc == 2 ? (li & 1) : 0;
       const int ar = a.nacc == 2 ? (li >> 1) : li;
-      if (!mbar_wait(&accf[ab], ar & 1, a.err, abort_flag, 4)) break;
+      if (dead || !mbar_wait(&accf[ab], ar & 1, a.err, abort_flag, 4)) {
+        dead = true;
+        if (a.dir == 0) break;
+      }
       tc_fence_after();
       const int c = ct * 128 + row;
       const int NT = a.ntmax;
@@ -390,32 +427,40 @@ legendre_tc_kernel(const __grid_constant__ TcLaunch L) {
           }
         }
       } else {
-        for (int p = 0; p < 2; ++p) {
-          const int nv = p ? mi.nv1 : mi.nv0;
-          for (int k0 = 0; k0 < nrow; k0 += 16) {
-            if (nt * 128 + k0 >= nv) break;  // uniform across the warp
-            uint32_t rd[16], rx[16];
-            tmem_ld16_nw(tbase + (p * 2) * NT + k0, rd);
-            tmem_ld16_nw(tbase + (p * 2 + 1) * NT + k0, rx);
+        // Columns k0..k0+15 of both parities go to shared memory as
+        // [c][2i + p] (coefficient n = nbase + 2 k0 + 2i + p), then warp w
+        // writes the contiguous runs of n of field-levels w, w + 4, ...:
+        // 16-byte stores of consecutive coefficients.
+        float *erow = ep + row * EP_LD;
+        const int nbase = m + 2 * nt * 128;
+        for (int k0 = 0; k0 < nrow; k0 += 16) {
+          if (nt * 128 + k0 >= mi.nv0) break;  // nv0 >= nv1; uniform over the epilogue warps
+          if (!dead) {
+            uint32_t r0[16], x0[16], r1[16], x1[16];
+            tmem_ld16_nw(tbase + k0, r0);
+            tmem_ld16_nw(tbase + NT + k0, x0);
+            tmem_ld16_nw(tbase + 2 * NT + k0, r1);
+            tmem_ld16_nw(tbase + 3 * NT + k0, x1);
             tmem_wait_ld();
-            float d[16], x[16];
 #pragma unroll
             for (int i = 0; i < 16; ++i) {
-              d[i] = __uint_as_float(rd[i]);
-              x[i] = __uint_as_float(rx[i]);
-            }
-            if (c < C2B) {
-#pragma unroll
-              for (int i = 0; i < 16; ++i) {
-                const int k = nt * 128 + k0 + i;
-                if (k < nv) {
-                  const int n = m + p + 2 * k;
-                  const double v = (m == 0 && (c & 1)) ? 0.0 : f32_to_f64((d[i] + x[i]) * us);
-                  a.spec_out[((long long)(c >> 1) * a.ncoef + idx_mn(a.N, m, n)) * 2 + (c & 1)] = v;
-                }
-              }
+              erow[2 * i] = (__uint_as_float(r0[i]) + __uint_as_float(x0[i])) * us;
+              erow[2 * i + 1] = (__uint_as_float(r1[i]) + __uint_as_float(x1[i])) * us;
             }
           }
+          epi_sync();
+          const int n = nbase + 2 * k0 + lane;
+          if (!dead && n <= a.N) {
+            double2 *dst = reinterpret_cast<double2 *>(a.spec_out) + idx_mn(a.N, m, n);
+            for (int bl = quad; bl < 64; bl += 4) {
+              const int c0 = ct * 128 + 2 * bl;
+              if (c0 >= C2B) break;
+              const double re = f32_to_f64(ep[2 * bl * EP_LD + lane]);
+              const double im = m == 0 ? 0.0 : f32_to_f64(ep[(2 * bl + 1) * EP_LD + lane]);
+              dst[(long long)(c0 >> 1) * a.ncoef] = make_double2(re, im);
+            }
+          }
+          epi_sync();
         }
       }
       tc_fence_before();
@@ -830,7 +875,7 @@ int build_tiles(Plan &P) {
   return DCCM_OK;
 }
 
-static size_t tc_smem_bytes() { return 1024 + (size_t)NSTAGE * STAGE_BYTES + 128; }
+static size_t tc_smem_bytes() { return 1024 + (size_t)NSTAGE * STAGE_BYTES + 128 + EP_BYTES; }
 
 // One persistent launch over ngroups plans (truncation groups) of one
 // direction: dir 0 (inverse) reads the plan's packed spectra (pack_spectra
