@@ -232,7 +232,7 @@ def fp64_peak(stream=None):
 
 def tune_set(knob, value):
     """dccm_tune_set: process-wide launch-shape knob (tc_ctas, fft_bb,
-    flux_threads, remap_threads, serial, upload_order, host_path); 0 = the
+    flux_threads, flux_ctas, remap_threads, serial, upload_order, host_path); 0 = the
     default."""
     _check(load().dccm_tune_set(knob.encode(), int(value)), "dccm_tune_set")
 
@@ -648,6 +648,7 @@ class Step:
                "dccm_step_autotune")
         chosen = dict(zip(self.KNOBS, list(out)))
         chosen["serial"] = tune_get("serial")
+        chosen["flux_ctas"] = tune_get("flux_ctas")
         return chosen
 
     def run_timed(self, stream=None):
@@ -665,15 +666,16 @@ class Step:
                "dccm_step_run_host")
 
     def autotune_host(self, h2d, d2h=None, stream=None):
-        """dccm_step_autotune_host: upload order and copy path for these
-        copy lists, by timing (the step runs 384 times); host_path is
-        1 + the mask of copy groups moved through the host mapping."""
+        """dccm_step_autotune_host: upload order, copy path and flux CTA cap
+        for these copy lists, by timing (the step runs about 400 times);
+        host_path is 1 + the mask of copy groups moved through the host
+        mapping, flux_ctas 0 the flux kernel's full grid."""
         c = h2d if isinstance(h2d, HostCopies) else HostCopies(h2d, d2h or [])
-        out = (ctypes.c_int * 2)()
+        out = (ctypes.c_int * 3)()
         ms = (ctypes.c_float * 32)()
         _check(load().dccm_step_autotune_host(self.h, _stream(stream), c.h2d, c.nh2d, c.d2h, c.nd2h, out, ms),
                "dccm_step_autotune_host")
-        return {"upload_order": out[0], "host_path": out[1],
+        return {"upload_order": out[0], "host_path": out[1], "flux_ctas": out[2],
                 "candidates_ms": {"%d,%d" % (1 + k // 16, 1 + k % 16): ms[k] for k in range(32)}}
 
     def host_release(self):

@@ -33,6 +33,7 @@ struct Tunables {
   int tc_ctas = 0;        // persistent CTAs of the tensor-core Legendre kernel
   int fft_bb = 0;         // warps per FFT CTA (4, 8, 16)
   int flux_threads = 0;   // threads per CTA of the bulk-flux kernel
+  int flux_ctas = 0;      // CTA cap of the bulk-flux kernel's grid-stride loop (0: 16 per SM)
   int remap_threads = 0;  // threads per CTA of the remap kernel
   int serial = 0;         // 1: launch_pdl makes ordinary launches
   int upload_order = 0;   // dccm_step_run_host: 1 transforms' inputs first, 2 surface inputs first

@@ -305,7 +305,9 @@ int launch(const Ptrs &p, const dccm_sfc_grid *g, double sig1, cudaStream_t s) {
   geo.sig1k = pow(sig1, (GasRUniv / MolWtDry) / CpDry);
   const int threads = tunables().flux_threads > 0 ? tunables().flux_threads : 128;
   int64_t blocks = (geo.ncol + threads - 1) / threads;
-  const int64_t cap = (int64_t)sm_count() * 16;
+  // In the coupling step the flux runs beside the transforms: fewer CTAs
+  // leave them more issue slots (flux_ctas, chosen on whole-step timings).
+  const int64_t cap = tunables().flux_ctas > 0 ? (int64_t)tunables().flux_ctas : (int64_t)sm_count() * 16;
   if (blocks > cap) blocks = cap;
   bulk_flux_column<<<(unsigned)blocks, threads, 0, s>>>(p, geo);
   DCCM_LAUNCH_CHECK();

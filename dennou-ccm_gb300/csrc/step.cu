@@ -59,8 +59,9 @@ struct dccm_step {
   cudaGraphExec_t hexec = nullptr;
   std::vector<void *> host_tabs;  // device segment tables of that graph
   bool sfc_first = false;         // that graph uploads the surface inputs first
-  // choices of dccm_step_autotune_host (0: the process-wide knobs)
-  int host_order = 0, host_path = 0;
+  // choices of dccm_step_autotune_host (0: the process-wide knobs; flux
+  // CTA cap -1: the process-wide knob)
+  int host_order = 0, host_path = 0, host_flux_ctas = -1;
   // stage times of the last dccm_step_run_timed (ms), for the upload order
   float stage_ms[6] = {};
   bool have_stage_ms = false;
@@ -724,7 +725,12 @@ static int build_host_graph(dccm_step *st, const dccm_host_copy *h2d, int nh2d, 
   HostSets hs;
   DCCM_TRY(prepare_sets(st, hp, hs));
   cudaGraph_t g = nullptr;
-  DCCM_TRY(capture(st, &hs, &g));
+  Tunables &T = tunables();
+  const int flux_ctas = T.flux_ctas;
+  if (st->host_flux_ctas >= 0) T.flux_ctas = st->host_flux_ctas;
+  const int rc = capture(st, &hs, &g);
+  T.flux_ctas = flux_ctas;
+  DCCM_TRY(rc);
   st->hgraph = g;
   DCCM_CUDA(cudaGraphInstantiate(&st->hexec, g, 0));
   st->host_h2d.assign(h2d, h2d + nh2d);
@@ -775,43 +781,67 @@ extern "C" int dccm_step_autotune_host(dccm_step *st, void *stream, const dccm_h
                                        const dccm_host_copy *d2h, int nd2h, int *chosen, float *ms) {
   constexpr int NC = 32;  // (order 1..2) x (path mask 0..15)
   if (!st || (nh2d > 0 && !h2d) || (nd2h > 0 && !d2h) || nh2d < 0 || nd2h < 0) return DCCM_ERR_INVALID_ARG;
-  if (chosen) chosen[0] = chosen[1] = 0;
+  if (chosen) chosen[0] = chosen[1] = chosen[2] = 0;
   if (ms)
     for (int k = 0; k < NC; ++k) ms[k] = 0.f;
   if (!page_locked(h2d, nh2d, d2h, nd2h)) return DCCM_OK;  // pageable: nothing to choose
   cudaStream_t s = as_stream(stream);
-  // Two rounds over the candidates, each the median of 4 replays after 2;
-  // a candidate's time is its better round (rounds interleave the
-  // candidates, so a drift of the clocks hits all of them).
+  // Device time of one candidate: the median of 4 replays after 2.
+  auto time_one = [&](float *t_out) -> int {
+    DCCM_TRY(build_host_graph(st, h2d, nh2d, d2h, nd2h));
+    std::vector<float> v;
+    for (int r = 0; r < 6; ++r) {
+      DCCM_CUDA(cudaEventRecord(st->ev[0], s));
+      DCCM_CUDA(cudaGraphLaunch(st->hexec, s));
+      DCCM_CUDA(cudaEventRecord(st->ev[1], s));
+      DCCM_CUDA(cudaEventSynchronize(st->ev[1]));
+      float t = 0.f;
+      DCCM_CUDA(cudaEventElapsedTime(&t, st->ev[0], st->ev[1]));
+      if (r >= 2) v.push_back(t);
+    }
+    std::sort(v.begin(), v.end());
+    *t_out = 0.5f * (v[1] + v[2]);
+    return DCCM_OK;
+  };
+  // Two rounds over the candidates; a candidate's time is its better round
+  // (rounds interleave the candidates, so a drift of the clocks hits all
+  // of them).  The flux grid follows the process-wide knob meanwhile.
+  st->host_flux_ctas = -1;
   float best_t[NC];
   for (int c = 0; c < NC; ++c) best_t[c] = 1e30f;
   for (int round = 0; round < 2; ++round)
     for (int c = 0; c < NC; ++c) {
       st->host_order = 1 + c / 16;
       st->host_path = 1 + c % 16;
-      DCCM_TRY(build_host_graph(st, h2d, nh2d, d2h, nd2h));
-      std::vector<float> v;
-      for (int r = 0; r < 6; ++r) {
-        DCCM_CUDA(cudaEventRecord(st->ev[0], s));
-        DCCM_CUDA(cudaGraphLaunch(st->hexec, s));
-        DCCM_CUDA(cudaEventRecord(st->ev[1], s));
-        DCCM_CUDA(cudaEventSynchronize(st->ev[1]));
-        float t = 0.f;
-        DCCM_CUDA(cudaEventElapsedTime(&t, st->ev[0], st->ev[1]));
-        if (r >= 2) v.push_back(t);
-      }
-      std::sort(v.begin(), v.end());
-      best_t[c] = std::min(best_t[c], 0.5f * (v[1] + v[2]));
+      float t;
+      DCCM_TRY(time_one(&t));
+      best_t[c] = std::min(best_t[c], t);
     }
   int bc = 0;
   for (int c = 1; c < NC; ++c)
     if (best_t[c] < best_t[bc]) bc = c;
   st->host_order = 1 + bc / 16;
   st->host_path = 1 + bc % 16;
+  // The flux grid's CTA cap for this graph: with host copies the surface
+  // branch's results are the first downloads, so a faster flux can win
+  // over the cap chosen for the step without copies.  The process-wide
+  // cap against the full grid (0), two interleaved rounds.
+  if (tunables().flux_ctas != 0) {
+    float tk[2] = {1e30f, 1e30f};
+    for (int round = 0; round < 2; ++round)
+      for (int k = 0; k < 2; ++k) {
+        st->host_flux_ctas = k ? 0 : -1;
+        float t;
+        DCCM_TRY(time_one(&t));
+        tk[k] = std::min(tk[k], t);
+      }
+    st->host_flux_ctas = tk[1] < tk[0] ? 0 : -1;
+  }
   DCCM_TRY(build_host_graph(st, h2d, nh2d, d2h, nd2h));
   if (chosen) {
     chosen[0] = st->host_order;
     chosen[1] = st->host_path;
+    chosen[2] = st->host_flux_ctas >= 0 ? st->host_flux_ctas : tunables().flux_ctas;
   }
   if (ms)
     for (int k = 0; k < NC; ++k) ms[k] = best_t[k];
@@ -889,6 +919,7 @@ static bool cache_lookup(const char *path, const std::string &key, Tunables &t) 
     if ((p = strstr(line, "\"flux_threads\": "))) v.flux_threads = atoi(p + 16);
     if ((p = strstr(line, "\"remap_threads\": "))) v.remap_threads = atoi(p + 17);
     if ((p = strstr(line, "\"serial\": "))) v.serial = atoi(p + 10);
+    if ((p = strstr(line, "\"flux_ctas\": "))) v.flux_ctas = atoi(p + 13);
     t = v;
     found = true;
   }
@@ -903,9 +934,9 @@ static void cache_store(const char *path, const std::string &key, const Tunables
   if (!fp) return;
   fprintf(fp,
           "{\"key\": \"%s\", \"tc_ctas\": %d, \"fft_bb\": %d, \"flux_threads\": %d, \"remap_threads\": %d, "
-          "\"serial\": %d, \"step_ms\": %.4f, \"stage_ms\": [%.4f, %.4f, %.4f, %.4f, %.4f, %.4f]}\n",
-          key.c_str(), t.tc_ctas, t.fft_bb, t.flux_threads, t.remap_threads, t.serial, step_ms, ms[0], ms[1],
-          ms[2], ms[3], ms[4], ms[5]);
+          "\"serial\": %d, \"flux_ctas\": %d, \"step_ms\": %.4f, \"stage_ms\": [%.4f, %.4f, %.4f, %.4f, %.4f, %.4f]}\n",
+          key.c_str(), t.tc_ctas, t.fft_bb, t.flux_threads, t.remap_threads, t.serial, t.flux_ctas, step_ms, ms[0],
+          ms[1], ms[2], ms[3], ms[4], ms[5]);
   fclose(fp);
 }
 
@@ -1004,15 +1035,22 @@ extern "C" int dccm_step_autotune(dccm_step *st, const char *cache_path, int *ch
         return rc;
       }
     }
-    // Whole-graph pass: the stage pass's Legendre CTA count first, so a
-    // tie keeps it.
-    const int tc0 = T.tc_ctas;
-    std::vector<int> tc_cand = {tc0};
-    for (int c : {sms, sms * 3 / 4, sms / 2, sms / 4})
-      if (c != tc0) tc_cand.push_back(c);
+    // Whole-graph pass: the stage pass's choices first, so a tie keeps
+    // them.  The flux runs beside the transforms, so its CTA size and its
+    // grid's CTA cap are judged here as well (fewer flux warps leave the
+    // transforms more issue slots; the stage pass times the flux alone).
+    T.flux_ctas = 0;  // from the full grid, whatever an earlier step chose
+    auto first = [](int v, std::initializer_list<int> rest) {
+      std::vector<int> c = {v};
+      for (int x : rest)
+        if (x != v) c.push_back(x);
+      return c;
+    };
     Knob graph_knobs[] = {
         {&T.serial, {0, 1}, -1, -1},
-        {&T.tc_ctas, tc_cand, -1, -1},
+        {&T.tc_ctas, first(T.tc_ctas, {sms, sms * 3 / 4, sms / 2, sms / 4}), -1, -1},
+        {&T.flux_threads, first(T.flux_threads, {64, 128, 256}), -1, -1},
+        {&T.flux_ctas, {0, sms * 4, sms * 2, sms}, -1, -1},
     };
     float step_ms = 0.f;
     for (Knob &kb : graph_knobs) {
@@ -1046,6 +1084,7 @@ extern "C" int dccm_tune_set(const char *knob, int value) {
   else if (!strcmp(knob, "fft_bb")) T.fft_bb = value;
   else if (!strcmp(knob, "flux_threads")) T.flux_threads = value;
   else if (!strcmp(knob, "remap_threads")) T.remap_threads = value;
+  else if (!strcmp(knob, "flux_ctas")) T.flux_ctas = value;
   else if (!strcmp(knob, "serial")) T.serial = value ? 1 : 0;
   else if (!strcmp(knob, "upload_order")) {
     if (value > 2) return DCCM_ERR_INVALID_ARG;
@@ -1065,6 +1104,7 @@ extern "C" int dccm_tune_get(const char *knob, int *value) {
   else if (!strcmp(knob, "fft_bb")) *value = T.fft_bb;
   else if (!strcmp(knob, "flux_threads")) *value = T.flux_threads;
   else if (!strcmp(knob, "remap_threads")) *value = T.remap_threads;
+  else if (!strcmp(knob, "flux_ctas")) *value = T.flux_ctas;
   else if (!strcmp(knob, "serial")) *value = T.serial;
   else if (!strcmp(knob, "upload_order")) *value = T.upload_order;
   else if (!strcmp(knob, "host_path")) *value = T.host_path;

@@ -468,13 +468,17 @@ int dccm_step_host_release(dccm_step *step);
  * engines with host-contiguous runs through a staging buffer.  It replays
  * the step with each of the 32 combinations (2 interleaved rounds of 6
  * replays on stream: the step's outputs are written as by
- * dccm_step_run_host), keeps the fastest for this step and leaves its
- * graph recorded.  chosen (2 ints, may be NULL) receives the order and
- * host_path; both 0 with pageable buffers, for which there is nothing to
- * choose.  ms (32 floats, may be NULL) receives each combination's device
- * time per step at index 16 (order - 1) + mask.  The process-wide knobs
- * "upload_order" and "host_path" (dccm_tune_set) apply to steps that have
- * not been tuned this way. */
+ * dccm_step_run_host), keeps the fastest for this step, then times the
+ * winner with the flux kernel's full grid against the process-wide
+ * "flux_ctas" cap (with host copies the surface results are the first
+ * downloads, so the fastest flux can win) and leaves the graph recorded.
+ * chosen (3 ints, may be NULL) receives the order, host_path and the flux
+ * CTA cap of this graph (0: the full grid); all 0 with pageable buffers,
+ * for which there is nothing to choose.  ms (32 floats, may be NULL)
+ * receives each combination's device time per step at index
+ * 16 (order - 1) + mask.  The process-wide knobs "upload_order",
+ * "host_path" and "flux_ctas" (dccm_tune_set) apply to steps that have not
+ * been tuned this way. */
 int dccm_step_autotune_host(dccm_step *step, void *stream, const dccm_host_copy *h2d, int nh2d,
                             const dccm_host_copy *d2h, int nd2h, int *chosen, float *ms);
 
@@ -483,14 +487,15 @@ int dccm_step_autotune_host(dccm_step *step, void *stream, const dccm_host_copy 
  * CTAs of the tensor-core Legendre kernel, "fft_bb": warps per FFT CTA
  * (4, 8 or 16), "flux_threads", "remap_threads": CTA sizes), then "serial"
  * (1: ordinary launches instead of programmatic dependent launches along
- * the transform chain) and "tc_ctas" again on replays of the whole step
- * graph, where the two branches run concurrently; applies the winners
- * and records the step's graph again.  With cache_path the choice is read
+ * the transform chain), "tc_ctas" again and "flux_ctas" (CTA cap of the
+ * flux kernel's grid, 0: 16 per SM) on replays of the whole step graph,
+ * where the two branches run concurrently; applies the winners and
+ * records the step's graph again.  With cache_path the choice is read
  * from / appended to that file (one JSON object per line, keyed by the
  * GPU name and SM count and the step's shapes).  chosen (4 ints, may be
  * NULL) receives tc_ctas, fft_bb, flux_threads, remap_threads (read
- * "serial" with dccm_tune_get).  The knobs are process-wide defaults of
- * later launches too. */
+ * "serial" and "flux_ctas" with dccm_tune_get).  The knobs are
+ * process-wide defaults of later launches too. */
 int dccm_step_autotune(dccm_step *step, const char *cache_path, int *chosen);
 int dccm_tune_set(const char *knob, int value);
 int dccm_tune_get(const char *knob, int *value);

@@ -143,8 +143,9 @@ def test_host_copies_match_device_run(dccm, oracle, synth, cuda, pinned):
         if pinned:
             assert choice["upload_order"] in (1, 2) and 1 <= choice["host_path"] <= 16 and len(ms) == 32
             assert min(ms.values()) == ms["%d,%d" % (choice["upload_order"], choice["host_path"])] > 0
+            assert choice["flux_ctas"] in (0, dccm.tune_get("flux_ctas"))
         else:
-            assert choice == {"upload_order": 0, "host_path": 0} and set(ms.values()) == {0.0}
+            assert choice == {"upload_order": 0, "host_path": 0, "flux_ctas": 0} and set(ms.values()) == {0.0}
         check(choice)
     finally:
         for k, v in saved.items():
@@ -190,22 +191,24 @@ def test_autotune_keeps_results_and_caches(dccm, oracle, synth, cuda, tmp_path):
         torch.cuda.synchronize()
         return [o.cpu().clone() for o in outs]
 
-    saved = {k: dccm.tune_get(k) for k in dccm.Step.KNOBS + ["serial"]}
+    saved = {k: dccm.tune_get(k) for k in dccm.Step.KNOBS + ["serial", "flux_ctas"]}
     try:
         want = run()
         cache = str(tmp_path / "tune.jsonl")
         first = step.autotune(cache)
-        assert set(first) == set(dccm.Step.KNOBS + ["serial"]) and first["serial"] in (0, 1)
+        assert set(first) == set(dccm.Step.KNOBS + ["serial", "flux_ctas"]) and first["serial"] in (0, 1)
         assert all(torch.equal(a, b) for a, b in zip(run(), want))
         line = open(cache).read()
-        assert '"serial": ' in line and '"step_ms": ' in line
+        assert '"serial": ' in line and '"flux_ctas": ' in line and '"step_ms": ' in line
         assert step.autotune(cache) == first
-        for serial in (0, 1):  # a step recorded in either launch mode, same bits
-            dccm.tune_set("serial", serial)
+        # a step recorded in either launch mode, or with the flux grid capped
+        # at a few CTAs (each walks many columns), gives the same bits
+        for knob, v in (("serial", 0), ("serial", 1), ("flux_ctas", 3)):
+            dccm.tune_set(knob, v)
             S = bench.gpu_setup(w, inp, dccm, synth, torch, torch.device("cuda", 0))
             step = S["steps"]["mixed"]
             outs = [S["grid"][0], S["spec_out"][0]] + [S["dflux"][n] for n in dccm.FLUX_OUT]
-            assert all(torch.equal(a, b) for a, b in zip(run(), want)), serial
+            assert all(torch.equal(a, b) for a, b in zip(run(), want)), (knob, v)
     finally:
         for k, v in saved.items():
             dccm.tune_set(k, v)
