@@ -435,9 +435,9 @@ def host_copies(S, groups, dccm, torch):
 # each stage's kernels in one ncu capture of `bench.py --profile-steps`,
 # kept with the profiles of the c3 step; null where not captured.
 TRAFFIC = {
-    "c3": {"legendre_inverse": int((7.683584 + 12.144896) * 1e6 + 2304), "fft_inverse": int(11.3408e6 + 3584),
-           "fft_forward": int(33.62304e6 + 57344), "legendre_forward": int(18.947072e6 + 1792),
-           "remap": int(4.069376e6), "bulk_flux": int(7.708928e6 + 768)},
+    "c3": {"legendre_inverse": int((7.686912 + 12.131584) * 1e6 + 1280), "fft_inverse": int(11.341056e6 + 512),
+           "fft_forward": int(33.623296e6 + 56064), "legendre_forward": int(18.93888e6),
+           "remap": int(4.062976e6), "bulk_flux": int(7.707392e6 + 768)},
 }
 # FP64 peak: measured on the device by dccm_fp64_peak (independent DFMA
 # chains on every SM) at the start of the run; the nominal figure (2 DFMA
