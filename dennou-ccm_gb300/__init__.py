@@ -667,9 +667,10 @@ class Step:
 
     def autotune_host(self, h2d, d2h=None, stream=None):
         """dccm_step_autotune_host: upload order, copy path and flux CTA cap
-        for these copy lists, by timing (the step runs about 400 times);
+        for these copy lists, by timing (the step runs about 420 times);
         host_path is 1 + the mask of copy groups moved through the host
-        mapping, flux_ctas 0 the flux kernel's full grid."""
+        mapping (bit 4: the flux kernel reads and writes its host rows
+        itself), flux_ctas 0 the flux kernel's full grid."""
         c = h2d if isinstance(h2d, HostCopies) else HostCopies(h2d, d2h or [])
         out = (ctypes.c_int * 3)()
         ms = (ctypes.c_float * 32)()

@@ -10,7 +10,10 @@
 // behaviours without a single defined result are given the meaning stated
 // in dccm_gb300.h (per-type sea-ice flag in the final loop; slot-3 latent
 // heat flux as the fraction-weighted merge of slots 1 and 2).
+#include <string.h>
+
 #include "common.cuh"
+#include "flux_rows.cuh"
 
 namespace dccm {
 namespace flux {
@@ -76,7 +79,29 @@ __device__ __forceinline__ void bulk_coef_l82(double Ri, double z0m, double z0h,
   cq = fmax(fmin(th, QVapBulkCoefMax), QVapBulkCoefMin);
 }
 
-__global__ void __launch_bounds__(256) bulk_flux_column(Ptrs p, Geom g) {
+// Input row k of column t (linear interior index) at device element c: the
+// bound host row, or the device array.  HOST = false is the kernel without
+// host rows (the table is not read).
+template <bool HOST>
+__device__ __forceinline__ double rd(const HostRows &h, int k, const double *dev, int64_t c, int64_t t) {
+  if (HOST && h.in[k]) return h.in[k][t];
+  return dev[c];
+}
+// A bound input's value into its device row: after every input is read, so
+// that no load waits behind these stores.
+template <bool HOST>
+__device__ __forceinline__ void mirror(const HostRows &h, int k, int64_t t, double v) {
+  if (HOST && h.in[k]) h.din[k][t] = v;
+}
+// Output row k: the device array, and the bound host row.
+template <bool HOST>
+__device__ __forceinline__ void wr(const HostRows &h, int k, double *dev, int64_t c, int64_t t, double v) {
+  dev[c] = v;
+  if (HOST && h.out[k]) h.out[k][t] = v;
+}
+
+template <bool HOST>
+__global__ void __launch_bounds__(256) bulk_flux_column(Ptrs p, Geom g, const __grid_constant__ HostRows h) {
   constexpr double GasRDry = GasRUniv / MolWtDry;
   constexpr double GasRWet = GasRUniv / MolWtWet;
   constexpr double EpsV = MolWtWet / MolWtDry;
@@ -89,13 +114,13 @@ __global__ void __launch_bounds__(256) bulk_flux_column(Ptrs p, Geom g) {
     const int64_t c = (int64_t)(g.IS - 1 + ii) + (int64_t)g.IA * (g.JS - 1 + jj);
     const int64_t P = g.plane;
 
-    const double SIceCon = p.Ice[c];
-    const double Ps = p.Ps[c];
-    const double Ta = p.Ta[c];
-    const double q1 = p.q1[c];
-    const double U = p.U[c], V = p.V[c];
-    const double zs = p.Zs[c];
-    const double SDw = p.SDw[c], LDw = p.LDw[c];
+    const double SIceCon = rd<HOST>(h, I_ICE, p.Ice, c, t);
+    const double Ps = rd<HOST>(h, I_PS, p.Ps, c, t);
+    const double Ta = rd<HOST>(h, I_TA, p.Ta, c, t);
+    const double q1 = rd<HOST>(h, I_Q1, p.q1, c, t);
+    const double U = rd<HOST>(h, I_U, p.U, c, t), V = rd<HOST>(h, I_V, p.V, c, t);
+    const double zs = rd<HOST>(h, I_ZS, p.Zs, c, t);
+    const double SDw = rd<HOST>(h, I_SDW, p.SDw, c, t), LDw = rd<HOST>(h, I_LDW, p.LDw, c, t);
     const double z0m = RoughLength;
     const double z0h = RoughLenHeatFactor * z0m;
     const double humd = 1.0;
@@ -116,8 +141,8 @@ __global__ void __launch_bounds__(256) bulk_flux_column(Ptrs p, Geom g) {
     const bool ice = Frac[1] > 1e-12;
 #pragma unroll
     for (int n = 0; n < 2; ++n) {
-      Tsn[n] = p.Ts[c + P * n];
-      Albn[n] = p.Alb[c + P * n];
+      Tsn[n] = rd<HOST>(h, I_TS + n, p.Ts, c + P * n, t);
+      Albn[n] = rd<HOST>(h, I_ALB + n, p.Alb, c + P * n, t);
       if (n == 1 && !ice) {
         rTs[n] = QSat[n] = SVT[n] = 0.0;
         continue;
@@ -191,17 +216,25 @@ __global__ void __launch_bounds__(256) bulk_flux_column(Ptrs p, Geom g) {
     }
 
     // Implicit-coupling back-substitution (:355-382).
-    const double c11 = p.C1[c], c12 = p.C1[c + P], c13 = p.C1[c + 2 * P], c14 = p.C1[c + 3 * P];
-    const double c21 = p.C2[c], c22 = p.C2[c + P], c23 = p.C2[c + 2 * P], c24 = p.C2[c + 3 * P];
+    const double c11 = rd<HOST>(h, I_C1, p.C1, c, t), c12 = rd<HOST>(h, I_C1 + 1, p.C1, c + P, t),
+                 c13 = rd<HOST>(h, I_C1 + 2, p.C1, c + 2 * P, t), c14 = rd<HOST>(h, I_C1 + 3, p.C1, c + 3 * P, t);
+    const double c21 = rd<HOST>(h, I_C2, p.C2, c, t), c22 = rd<HOST>(h, I_C2 + 1, p.C2, c + P, t),
+                 c23 = rd<HOST>(h, I_C2 + 2, p.C2, c + 2 * P, t), c24 = rd<HOST>(h, I_C2 + 3, p.C2, c + 3 * P, t);
+    if (HOST) {  // every input has been read: the bound ones into their device rows
+      const double vin[NIN] = {SIceCon, Ps, Ta, q1, U, V, zs, SDw, LDw, Tsn[0], Tsn[1], Albn[0], Albn[1],
+                               c11, c12, c13, c14, c21, c22, c23, c24};
+#pragma unroll
+      for (int k = 0; k < NIN; ++k) mirror<HOST>(h, k, t, vin[k]);
+    }
     const double DFsDT1 = -CpDry * SfcExner * CTemp3 * rExner;
     const double f1 = 1.0 / (c11 + CVel3) * (WSX3 + c21);
     const double f2 = 1.0 / (c12 + CVel3) * (WSY3 + c22);
     const double f3 = 1.0 / (c13 - DFsDT1) * (Sen3 + c23);
     const double f4 = 1.0 / (c14 + humd * CQ3) * (QV3 + c24);
-    p.DelV[c] = f1;
-    p.DelV[c + P] = f2;
-    p.DelV[c + 2 * P] = f3;
-    p.DelV[c + 3 * P] = f4;
+    wr<HOST>(h, O_DELV, p.DelV, c, t, f1);
+    wr<HOST>(h, O_DELV + 1, p.DelV, c + P, t, f2);
+    wr<HOST>(h, O_DELV + 2, p.DelV, c + 2 * P, t, f3);
+    wr<HOST>(h, O_DELV + 3, p.DelV, c + 3 * P, t, f4);
 
     const double sfac = CpDry * SfcExner * rExner;
     double Lat3 = 0.0;
@@ -229,32 +262,34 @@ __global__ void __launch_bounds__(256) bulk_flux_column(Ptrs p, Geom g) {
         dfdt = +4.0 * StB * (Tsn[n] * Tsn[n] * Tsn[n]) + CpDry * CTemp[n] +
                aL[n] * humd * CQ[n] * (aL[n] * QSat[n] * (1.0 / GasRWet) * (rTs[n] * rTs[n]));
       }
-      p.Fns[c + P * n] = fns;
-      p.Fsr[c + P * n] = fsr;
-      p.DFdT[c + P * n] = dfdt;
-      p.WSX[c + P * n] = WSX[n];
-      p.WSY[c + P * n] = WSY[n];
-      p.Sen[c + P * n] = Sen[n];
-      p.QV[c + P * n] = QV[n];
-      p.Lat[c + P * n] = LatH[n];
-      p.CVel[c + P * n] = CVel[n];
-      p.CTemp[c + P * n] = CTemp[n];
-      p.CQ[c + P * n] = CQ[n];
-      p.SUw[c + P * n] = SUw[n];
-      p.LUw[c + P * n] = LUw[n];
+      const int64_t cn = c + P * n;
+      wr<HOST>(h, O_FNS + n, p.Fns, cn, t, fns);
+      wr<HOST>(h, O_FSR + n, p.Fsr, cn, t, fsr);
+      wr<HOST>(h, O_DFDT + n, p.DFdT, cn, t, dfdt);
+      wr<HOST>(h, O_WSX + n, p.WSX, cn, t, WSX[n]);
+      wr<HOST>(h, O_WSY + n, p.WSY, cn, t, WSY[n]);
+      wr<HOST>(h, O_SEN + n, p.Sen, cn, t, Sen[n]);
+      wr<HOST>(h, O_QV + n, p.QV, cn, t, QV[n]);
+      wr<HOST>(h, O_LAT + n, p.Lat, cn, t, LatH[n]);
+      wr<HOST>(h, O_CVEL + n, p.CVel, cn, t, CVel[n]);
+      wr<HOST>(h, O_CTEMP + n, p.CTemp, cn, t, CTemp[n]);
+      wr<HOST>(h, O_CQ + n, p.CQ, cn, t, CQ[n]);
+      wr<HOST>(h, O_SUW + n, p.SUw, cn, t, SUw[n]);
+      wr<HOST>(h, O_LUW + n, p.LUw, cn, t, LUw[n]);
     }
-    p.WSX[c + 2 * P] = WSX3;
-    p.WSY[c + 2 * P] = WSY3;
-    p.Sen[c + 2 * P] = Sen3;
-    p.QV[c + 2 * P] = QV3;
-    p.Lat[c + 2 * P] = Lat3;
-    p.CVel[c + 2 * P] = CVel3;
-    p.CTemp[c + 2 * P] = CTemp3;
-    p.CQ[c + 2 * P] = CQ3;
-    p.SUw[c + 2 * P] = SUw3;
-    p.LUw[c + 2 * P] = LUw3;
-    p.Ts[c + 2 * P] = Ts3;
-    p.Alb[c + 2 * P] = Alb3;
+    const int64_t c3 = c + 2 * P;
+    wr<HOST>(h, O_WSX + 2, p.WSX, c3, t, WSX3);
+    wr<HOST>(h, O_WSY + 2, p.WSY, c3, t, WSY3);
+    wr<HOST>(h, O_SEN + 2, p.Sen, c3, t, Sen3);
+    wr<HOST>(h, O_QV + 2, p.QV, c3, t, QV3);
+    wr<HOST>(h, O_LAT + 2, p.Lat, c3, t, Lat3);
+    wr<HOST>(h, O_CVEL + 2, p.CVel, c3, t, CVel3);
+    wr<HOST>(h, O_CTEMP + 2, p.CTemp, c3, t, CTemp3);
+    wr<HOST>(h, O_CQ + 2, p.CQ, c3, t, CQ3);
+    wr<HOST>(h, O_SUW + 2, p.SUw, c3, t, SUw3);
+    wr<HOST>(h, O_LUW + 2, p.LUw, c3, t, LUw3);
+    wr<HOST>(h, O_TS3, p.Ts, c3, t, Ts3);
+    wr<HOST>(h, O_ALB3, p.Alb, c3, t, Alb3);
   }
 }
 
@@ -291,7 +326,7 @@ static Ptrs make_ptrs(const dccm_sfc_bulk_flux_args *a) {
   return p;
 }
 
-int launch(const Ptrs &p, const dccm_sfc_grid *g, double sig1, cudaStream_t s) {
+int launch(const Ptrs &p, const dccm_sfc_grid *g, double sig1, cudaStream_t s, const HostRows *hr = nullptr) {
   Geom geo;
   geo.plane = (int64_t)g->IA * g->JA;
   geo.IA = g->IA;
@@ -309,9 +344,49 @@ int launch(const Ptrs &p, const dccm_sfc_grid *g, double sig1, cudaStream_t s) {
   // leave them more issue slots (flux_ctas, chosen on whole-step timings).
   const int64_t cap = tunables().flux_ctas > 0 ? (int64_t)tunables().flux_ctas : (int64_t)sm_count() * 16;
   if (blocks > cap) blocks = cap;
-  bulk_flux_column<<<(unsigned)blocks, threads, 0, s>>>(p, geo);
+  HostRows none;
+  if (!hr) {
+    memset(&none, 0, sizeof none);
+    hr = &none;
+  }
+  if (hr->any)
+    bulk_flux_column<true><<<(unsigned)blocks, threads, 0, s>>>(p, geo, *hr);
+  else
+    bulk_flux_column<false><<<(unsigned)blocks, threads, 0, s>>>(p, geo, *hr);
   DCCM_LAUNCH_CHECK();
   return DCCM_OK;
+}
+
+double *in_row(const dccm_sfc_bulk_flux_args &a, const dccm_sfc_grid &g, int k) {
+  const void *base[NIN] = {a.SIceCon, a.SfcPress, a.SfcAirTemp, a.QVap1, a.WindU, a.WindV, a.SfcHeight,
+                           a.SDwRFlx, a.LDwRFlx, a.SfcTemp, a.SfcTemp, a.SfcAlbedo, a.SfcAlbedo,
+                           a.ImplCplCoef1, a.ImplCplCoef1, a.ImplCplCoef1, a.ImplCplCoef1,
+                           a.ImplCplCoef2, a.ImplCplCoef2, a.ImplCplCoef2, a.ImplCplCoef2};
+  int slot = 0;
+  if (k >= I_TS && k < I_ALB) slot = k - I_TS;
+  else if (k >= I_ALB && k < I_C1) slot = k - I_ALB;
+  else if (k >= I_C1 && k < I_C2) slot = k - I_C1;
+  else if (k >= I_C2) slot = k - I_C2;
+  return row_start(base[k], g, slot);
+}
+
+double *out_row(const dccm_sfc_bulk_flux_args &a, const dccm_sfc_grid &g, int k) {
+  if (k < O_FNS) return row_start(a.DelVarImplCPL, g, k - O_DELV);
+  if (k < O_FSR) return row_start(a.SfcHFlx_ns, g, k - O_FNS);
+  if (k < O_DFDT) return row_start(a.SfcHFlx_sr, g, k - O_FSR);
+  if (k < O_WSX) return row_start(a.DSfcHFlxDTs, g, k - O_DFDT);
+  if (k == O_TS3) return row_start(a.SfcTemp, g, 2);
+  if (k == O_ALB3) return row_start(a.SfcAlbedo, g, 2);
+  const void *three[10] = {a.WindStressX, a.WindStressY, a.SenHFlx, a.QVapMFlx, a.LatHFlx,
+                           a.SfcVelTransCoef, a.SfcTempTransCoef, a.SfcQVapTransCoef, a.SUwRFlx, a.LUwRFlx};
+  return row_start(three[(k - O_WSX) / 3], g, (k - O_WSX) % 3);
+}
+
+int launch_rows(const dccm_sfc_bulk_flux_args *a, const dccm_sfc_grid *g, const HostRows *h, cudaStream_t s) {
+  DCCM_TRY(check_args(a));
+  DCCM_TRY(check_grid(g));
+  if (h && h->any && g->JE != g->JS) return DCCM_ERR_UNSUPPORTED;  // host rows: one interior row
+  return launch(make_ptrs(a), g, a->a_Sig1Info[0], s, h);
 }
 
 // Host entry point state: one device staging area per process.

@@ -21,6 +21,7 @@
 #include <new>
 #include <vector>
 
+#include "flux_rows.cuh"
 #include "sht_plan.cuh"
 
 struct dccm_sht_plan {
@@ -62,6 +63,10 @@ struct dccm_step {
   // choices of dccm_step_autotune_host (0: the process-wide knobs; flux
   // CTA cap -1: the process-wide knob)
   int host_order = 0, host_path = 0, host_flux_ctas = -1;
+  // surface rows of that graph's copies bound to the flux kernel (host_path
+  // bit 4), used while the graph is recorded
+  dccm::flux::HostRows hrows = {};
+  bool host_capture = false;
   // stage times of the last dccm_step_run_timed (ms), for the upload order
   float stage_ms[6] = {};
   bool have_stage_ms = false;
@@ -174,7 +179,12 @@ static int stage_remap(dccm_step *st, cudaStream_t s) {
 }
 extern "C" int dccm_sfc_bulk_flux_get_dev(const dccm_sfc_bulk_flux_args *, const dccm_sfc_grid *, void *);
 static int stage_flux(dccm_step *st, cudaStream_t s) {
-  if (st->d.flux) DCCM_TRY(dccm_sfc_bulk_flux_get_dev(&st->flux, &st->fgrid, (void *)s));
+  if (st->d.flux) {
+    if (st->host_capture && st->hrows.any)
+      DCCM_TRY(flux::launch_rows(&st->flux, &st->fgrid, &st->hrows, s));
+    else
+      DCCM_TRY(dccm_sfc_bulk_flux_get_dev(&st->flux, &st->fgrid, (void *)s));
+  }
   DCCM_TRY(run_remaps(st->remaps_post, s));
   if (st->d.implcpl)
     DCCM_TRY(dccm_implcpl_backward_dev(st->d.implcpl, st->icf.xyz_DUDt, st->icf.xyz_DVDt, st->icf.xyz_DTempDt,
@@ -290,11 +300,14 @@ static int upload_segs(dccm_step *st, const std::vector<Seg> &segs, SegTab &t) {
 // spectra), bit 3 the surface downloads; a set bit moves every copy of the
 // group whose host buffer has a device mapping in the group's one kernel
 // (SMs read or write the host memory over the link), a clear bit uses
-// staging and copy engines as described above.
-constexpr int PATH_SHT_IN = 1, PATH_SFC_IN = 2, PATH_SHT_OUT = 4, PATH_SFC_OUT = 8;
+// staging and copy engines as described above.  Bit 4: the surface copies
+// that are exactly one row of the flux kernel (bind_flux_rows) are left to
+// the flux kernel, which reads and writes those host rows itself as it
+// computes the columns.
+constexpr int PATH_SHT_IN = 1, PATH_SFC_IN = 2, PATH_SHT_OUT = 4, PATH_SFC_OUT = 8, PATH_SFC_DIRECT = 16;
 static int path_mask(const dccm_step *st) {
   const int p = st->host_path ? st->host_path : tunables().host_path;
-  return p >= 1 && p <= 16 ? p - 1 : 0;
+  return p >= 1 && p <= 32 ? p - 1 : 0;
 }
 
 static int prepare_set(dccm_step *st, std::vector<dccm_host_copy> v, bool h2d, CopySet &cs, bool mapped_all) {
@@ -717,18 +730,91 @@ static void sort_copies(dccm_step *st, const dccm_host_copy *h2d, int nh2d, cons
 }
 
 // Records the graph of dccm_step_run_host for these (page-locked) copy lists.
+// Whether the flux kernel can take surface rows from the copy lists: a flux
+// with one interior row (the ocean column list) and nothing after it in the
+// surface branch that reads its outputs.
+static bool flux_rows_possible(const dccm_step *st) {
+  return st->d.flux && !st->d.implcpl && st->remaps_post.empty() && st->fgrid.JE == st->fgrid.JS &&
+         st->fgrid.IE >= st->fgrid.IS;
+}
+
+// Moves the surface copies that are exactly one flux row (input rows that no
+// remap writes; output rows) out of the copy groups into st->hrows.  A row
+// that two uploads target stays with the copies; of several downloads of
+// one row the first is bound.  Host buffers need a device mapping.
+static void bind_flux_rows(dccm_step *st, HostPlan &hp) {
+  using namespace dccm::flux;
+  memset(&st->hrows, 0, sizeof st->hrows);
+  if (!flux_rows_possible(st)) return;
+  const size_t row_bytes = (size_t)(st->fgrid.IE - st->fgrid.IS + 1) * sizeof(double);
+  std::vector<Span> remap_dst;
+  for (const dccm_step_remap &r : st->remaps) {
+    if (!r.plan || r.nfields <= 0) continue;
+    int64_t nnz = 0, ns = 0, nr = 0;
+    dccm_remap_plan_info(r.plan, &nnz, &ns, &nr);
+    const int nsub = r.nsub > 0 ? r.nsub : r.nfields;
+    const int64_t ld2 = r.nsub > 0 ? r.ld_dst2 : 0;
+    for (int f = 0; f < r.nfields; ++f)
+      add_span(remap_dst, r.dst + (f % nsub) * r.ld_dst + (f / nsub) * ld2, (size_t)nr * sizeof(double));
+  }
+  auto mapped = [](const void *host) -> void * {
+    cudaPointerAttributes a;
+    void *d = nullptr;
+    if (cudaPointerGetAttributes(&a, host) == cudaSuccess && a.type == cudaMemoryTypeHost) d = a.devicePointer;
+    cudaGetLastError();
+    return d;
+  };
+  int uses[NIN] = {};
+  for (const dccm_host_copy &c : hp.sfc_in)
+    for (int k = 0; k < NIN; ++k)
+      if (c.dev == in_row(st->flux, st->fgrid, k)) ++uses[k];
+  std::vector<dccm_host_copy> keep;
+  for (const dccm_host_copy &c : hp.sfc_in) {
+    int row = -1;
+    for (int k = 0; k < NIN && row < 0; ++k)
+      if (c.dev == in_row(st->flux, st->fgrid, k) && c.bytes == row_bytes && uses[k] == 1) row = k;
+    void *hd = row >= 0 && !hits(remap_dst, c.dev, c.bytes) ? mapped(c.host) : nullptr;
+    if (!hd) {
+      keep.push_back(c);
+      continue;
+    }
+    st->hrows.in[row] = (const double *)hd;
+    st->hrows.din[row] = in_row(st->flux, st->fgrid, row);
+    st->hrows.any = 1;
+  }
+  hp.sfc_in.swap(keep);
+  keep.clear();
+  for (const dccm_host_copy &c : hp.sfc_out) {
+    int row = -1;
+    for (int k = 0; k < NOUT && row < 0; ++k)
+      if (c.dev == out_row(st->flux, st->fgrid, k) && c.bytes == row_bytes && !st->hrows.out[k]) row = k;
+    void *hd = row >= 0 ? mapped(c.host) : nullptr;
+    if (!hd) {
+      keep.push_back(c);
+      continue;
+    }
+    st->hrows.out[row] = (double *)hd;
+    st->hrows.any = 1;
+  }
+  hp.sfc_out.swap(keep);
+}
+
 static int build_host_graph(dccm_step *st, const dccm_host_copy *h2d, int nh2d, const dccm_host_copy *d2h,
                             int nd2h) {
   drop_host_graph(st);
   HostPlan hp;
   sort_copies(st, h2d, nh2d, d2h, nd2h, hp);
+  memset(&st->hrows, 0, sizeof st->hrows);
+  if (path_mask(st) & PATH_SFC_DIRECT) bind_flux_rows(st, hp);
   HostSets hs;
   DCCM_TRY(prepare_sets(st, hp, hs));
   cudaGraph_t g = nullptr;
   Tunables &T = tunables();
   const int flux_ctas = T.flux_ctas;
   if (st->host_flux_ctas >= 0) T.flux_ctas = st->host_flux_ctas;
+  st->host_capture = true;
   const int rc = capture(st, &hs, &g);
+  st->host_capture = false;
   T.flux_ctas = flux_ctas;
   DCCM_TRY(rc);
   st->hgraph = g;
@@ -822,6 +908,26 @@ extern "C" int dccm_step_autotune_host(dccm_step *st, void *stream, const dccm_h
     if (best_t[c] < best_t[bc]) bc = c;
   st->host_order = 1 + bc / 16;
   st->host_path = 1 + bc % 16;
+  // The surface rows left to the flux kernel (host_path bit 4), with either
+  // upload order, against that winner: two interleaved rounds.
+  if (flux_rows_possible(st)) {
+    const int ord[3] = {st->host_order, 1, 2};
+    const int path[3] = {st->host_path, 1 + ((bc % 16) | PATH_SFC_DIRECT), 1 + ((bc % 16) | PATH_SFC_DIRECT)};
+    float tk[3] = {1e30f, 1e30f, 1e30f};
+    for (int round = 0; round < 2; ++round)
+      for (int k = 0; k < 3; ++k) {
+        st->host_order = ord[k];
+        st->host_path = path[k];
+        float t;
+        DCCM_TRY(time_one(&t));
+        tk[k] = std::min(tk[k], t);
+      }
+    int kb = 0;
+    for (int k = 1; k < 3; ++k)
+      if (tk[k] < tk[kb]) kb = k;
+    st->host_order = ord[kb];
+    st->host_path = path[kb];
+  }
   // The flux grid's CTA cap for this graph: with host copies the surface
   // branch's results are the first downloads, so a faster flux can win
   // over the cap chosen for the step without copies.  The process-wide
@@ -1090,7 +1196,7 @@ extern "C" int dccm_tune_set(const char *knob, int value) {
     if (value > 2) return DCCM_ERR_INVALID_ARG;
     T.upload_order = value;
   } else if (!strcmp(knob, "host_path")) {
-    if (value > 16) return DCCM_ERR_INVALID_ARG;
+    if (value > 32) return DCCM_ERR_INVALID_ARG;
     T.host_path = value;
   }
   else return DCCM_ERR_INVALID_ARG;

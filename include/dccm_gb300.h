@@ -465,11 +465,19 @@ int dccm_step_host_release(dccm_step *step);
  * transforms' uploads, bit 1 the surface uploads, bit 2 the transforms'
  * downloads (grid, spectra), bit 3 the surface downloads: a set bit moves
  * the group in one kernel through the host mapping, a clear bit by copy
- * engines with host-contiguous runs through a staging buffer.  It replays
+ * engines with host-contiguous runs through a staging buffer.  Bit 4 (a
+ * flux on one interior row, no implicit coupling or remaps after it): the
+ * surface copies that are exactly one interior row of a flux input or
+ * output are done by the flux kernel itself, which reads those host rows
+ * and writes its results to them through their device mapping as it
+ * computes the columns (and still fills the device arrays, as the copies
+ * would).  It replays
  * the step with each of the 32 combinations (2 interleaved rounds of 6
  * replays on stream: the step's outputs are written as by
- * dccm_step_run_host), keeps the fastest for this step, then times the
- * winner with the flux kernel's full grid against the process-wide
+ * dccm_step_run_host), keeps the fastest, times it against the same mask
+ * with bit 4 under either upload order and keeps the fastest of the three,
+ * then times the winner with the flux kernel's full grid against the
+ * process-wide
  * "flux_ctas" cap (with host copies the surface results are the first
  * downloads, so the fastest flux can win) and leaves the graph recorded.
  * chosen (3 ints, may be NULL) receives the order, host_path and the flux

@@ -128,12 +128,21 @@ def test_host_copies_match_device_run(dccm, oracle, synth, cuda, pinned):
         for _ in range(2):
             for h, _ in d2h:
                 h.zero_()
+            for _, d in h2d + d2h:
+                d.zero_()
+            torch.cuda.synchronize()
             step.run_host(hc)
             for (h, _), ref in zip(d2h, want):
                 assert torch.equal(h, ref), tag
+            # the device arrays as the copies leave them (also when the flux
+            # kernel reads and writes the host rows itself, path bit 4)
+            for (_, d), ref in zip(d2h, want):
+                assert torch.equal(d.cpu(), ref), tag
+            for h, d in h2d:
+                assert torch.equal(d.cpu(), h), tag
     try:
         for order in (1, 2, 0):
-            for path in (1, 16, 1 + 2, 1 + 4 + 8):
+            for path in (1, 16, 1 + 2, 1 + 4 + 8, 1 + 16, 32):
                 dccm.tune_set("upload_order", order)
                 dccm.tune_set("host_path", path)
                 step.host_release()
@@ -141,8 +150,11 @@ def test_host_copies_match_device_run(dccm, oracle, synth, cuda, pinned):
         choice = step.autotune_host(hc)
         ms = choice.pop("candidates_ms")
         if pinned:
-            assert choice["upload_order"] in (1, 2) and 1 <= choice["host_path"] <= 16 and len(ms) == 32
-            assert min(ms.values()) == ms["%d,%d" % (choice["upload_order"], choice["host_path"])] > 0
+            assert choice["upload_order"] in (1, 2) and 1 <= choice["host_path"] <= 32 and len(ms) == 32
+            base = (choice["host_path"] - 1) % 16 + 1  # without bit 4: the best of the 32
+            assert min(ms.values()) in (ms["1,%d" % base], ms["2,%d" % base]) and min(ms.values()) > 0
+            if choice["host_path"] <= 16:
+                assert min(ms.values()) == ms["%d,%d" % (choice["upload_order"], choice["host_path"])]
             assert choice["flux_ctas"] in (0, dccm.tune_get("flux_ctas"))
         else:
             assert choice == {"upload_order": 0, "host_path": 0, "flux_ctas": 0} and set(ms.values()) == {0.0}
