@@ -467,17 +467,23 @@ def stage_work(S, inp, groups):
             "remap": (remap, None), "bulk_flux": (504 * S["ncol"], None)}
 
 
-def roofline(S, inp, groups, stage_ms, workload, fp64_peak):
+def roofline(S, inp, groups, stage_ms, workload, fp64_peak, flux_alone=None):
     """Per-stage roofline against the measured copy bandwidth; the dominant
     (longest) stage is the headline.  Legendre stages also report their
     tensor rate (useful flops over the measured BF16 peak); the flux
     kernel, bound by the FP64 pipe, reports its FP64 rate as counted by ncu
-    over the FP64 peak (2 DFMA lanes per SM and clock)."""
+    over the FP64 peak (2 DFMA lanes per SM and clock).  flux_alone: the
+    flux kernel timed alone on its full grid when the step caps its grid;
+    its roofline is then taken from that time (the step's time and cap are
+    kept beside it)."""
     hbm, bf16, src_peak = peaks()
     names = dccm_stages()
     work = stage_work(S, inp, groups)
     traffic = TRAFFIC.get(workload, {})
     stages = {}
+    stage_ms = list(stage_ms)
+    if flux_alone:
+        stage_ms[names.index("bulk_flux")] = flux_alone["ms"]
     for n, ms in zip(names, stage_ms):
         q, fl = work[n]
         ach = q / (ms / 1e3) / 1e9
@@ -489,6 +495,9 @@ def roofline(S, inp, groups, stage_ms, workload, fp64_peak):
                             "algorithmic_flops": fl}
         stages[n] = st
     stages["bulk_flux"]["limiter"] = "FP64 pipe, not HBM"
+    if flux_alone:
+        stages["bulk_flux"]["launch"] = ("full grid, timed alone; in the step its grid is capped at %d CTAs "
+                                         "(%.4f ms there)" % (flux_alone["step_cta_cap"], flux_alone["ms_in_step"]))
     f64 = FLUX_FP64_FLOPS_PER_COLUMN * S["ncol"]
     if f64:
         tf = f64 / (stages["bulk_flux"]["ms"] / 1e3) / 1e12
@@ -690,7 +699,27 @@ def gpu_bench(args, w, inp, rank, world):
         stage_ms += np.array(S["steps"]["mixed"].run_timed(stream))
     stage_ms /= nt
     fp64_peak = dccm.fp64_peak(stream)
-    roof = roofline(S, inp, groups, stage_ms, args.workload, fp64_peak)
+    # The whole-step autotune may cap the flux kernel's grid (it runs beside
+    # the transforms and then leaves them issue slots); the kernel's own
+    # roofline is taken on its full grid, timed alone the same way.
+    flux_alone = None
+    cap = tuned["mixed"].get("flux_ctas", 0)
+    if cap:
+        saved_cap = dccm.tune_get("flux_ctas")
+        dccm.tune_set("flux_ctas", 0)
+        ts = []
+        for k in range(max(3, args.warmup) + nt):
+            flush.fill_(float(k))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            dccm.DSFCM_Util_SfcBulkFlux_Get(S["dflux"], *S["fgrid"], device=True, stream=stream)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if k >= max(3, args.warmup):
+                ts.append(e0.elapsed_time(e1))
+        dccm.tune_set("flux_ctas", saved_cap)
+        flux_alone = {"ms": float(np.mean(ts)), "ms_in_step": float(stage_ms[5]), "step_cta_cap": cap}
+    roof = roofline(S, inp, groups, stage_ms, args.workload, fp64_peak, flux_alone)
     roof["fp64_peak"] = {"measured": fp64_peak, "nominal": FP64_NOMINAL_TFLOPS, "unit": "TFLOP/s"}
 
     # end to end through the public API with host buffers (pinned)
