@@ -1143,7 +1143,7 @@ extern "C" int dccm_step_autotune(dccm_step *st, const char *cache_path, int *ch
     }
     // Whole-graph pass: the stage pass's choices first, so a tie keeps
     // them.  The flux runs beside the transforms, so its CTA size and its
-    // grid's CTA cap are judged here as well (fewer flux warps leave the
+    // grid's CTA cap are chosen here as well (fewer flux warps leave the
     // transforms more issue slots; the stage pass times the flux alone).
     T.flux_ctas = 0;  // from the full grid, whatever an earlier step chose
     auto first = [](int v, std::initializer_list<int> rest) {
