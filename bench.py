@@ -138,7 +138,7 @@ def remap_index(w, inp, g, gen):
 
 # --------------------------------------------------------------- clocks
 # NVML poller run as its own process (so that it takes no time from the
-# launching thread): SM clock and clock-event reason bits every 0.5 ms until its
+# launching thread): SM clock and clock-event reason bits every 0.1 ms until its
 # standard input closes, then one JSON summary line.  argv[1]: the PCI bus id
 # of the GPU in use, or "" when NVML sees one GPU.  Read-only NVML queries.
 _NVML_POLL = r"""
@@ -155,9 +155,12 @@ else:
 get_rs = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or lib.nvmlDeviceGetCurrentClocksThrottleReasons
 clk, cmax, rs = ctypes.c_uint(), ctypes.c_uint(), ctypes.c_ulonglong()
 lib.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(cmax))
+for _ in range(3):  # first calls of each query are slow: before the region
+    lib.nvmlDeviceGetClockInfo(h, 1, ctypes.byref(clk))
+    get_rs(h, ctypes.byref(rs))
 sm, bits = [], 0
 print("ready", flush=True)
-while not select.select([sys.stdin], [], [], 0.0005)[0]:
+while not select.select([sys.stdin], [], [], 0.0001)[0]:
     if lib.nvmlDeviceGetClockInfo(h, 1, ctypes.byref(clk)) == 0 and get_rs(h, ctypes.byref(rs)) == 0:
         sm.append(clk.value)
         bits |= rs.value
@@ -168,7 +171,7 @@ print(json.dumps({"n": len(sm), "median": sm[len(sm) // 2] if sm else None, "max
 
 class Clocks:
     """SM clock and clock-event reasons sampled from the warm-up through the
-    end of the timed region: an NVML poller process (every 0.5 ms), or
+    end of the timed region: an NVML poller process (every 0.1 ms), or
     nvidia-smi -lms 20 where NVML cannot be loaded."""
 
     # NVML clocks event (throttle) reason bits
@@ -216,7 +219,7 @@ class Clocks:
                 return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "source": "nvml"}
             return {"sm_mhz": float(r["median"]), "sm_max_mhz": float(r["max"]),
                     "reasons": sorted(nm for bit, nm in self.REASONS.items() if r["bits"] & bit),
-                    "samples": r["n"], "source": "nvml, 0.5 ms"}
+                    "samples": r["n"], "source": "nvml, 0.1 ms"}
         if self.p is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.p.terminate()
