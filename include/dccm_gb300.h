@@ -465,28 +465,25 @@ int dccm_step_host_release(dccm_step *step);
  * transforms' uploads, bit 1 the surface uploads, bit 2 the transforms'
  * downloads (grid, spectra), bit 3 the surface downloads: a set bit moves
  * the group in one kernel through the host mapping, a clear bit by copy
- * engines with host-contiguous runs through a staging buffer.  Bit 4 (a
- * flux on one interior row, no implicit coupling or remaps after it): the
- * surface copies that are exactly one interior row of a flux input or
- * output are done by the flux kernel itself, which reads those host rows
- * and writes its results to them through their device mapping as it
- * computes the columns (and still fills the device arrays, as the copies
- * would).  It replays
- * the step with each of the 32 combinations (2 interleaved rounds of 6
- * replays on stream: the step's outputs are written as by
- * dccm_step_run_host), keeps the fastest, times it against the same mask
- * with bit 4 under either upload order and keeps the fastest of the three,
- * then times the winner with the flux kernel's full grid against the
- * process-wide
- * "flux_ctas" cap (with host copies the surface results are the first
- * downloads, so the fastest flux can win) and leaves the graph recorded.
- * chosen (3 ints, may be NULL) receives the order, host_path and the flux
- * CTA cap of this graph (0: the full grid); all 0 with pageable buffers,
- * for which there is nothing to choose.  ms (32 floats, may be NULL)
- * receives each combination's device time per step at index
- * 16 (order - 1) + mask.  The process-wide knobs "upload_order",
- * "host_path" and "flux_ctas" (dccm_tune_set) apply to steps that have not
- * been tuned this way. */
+ * engines with host-contiguous runs through a staging buffer.  Bit 4 (a flux
+ * on one interior row, no implicit coupling or remaps after it): the surface
+ * copies that are exactly one interior row of a flux input or output are
+ * done by the flux kernel itself, which reads those host rows and writes its
+ * results to them through their device mapping as it computes the columns
+ * (and still fills the device arrays, as the copies would).  It replays the
+ * step with each of the 32 combinations (2 interleaved rounds of 6 replays
+ * on stream, each after a 256 MB device write; the step's outputs are
+ * written as by dccm_step_run_host), keeps the fastest, times it against the
+ * same mask with bit 4 under either upload order and keeps the fastest of
+ * the three, then times the winner with the flux kernel's full grid against
+ * the process-wide "flux_ctas" cap (with host copies the surface results are
+ * the first downloads, so the fastest flux can win) and leaves the graph
+ * recorded.  chosen (3 ints, may be NULL) receives the order, host_path and
+ * the flux CTA cap of this graph (0: the full grid); all 0 with pageable
+ * buffers, for which there is nothing to choose.  ms (32 floats, may be NULL)
+ * receives each combination's device time per step at index 16 (order - 1) +
+ * mask.  The process-wide knobs "upload_order", "host_path" and "flux_ctas"
+ * (dccm_tune_set) apply to steps that have not been tuned this way. */
 int dccm_step_autotune_host(dccm_step *step, void *stream, const dccm_host_copy *h2d, int nh2d,
                             const dccm_host_copy *d2h, int nd2h, int *chosen, float *ms);
 
@@ -498,7 +495,9 @@ int dccm_step_autotune_host(dccm_step *step, void *stream, const dccm_host_copy 
  * the transform chain), "tc_ctas" again and "flux_ctas" (CTA cap of the
  * flux kernel's grid, 0: 16 per SM) on replays of the whole step graph,
  * where the two branches run concurrently; applies the winners and
- * records the step's graph again.  With cache_path the choice is read
+ * records the step's graph again.  Every timed run follows a 256 MB
+ * device write, so that the step finds L2 as it does between the model's
+ * other work.  With cache_path the choice is read
  * from / appended to that file (one JSON object per line, keyed by the
  * GPU name and SM count and the step's shapes).  chosen (4 ints, may be
  * NULL) receives tc_ctas, fft_bb, flux_threads, remap_threads (read
