@@ -919,8 +919,8 @@ def main():
             import torch
             torch.distributed.destroy_process_group()
         return
-    cpu = None
-    if not args.no_cpu_baseline:
+    cpu = None  # the CPU baseline is a single-GPU figure: measured at N = 1 only
+    if not args.no_cpu_baseline and world == 1:
         step_s, nsample = cpu_measure(oracle, synth, w, inp, r["tables"], 3, 1, budget_s=15.0)
         cpu = {"value": nfl / step_s, "unit": "field-levels/s", "cores": oracle.get_threads(), "kind": "port",
                "sample": "3 steps: transforms of %d of %d field-levels (scaled), every remap and the bulk flux; "
