@@ -485,7 +485,8 @@ struct PackGroup {
   const int *xpos;
   unsigned short *A;
   long long ncoef, KX;
-  int C2Bp, f0;
+  long long blk0;  // first block of this group; bx blocks per field-level
+  int C2Bp, bx;
   int nsplit;        // 3: BF16 x 3; 2: FP16 hi + lo scaled by 2^(14 - cexp[b])
   const int *cexp;   // FP16: exponent of the field-level's largest |coefficient|
 };
@@ -497,17 +498,21 @@ struct PackLaunch {
 __global__ void __launch_bounds__(256) pack_spectra_kernel(const __grid_constant__ PackLaunch L) {
   pdl_wait();  // Apack is read by the previous step's synthesis
   pdl_trigger();
+  // Block -> (group, field-level b, chunk cx): each group has its own number
+  // of chunks per field-level (a group of short spectra launches no empty
+  // blocks for the longest group's coefficient range).
+  const long long blk = blockIdx.x;
   int gi = 0;
-  while (gi + 1 < L.ngroups && (int)blockIdx.y >= L.g[gi + 1].f0) ++gi;
+  while (gi + 1 < L.ngroups && blk >= L.g[gi + 1].blk0) ++gi;
   const PackGroup &G = L.g[gi];
-  const int b = blockIdx.y - G.f0;
+  const int b = (int)((blk - G.blk0) / G.bx);
+  const int cx = (int)((blk - G.blk0) % G.bx);
   const size_t plane = (size_t)G.C2Bp * G.KX;
   const double2 *src = G.spec + (size_t)b * G.ncoef;
   unsigned short *dst = G.A + (size_t)(2 * b) * G.KX;
   if (G.nsplit == 2) {
     const int sc = 14 - G.cexp[b];
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < G.ncoef;
-         i += (long long)gridDim.x * blockDim.x) {
+    for (long long i = cx * (long long)blockDim.x + threadIdx.x; i < G.ncoef; i += (long long)G.bx * blockDim.x) {
       const double2 v = __ldg(src + i);
       const int x = __ldg(G.xpos + i);
       unsigned short h0, l0, h1, l1;
@@ -522,8 +527,8 @@ __global__ void __launch_bounds__(256) pack_spectra_kernel(const __grid_constant
     return;
   }
   // two coefficients a thread per round, both loads in flight together
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long i0 = blockIdx.x * (long long)blockDim.x + threadIdx.x; i0 < G.ncoef; i0 += 2 * stride) {
+  const long long stride = (long long)G.bx * blockDim.x;
+  for (long long i0 = cx * (long long)blockDim.x + threadIdx.x; i0 < G.ncoef; i0 += 2 * stride) {
     double2 v[2];
     int x[2];
 #pragma unroll
@@ -585,8 +590,8 @@ int pack_spectra(Plan *const *plans, const int *batch, const double *const *spec
   if (ngroups < 1 || ngroups > MAXG) return DCCM_ERR_UNSUPPORTED;
   PackLaunch L;
   memset(&L, 0, sizeof L);
-  int ng = 0, nf = 0;
-  long long maxc = 0;
+  int ng = 0;
+  long long nblk = 0;
   for (int g = 0; g < ngroups; ++g) {
     if (batch[g] <= 0) continue;
     const Plan &P = *plans[g];
@@ -598,19 +603,19 @@ int pack_spectra(Plan *const *plans, const int *batch, const double *const *spec
     G.ncoef = P.ncoef;
     G.KX = P.KX;
     G.C2Bp = P.C2Bp;
-    G.f0 = nf;
     G.nsplit = P.nsplit;
     G.cexp = P.d_cexp;
+    // two coefficients a thread: ncoef / 512 blocks a field-level, at most 64
+    long long bx = (P.ncoef + 511) / 512;
+    G.bx = (int)(bx < 1 ? 1 : (bx > 64 ? 64 : bx));
+    G.blk0 = nblk;
+    nblk += (long long)G.bx * batch[g];
     if (P.nsplit == 2) DCCM_TRY(field_exponents(spec[g], 2 * P.ncoef, batch[g], P.d_cexp, s));
-    nf += batch[g];
-    maxc = P.ncoef > maxc ? P.ncoef : maxc;
   }
   L.ngroups = ng;
-  if (nf == 0) return DCCM_OK;
-  if (nf > 65535) return DCCM_ERR_UNSUPPORTED;
-  long long bx = (maxc + 511) / 512;  // two coefficients a thread
-  if (bx > 64) bx = 64;
-  DCCM_CUDA(launch_pdl(pack_spectra_kernel, dim3((unsigned)bx, (unsigned)nf), dim3(256), 0, s, L));
+  if (nblk == 0) return DCCM_OK;
+  if (nblk > 0x7FFFFFFFLL) return DCCM_ERR_UNSUPPORTED;
+  DCCM_CUDA(launch_pdl(pack_spectra_kernel, dim3((unsigned)nblk), dim3(256), 0, s, L));
   return DCCM_OK;
 }
 
