@@ -132,6 +132,16 @@ _SIGS = {
     "dccm_sht_inverse": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
     "dccm_sht_forward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
     "dccm_sht_status": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "dccm_sht_xya_wa_dev": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                           ctypes.c_void_p]),
+    "dccm_sht_wa_xya_dev": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                           ctypes.c_void_p]),
+    "dccm_sht_xya_wa": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
+    "dccm_sht_wa_xya": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
+    "dccm_sht_spec_from_wa_dev": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                                 ctypes.c_int, ctypes.c_void_p]),
+    "dccm_sht_wa_from_spec_dev": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                                 ctypes.c_int, ctypes.c_void_p]),
     "dccm_sht_ensemble_create": (ctypes.c_int, [ctypes.c_int] + [ctypes.c_void_p] * 4 + [ctypes.c_int,
                                                                                      ctypes.c_void_p]),
     "dccm_sht_ensemble_destroy": (ctypes.c_int, [ctypes.c_void_p]),
@@ -231,8 +241,9 @@ def fp64_peak(stream=None):
 
 
 def tune_set(knob, value):
-    """dccm_tune_set: process-wide launch-shape knob (tc_ctas, fft_bb,
-    flux_threads, flux_ctas, remap_threads, serial, upload_order, host_path); 0 = the
+    """dccm_tune_set: process-wide knob (launch shapes tc_ctas, fft_bb,
+    flux_threads, flux_ctas, remap_threads, serial; host copies upload_order,
+    host_path; failure path wait_limit_ms, tc_withhold_loads); 0 = the
     default."""
     _check(load().dccm_tune_set(knob.encode(), int(value)), "dccm_tune_set")
 
@@ -509,10 +520,63 @@ class ShtPlan:
         st = load().dccm_sht_status(self.h, ctypes.byref(e))
         return st, e.value
 
+    # SPML's real layout wa[b][l], l = l_nm(n, m) - 1 (see l_nm below)
+    @property
+    def nwa(self):
+        return (self.N + 1) ** 2
+
+    def xya_wa(self, wa):
+        """SPML xya_wa: wa [batch, (N+1)^2] -> grid [batch, J, I] (host arrays)."""
+        wa = np.ascontiguousarray(wa, np.float64)
+        B = wa.shape[0]
+        xya = np.zeros((B, self.J, self.I))
+        _check(load().dccm_sht_xya_wa(self.h, _p(wa), _p(xya), B), "dccm_sht_xya_wa")
+        return xya
+
+    def wa_xya(self, xya):
+        """SPML wa_xya: grid [batch, J, I] -> wa [batch, (N+1)^2] (host arrays)."""
+        xya = np.ascontiguousarray(xya, np.float64)
+        B = xya.shape[0]
+        wa = np.zeros((B, self.nwa))
+        _check(load().dccm_sht_wa_xya(self.h, _p(xya), _p(wa), B), "dccm_sht_wa_xya")
+        return wa
+
+    def xya_wa_dev(self, wa, xya, batch, stream=None):
+        _check(load().dccm_sht_xya_wa_dev(self.h, _p(wa), _p(xya), int(batch), _stream(stream)),
+               "dccm_sht_xya_wa_dev")
+
+    def wa_xya_dev(self, xya, wa, batch, stream=None):
+        _check(load().dccm_sht_wa_xya_dev(self.h, _p(xya), _p(wa), int(batch), _stream(stream)),
+               "dccm_sht_wa_xya_dev")
+
+    def spec_from_wa_dev(self, wa, spec, batch, stream=None):
+        _check(load().dccm_sht_spec_from_wa_dev(self.h, _p(wa), _p(spec), int(batch), _stream(stream)),
+               "dccm_sht_spec_from_wa_dev")
+
+    def wa_from_spec_dev(self, spec, wa, batch, stream=None):
+        _check(load().dccm_sht_wa_from_spec_dev(self.h, _p(spec), _p(wa), int(batch), _stream(stream)),
+               "dccm_sht_wa_from_spec_dev")
+
     def __del__(self):
         if getattr(self, "h", None) and _lib is not None:
             _lib.dccm_sht_plan_destroy(self.h)
             self.h = None
+
+
+def l_nm(n, m):
+    """SPML's l_nm: 1-based position of total wavenumber n, zonal
+    wavenumber m (-n <= m <= n) in a wa array: n(n+1) + m + 1; Re s_n^m at
+    m >= 0, Im s_n^|m| at m < 0 (works element-wise on numpy arrays)."""
+    return n * (n + 1) + m + 1
+
+
+def nm_l(l):
+    """SPML's nm_l: (n, m) of the 1-based wa position l (element-wise)."""
+    l0 = np.asarray(l) - 1
+    n = np.floor(np.sqrt(l0)).astype(np.int64)
+    n = np.where((n + 1) ** 2 <= l0, n + 1, n)
+    n = np.where(n * n > l0, n - 1, n)
+    return n, l0 - n * (n + 1)
 
 
 class Ensemble:

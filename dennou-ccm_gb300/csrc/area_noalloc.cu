@@ -1,16 +1,18 @@
 // Global area integral that allocates no device memory.
 //
 // dccm_area_integral_dev reduces through a small device buffer that it
-// allocates on every call.  Some callers cannot do that:
-//   - a model that reserves all of the GPU's memory for its own allocator
-//     at start-up, leaving nothing for a library's cudaMalloc;
-//   - code that must not synchronise the device, which cudaMalloc and
-//     cudaFree can do implicitly;
-//   - code issuing work while a stream is captured into a CUDA graph, when
-//     ordinary allocation calls are not permitted.
-// This variant keeps its scratch (one partial sum per block, plus the final
-// result) in a fixed array that lives in the library's device image, so
-// each GPU that loads the library holds it until the process exits.
+// allocates on every call.  Some callers cannot do that: a model that
+// reserves all of the GPU's memory for its own allocator at start-up leaves
+// nothing for a library's cudaMalloc, and a component linked into such a
+// model (the coupler's diagnostics, for instance) must work inside what the
+// model already holds.  This variant keeps its scratch (one partial sum per
+// block, plus the final result) in a fixed array that lives in the
+// library's device image, so each GPU that loads the library holds it
+// until the process exits.
+//
+// What it does not avoid: like dccm_area_integral_dev it copies the result
+// into the caller's host double and synchronises the stream before it
+// returns, so it blocks the calling thread until the integral is done.
 //
 // Limits and sharing:
 //   - at most NOALLOC_MAX_PARTIALS blocks of NOALLOC_BLOCK_ELEMS elements,
@@ -23,12 +25,14 @@
 //     the final slot before copying it out, so nothing has to be cleared
 //     between calls (the array keeps the last call's values).
 // The host must pass kernels a device address of the array, which in host
-// code the array's name is not: on each device the first call looks the
-// address up with cudaGetSymbolAddress, with that device current, and
-// caches it.  That first call should come before any stream capture.
+// code the array's name is not: the first call in each CUDA context (per
+// device, and again after cudaDeviceReset has replaced a device's primary
+// context) looks the address up with cudaGetSymbolAddress, with that
+// device current, and keeps it for the calls that follow in that context.
 #include <mutex>
 
 #include "common.cuh"
+#include "nvtx.cuh"
 
 namespace dccm {
 namespace noalloc {
@@ -47,6 +51,24 @@ __device__ __forceinline__ void two_sum(double a, double b, double &s, double &e
   s = __dadd_rn(a, b);
   const double bb = __dsub_rn(s, a);
   e = __dadd_rn(__dsub_rn(a, __dsub_rn(s, bb)), __dsub_rn(b, bb));
+}
+
+// Tree reduction of the block's (sum, compensation) pairs in shared memory;
+// the result is in ss[0], cs[0] for thread 0.
+__device__ __forceinline__ void block_pairs(double s, double c, double (&ss)[NOALLOC_THREADS],
+                                            double (&cs)[NOALLOC_THREADS]) {
+  ss[threadIdx.x] = s;
+  cs[threadIdx.x] = c;
+  __syncthreads();
+  for (int w = NOALLOC_THREADS / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+      double s2, e;
+      two_sum(ss[threadIdx.x], ss[threadIdx.x + w], s2, e);
+      ss[threadIdx.x] = s2;
+      cs[threadIdx.x] = __dadd_rn(__dadd_rn(cs[threadIdx.x], cs[threadIdx.x + w]), e);
+    }
+    __syncthreads();
+  }
 }
 
 // Same compensated accumulation as the allocating kernel, but block b owns
@@ -68,48 +90,73 @@ area_partial_fixed(const double *__restrict__ f, const double *__restrict__ a, i
     }
   }
   __shared__ double ss[NOALLOC_THREADS], cs[NOALLOC_THREADS];
-  ss[threadIdx.x] = s;
-  cs[threadIdx.x] = c;
-  __syncthreads();
-  for (int w = NOALLOC_THREADS / 2; w > 0; w >>= 1) {
-    if (threadIdx.x < w) {
-      double s2, e;
-      two_sum(ss[threadIdx.x], ss[threadIdx.x + w], s2, e);
-      ss[threadIdx.x] = s2;
-      cs[threadIdx.x] = __dadd_rn(__dadd_rn(cs[threadIdx.x], cs[threadIdx.x + w]), e);
-    }
-    __syncthreads();
-  }
+  block_pairs(s, c, ss, cs);
   if (threadIdx.x == 0) part[blockIdx.x] = make_double2(ss[0], cs[0]);
 }
 
-__global__ void area_final_fixed(double2 *__restrict__ scratch, int np) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+// One block: thread t sums partials t, t + 256, ... (compensated), then the
+// block's tree gives the total.
+__global__ void __launch_bounds__(NOALLOC_THREADS) area_final_fixed(double2 *__restrict__ scratch, int np) {
   double s = 0.0, c = 0.0;
-  for (int i = 0; i < np; ++i) {
+  for (int i = threadIdx.x; i < np; i += NOALLOC_THREADS) {
     double e;
     two_sum(s, scratch[i].x, s, e);
     c = __dadd_rn(__dadd_rn(c, e), scratch[i].y);
   }
-  scratch[NOALLOC_MAX_PARTIALS] = make_double2(__dadd_rn(s, c), 0.0);
+  __shared__ double ss[NOALLOC_THREADS], cs[NOALLOC_THREADS];
+  block_pairs(s, c, ss, cs);
+  if (threadIdx.x == 0) scratch[NOALLOC_MAX_PARTIALS] = make_double2(__dadd_rn(ss[0], cs[0]), 0.0);
 }
 
-// Device address of g_scratch per device ordinal, looked up once.
-constexpr int MAX_DEVICES = 64;
-static double2 *g_addr[MAX_DEVICES] = {nullptr};
+// Device address of g_scratch in each CUDA context.  The key is the
+// context's process-unique id (cuCtxGetId), so a context that replaced an
+// earlier one on the same device (after cudaDeviceReset) looks it up again.
+typedef int (*CtxGetCurrentFn)(void **);
+typedef int (*CtxGetIdFn)(void *, unsigned long long *);
+constexpr int MAX_CONTEXTS = 64;
+struct Slot {
+  unsigned long long ctx_id;
+  double2 *addr;
+};
+static Slot g_slots[MAX_CONTEXTS];
+static int g_nslots = 0;
 static std::mutex g_mutex;
 
+static void *driver_fn(const char *name) {
+  void *p = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion(name, &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess)
+    return nullptr;
+  return p;
+}
+
 static int scratch_address(double2 **out) {
-  int dev = 0;
-  DCCM_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= MAX_DEVICES) return DCCM_ERR_UNSUPPORTED;
-  std::lock_guard<std::mutex> lock(g_mutex);
-  if (!g_addr[dev]) {
-    void *p = nullptr;
-    DCCM_CUDA(cudaGetSymbolAddress(&p, g_scratch));
-    g_addr[dev] = static_cast<double2 *>(p);
+  static CtxGetCurrentFn get_ctx = reinterpret_cast<CtxGetCurrentFn>(driver_fn("cuCtxGetCurrent"));
+  static CtxGetIdFn get_id = reinterpret_cast<CtxGetIdFn>(driver_fn("cuCtxGetId"));
+  if (!get_ctx || !get_id) return DCCM_ERR_UNSUPPORTED;
+  void *ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_ctx(&ctx) != 0) return DCCM_ERR_CUDA;
+  if (!ctx) {  // no context current on this thread yet: the device's primary one
+    int dev = 0;
+    DCCM_CUDA(cudaGetDevice(&dev));
+    DCCM_CUDA(cudaSetDevice(dev));
+    if (get_ctx(&ctx) != 0 || !ctx) return DCCM_ERR_CUDA;
   }
-  *out = g_addr[dev];
+  if (get_id(ctx, &id) != 0) return DCCM_ERR_CUDA;
+  std::lock_guard<std::mutex> lock(g_mutex);
+  for (int k = 0; k < g_nslots; ++k)
+    if (g_slots[k].ctx_id == id) {
+      *out = g_slots[k].addr;
+      return DCCM_OK;
+    }
+  void *p = nullptr;
+  DCCM_CUDA(cudaGetSymbolAddress(&p, g_scratch));
+  Slot sl = {id, static_cast<double2 *>(p)};
+  if (g_nslots < MAX_CONTEXTS) g_slots[g_nslots++] = sl;
+  else g_slots[id % MAX_CONTEXTS] = sl;  // more contexts than slots: reuse one
+  *out = sl.addr;
   return DCCM_OK;
 }
 
@@ -120,6 +167,7 @@ using namespace dccm;
 
 extern "C" int dccm_area_integral_noalloc_dev(const double *f, const double *area, int64_t n,
                                               double *result, void *stream) {
+  DCCM_NVTX_FUNC();
   if (!f || !area || !result || n < 0) return DCCM_ERR_INVALID_ARG;
   if (n > noalloc::NOALLOC_MAX_N) return DCCM_ERR_SHAPE;
   double2 *scratch = nullptr;
@@ -130,7 +178,7 @@ extern "C" int dccm_area_integral_noalloc_dev(const double *f, const double *are
     noalloc::area_partial_fixed<<<np, noalloc::NOALLOC_THREADS, 0, s>>>(f, area, n, scratch);
     DCCM_LAUNCH_CHECK();
   }
-  noalloc::area_final_fixed<<<1, 32, 0, s>>>(scratch, np);
+  noalloc::area_final_fixed<<<1, noalloc::NOALLOC_THREADS, 0, s>>>(scratch, np);
   DCCM_LAUNCH_CHECK();
   DCCM_CUDA(cudaMemcpyAsync(result, &scratch[noalloc::NOALLOC_MAX_PARTIALS].x, sizeof(double),
                             cudaMemcpyDeviceToHost, s));

@@ -26,6 +26,7 @@
 
 #include "common.cuh"
 #include "remap_table.cuh"
+#include "nvtx.cuh"
 
 namespace dccm {
 namespace bilin {
@@ -118,6 +119,7 @@ using namespace dccm;
 extern "C" int dccm_bilinear_generate(const double *x_LonS, int nxs, const double *y_LatS, int nys,
                                       const double *x_LonR, int nxr, const double *y_LatR, int nyr,
                                       const uint8_t *dst_mask, dccm_remap_table **table) {
+  DCCM_NVTX_FUNC();
   if (!table || !x_LonS || !y_LatS || !x_LonR || !y_LatR) return DCCM_ERR_INVALID_ARG;
   *table = nullptr;
   if (nxs < 1 || nys < 1 || nxr < 1 || nyr < 1 || nyr > 65535) return DCCM_ERR_SHAPE;
@@ -219,6 +221,7 @@ extern "C" int dccm_bilinear_generate(const double *x_LonS, int nxs, const doubl
 extern "C" int dccm_exchange_grid(const double *y_LatA, const double *y_IntWtLatA, int JMA, const double *y_LatO,
                                   const double *y_IntWtLatO, int JMO, double *y_LatX, double *y_IntWtLatX,
                                   int *JMX) {
+  DCCM_NVTX_FUNC();
   if (!y_LatA || !y_IntWtLatA || !y_IntWtLatO || !y_LatX || !y_IntWtLatX || !JMX) return DCCM_ERR_INVALID_ARG;
   if (JMA < 1 || JMO < 1) return DCCM_ERR_SHAPE;
   (void)y_LatO;

@@ -38,6 +38,9 @@ struct Tunables {
   int serial = 0;         // 1: launch_pdl makes ordinary launches
   int upload_order = 0;   // dccm_step_run_host: 1 transforms' inputs first, 2 surface inputs first
   int host_path = 0;      // dccm_step_run_host: 1 + mask of the copy groups moved through the host mapping (0: 1)
+  int wait_limit_ms = 0;  // limit of the tensor-core kernel's bounded waits (0: 1000 ms)
+  int tc_withhold_loads = 0;  // 1: the tensor-core kernel's load thread issues no copies, so its
+                              // waits expire (tests the timeout path; nothing is left in flight)
 };
 Tunables &tunables();
 

@@ -14,6 +14,7 @@
 
 #include "common.cuh"
 #include "flux_rows.cuh"
+#include "nvtx.cuh"
 
 namespace dccm {
 namespace flux {
@@ -400,6 +401,7 @@ using namespace dccm;
 
 extern "C" int dccm_sfc_bulk_flux_get_dev(const dccm_sfc_bulk_flux_args *a,
                                           const dccm_sfc_grid *g, void *stream) {
+  DCCM_NVTX_FUNC();
   DCCM_TRY(flux::check_args(a));
   DCCM_TRY(flux::check_grid(g));
   return flux::launch(flux::make_ptrs(a), g, a->a_Sig1Info[0], as_stream(stream));
@@ -423,6 +425,7 @@ static int copy_interior(void *dst, const void *src, const dccm_sfc_grid *g, int
 }
 
 extern "C" int dccm_sfc_bulk_flux_get(const dccm_sfc_bulk_flux_args *a, const dccm_sfc_grid *g) {
+  DCCM_NVTX_FUNC();
   DCCM_TRY(flux::check_args(a));
   DCCM_TRY(flux::check_grid(g));
   if (g->IE < g->IS || g->JE < g->JS) return DCCM_OK;

@@ -27,6 +27,7 @@
 #include <new>
 
 #include "common.cuh"
+#include "nvtx.cuh"
 
 struct dccm_implcpl {
   int ncol = 0, kmax = 0, ncmax = 0, ih2o = 1;
@@ -295,6 +296,7 @@ using namespace dccm;
 
 extern "C" int dccm_implcpl_create(int ncol, int kmax, int ncmax, int index_h2ovap,
                                    const dccm_implcpl_consts *consts, dccm_implcpl **plan) {
+  DCCM_NVTX_FUNC();
   if (!plan || !consts) return DCCM_ERR_INVALID_ARG;
   *plan = nullptr;
   if (ncol < 1 || kmax < 2 || ncmax < 1 || index_h2ovap < 1 || index_h2ovap > ncmax) return DCCM_ERR_INVALID_ARG;
@@ -319,6 +321,7 @@ extern "C" int dccm_implcpl_create(int ncol, int kmax, int ncmax, int index_h2ov
 }
 
 extern "C" int dccm_implcpl_destroy(dccm_implcpl *p) {
+  DCCM_NVTX_FUNC();
   if (!p) return DCCM_OK;
   if (p->d_mtx) cudaFree(p->d_mtx);
   p->stage.release();
@@ -330,6 +333,7 @@ extern "C" int dccm_implcpl_destroy(dccm_implcpl *p) {
 static size_t mstride(const dccm_implcpl *p) { return (size_t)3 * p->kmax * p->ncol; }
 
 extern "C" int dccm_implcpl_forward_dev(dccm_implcpl *p, const dccm_implcpl_forward_args *a, void *stream) {
+  DCCM_NVTX_FUNC();
   if (!p || !a) return DCCM_ERR_INVALID_ARG;
   const void *need[] = {a->xyr_MomFluxX, a->xyr_MomFluxY, a->xyr_HeatFlux, a->xyrf_QMixFlux, a->xyr_Press,
                         a->xyz_Exner, a->xyr_Exner, a->xyr_VirTemp, a->xyz_Height, a->xyr_VelDiffCoef,
@@ -381,6 +385,7 @@ extern "C" int dccm_implcpl_forward_dev(dccm_implcpl *p, const dccm_implcpl_forw
 
 extern "C" int dccm_implcpl_backward_dev(dccm_implcpl *p, double *xyz_DUDt, double *xyz_DVDt,
                                          double *xyz_DTempDt, double *xyzf_DQMixDt, void *stream) {
+  DCCM_NVTX_FUNC();
   if (!p || !xyz_DUDt || !xyz_DVDt || !xyz_DTempDt || !xyzf_DQMixDt) return DCCM_ERR_INVALID_ARG;
   implcpl::Bwd b;
   b.uv = p->d_mtx;
@@ -416,6 +421,7 @@ static int host_stream(dccm_implcpl *p) {
 }
 
 extern "C" int dccm_implcpl_forward(dccm_implcpl *p, const dccm_implcpl_forward_args *a) {
+  DCCM_NVTX_FUNC();
   if (!p || !a) return DCCM_ERR_INVALID_ARG;
   DCCM_TRY(host_stream(p));
   const size_t n = p->ncol, K = p->kmax, nc = p->ncmax;
@@ -488,6 +494,7 @@ extern "C" int dccm_implcpl_forward(dccm_implcpl *p, const dccm_implcpl_forward_
 
 extern "C" int dccm_implcpl_backward(dccm_implcpl *p, double *xyz_DUDt, double *xyz_DVDt, double *xyz_DTempDt,
                                      double *xyzf_DQMixDt) {
+  DCCM_NVTX_FUNC();
   if (!p || !xyz_DUDt || !xyz_DVDt || !xyz_DTempDt || !xyzf_DQMixDt) return DCCM_ERR_INVALID_ARG;
   DCCM_TRY(host_stream(p));
   const size_t full = (size_t)p->ncol * p->kmax, nc = p->ncmax;
@@ -510,6 +517,7 @@ extern "C" int dccm_implcpl_backward(dccm_implcpl *p, double *xyz_DUDt, double *
 }
 
 extern "C" int dccm_implcpl_matrices(dccm_implcpl *p, double *uv, double *temp, double *qmix) {
+  DCCM_NVTX_FUNC();
   if (!p) return DCCM_ERR_INVALID_ARG;
   double *h[3] = {uv, temp, qmix};
   for (int i = 0; i < 3; ++i)

@@ -27,8 +27,9 @@
 // fold, stores coalesced along c; forward: both parities through shared
 // memory, stores coalesced along n).  Two shared-memory stages and two TMEM
 // accumulator sets overlap loads, MMAs and epilogue of consecutive items.
-// Every mbarrier wait is bounded by a 1 s globaltimer limit; on expiry the
-// kernel records an error code, stops issuing work, and still frees its TMEM.
+// Every mbarrier wait is bounded by a globaltimer limit (1 s, knob
+// "wait_limit_ms"); on expiry the kernel records an error code, stops
+// issuing work, and still frees its TMEM.
 #include <cuda_bf16.h>
 #include <string.h>
 
@@ -81,14 +82,14 @@ struct TcArgs {
 // Bounded wait: returns false (and records code) if the phase did not
 // complete within the limit or another role already gave up.
 __device__ __forceinline__ bool mbar_wait(uint64_t *b, uint32_t parity, int *err, volatile int *abort_flag,
-                                          int code) {
+                                          int code, unsigned long long limit_ns) {
   if (mbar_try(b, parity)) return true;
   const unsigned long long t0 = gtimer();
   for (uint32_t it = 1;; ++it) {
     if (mbar_try(b, parity)) return true;
     if ((it & 255) == 0) {
       if (*abort_flag) return false;
-      if (gtimer() - t0 > WAIT_LIMIT_NS) {
+      if (gtimer() - t0 > limit_ns) {
         *abort_flag = 1;
         atomicCAS(err, 0, code);
         return false;
@@ -185,6 +186,8 @@ struct TcLaunch {
   TcArgs g[MAXG];
   int start[MAXG + 1];  // prefix of work items over groups
   int ngroups;
+  unsigned long long wait_ns;  // limit of every mbarrier wait
+  int withhold;  // 1: the load thread issues nothing (exercises the waits' expiry; nothing is in flight)
 };
 
 // Work item it -> group and (m, ct, nt); items of a group are ordered
@@ -270,7 +273,7 @@ legendre_tc_kernel(const __grid_constant__ TcLaunch L) {
 
   if (warp == 0) {
     // ---------------------------------------------------------- TMA
-    if (lane == 0) {
+    if (lane == 0 && !L.withhold) {
       int g = 0;  // chunk counter
       bool ok = true;
       for (int k = 0, it = cta_item(0); it < nitems && ok; it = cta_item(++k)) {
@@ -285,7 +288,7 @@ legendre_tc_kernel(const __grid_constant__ TcLaunch L) {
           const int x0 = p ? mi.x1 : mi.x0;
           for (int q = 0; q < nq; ++q, ++g) {
             const int s = g % NSTAGE;
-            if (!mbar_wait(&empty[s], ((g / NSTAGE) & 1) ^ 1, a.err, abort_flag, 1)) { ok = false; break; }
+            if (!mbar_wait(&empty[s], ((g / NSTAGE) & 1) ^ 1, a.err, abort_flag, 1, L.wait_ns)) { ok = false; break; }
             unsigned char *As = stage + s * STAGE_BYTES;
             unsigned char *Bs = As + 3 * A_SPLIT_BYTES;
             mbar_arrive_tx(&full[s], (uint32_t)(a.nsplit * (A_SPLIT_BYTES + a.brows * 128)));
@@ -322,7 +325,7 @@ legendre_tc_kernel(const __grid_constant__ TcLaunch L) {
         const int ncross = a.nsplit == 3 ? 5 : 2;
         const int ab = a.nacc == 2 ? (li & 1) : 0;
         const int ar = a.nacc == 2 ? (li >> 1) : li;  // use count of this accumulator set
-        if (!mbar_wait(&acce[ab], (ar & 1) ^ 1, a.err, abort_flag, 2)) { ok = false; break; }
+        if (!mbar_wait(&acce[ab], (ar & 1) ^ 1, a.err, abort_flag, 2, L.wait_ns)) { ok = false; break; }
         tc_fence_after();
         for (int p = 0; p < 2 && ok; ++p) {
           const int kv = p ? mi.kv1 : mi.kv0;
@@ -332,7 +335,7 @@ legendre_tc_kernel(const __grid_constant__ TcLaunch L) {
           int accm = 0, accx = 0;
           for (int q = 0; q < nq; ++q, ++g) {
             const int s = g % NSTAGE;
-            if (!mbar_wait(&full[s], (g / NSTAGE) & 1, a.err, abort_flag, 3)) { ok = false; break; }
+            if (!mbar_wait(&full[s], (g / NSTAGE) & 1, a.err, abort_flag, 3, L.wait_ns)) { ok = false; break; }
             tc_fence_after();
             const uint32_t As = smem_u32(stage + s * STAGE_BYTES);
             const uint32_t Bs = As + 3 * A_SPLIT_BYTES;
@@ -384,7 +387,7 @@ legendre_tc_kernel(const __grid_constant__ TcLaunch L) {
       const int nrow = min(128, mi.nr - nt * 128);
       const int ab = a.nacc == 2 ? (li & 1) : 0;
       const int ar = a.nacc == 2 ? (li >> 1) : li;
-      if (dead || !mbar_wait(&accf[ab], ar & 1, a.err, abort_flag, 4)) {
+      if (dead || !mbar_wait(&accf[ab], ar & 1, a.err, abort_flag, 4, L.wait_ns)) {
         dead = true;
         if (a.dir == 0) break;
       }
@@ -934,6 +937,9 @@ int legendre_tc_multi(Plan *const *plans, const int *batch, const void *const *i
   }
   L.start[ng] = items;
   L.ngroups = ng;
+  L.wait_ns = tunables().wait_limit_ms > 0 ? 1000000ull * (unsigned long long)tunables().wait_limit_ms
+                                           : WAIT_LIMIT_NS;
+  L.withhold = tunables().tc_withhold_loads;
   if (items <= 0) return DCCM_OK;
   int ctas = tunables().tc_ctas > 0 ? tunables().tc_ctas : sm_count();
   const int grid = items < ctas ? items : ctas;

@@ -3,6 +3,7 @@
 // thread runs 8 independent DFMA chains; the result is stored only under
 // a condition the values never meet, so no chain can be removed.
 #include "common.cuh"
+#include "nvtx.cuh"
 
 namespace dccm {
 namespace peak {
@@ -29,6 +30,7 @@ __global__ void __launch_bounds__(256) dfma_kernel(int iters, double b, double c
 using namespace dccm;
 
 extern "C" int dccm_fp64_peak(void *stream, double *tflops) {
+  DCCM_NVTX_FUNC();
   if (!tflops) return DCCM_ERR_INVALID_ARG;
   cudaStream_t s = as_stream(stream);
   const int blocks = sm_count() * 8, threads = 256, iters = 4096;

@@ -34,6 +34,7 @@
 
 #include "remap_table.cuh"
 #include "common.cuh"
+#include "nvtx.cuh"
 
 
 struct dccm_remap_plan {
@@ -511,6 +512,7 @@ extern "C" int dccm_j99_generate(const double *x_LonS, int nxs, const double *y_
                                  const double *x_LonIntWtD, const double *y_LatIntWtD,
                                  int accuracy_order, int weight_mode, const uint8_t *dst_mask,
                                  dccm_remap_table **table) {
+  DCCM_NVTX_FUNC();
   (void)x_LonIntWtS;
   (void)x_LonIntWtD;
   if (!table || !x_LonS || !y_LatS || !x_LonD || !y_LatD || !y_LatIntWtS || !y_LatIntWtD)
@@ -540,6 +542,7 @@ extern "C" int dccm_remap_table_size(const dccm_remap_table *t, int64_t *nrow) {
 
 extern "C" int dccm_remap_table_rows(const dccm_remap_table *t, int32_t *iD, int32_t *jD,
                                      int32_t *iS, int32_t *jS, double *w) {
+  DCCM_NVTX_FUNC();
   if (!t) return DCCM_ERR_INVALID_ARG;
   const size_t n = t->w.size();
   if (n == 0) return DCCM_OK;
@@ -553,6 +556,7 @@ extern "C" int dccm_remap_table_rows(const dccm_remap_table *t, int32_t *iD, int
 }
 
 extern "C" int dccm_remap_table_write(const dccm_remap_table *t, const char *path) {
+  DCCM_NVTX_FUNC();
   if (!t || !path) return DCCM_ERR_INVALID_ARG;
   FILE *fp = fopen(path, "w");
   if (!fp) return DCCM_ERR_IO;
@@ -583,6 +587,7 @@ static bool parse_row(char *line, int32_t v[4], double *w) {
 }
 
 extern "C" int dccm_remap_table_read(const char *path, dccm_remap_table **table) {
+  DCCM_NVTX_FUNC();
   if (!path || !table) return DCCM_ERR_INVALID_ARG;
   *table = nullptr;
   FILE *fp = fopen(path, "r");
@@ -615,6 +620,7 @@ extern "C" int dccm_remap_table_read(const char *path, dccm_remap_table **table)
 
 extern "C" int dccm_remap_table_index(const dccm_remap_table *t, int GNXS, int GNXR,
                                       int32_t *send_index, int32_t *recv_index, double *coef) {
+  DCCM_NVTX_FUNC();
   if (!t) return DCCM_ERR_INVALID_ARG;
   const size_t n = t->w.size();
   if (n == 0) return DCCM_OK;
@@ -628,6 +634,7 @@ extern "C" int dccm_remap_table_index(const dccm_remap_table *t, int GNXS, int G
 }
 
 extern "C" int dccm_remap_table_destroy(dccm_remap_table *t) {
+  DCCM_NVTX_FUNC();
   delete t;
   return DCCM_OK;
 }
@@ -635,6 +642,7 @@ extern "C" int dccm_remap_table_destroy(dccm_remap_table *t) {
 extern "C" int dccm_remap_plan_create(int64_t n_send, int64_t n_recv, int64_t nop,
                                       const int32_t *send_index, const int32_t *recv_index,
                                       const double *coef, dccm_remap_plan **plan) {
+  DCCM_NVTX_FUNC();
   if (!plan) return DCCM_ERR_INVALID_ARG;
   *plan = nullptr;
   if (n_send < 0 || n_recv < 0 || nop < 0) return DCCM_ERR_INVALID_ARG;
@@ -678,6 +686,7 @@ extern "C" int dccm_remap_plan_create(int64_t n_send, int64_t n_recv, int64_t no
 }
 
 extern "C" int dccm_remap_plan_destroy(dccm_remap_plan *p) {
+  DCCM_NVTX_FUNC();
   if (!p) return DCCM_OK;
   if (p->d_rowptr) cudaFree(p->d_rowptr);
   if (p->d_ent) cudaFree(p->d_ent);
@@ -698,6 +707,7 @@ extern "C" int dccm_remap_plan_info(const dccm_remap_plan *p, int64_t *nnz, int6
 
 extern "C" int dccm_remap_apply_dev(dccm_remap_plan *p, const double *src, int64_t ld_src,
                                     double *dst, int64_t ld_dst, int nfields, void *stream) {
+  DCCM_NVTX_FUNC();
   if (!p || (nfields > 0 && (!src || !dst)) || nfields < 0) return DCCM_ERR_INVALID_ARG;
   if (nfields > 1 && (ld_src < p->n_send || ld_dst < p->n_recv)) return DCCM_ERR_SHAPE;
   return remap::apply(p, src, ld_src, dst, ld_dst, nfields, as_stream(stream));
@@ -706,6 +716,7 @@ extern "C" int dccm_remap_apply_dev(dccm_remap_plan *p, const double *src, int64
 extern "C" int dccm_interpolate_data(dccm_remap_plan *p, int64_t sn1, int64_t sn2,
                                      const double *send_data, int64_t rn1, int64_t rn2,
                                      double *recv_data, int num_of_data) {
+  DCCM_NVTX_FUNC();
   if (!p || !send_data || !recv_data || num_of_data < 0) return DCCM_ERR_INVALID_ARG;
   if (sn1 < p->n_send || rn1 < p->n_recv || num_of_data > sn2 || num_of_data > rn2)
     return DCCM_ERR_SHAPE;
@@ -728,6 +739,7 @@ extern "C" int dccm_interpolate_data(dccm_remap_plan *p, int64_t sn1, int64_t sn
 
 extern "C" int dccm_area_integral_dev(const double *f, const double *area, int64_t n,
                                       double *result, void *stream) {
+  DCCM_NVTX_FUNC();
   if (!f || !area || !result || n < 0) return DCCM_ERR_INVALID_ARG;
   cudaStream_t s = as_stream(stream);
   const int threads = 256;

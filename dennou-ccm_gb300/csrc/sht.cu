@@ -22,6 +22,7 @@
 #include <new>
 
 #include "sht_plan.cuh"
+#include "nvtx.cuh"
 
 struct dccm_sht_plan {
   dccm::sht::Plan P;
@@ -93,10 +94,12 @@ __global__ void pnm_kernel(int N, int Jh, const double *__restrict__ mu, double 
 static void destroy(Plan &P) {
   void *ptrs[] = {P.d_mu,      P.d_w,        P.d_pnm,       P.d_tw64,  P.d_tw32,  P.d_twl32,
                   P.tinv.d,    P.tfwd.d,     P.tinv.d_mi,   P.tfwd.d_mi, P.tinv.d_items,
-                  P.tfwd.d_items, P.d_work,  P.d_err,       P.d_apack, P.d_xpos,   P.d_cexp};
+                  P.tfwd.d_items, P.d_work,  P.d_err,       P.d_apack, P.d_xpos,   P.d_cexp,
+                  P.d_wa_pos, P.d_wa_src};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   P.stage.release();
+  P.wa_spec.release();
   if (P.stream) cudaStreamDestroy(P.stream);
 }
 
@@ -186,6 +189,7 @@ using namespace dccm;
 
 extern "C" int dccm_sht_plan_create(int nmax, int imax, int jmax, int precision, int max_batch,
                                     dccm_sht_plan **plan) {
+  DCCM_NVTX_FUNC();
   if (!plan) return DCCM_ERR_INVALID_ARG;
   *plan = nullptr;
   if (precision != DCCM_SHT_FP64 && precision != DCCM_SHT_MIXED && precision != DCCM_SHT_MIXED_FP16)
@@ -206,6 +210,7 @@ extern "C" int dccm_sht_plan_create(int nmax, int imax, int jmax, int precision,
 }
 
 extern "C" int dccm_sht_plan_destroy(dccm_sht_plan *p) {
+  DCCM_NVTX_FUNC();
   if (!p) return DCCM_OK;
   sht::destroy(p->P);
   delete p;
@@ -236,6 +241,7 @@ extern "C" int dccm_sht_gauss(const dccm_sht_plan *p, double *mu, double *w) {
 }
 
 extern "C" int dccm_sht_pnm(const dccm_sht_plan *p, double *pnm) {
+  DCCM_NVTX_FUNC();
   if (!p || !pnm) return DCCM_ERR_INVALID_ARG;
   DCCM_CUDA(cudaMemcpy(pnm, p->P.d_pnm, (size_t)p->P.ncoef * p->P.Jh * sizeof(double),
                        cudaMemcpyDeviceToHost));
@@ -250,6 +256,7 @@ static int check_batch(const dccm_sht_plan *p, int batch) {
 
 extern "C" int dccm_sht_inverse_dev(dccm_sht_plan *p, const double *spec, double *grid, int batch,
                                     void *stream) {
+  DCCM_NVTX_FUNC();
   DCCM_TRY(check_batch(p, batch));
   if (batch > 0 && (!spec || !grid)) return DCCM_ERR_INVALID_ARG;
   return sht::inverse(p->P, spec, grid, batch, as_stream(stream));
@@ -257,12 +264,14 @@ extern "C" int dccm_sht_inverse_dev(dccm_sht_plan *p, const double *spec, double
 
 extern "C" int dccm_sht_forward_dev(dccm_sht_plan *p, const double *grid, double *spec, int batch,
                                     void *stream) {
+  DCCM_NVTX_FUNC();
   DCCM_TRY(check_batch(p, batch));
   if (batch > 0 && (!spec || !grid)) return DCCM_ERR_INVALID_ARG;
   return sht::forward(p->P, grid, spec, batch, as_stream(stream));
 }
 
 extern "C" int dccm_sht_status(dccm_sht_plan *p, int *device_error) {
+  DCCM_NVTX_FUNC();
   if (!p) return DCCM_ERR_INVALID_ARG;
   DCCM_CUDA(cudaDeviceSynchronize());
   int e = 0;
@@ -297,6 +306,7 @@ static int host_call(dccm_sht_plan *p, const double *in, size_t in_n, double *ou
 }
 
 extern "C" int dccm_sht_inverse(dccm_sht_plan *p, const double *spec, double *grid, int batch) {
+  DCCM_NVTX_FUNC();
   DCCM_TRY(check_batch(p, batch));
   if (batch == 0) return DCCM_OK;
   if (!spec || !grid) return DCCM_ERR_INVALID_ARG;
@@ -305,6 +315,7 @@ extern "C" int dccm_sht_inverse(dccm_sht_plan *p, const double *spec, double *gr
 }
 
 extern "C" int dccm_sht_forward(dccm_sht_plan *p, const double *grid, double *spec, int batch) {
+  DCCM_NVTX_FUNC();
   DCCM_TRY(check_batch(p, batch));
   if (batch == 0) return DCCM_OK;
   if (!spec || !grid) return DCCM_ERR_INVALID_ARG;
@@ -324,6 +335,7 @@ struct dccm_sht_ensemble {
 
 extern "C" int dccm_sht_ensemble_create(int ngroups, const int *nmax, const int *imax, const int *jmax,
                                         const int *max_batch, int precision, dccm_sht_ensemble **ens) {
+  DCCM_NVTX_FUNC();
   if (!ens) return DCCM_ERR_INVALID_ARG;
   *ens = nullptr;
   if (ngroups < 1 || ngroups > 8 || !nmax || !imax || !jmax || !max_batch) return DCCM_ERR_INVALID_ARG;
@@ -344,6 +356,7 @@ extern "C" int dccm_sht_ensemble_create(int ngroups, const int *nmax, const int 
 }
 
 extern "C" int dccm_sht_ensemble_destroy(dccm_sht_ensemble *e) {
+  DCCM_NVTX_FUNC();
   if (!e) return DCCM_OK;
   for (dccm_sht_plan *p : e->plans) dccm_sht_plan_destroy(p);
   delete e;
@@ -402,17 +415,20 @@ int ensemble_forward(dccm_sht_ensemble *e, const double *const *grid, double *co
 
 extern "C" int dccm_sht_ensemble_inverse_dev(dccm_sht_ensemble *e, const double *const *spec,
                                              double *const *grid, const int *batch, void *stream) {
+  DCCM_NVTX_FUNC();
   DCCM_TRY(ens_check(e, spec, grid, batch));
   return sht::ensemble_inverse(e, spec, grid, batch, as_stream(stream));
 }
 
 extern "C" int dccm_sht_ensemble_forward_dev(dccm_sht_ensemble *e, const double *const *grid,
                                              double *const *spec, const int *batch, void *stream) {
+  DCCM_NVTX_FUNC();
   DCCM_TRY(ens_check(e, grid, spec, batch));
   return sht::ensemble_forward(e, grid, spec, batch, as_stream(stream));
 }
 
 extern "C" int dccm_sht_ensemble_status(dccm_sht_ensemble *e, int *device_error) {
+  DCCM_NVTX_FUNC();
   if (!e) return DCCM_ERR_INVALID_ARG;
   int worst = 0, st = DCCM_OK;
   for (dccm_sht_plan *p : e->plans) {

@@ -77,6 +77,10 @@ struct Plan {
   int *d_cexp = nullptr;       // FP16: per field-level scale exponents, [inverse | forward][max_batch]
   DevBuf stage;                // host entry point staging
   cudaStream_t stream = nullptr;
+  // SPML real layout (spml.cu), set up by the first call that uses it:
+  int2 *d_wa_pos = nullptr;    // per spectral index k: wa positions of Re and Im (-1: none)
+  int *d_wa_src = nullptr;     // per wa position l: 2 k + (0: Re, 1: Im)
+  DevBuf wa_spec;              // [max_batch][ncoef] complex spectra between layout and transform
 };
 
 __host__ __device__ inline int64_t idx_mn(int N, int m, int n) {

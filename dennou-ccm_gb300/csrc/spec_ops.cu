@@ -24,6 +24,7 @@
 // one load, two FP64 multiplies and one store: HBM-bound, 32 bytes per
 // coefficient and field-level.
 #include "common.cuh"
+#include "nvtx.cuh"
 
 namespace dccm {
 namespace spec {
@@ -107,6 +108,7 @@ using namespace dccm;
 
 extern "C" int dccm_spec_apply_dev(int nmax, const dccm_spec_op *o, const double *spec_in, double *spec_out,
                                    int batch, void *stream) {
+  DCCM_NVTX_FUNC();
   static thread_local spec::NTable t;
   DCCM_TRY(spec::factors(nmax, o, t));
   if (batch < 0 || (batch > 0 && (!spec_in || !spec_out))) return DCCM_ERR_INVALID_ARG;
@@ -125,6 +127,7 @@ extern "C" int dccm_spec_apply_dev(int nmax, const dccm_spec_op *o, const double
 
 extern "C" int dccm_spec_apply(int nmax, const dccm_spec_op *o, const double *spec_in, double *spec_out,
                                int batch) {
+  DCCM_NVTX_FUNC();
   static thread_local spec::NTable t;
   DCCM_TRY(spec::factors(nmax, o, t));
   if (batch < 0 || (batch > 0 && (!spec_in || !spec_out))) return DCCM_ERR_INVALID_ARG;

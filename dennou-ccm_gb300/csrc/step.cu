@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "flux_rows.cuh"
+#include "nvtx.cuh"
 #include "sht_plan.cuh"
 
 struct dccm_sht_plan {
@@ -544,6 +545,7 @@ static int record(dccm_step *st) {
 }
 
 extern "C" int dccm_step_create(const dccm_step_desc *d, dccm_step **out) {
+  DCCM_NVTX_FUNC();
   if (!d || !out) return DCCM_ERR_INVALID_ARG;
   *out = nullptr;
   if (d->nfl < 0 || d->nremap < 0 || (d->nremap > 0 && !d->remaps)) return DCCM_ERR_INVALID_ARG;
@@ -604,6 +606,7 @@ extern "C" int dccm_step_create(const dccm_step_desc *d, dccm_step **out) {
 }
 
 extern "C" int dccm_step_destroy(dccm_step *st) {
+  DCCM_NVTX_FUNC();
   if (!st) return DCCM_OK;
   drop_host_graph(st);
   if (st->exec) cudaGraphExecDestroy(st->exec);
@@ -619,18 +622,23 @@ extern "C" int dccm_step_destroy(dccm_step *st) {
 }
 
 extern "C" int dccm_step_run(dccm_step *st, void *stream) {
+  DCCM_NVTX_FUNC();
   if (!st || !st->exec) return DCCM_ERR_INVALID_ARG;
   DCCM_CUDA(cudaGraphLaunch(st->exec, as_stream(stream)));
   return DCCM_OK;
 }
 
 extern "C" int dccm_step_run_timed(dccm_step *st, void *stream, float *ms) {
+  DCCM_NVTX_FUNC();
   if (!st || !ms) return DCCM_ERR_INVALID_ARG;
   cudaStream_t s = as_stream(stream);
   int (*stages[6])(dccm_step *, cudaStream_t) = {stage_leg_inv, stage_fft_inv, stage_fft_fwd,
                                                   stage_leg_fwd, stage_remap,   stage_flux};
+  static const char *names[6] = {"stage:legendre_inverse", "stage:fft_inverse", "stage:fft_forward",
+                                 "stage:legendre_forward", "stage:remap", "stage:bulk_flux"};
   DCCM_CUDA(cudaEventRecord(st->ev[0], s));
   for (int k = 0; k < 6; ++k) {
+    NvtxRange r(names[k]);
     DCCM_TRY(stages[k](st, s));
     DCCM_CUDA(cudaEventRecord(st->ev[k + 1], s));
   }
@@ -850,6 +858,7 @@ static bool page_locked(const dccm_host_copy *h2d, int nh2d, const dccm_host_cop
 
 extern "C" int dccm_step_run_host(dccm_step *st, void *stream, const dccm_host_copy *h2d, int nh2d,
                                   const dccm_host_copy *d2h, int nd2h) {
+  DCCM_NVTX_FUNC();
   if (!st || (nh2d > 0 && !h2d) || (nd2h > 0 && !d2h) || nh2d < 0 || nd2h < 0) return DCCM_ERR_INVALID_ARG;
   cudaStream_t s = as_stream(stream);
   // The copy lists of the recorded host graph again: replay it.
@@ -878,6 +887,7 @@ extern "C" int dccm_step_run_host(dccm_step *st, void *stream, const dccm_host_c
 
 extern "C" int dccm_step_autotune_host(dccm_step *st, void *stream, const dccm_host_copy *h2d, int nh2d,
                                        const dccm_host_copy *d2h, int nd2h, int *chosen, float *ms) {
+  DCCM_NVTX_FUNC();
   constexpr int NC = 32;  // (order 1..2) x (path mask 0..15)
   if (!st || (nh2d > 0 && !h2d) || (nd2h > 0 && !d2h) || nh2d < 0 || nd2h < 0) return DCCM_ERR_INVALID_ARG;
   if (chosen) chosen[0] = chosen[1] = chosen[2] = 0;
@@ -969,6 +979,7 @@ extern "C" int dccm_step_autotune_host(dccm_step *st, void *stream, const dccm_h
 }
 
 extern "C" int dccm_step_host_release(dccm_step *st) {
+  DCCM_NVTX_FUNC();
   if (!st) return DCCM_ERR_INVALID_ARG;
   DCCM_CUDA(cudaDeviceSynchronize());
   drop_host_graph(st);
@@ -1139,6 +1150,7 @@ static int tune_knob(dccm_step *st, cudaStream_t s, Knob &kb, float *best_t) {
 }
 
 extern "C" int dccm_step_autotune(dccm_step *st, const char *cache_path, int *chosen) {
+  DCCM_NVTX_FUNC();
   if (!st) return DCCM_ERR_INVALID_ARG;
   Tunables &T = tunables();
   const Tunables saved = T;
@@ -1219,6 +1231,11 @@ extern "C" int dccm_tune_set(const char *knob, int value) {
   } else if (!strcmp(knob, "host_path")) {
     if (value > 32) return DCCM_ERR_INVALID_ARG;
     T.host_path = value;
+  } else if (!strcmp(knob, "wait_limit_ms")) {
+    if (value > 60000) return DCCM_ERR_INVALID_ARG;
+    T.wait_limit_ms = value;
+  } else if (!strcmp(knob, "tc_withhold_loads")) {
+    T.tc_withhold_loads = value ? 1 : 0;
   }
   else return DCCM_ERR_INVALID_ARG;
   return DCCM_OK;
@@ -1235,6 +1252,8 @@ extern "C" int dccm_tune_get(const char *knob, int *value) {
   else if (!strcmp(knob, "serial")) *value = T.serial;
   else if (!strcmp(knob, "upload_order")) *value = T.upload_order;
   else if (!strcmp(knob, "host_path")) *value = T.host_path;
+  else if (!strcmp(knob, "wait_limit_ms")) *value = T.wait_limit_ms;
+  else if (!strcmp(knob, "tc_withhold_loads")) *value = T.tc_withhold_loads;
   else return DCCM_ERR_INVALID_ARG;
   return DCCM_OK;
 }

@@ -261,16 +261,16 @@ int dccm_area_integral_dev(const double *f, const double *area, int64_t n,
 
 /* The same compensated integral without allocating any device memory.
  * No counterpart in the reference: this is for callers that cannot call
- * cudaMalloc (a model that has already reserved the whole GPU for its own
- * allocator, code that must not synchronise the device, code running while
- * a stream is captured into a graph).  Its scratch is a fixed 256 KB array
- * in the library's device image, held by every GPU that loads the library
- * until the process exits.  Limit: n <= 67,108,864 (2^26) elements, else
- * DCCM_ERR_SHAPE.  All calls share that array, so calls that overlap on the
- * GPU race; serialise them.  The first call on each device looks up the
- * array's device address (with that device current) and should be made
- * before any stream capture.  Synchronises the stream and writes *result
- * (host). */
+ * cudaMalloc, such as a model that has already reserved the whole GPU for
+ * its own allocator, so that a component linked into it has no memory
+ * left to allocate.  Its scratch is a fixed 256 KB array in the library's
+ * device image, held by every GPU that loads the library until the process
+ * exits.  Limit: n <= 67,108,864 (2^26) elements, else DCCM_ERR_SHAPE.  All
+ * calls share that array, so calls that overlap on the GPU race; serialise
+ * them.  The first call in each CUDA context looks up the array's device
+ * address (with that context current).  Like dccm_area_integral_dev it
+ * copies the result to *result (host) and synchronises the stream before
+ * returning. */
 int dccm_area_integral_noalloc_dev(const double *f, const double *area, int64_t n,
                                    double *result, void *stream);
 
@@ -331,6 +331,31 @@ int dccm_sht_forward(dccm_sht_plan *plan, const double *grid, double *spec, int 
 /* Synchronises the device and reports (then clears) the error flag that
  * bounded device waits set; DCCM_ERR_TIMEOUT if one gave up. */
 int dccm_sht_status(dccm_sht_plan *plan, int *device_error);
+
+/* The same transforms in SPML's real spectral layout, the arrays a DCPAM
+ * caller holds: SPML's xya_wa (spectral -> grid) and wa_xya (grid ->
+ * spectral) of its wa_module, called by the dynamics through libdcpam5
+ * (atm/dcpam_main_mod.f90:2173-2180); w_Initial and the axes as above
+ * (tool/gmapgen/gmapgen_main.f90:262-305).  wa[b][l] doubles, (N+1)^2 per
+ * field-level (Fortran wa((nmax+1)**2, kmax)), l = l_nm(n, m) - 1 =
+ * n(n+1) + m for m = -n..n: Re s_n^m at m >= 0, Im s_n^|m| at m < 0.
+ * SPML's expansion, normalisation and phase are this library's (above), so
+ * the layouts differ by a permutation only; it is restated from SPML's
+ * published l_nm / nm_l (SPML is external: unpinned against its code).
+ * xya as grid above.  Batch <= max_batch.  The first call on a plan sets up
+ * its permutation tables and a spectral buffer of max_batch field-levels
+ * (device allocation: make it before any stream capture).  The _dev forms
+ * are stream-ordered; the host forms return when the result is in host
+ * memory and report DCCM_ERR_TIMEOUT as dccm_sht_inverse does. */
+int dccm_sht_xya_wa_dev(dccm_sht_plan *plan, const double *wa, double *xya, int batch, void *stream);
+int dccm_sht_wa_xya_dev(dccm_sht_plan *plan, const double *xya, double *wa, int batch, void *stream);
+int dccm_sht_xya_wa(dccm_sht_plan *plan, const double *wa, double *xya, int batch);
+int dccm_sht_wa_xya(dccm_sht_plan *plan, const double *xya, double *wa, int batch);
+/* The permutations alone, device arrays, stream-ordered: SPML wa <-> this
+ * library's spec (for callers that feed dccm_step_* or dccm_spec_apply_dev,
+ * which take the native layout). */
+int dccm_sht_spec_from_wa_dev(dccm_sht_plan *plan, const double *wa, double *spec, int batch, void *stream);
+int dccm_sht_wa_from_spec_dev(dccm_sht_plan *plan, const double *spec, double *wa, int batch, void *stream);
 
 /* Ensemble of mixed truncations: ngroups (<= 8) truncation groups, each a
  * plan as above holding the field-levels of all members of that truncation
@@ -504,6 +529,15 @@ int dccm_step_autotune_host(dccm_step *step, void *stream, const dccm_host_copy 
  * "serial" and "flux_ctas" with dccm_tune_get).  The knobs are
  * process-wide defaults of later launches too. */
 int dccm_step_autotune(dccm_step *step, const char *cache_path, int *chosen);
+/* Process-wide knobs of later launches (and of graphs recorded later): the
+ * launch shapes above, "upload_order" and "host_path" (dccm_step_run_host),
+ * and two of the failure path: "wait_limit_ms", the limit of every bounded
+ * wait of the tensor-core Legendre kernel (0: 1000 ms; at most 60000), and
+ * "tc_withhold_loads" (1: that kernel's load thread issues no copies, so
+ * that its waits expire and the call reports DCCM_ERR_TIMEOUT through
+ * dccm_sht_status / the host entry points; nothing is left in flight, and
+ * the next launch with the knob at 0 is unaffected: a test of the timeout
+ * path, never for production).  Unknown knob or value: DCCM_ERR_INVALID_ARG. */
 int dccm_tune_set(const char *knob, int value);
 int dccm_tune_get(const char *knob, int *value);
 

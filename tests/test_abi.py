@@ -81,3 +81,38 @@ def test_null_arguments_rejected(dccm):
     assert lib.dccm_remap_plan_create(4, 4, 1, None, None, None, ctypes.byref(h)) == -1
     assert lib.dccm_sfc_bulk_flux_get(None, None) == -1
     assert lib.dccm_remap_table_read(None, ctypes.byref(h)) == -1
+
+
+def test_failure_path_knobs(dccm):
+    """The wait limit and the test-only load withholding are process-wide
+    knobs with checked ranges (setting them launches nothing)."""
+    saved = {k: dccm.tune_get(k) for k in ("wait_limit_ms", "tc_withhold_loads")}
+    try:
+        dccm.tune_set("wait_limit_ms", 60000)
+        assert dccm.tune_get("wait_limit_ms") == 60000
+        for bad in (("wait_limit_ms", 60001), ("wait_limit_ms", -1), ("no_such_knob", 1)):
+            try:
+                dccm.tune_set(*bad)
+                raise AssertionError("accepted %r" % (bad,))
+            except dccm.DccmError as e:
+                assert e.status == -1
+        dccm.tune_set("tc_withhold_loads", 5)
+        assert dccm.tune_get("tc_withhold_loads") == 1
+    finally:
+        for k, v in saved.items():
+            dccm.tune_set(k, v)
+
+
+def test_spml_index_functions(dccm):
+    """l_nm / nm_l (SPML's storage rule of its wa arrays) are inverse to each
+    other and cover 1..(N+1)^2 exactly once."""
+    N = 42
+    ls = []
+    for n in range(N + 1):
+        for m in range(-n, n + 1):
+            l = dccm.l_nm(n, m)
+            assert tuple(int(x) for x in dccm.nm_l(l)) == (n, m)
+            ls.append(l)
+    assert sorted(ls) == list(range(1, (N + 1) ** 2 + 1))
+    n, m = dccm.nm_l(np.arange(1, (N + 1) ** 2 + 1))
+    assert np.array_equal(dccm.l_nm(n, m), np.arange(1, (N + 1) ** 2 + 1))

@@ -1,10 +1,9 @@
 """The area integral that allocates no device memory.
 
 dccm_area_integral_noalloc_dev exists for callers that cannot call
-cudaMalloc: a model that has already reserved all of the GPU for its own
-allocator, code that must not synchronise the device, or code issuing work
-while a stream is captured into a graph.  It keeps its scratch in a fixed
-array inside the library.  Here it is called through the C ABI and must
+cudaMalloc, such as a model that has already reserved all of the GPU for
+its own allocator.  It keeps its scratch in a fixed array inside the
+library.  Here it is called through the C ABI and must
 agree with the allocating dccm_area_integral_dev, within the tolerance the
 other compensated-sum tests use, on two calls in a row.  The second call is
 smaller than the first, so stale partial sums left in the shared array by
