@@ -436,12 +436,18 @@ def host_copies(S, groups, dccm, torch):
 
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of
 # each stage's kernels in one ncu capture of `bench.py --profile-steps`,
-# kept with the profiles of the c3 step; null where not captured.
+# kept with the profiles of the c3 step; null where not captured.  The c3
+# step's working set (about 85 MB) fits the 126 MB L2, so a kernel's
+# writes can stay in L2 past its end and its DRAM bytes can fall below its
+# algorithmic bytes; the L2 bytes of the same launches (lts__t_bytes.sum,
+# every request L2 serves) are reported beside them.
 TRAFFIC = {
     "c3": {"legendre_inverse": int((7.686912 + 12.131584) * 1e6 + 1280), "fft_inverse": int(11.341056e6 + 512),
            "fft_forward": int(33.623296e6 + 56064), "legendre_forward": int(18.93888e6),
            "remap": int(4.062976e6), "bulk_flux": int(7.707392e6 + 768)},
 }
+L2_BYTES = {}
+TRAFFIC_SOURCE = "ncu of bench.py --workload c3 --profile-steps 3 (profiles/stages_c3_ncu.md)"
 # FP64 peak: measured on the device by dccm_fp64_peak (independent DFMA
 # chains on every SM) at the start of the run; the nominal figure (2 DFMA
 # lanes per SM and clock at the maximum SM clock) is reported beside it.
@@ -455,34 +461,63 @@ def stage_work(S, inp, groups):
     tensor work (six BF16 products of the split operands) is far below the
     byte time, so both Legendre stages are bandwidth-bound.  FFT: FP32
     Fourier coefficients <-> FP64 grid.  Remap: 16 bytes per table entry,
-    row pointers, source fields once and destination rows.  Flux: 504
-    bytes per ocean column (inputs and outputs, FP64)."""
+    source fields once and destination rows (the sliced layout's padding
+    and slice descriptors are overhead, not counted).  Flux: 504 bytes per
+    ocean column (inputs and outputs, FP64)."""
     spec = sum(g.nfl * (g.N + 1) * (g.N + 2) // 2 * 16 for g in groups)
     four = sum(g.nfl * g.J * (g.N + 1) * 2 * 4 for g in groups)
     table = sum((g.N + 1) * (g.N + 2) // 2 * (g.J // 2) * 6 for g in groups)
     grid = sum(g.nfl * g.J * g.I * 8 for g in groups)
     flops = sum(2.0 * g.J * (g.N + 1) * (g.N + 2) / 2 * g.nfl for g in groups)
     n1 = len(inp["ocean"])
-    remap = sum(16 * len(tb[2]) + 8 * (n1 + 1) + 8 * 6 * len(g.members) * (g.I * g.J + n1)
+    remap = sum(16 * len(tb[2]) + 8 * 6 * len(g.members) * (g.I * g.J + n1)
                 for g, tb in zip(groups, S["tables"]))
     return {"legendre_inverse": (spec + four + table, flops), "fft_inverse": (four + grid, None),
             "fft_forward": (grid + four, None), "legendre_forward": (four + spec + table, flops),
             "remap": (remap, None), "bulk_flux": (504 * S["ncol"], None)}
 
 
-def roofline(S, inp, groups, stage_ms, workload, fp64_peak, flux_alone=None):
-    """Per-stage roofline against the measured copy bandwidth; the dominant
-    (longest) stage is the headline.  Legendre stages also report their
-    tensor rate (useful flops over the measured BF16 peak); the flux
-    kernel, bound by the FP64 pipe, reports its FP64 rate as counted by ncu
-    over the FP64 peak (2 DFMA lanes per SM and clock).  flux_alone: the
-    flux kernel timed alone on its full grid when the step caps its grid;
-    its roofline is then taken from that time (the step's time and cap are
-    kept beside it)."""
+def stage_work_f64(groups):
+    """The FP64 path's algorithmic work per stage: Legendre 2 J Ncoef FP64
+    flops per field-level (complex x real multiply-adds over the latitude
+    pairs, both parities), bytes of the FP64 spectra, the FP64 Fourier
+    coefficients (16 J (N+1) per field-level) and the FP64 Pbar table
+    (8 Ncoef J/2); FFT 5 I log2(I) flops per row pair (complex FFT of the
+    packed pair), bytes of the grid and the Fourier coefficients."""
+    out = {}
+    spec = sum(g.nfl * (g.N + 1) * (g.N + 2) // 2 * 16 for g in groups)
+    four = sum(g.nfl * g.J * (g.N + 1) * 16 for g in groups)
+    table = sum((g.N + 1) * (g.N + 2) // 2 * (g.J // 2) * 8 for g in groups)
+    grid = sum(g.nfl * g.J * g.I * 8 for g in groups)
+    leg = sum(2.0 * g.J * (g.N + 1) * (g.N + 2) / 2 * g.nfl for g in groups)
+    fft = sum(5.0 * g.I * np.log2(g.I) * (g.J // 2) * g.nfl for g in groups)
+    out["legendre_inverse"] = (spec + four + table, leg)
+    out["fft_inverse"] = (four + grid, fft)
+    out["fft_forward"] = (grid + four, fft)
+    out["legendre_forward"] = (four + spec + table, leg)
+    return out
+
+
+CHAIN = ["legendre_inverse", "fft_inverse", "fft_forward", "legendre_forward"]
+
+
+def roofline(S, inp, groups, stage_ms, workload, fp64_peak, flux_alone=None, products=6):
+    """Per-stage roofline against the copy bandwidth, and the headline: the
+    transform chain (spectra pack + Legendre synthesis, inverse FFT, forward
+    FFT, Legendre analysis), the step's critical path, as one entry (its
+    algorithmic bytes over the sum of its stage times).  Legendre stages
+    also report their tensor rate against the BF16 peak divided by the
+    products per multiply-add (6 for BF16 x 3, 3 for FP16 hi + lo), with
+    the raw fraction of the BF16 peak beside it.  The flux kernel, bound by
+    the FP64 pipe, reports its FP64 instruction rate (ncu counts per
+    column) over the measured FP64 peak.  flux_alone: the flux kernel timed
+    alone on its full grid when the step caps its grid; its roofline is then
+    taken from that time (the step's time and cap are kept beside it)."""
     hbm, bf16, src_peak = peaks()
     names = dccm_stages()
     work = stage_work(S, inp, groups)
     traffic = TRAFFIC.get(workload, {})
+    l2b = L2_BYTES.get(workload, {})
     stages = {}
     stage_ms = list(stage_ms)
     if flux_alone:
@@ -491,22 +526,24 @@ def roofline(S, inp, groups, stage_ms, workload, fp64_peak, flux_alone=None):
         q, fl = work[n]
         ach = q / (ms / 1e3) / 1e9
         st = {"ms": float(ms), "bound": "hbm", "achieved": ach, "unit": "GB/s", "peak": hbm, "frac": ach / hbm,
-              "algorithmic_bytes": q, "traffic": traffic.get(n)}
+              "algorithmic_bytes": q, "traffic": traffic.get(n), "l2_bytes": l2b.get(n)}
         if fl is not None:
             tf = fl / (ms / 1e3) / 1e12
-            st["tensor"] = {"achieved": tf, "unit": "TFLOP/s", "peak": bf16, "frac": tf / bf16,
+            st["tensor"] = {"achieved": tf, "unit": "TFLOP/s", "peak": bf16 / products, "frac": tf / (bf16 / products),
+                            "products_per_mac": products, "raw_peak": bf16, "raw_frac": tf / bf16,
                             "algorithmic_flops": fl}
         stages[n] = st
     stages["bulk_flux"]["limiter"] = "FP64 pipe, not HBM"
     if flux_alone:
         stages["bulk_flux"]["launch"] = ("full grid, timed alone; in the step its grid is capped at %d CTAs "
                                          "(%.4f ms there)" % (flux_alone["step_cta_cap"], flux_alone["ms_in_step"]))
-    f64 = FLUX_FP64_FLOPS_PER_COLUMN * S["ncol"]
-    if f64:
-        tf = f64 / (stages["bulk_flux"]["ms"] / 1e3) / 1e12
-        stages["bulk_flux"]["fp64"] = {"achieved": tf, "unit": "TFLOP/s", "peak": fp64_peak,
-                                       "peak_source": "measured (dccm_fp64_peak)", "frac": tf / fp64_peak,
-                                       "flops_per_launch": f64}
+    f64 = FLUX_FP64_INSTR_PER_COLUMN * S["ncol"]
+    tf = f64 / (stages["bulk_flux"]["ms"] / 1e3) / 1e12
+    stages["bulk_flux"]["fp64"] = {"achieved": tf, "unit": "TFLOP/s", "peak": fp64_peak,
+                                   "peak_source": "measured (dccm_fp64_peak)", "frac": tf / fp64_peak,
+                                   "flops_per_launch": f64,
+                                   "count": "FP64 pipe work per column from ncu instruction counts (DADD + DMUL "
+                                            "+ 2 DFMA), the same for every ice-free column"}
     # the remap keeps the reference's separately rounded products and sums
     # (bit-exact): one DMUL and one DADD per table entry and field, reported
     # beside its bytes
@@ -515,21 +552,46 @@ def roofline(S, inp, groups, stage_ms, workload, fp64_peak, flux_alone=None):
     stages["remap"]["fp64"] = {"achieved": tf, "unit": "TFLOP/s", "peak": fp64_peak,
                                "peak_source": "measured (dccm_fp64_peak)", "frac": tf / fp64_peak,
                                "flops_per_launch": rf}
-    stages["remap"]["limiter"] = "latency of the dependent gathers (record, then source value), not HBM"
-    dom = names[int(np.argmax(stage_ms))]
-    roof = dict(stages[dom])
-    roof.update({"kernel": dom, "peak_source": src_peak, "stages": stages,
-                 "traffic_source": ("ncu --set full of bench.py --workload c3 --profile-steps 3"
-                                    if workload in TRAFFIC else None)})
+    cq = sum(work[n][0] for n in CHAIN)
+    cms = sum(stage_ms[names.index(n)] for n in CHAIN)
+    ctr = [traffic.get(n) for n in CHAIN]
+    cl2 = [l2b.get(n) for n in CHAIN]
+    ach = cq / (cms / 1e3) / 1e9
+    roof = {"kernel": "transform chain: spectra pack + Legendre synthesis (tcgen05), inverse FFT, forward FFT, "
+                      "Legendre analysis (tcgen05)",
+            "bound": "hbm", "achieved": ach, "unit": "GB/s", "peak": hbm, "frac": ach / hbm, "ms": cms,
+            "algorithmic_bytes": cq, "traffic": sum(ctr) if all(x is not None for x in ctr) else None,
+            "l2_bytes": sum(cl2) if all(x is not None for x in cl2) else None,
+            "peak_source": src_peak, "critical_path": True,
+            "traffic_source": (TRAFFIC_SOURCE if workload in TRAFFIC else None),
+            "stages": stages}
     return roof
 
 
-# FP64 flops of the flux kernel per ocean column (DADD + DMUL + 2 DFMA
+def roofline_f64(groups, stage_ms, fp64_peak):
+    """Stage rooflines of the FP64 step (the denominator of mixed / FP64):
+    FP64 flops over the measured FP64 peak, bytes over the copy bandwidth."""
+    hbm, _, _ = peaks()
+    work = stage_work_f64(groups)
+    names = dccm_stages()
+    out = {}
+    for n in CHAIN:
+        ms = float(stage_ms[names.index(n)])
+        q, fl = work[n]
+        tf = fl / (ms / 1e3) / 1e12
+        out[n] = {"ms": ms, "fp64": {"achieved": tf, "unit": "TFLOP/s", "peak": fp64_peak, "frac": tf / fp64_peak,
+                                     "algorithmic_flops": fl},
+                  "hbm": {"achieved": q / (ms / 1e3) / 1e9, "unit": "GB/s", "peak": hbm,
+                          "frac": q / (ms / 1e3) / 1e9 / hbm, "algorithmic_bytes": q}}
+    return out
+
+
+# FP64 pipe work of the flux kernel per ocean column (DADD + DMUL + 2 DFMA
 # thread instructions per cycle x elapsed cycles, ncu sass counters, c3:
-# 25.4 M flops for 45,478 columns).  Every
-# column does the same work when there is no sea ice (all workloads here:
-# the ice physics is skipped where SIceCon = 0).
-FLUX_FP64_FLOPS_PER_COLUMN = (20.948747 + 41.897494 + 2 * 114.69439) * 86836.697368 / 45478
+# 25.4 M for 45,478 columns).  Every column does the same work when there
+# is no sea ice (all workloads here: the ice physics is skipped where
+# SIceCon = 0), so the per-column figure carries to every workload.
+FLUX_FP64_INSTR_PER_COLUMN = (20.948747 + 41.897494 + 2 * 114.69439) * 86836.697368 / 45478
 
 
 # FP64 flops of the implicit-coupling sweeps per column and level, one
@@ -702,6 +764,13 @@ def gpu_bench(args, w, inp, rank, world):
         stage_ms += np.array(S["steps"]["mixed"].run_timed(stream))
     stage_ms /= nt
     fp64_peak = dccm.fp64_peak(stream)
+    # the FP64 step's stages the same way: the denominator of mixed / FP64
+    stage_f64 = np.zeros(6)
+    for k in range(nt):
+        flush.fill_(float(k))
+        stage_f64 += np.array(S["steps"]["fp64"].run_timed(stream))
+    stage_f64 /= nt
+    roof_f64 = roofline_f64(groups, stage_f64, fp64_peak)
     # The whole-step autotune may cap the flux kernel's grid (it runs beside
     # the transforms and then leaves them issue slots); the kernel's own
     # roofline is taken on its full grid, timed alone the same way.
@@ -763,7 +832,8 @@ def gpu_bench(args, w, inp, rank, world):
                    "surface_branch": "implicit coupling forward, remaps (+ ImplCplCoef1/2), flux, "
                                      "DelVarImplCPL back to level 1, implicit coupling backward"}
         del C
-    return dict(t_mixed=t_mixed, t_fp64=t_fp64, t_fp16=t_fp16, err_fp16=err_fp16, t_e2e=t_e2e, clocks=ck, roof=roof, err=err, h2d=h2d_bytes,
+    return dict(t_mixed=t_mixed, t_fp64=t_fp64, t_fp16=t_fp16, err_fp16=err_fp16, t_e2e=t_e2e, clocks=ck, roof=roof,
+                roof_f64=roof_f64, stage_f64=[float(x) for x in stage_f64], err=err, h2d=h2d_bytes,
                 d2h=d2h_bytes, nfl=nfl, launches=launches, tables=S["tables"], tuned=dict(tuned, host=host_tuned),
                 implcpl=ic, spec_ops=so, coupled=coupled)
 
@@ -925,24 +995,34 @@ def main():
         cpu = {"value": nfl / step_s, "unit": "field-levels/s", "cores": oracle.get_threads(), "kind": "port",
                "sample": "3 steps: transforms of %d of %d field-levels (scaled), every remap and the bulk flux; "
                          "C FP64 oracle, OpenMP" % (nsample, nfl)}
+    roof = dict(r["roof"])
+    stages = roof.pop("stages")
+    f64_frac = {n: round(v["fp64"]["frac"], 4) for n, v in r["roof_f64"].items()}
+    # Order: the voluminous per-leg detail first, the figures a reader
+    # checks first (roofline headline, end to end, FP64 comparison) last,
+    # where a truncated tail of the output still shows them.
     line = {
         "metric": metric, "value": job_throughput(world, nfl, r["t_mixed"]), "unit": "field-levels/s", "n_gpus": world,
         "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": r["t_mixed"] * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "bf16x3+f32 (Legendre), f32 (FFT), f64 (remap, flux)",
         "data": "synthetic (seeded PCG64; n^-3 spectra, SST-based surface state)", "config": config,
-        "fp64_gpu": {"value": job_throughput(world, nfl, r["t_fp64"]), "ms_per_step": r["t_fp64"] * 1e3,
-                     "mixed_over_fp64": r["t_fp64"] / r["t_mixed"]},
+        "implicit_coupling": r["implcpl"], "spectral_operators": r["spec_ops"], "coupled_step": r["coupled"],
+        "roofline_stages": stages, "fp64_gpu_stages": r["roof_f64"],
         "fp16_variant": {"value": job_throughput(world, nfl, r["t_fp16"]), "ms_per_step": r["t_fp16"] * 1e3,
                          "over_fp64": r["t_fp64"] / r["t_fp16"],
                          "legendre": "FP16 hi + lo, per-m and per-field-level power-of-two scales",
                          "accuracy": r["err_fp16"]},
         "accuracy": r["err"],
+        "gpu_launches": r["launches"] * args.steps, "clocks": r["clocks"], "cpu_baseline": cpu,
+        "roofline": roof,
         "e2e": {"value": job_throughput(world, nfl, r["t_e2e"]), "unit": "field-levels/s", "h2d_bytes_per_step": r["h2d"],
                 "d2h_bytes_per_step": r["d2h"], "ms_per_step": r["t_e2e"] * 1e3},
-        "gpu_launches": r["launches"] * args.steps,
-        "roofline": r["roof"], "clocks": r["clocks"], "cpu_baseline": cpu,
-        "implicit_coupling": r["implcpl"], "spectral_operators": r["spec_ops"], "coupled_step": r["coupled"],
+        "stage_ms": {n: round(v["ms"], 5) for n, v in stages.items()},
+        "fp64_gpu": {"value": job_throughput(world, nfl, r["t_fp64"]), "ms_per_step": r["t_fp64"] * 1e3,
+                     "mixed_over_fp64": r["t_fp64"] / r["t_mixed"],
+                     "stage_ms": {n: round(x, 5) for n, x in zip(dccm_stages()[:4], r["stage_f64"][:4])},
+                     "stage_fp64_frac": f64_frac},
     }
     print(json.dumps(line))
     if world > 1:

@@ -713,6 +713,8 @@ class Step:
         chosen = dict(zip(self.KNOBS, list(out)))
         chosen["serial"] = tune_get("serial")
         chosen["flux_ctas"] = tune_get("flux_ctas")
+        chosen["remap_fc"] = tune_get("remap_fc")
+        chosen["tc_shape"] = tune_get("tc_shape")
         return chosen
 
     def run_timed(self, stream=None):

@@ -30,11 +30,13 @@ void set_cuda_error(cudaError_t e);
 // default).  dccm_step_autotune chooses them per step by timing candidates;
 // dccm_tune_set / dccm_tune_get expose them.
 struct Tunables {
-  int tc_ctas = 0;        // persistent CTAs of the tensor-core Legendre kernel
+  int tc_ctas = 0;        // persistent CTAs of the tensor-core Legendre kernel (at most one wave)
+  int tc_shape = 0;       // tensor-core Legendre kernel: 0 narrow where the table allows (2 CTAs an SM), 1 wide
   int fft_bb = 0;         // warps per FFT CTA (4, 8, 16)
   int flux_threads = 0;   // threads per CTA of the bulk-flux kernel
   int flux_ctas = 0;      // CTA cap of the bulk-flux kernel's grid-stride loop (0: 16 per SM)
   int remap_threads = 0;  // threads per CTA of the remap kernel
+  int remap_fc = 0;       // fields per thread of the remap kernel (1, 2, 3, 4, 6; 0: 3, or all below 6)
   int serial = 0;         // 1: launch_pdl makes ordinary launches
   int upload_order = 0;   // dccm_step_run_host: 1 transforms' inputs first, 2 surface inputs first
   int host_path = 0;      // dccm_step_run_host: 1 + mask of the copy groups moved through the host mapping (0: 1)

@@ -42,11 +42,23 @@ namespace sht {
 
 constexpr int TC_THREADS = 192;
 constexpr int A_SPLIT_BYTES = 128 * 128;     // 128 rows (c) x 64 bf16 (K)
-constexpr int B_SPLIT_BYTES = 128 * 128;     // 128 rows (N) x 64 bf16 (K); a table whose N tiles all fit
-                                              // 64 rows loads boxes of 64 rows (half) into the same slot
-constexpr int STAGE_BYTES = 3 * A_SPLIT_BYTES + 3 * B_SPLIT_BYTES;  // 96 KB
-constexpr int NSTAGE = 2;
-constexpr int TMEM_COLS = 512;
+// Two shapes of the same kernel:
+//   wide   (any table): two 96 KB stages (B boxes of up to 128 N rows), all
+//          512 TMEM columns (two accumulator sets when they fit), one CTA
+//          per SM;
+//   narrow (tables whose N tiles all fit 64 rows, e.g. truncations up to
+//          T85 on their Gaussian grids): one 72 KB stage (B boxes of 64
+//          rows), 256 TMEM columns (one accumulator set), 90 KB of shared
+//          memory in all, so two CTAs share an SM and one CTA's loads and
+//          epilogue overlap the other's (a c3 launch has 172 items: one a
+//          CTA instead of up to two).
+template <bool NARROW> struct TcShape {
+  static constexpr int NSTAGE = NARROW ? 1 : 2;
+  static constexpr int B_SPLIT_BYTES = NARROW ? 64 * 128 : 128 * 128;  // N rows x 64 bf16 (K)
+  static constexpr int STAGE_BYTES = 3 * A_SPLIT_BYTES + 3 * B_SPLIT_BYTES;  // 72 KB or 96 KB
+  static constexpr int TMEM_COLS = NARROW ? 256 : 512;
+  static constexpr int MIN_CTAS = NARROW ? 2 : 1;  // resident CTAs per SM
+};
 // Analysis epilogue staging: 128 rows (c) x 32 floats (16 k of both
 // parities), rows padded to 33 floats (conflict-free row and column access).
 constexpr int EP_LD = 33;
@@ -215,8 +227,12 @@ __device__ __forceinline__ int group_of(const TcLaunch &L, int it) {
   return gi;
 }
 
-__global__ void __launch_bounds__(TC_THREADS, 1)
+template <bool NARROW>
+__global__ void __launch_bounds__(TC_THREADS, TcShape<NARROW>::MIN_CTAS)
 legendre_tc_kernel(const __grid_constant__ TcLaunch L) {
+  using Sh = TcShape<NARROW>;
+  constexpr int NSTAGE = Sh::NSTAGE, STAGE_BYTES = Sh::STAGE_BYTES, B_SPLIT_BYTES = Sh::B_SPLIT_BYTES;
+  constexpr int TMEM_COLS = Sh::TMEM_COLS;
   extern __shared__ __align__(1024) unsigned char smem_dyn[];
   // 1024-byte aligned stage area (swizzle atoms are address based).
   unsigned char *sm = reinterpret_cast<unsigned char *>(
@@ -883,7 +899,9 @@ int build_tiles(Plan &P) {
   return DCCM_OK;
 }
 
-static size_t tc_smem_bytes() { return 1024 + (size_t)NSTAGE * STAGE_BYTES + 128 + EP_BYTES; }
+template <bool NARROW> static size_t tc_smem_bytes() {
+  return 1024 + (size_t)TcShape<NARROW>::NSTAGE * TcShape<NARROW>::STAGE_BYTES + 128 + EP_BYTES;
+}
 
 // One persistent launch over ngroups plans (truncation groups) of one
 // direction: dir 0 (inverse) reads the plan's packed spectra (pack_spectra
@@ -896,8 +914,12 @@ int legendre_tc_multi(Plan *const *plans, const int *batch, const void *const *i
   static bool attr_done = false;
   if (ngroups < 1 || ngroups > MAXG) return DCCM_ERR_UNSUPPORTED;
   if (!attr_done) {
-    DCCM_CUDA(cudaFuncSetAttribute(legendre_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)tc_smem_bytes()));
+    DCCM_CUDA(cudaFuncSetAttribute(legendre_tc_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)tc_smem_bytes<false>()));
+    DCCM_CUDA(cudaFuncSetAttribute(legendre_tc_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)tc_smem_bytes<true>()));
+    DCCM_CUDA(cudaFuncSetAttribute(legendre_tc_kernel<true>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                   (int)cudaSharedmemCarveoutMaxShared));
     attr_done = true;
   }
   TcLaunch L;
@@ -908,6 +930,7 @@ int legendre_tc_multi(Plan *const *plans, const int *batch, const void *const *i
     if (!T.map_ok) return DCCM_ERR_UNSUPPORTED;
     ntmax = T.ntmax > ntmax ? T.ntmax : ntmax;
   }
+  const bool narrow = ntmax <= 64 && tunables().tc_shape == 0;
   for (int g = 0; g < ngroups; ++g) {
     if (batch[g] <= 0) continue;
     Plan &P = *plans[g];
@@ -923,7 +946,7 @@ int legendre_tc_multi(Plan *const *plans, const int *batch, const void *const *i
     a.err = plans[0]->d_err;
     a.ntmax = ntmax;
     a.brows = T.ntmax;
-    a.nacc = 8 * ntmax <= TMEM_COLS ? 2 : 1;
+    a.nacc = 8 * ntmax <= (narrow ? TcShape<true>::TMEM_COLS : TcShape<false>::TMEM_COLS) ? 2 : 1;
     a.nsplit = P.nsplit;
     a.cexp = dir == 0 ? P.d_cexp : P.d_cexp + P.max_batch;
     if (dir == 0) a.F = (float *)out[g];
@@ -941,9 +964,14 @@ int legendre_tc_multi(Plan *const *plans, const int *batch, const void *const *i
                                            : WAIT_LIMIT_NS;
   L.withhold = tunables().tc_withhold_loads;
   if (items <= 0) return DCCM_OK;
-  int ctas = tunables().tc_ctas > 0 ? tunables().tc_ctas : sm_count();
+  const int resident = (narrow ? TcShape<true>::MIN_CTAS : 1) * sm_count();  // persistent: at most one wave
+  int ctas = tunables().tc_ctas > 0 ? tunables().tc_ctas : resident;
+  ctas = ctas < resident ? ctas : resident;
   const int grid = items < ctas ? items : ctas;
-  DCCM_CUDA(launch_pdl(legendre_tc_kernel, dim3(grid), dim3(TC_THREADS), tc_smem_bytes(), s, L));
+  if (narrow)
+    DCCM_CUDA(launch_pdl(legendre_tc_kernel<true>, dim3(grid), dim3(TC_THREADS), tc_smem_bytes<true>(), s, L));
+  else
+    DCCM_CUDA(launch_pdl(legendre_tc_kernel<false>, dim3(grid), dim3(TC_THREADS), tc_smem_bytes<false>(), s, L));
   return DCCM_OK;
 }
 

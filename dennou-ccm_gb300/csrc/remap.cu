@@ -18,11 +18,20 @@
 // order: REF-mode weights are bit-identical to the restated reference.
 //
 // Apply.  The table is grouped by destination, so a stable counting sort
-// turns it into CSR without changing the per-row order.  One thread owns a
-// (destination row, field) pair; each nonzero is one 16-byte record (weight,
-// column) fetched with a single 128-bit load; sums start at zero and add the
-// separately rounded products in table order, which makes the result
-// bit-identical to the reference loop (:293-302).
+// groups it by row without changing the per-row order.  The rows are then
+// stored as a sliced ELL matrix: slices of 32 consecutive destination rows
+// (one warp), each slice as many record columns wide as its longest row,
+// record k of lane r at slice_base + 32 k + r, so that a warp's k-th records
+// are one coalesced 512-byte load.  A record is 16 bytes (weight, source
+// column; column -1 pads a short row).  One thread owns a destination row
+// and FC of the fields: it loads each record once and gathers the FC source
+// values of its column (all of a round's gathers in flight together);
+// sums start at zero and add the separately rounded products in table
+// order, which makes the result bit-identical to the reference loop
+// (:293-302); the first addition of a row, 0 + p, is p with -0 turned into
+// +0, which integer instructions give exactly without the FP64 pipe (the
+// pipe the kernel is bound by: one DMUL per entry and field, one DADD per
+// entry after the first).
 #include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -39,9 +48,10 @@
 
 struct dccm_remap_plan {
   int64_t n_send = 0, n_recv = 0, nnz = 0;
-  int64_t *d_rowptr = nullptr;  // n_recv+1
-  double2 *d_ent = nullptr;     // nnz records: x = weight, y = column (0-based) bits
-  dccm::DevBuf stage;           // host entry point staging
+  int64_t nslice = 0, nrec = 0;  // 32-row slices; records including padding
+  int2 *d_slices = nullptr;      // per slice: (first record / 32, width in records)
+  double2 *d_ent = nullptr;      // nrec records: x = weight, y = column (0-based, -1 pad) bits
+  dccm::DevBuf stage;            // host entry point staging
   cudaStream_t stream = nullptr;
 };
 
@@ -51,60 +61,92 @@ namespace remap {
 constexpr int UNSET = -2147483647;
 
 // ---------------------------------------------------------------- apply
+// Thread = destination row r (lane of its slice) x fields f0 .. f0+FC-1
+// (f0 = FC blockIdx.y).  Field f is read at src + f ld_src and written at
+// (f % nsub) ld_dst + (f / nsub) ld_dst2.  U records a round: their loads,
+// then their U x FC source gathers, are in flight before the in-order sums.
+template <int FC>
 __global__ void __launch_bounds__(256)
-csr_apply(const int64_t *__restrict__ rowptr, const double2 *__restrict__ ent,
-          const double *__restrict__ src, int64_t ld_src, double *__restrict__ dst,
-          int64_t ld_dst, int64_t nrow, int nfields, int nsub, int64_t ld_dst2) {
-  // One thread per (destination row, field), rows fastest: consecutive
-  // threads gather neighbouring source points and store consecutive rows;
-  // the six fields of a row re-read the same records from L1.  Field f is
-  // written at (f % nsub) * ld_dst + (f / nsub) * ld_dst2.
-  // Index arithmetic in 32 bits (the launcher guarantees nrow * nfields <
-  // 2^30, so t + stride cannot overflow): 64-bit division is a long
-  // emulated sequence on this GPU.
-  const int total = (int)(nrow * nfields);
-  const int nr = (int)nrow;
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
-    const int f = t / nr;
-    const int r = t - f * nr;
-    const int64_t b = rowptr[r], e = rowptr[r + 1];
-    const double *s = src + (int64_t)f * ld_src;
-    double acc = 0.0;
-    // four entries per round: their records, then their source values, are
-    // all in flight before the sums, which stay in table order (bit-exact)
-    constexpr int U = 4;
-    for (int64_t k0 = b; k0 < e; k0 += U) {
-      double2 q[U];
-      double x[U];
+sell_apply(const int2 *__restrict__ slices, const double2 *__restrict__ ent, const double *__restrict__ src,
+           int64_t ld_src, double *__restrict__ dst, int64_t ld_dst, int nrow, int nslice, int nfields,
+           int nsub, int64_t ld_dst2) {
+  constexpr int U = FC >= 6 ? 2 : 4;
+  const int lane = threadIdx.x & 31;
+  const int sl_i = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  if (sl_i >= nslice) return;
+  const int f0 = blockIdx.y * FC;
+  const int r = sl_i * 32 + lane;
+  const int2 sl = __ldg(slices + sl_i);
+  const double2 *e = ent + (int64_t)sl.x * 32 + lane;
+  const double *sp[FC];
 #pragma unroll
-      for (int u = 0; u < U; ++u)
-        if (k0 + u < e) q[u] = __ldg(ent + k0 + u);
+  for (int f = 0; f < FC; ++f) sp[f] = src + (int64_t)(f0 + f < nfields ? f0 + f : f0) * ld_src;
+  double acc[FC];
 #pragma unroll
-      for (int u = 0; u < U; ++u)
-        if (k0 + u < e) x[u] = __ldg(s + (int64_t)__double_as_longlong(q[u].y));
+  for (int f = 0; f < FC; ++f) acc[f] = 0.0;
+  for (int k0 = 0; k0 < sl.y; k0 += U) {
+    double2 q[U];
 #pragma unroll
-      for (int u = 0; u < U; ++u)
-        if (k0 + u < e) acc = __dadd_rn(acc, __dmul_rn(x[u], q[u].x));
+    for (int u = 0; u < U; ++u)
+      q[u] = k0 + u < sl.y ? __ldg(e + (int64_t)(k0 + u) * 32) : make_double2(0.0, __longlong_as_double(-1LL));
+    double x[U][FC];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const long long c = __double_as_longlong(q[u].y);
+#pragma unroll
+      for (int f = 0; f < FC; ++f) x[u][f] = (c >= 0 && f0 + f < nfields) ? __ldg(sp[f] + c) : 0.0;
     }
-    const int fs = f / nsub;
-    dst[(int64_t)(f - fs * nsub) * ld_dst + (int64_t)fs * ld_dst2 + r] = acc;
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      if (__double_as_longlong(q[u].y) < 0) continue;
+      if (u == 0 && k0 == 0) {
+        // the row's first entry: 0 + p, which is p except that -0 becomes +0;
+        // done on the integer pipes (the FP64 pipe is this kernel's limit)
+#pragma unroll
+        for (int f = 0; f < FC; ++f) {
+          const double pr = __dmul_rn(x[u][f], q[u].x);
+          acc[f] = (__double_as_longlong(pr) << 1) == 0 ? 0.0 : pr;
+        }
+      } else {
+#pragma unroll
+        for (int f = 0; f < FC; ++f) acc[f] = __dadd_rn(acc[f], __dmul_rn(x[u][f], q[u].x));
+      }
+    }
+  }
+  if (r >= nrow) return;
+#pragma unroll
+  for (int f = 0; f < FC; ++f) {
+    const int fg = f0 + f;
+    if (fg >= nfields) break;
+    const int fs = fg / nsub;
+    dst[(int64_t)(fg - fs * nsub) * ld_dst + (int64_t)fs * ld_dst2 + r] = acc[f];
   }
 }
 
 int apply2(dccm_remap_plan *p, const double *src, int64_t ld_src, double *dst, int64_t ld_dst, int nfields,
            int nsub, int64_t ld_dst2, cudaStream_t s) {
   if (p->n_recv == 0 || nfields == 0) return DCCM_OK;
-  if (p->n_recv * (int64_t)nfields >= (1LL << 30)) return DCCM_ERR_UNSUPPORTED;
+  if (p->n_recv >= (1LL << 31) - 32) return DCCM_ERR_UNSUPPORTED;
   if (nsub <= 0) {
     nsub = nfields;
     ld_dst2 = 0;
   }
-  const int threads = tunables().remap_threads > 0 ? tunables().remap_threads : 256;
-  int64_t blocks = (p->n_recv * nfields + threads - 1) / threads;
-  const int64_t cap = (int64_t)sm_count() * 16;
-  if (blocks > cap) blocks = cap;
-  csr_apply<<<(unsigned)blocks, threads, 0, s>>>(p->d_rowptr, p->d_ent, src, ld_src, dst, ld_dst,
-                                                 p->n_recv, nfields, nsub, ld_dst2);
+  int threads = tunables().remap_threads > 0 ? tunables().remap_threads : 128;
+  threads = threads < 32 ? 32 : (threads > 256 ? 256 : threads / 32 * 32);
+  int fc = tunables().remap_fc > 0 ? tunables().remap_fc : (nfields >= 6 ? 3 : nfields);
+  fc = fc >= 6 ? 6 : (fc >= 4 ? 4 : (fc >= 3 ? 3 : (fc >= 2 ? 2 : 1)));
+  const int64_t blocks = (p->nslice * 32 + threads - 1) / threads;
+  const int64_t ychunks = (nfields + fc - 1) / fc;
+  if (blocks > 0x7FFFFFFF || ychunks > 65535) return DCCM_ERR_UNSUPPORTED;
+  const dim3 grid((unsigned)blocks, (unsigned)ychunks);
+  const int nr = (int)p->n_recv, ns = (int)p->nslice;
+  switch (fc) {
+    case 6: sell_apply<6><<<grid, threads, 0, s>>>(p->d_slices, p->d_ent, src, ld_src, dst, ld_dst, nr, ns, nfields, nsub, ld_dst2); break;
+    case 4: sell_apply<4><<<grid, threads, 0, s>>>(p->d_slices, p->d_ent, src, ld_src, dst, ld_dst, nr, ns, nfields, nsub, ld_dst2); break;
+    case 3: sell_apply<3><<<grid, threads, 0, s>>>(p->d_slices, p->d_ent, src, ld_src, dst, ld_dst, nr, ns, nfields, nsub, ld_dst2); break;
+    case 2: sell_apply<2><<<grid, threads, 0, s>>>(p->d_slices, p->d_ent, src, ld_src, dst, ld_dst, nr, ns, nfields, nsub, ld_dst2); break;
+    default: sell_apply<1><<<grid, threads, 0, s>>>(p->d_slices, p->d_ent, src, ld_src, dst, ld_dst, nr, ns, nfields, nsub, ld_dst2); break;
+  }
   DCCM_LAUNCH_CHECK();
   return DCCM_OK;
 }
@@ -651,31 +693,50 @@ extern "C" int dccm_remap_plan_create(int64_t n_send, int64_t n_recv, int64_t no
     if (send_index[k] < 1 || send_index[k] > n_send || recv_index[k] < 1 ||
         recv_index[k] > n_recv)
       return DCCM_ERR_INDEX_RANGE;
+  if (n_recv >= (1LL << 31) - 32) return DCCM_ERR_UNSUPPORTED;
   // Stable counting sort by destination: per-row order = table order.
   std::vector<int64_t> rowptr(n_recv + 1, 0);
   for (int64_t k = 0; k < nop; ++k) rowptr[recv_index[k]]++;
   for (int64_t r = 0; r < n_recv; ++r) rowptr[r + 1] += rowptr[r];
+  // Sliced ELL: slice of rows 32 q .. 32 q + 31, width = its longest row.
+  const int64_t nslice = (n_recv + 31) / 32;
+  std::vector<int2> slices((size_t)nslice);
+  int64_t nrec = 0;
+  for (int64_t q = 0; q < nslice; ++q) {
+    int64_t wmax = 0;
+    for (int64_t r = q * 32; r < std::min<int64_t>(n_recv, q * 32 + 32); ++r)
+      wmax = std::max<int64_t>(wmax, rowptr[r + 1] - rowptr[r]);
+    if (nrec / 32 > 0x7FFFFFFF || wmax > 0x7FFFFFFF) return DCCM_ERR_UNSUPPORTED;
+    slices[(size_t)q] = make_int2((int)(nrec / 32), (int)wmax);
+    nrec += 32 * wmax;
+  }
+  const long long pad = -1;
+  double padbits;
+  memcpy(&padbits, &pad, sizeof pad);
+  std::vector<double2> ent((size_t)nrec, make_double2(0.0, padbits));
   std::vector<int64_t> fill(rowptr.begin(), rowptr.end() - 1);
-  std::vector<double2> ent(nop);
   for (int64_t k = 0; k < nop; ++k) {
     const int64_t r = recv_index[k] - 1;
     const long long col = (long long)(send_index[k] - 1);
     double colbits;
     memcpy(&colbits, &col, sizeof col);
-    ent[fill[r]++] = make_double2(coef[k], colbits);
+    const int64_t kk = fill[r]++ - rowptr[r];  // position of the entry within its row
+    ent[(size_t)((int64_t)slices[(size_t)(r / 32)].x * 32 + kk * 32 + r % 32)] = make_double2(coef[k], colbits);
   }
   dccm_remap_plan *p = new (std::nothrow) dccm_remap_plan();
   if (!p) return DCCM_ERR_NOMEM;
   p->n_send = n_send;
   p->n_recv = n_recv;
   p->nnz = nop;
-  cudaError_t e = cudaMalloc(&p->d_rowptr, (n_recv + 1) * sizeof(int64_t));
-  if (e == cudaSuccess && nop > 0) e = cudaMalloc(&p->d_ent, nop * sizeof(double2));
-  if (e == cudaSuccess)
-    e = cudaMemcpy(p->d_rowptr, rowptr.data(), (n_recv + 1) * sizeof(int64_t),
-                   cudaMemcpyHostToDevice);
-  if (e == cudaSuccess && nop > 0)
-    e = cudaMemcpy(p->d_ent, ent.data(), nop * sizeof(double2), cudaMemcpyHostToDevice);
+  p->nslice = nslice;
+  p->nrec = nrec;
+  cudaError_t e = cudaSuccess;
+  if (nslice > 0) e = cudaMalloc(&p->d_slices, nslice * sizeof(int2));
+  if (e == cudaSuccess && nrec > 0) e = cudaMalloc(&p->d_ent, nrec * sizeof(double2));
+  if (e == cudaSuccess && nslice > 0)
+    e = cudaMemcpy(p->d_slices, slices.data(), nslice * sizeof(int2), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && nrec > 0)
+    e = cudaMemcpy(p->d_ent, ent.data(), nrec * sizeof(double2), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
     set_cuda_error(e);
     dccm_remap_plan_destroy(p);
@@ -688,7 +749,7 @@ extern "C" int dccm_remap_plan_create(int64_t n_send, int64_t n_recv, int64_t no
 extern "C" int dccm_remap_plan_destroy(dccm_remap_plan *p) {
   DCCM_NVTX_FUNC();
   if (!p) return DCCM_OK;
-  if (p->d_rowptr) cudaFree(p->d_rowptr);
+  if (p->d_slices) cudaFree(p->d_slices);
   if (p->d_ent) cudaFree(p->d_ent);
   p->stage.release();
   if (p->stream) cudaStreamDestroy(p->stream);

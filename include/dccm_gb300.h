@@ -513,9 +513,13 @@ int dccm_step_autotune_host(dccm_step *step, void *stream, const dccm_host_copy 
                             const dccm_host_copy *d2h, int nd2h, int *chosen, float *ms);
 
 /* Autotuner: chooses the launch shapes of the step's kernels by timing
- * candidates of each knob on the stage it affects ("tc_ctas": persistent
- * CTAs of the tensor-core Legendre kernel, "fft_bb": warps per FFT CTA
- * (4, 8 or 16), "flux_threads", "remap_threads": CTA sizes), then "serial"
+ * candidates of each knob on the stage it affects ("tc_shape": 0 lets the
+ * tensor-core Legendre kernel run two CTAs an SM where its tables allow
+ * (N tiles of at most 64 rows, e.g. up to T85 on its Gaussian grid), 1
+ * keeps one CTA an SM with two load stages; "tc_ctas": persistent CTAs of
+ * that kernel, at most one wave, "fft_bb": warps per FFT CTA
+ * (4, 8 or 16), "flux_threads", "remap_threads": CTA sizes, "remap_fc":
+ * fields per thread of the remap, 1, 2, 3, 4 or 6), then "serial"
  * (1: ordinary launches instead of programmatic dependent launches along
  * the transform chain), "tc_ctas" again and "flux_ctas" (CTA cap of the
  * flux kernel's grid, 0: 16 per SM) on replays of the whole step graph,
@@ -526,7 +530,7 @@ int dccm_step_autotune_host(dccm_step *step, void *stream, const dccm_host_copy 
  * from / appended to that file (one JSON object per line, keyed by the
  * GPU name and SM count and the step's shapes).  chosen (4 ints, may be
  * NULL) receives tc_ctas, fft_bb, flux_threads, remap_threads (read
- * "serial" and "flux_ctas" with dccm_tune_get).  The knobs are
+ * "serial", "flux_ctas", "remap_fc" and "tc_shape" with dccm_tune_get).  The knobs are
  * process-wide defaults of later launches too. */
 int dccm_step_autotune(dccm_step *step, const char *cache_path, int *chosen);
 /* Process-wide knobs of later launches (and of graphs recorded later): the

@@ -133,3 +133,40 @@ def test_empty_table_zeroes_recv(dccm):
     out = np.full((7, 3), 4.0, order="F")
     plan.interpolate_data(np.ones((10, 3), order="F"), out, 3)
     assert np.all(out == 0.0)
+
+
+@pytest.mark.parametrize("fc,threads", [(0, 0), (1, 32), (2, 64), (3, 128), (4, 256), (6, 96)])
+def test_sliced_apply_ragged_rows_bit_exact(dccm, oracle, cuda, fc, threads):
+    """Rows of 0 to 40 entries (empty rows and long rows in one 32-row
+    slice), 7 fields (not a multiple of the fields a thread takes), every
+    launch shape: bit-exact against the oracle's COO loop, including the
+    sign of zero (0 + -0 = +0 for a row whose products are all -0)."""
+    torch = cuda
+    rng = np.random.default_rng(11)
+    nS, nD = 5000, 3001
+    counts = rng.integers(0, 6, nD)
+    counts[rng.choice(nD, 40, replace=False)] = rng.integers(20, 41, 40)
+    counts[:64] = 0  # two whole slices of empty rows
+    recv = np.repeat(np.arange(1, nD + 1), counts).astype(np.int32)
+    send = rng.integers(1, nS + 1, recv.size).astype(np.int32)
+    coef = rng.uniform(-1, 1, recv.size)
+    perm = rng.permutation(recv.size)  # table order is not row order
+    recv, send, coef = recv[perm], send[perm], coef[perm]
+    f = rng.standard_normal((nS, 7)) * 10.0
+    f[rng.choice(nS, 500, replace=False), :] = -0.0
+    coef[rng.choice(coef.size, 50, replace=False)] = 0.0
+    plan = dccm.RemapPlan(nS, nD, send, recv, coef)
+    ref = oracle.remap_apply(send, recv, coef, np.asfortranarray(f), nD)
+    saved = {k: dccm.tune_get(k) for k in ("remap_fc", "remap_threads")}
+    try:
+        dccm.tune_set("remap_fc", fc)
+        dccm.tune_set("remap_threads", threads)
+        src = torch.from_numpy(np.ascontiguousarray(f.T)).cuda()
+        dst = torch.full((7, nD), np.nan, dtype=torch.float64, device="cuda")
+        plan.apply_dev(src, nS, dst, nD, 7)
+        torch.cuda.synchronize()
+        got = dst.cpu().numpy().T
+        assert np.array_equal(got.view(np.int64), np.ascontiguousarray(ref).view(np.int64))
+    finally:
+        for k, v in saved.items():
+            dccm.tune_set(k, v)

@@ -203,19 +203,22 @@ def test_autotune_keeps_results_and_caches(dccm, oracle, synth, cuda, tmp_path):
         torch.cuda.synchronize()
         return [o.cpu().clone() for o in outs]
 
-    saved = {k: dccm.tune_get(k) for k in dccm.Step.KNOBS + ["serial", "flux_ctas"]}
+    saved = {k: dccm.tune_get(k) for k in dccm.Step.KNOBS + ["serial", "flux_ctas", "remap_fc", "tc_shape"]}
     try:
         want = run()
         cache = str(tmp_path / "tune.jsonl")
         first = step.autotune(cache)
-        assert set(first) == set(dccm.Step.KNOBS + ["serial", "flux_ctas"]) and first["serial"] in (0, 1)
+        assert set(first) == set(dccm.Step.KNOBS + ["serial", "flux_ctas", "remap_fc", "tc_shape"])
+        assert first["serial"] in (0, 1)
         assert all(torch.equal(a, b) for a, b in zip(run(), want))
         line = open(cache).read()
         assert '"serial": ' in line and '"flux_ctas": ' in line and '"step_ms": ' in line
         assert step.autotune(cache) == first
         # a step recorded in either launch mode, or with the flux grid capped
         # at a few CTAs (each walks many columns), gives the same bits
-        for knob, v in (("serial", 0), ("serial", 1), ("flux_ctas", 3)):
+        for knob, v in (("serial", 0), ("serial", 1), ("flux_ctas", 3), ("remap_fc", 1), ("remap_fc", 6),
+                        ("remap_fc", 4), ("remap_threads", 32), ("tc_shape", 1), ("tc_shape", 0),
+                        ("tc_ctas", 7)):
             dccm.tune_set(knob, v)
             S = bench.gpu_setup(w, inp, dccm, synth, torch, torch.device("cuda", 0))
             step = S["steps"]["mixed"]
