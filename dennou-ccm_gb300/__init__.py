@@ -241,8 +241,9 @@ def fp64_peak(stream=None):
 
 
 def tune_set(knob, value):
-    """dccm_tune_set: process-wide knob (launch shapes tc_ctas, fft_bb,
-    flux_threads, flux_ctas, remap_threads, serial; host copies upload_order,
+    """dccm_tune_set: process-wide knob (launch shapes tc_shape, tc_ctas,
+    fft_bb, flux_threads, flux_ctas, remap_threads, remap_fc,
+    serial; host copies upload_order,
     host_path; failure path wait_limit_ms, tc_withhold_loads); 0 = the
     default."""
     _check(load().dccm_tune_set(knob.encode(), int(value)), "dccm_tune_set")

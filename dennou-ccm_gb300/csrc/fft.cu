@@ -247,82 +247,79 @@ template <int R> __device__ __forceinline__ int slot_of(int m) { return (m % R) 
 
 // ------------------------------------------------------------- inverse
 // One CTA: latitude pair jj, field-levels [by*BB, by*BB + BB); warp bl
-// transforms field-level b0 + bl.  Planes (row, re/im, field-level).
-// Copy F[m][jn|js][2 b0 + c] of the CTA's field-levels into the staging
-// planes (row, re/im, field-level) at slot (m mod R) * 17 + m / R.
+// transforms field-level b0 + bl.  The CTA first assembles the spectrum of
+// every packed row pair z = g(jn) + i g(js) in shared memory, in the order
+// the lanes read it: Zs[bl][k mod R][brev5(k / R)] (float2, field-level
+// stride 32 R + 1 so that the eight field-levels a warp writes at once fall
+// in different banks).  Z_m = A_m + i B_m and Z_{I-m} = conj(A_m) +
+// i conj(B_m) from the Fourier coefficients A (row jn) and B (row js) in
+// F[m][j][c] (imaginary parts of m = 0 taken as 0), zero for N < k < I - N.
+// One thread per (m, field-level), field-levels fastest: a warp's float2
+// loads cover whole 64-byte runs of F per (m, row).  Each lane then reads
+// its R inputs with one conflict-free 64-bit load apiece.
+template <int R> __device__ __forceinline__ constexpr int zs_stride() { return 32 * R + 1; }
+
 template <int R>
-__device__ __forceinline__ void stage_fourier(const FftGroup &G, int jn, int js, int b0, int nb, float *st) {
-  constexpr int PS = R * 17 + 1;
-  const int lbb = G.lbb, lcw = G.lbb + 1;
+__device__ __forceinline__ void stage_z(const FftGroup &G, int jn, int js, int b0, int nb, float2 *zs) {
+  constexpr int I = 32 * R, ZB = zs_stride<R>();
+  const int N = G.N, lbb = G.lbb, bmask = G.BB - 1;
   const long long C2B = 2LL * G.batch;
   const float *F = static_cast<const float *>(G.in);
-  const int tot = (G.N + 1) << (lcw + 1);  // (m, row, c), c fastest
-  // four elements a thread per round: their global loads are all in flight
-  // before the first shared store (eight measured slower at T341)
-  constexpr int U = 4;
+  const int tot = (N + 1) << lbb;  // (m, bl), bl fastest
+  constexpr int U = 2;             // both rows of two units in flight before the stores
+#pragma unroll 1
   for (int t0 = threadIdx.x; t0 < tot; t0 += U * blockDim.x) {
-    float v[U];
+    float2 a[U], b[U];
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       const int t = t0 + u * blockDim.x;
-      const int c = t & ((1 << lcw) - 1);
-      const int row = (t >> lcw) & 1;
-      const int m = t >> (lcw + 1);
-      v[u] = 0.f;
-      if (t < tot && c < 2 * nb) v[u] = F[((long long)m * G.J + (row ? js : jn)) * C2B + 2LL * b0 + c];
+      const int bl = t & bmask, m = t >> lbb;
+      a[u] = b[u] = make_float2(0.f, 0.f);
+      if (t < tot && bl < nb) {
+        const long long c = 2LL * (b0 + bl);
+        a[u] = *reinterpret_cast<const float2 *>(F + ((long long)m * G.J + jn) * C2B + c);
+        b[u] = *reinterpret_cast<const float2 *>(F + ((long long)m * G.J + js) * C2B + c);
+      }
     }
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       const int t = t0 + u * blockDim.x;
-      if (t < tot) {
-        const int c = t & ((1 << lcw) - 1);
-        const int row = (t >> lcw) & 1;
-        const int m = t >> (lcw + 1);
-        st[(((row * 2 + (c & 1)) << lbb) + (c >> 1)) * PS + slot_of<R>(m)] = v[u];
+      if (t >= tot) break;
+      const int bl = t & bmask, m = t >> lbb;
+      float2 *z = zs + bl * ZB;
+      const float ai = m ? a[u].y : 0.f, bi = m ? b[u].y : 0.f;
+      z[(m % R) * 32 + brev5(m / R)] = make_float2(a[u].x - bi, ai + b[u].x);
+      if (m) {
+        const int k = I - m;
+        z[(k % R) * 32 + brev5(k / R)] = make_float2(a[u].x + bi, b[u].x - ai);
       }
     }
   }
-}
-
-// Z_k of the inverse from the staged coefficients of field-level bl: q is k
-// mod R (q = k1 + R0 wq), kl = k / R the lane's bit-reversed index.
-template <int R>
-__device__ __forceinline__ float2 inverse_input(const float *st, int lbb, int bl, int N, int q, int kl) {
-  constexpr int I = 32 * R, PS = R * 17 + 1;
-  const float *Ar = st + ((0 << lbb) + bl) * PS, *Ai = st + ((1 << lbb) + bl) * PS;
-  const float *Br = st + ((2 << lbb) + bl) * PS, *Bi = st + ((3 << lbb) + bl) * PS;
-  const int k = q + R * kl;
-  float2 z = make_float2(0.f, 0.f);
-  if (k <= N) {  // m = k
-    const int sl = q * 17 + kl;
-    const float ar = Ar[sl], br = Br[sl];
-    const float ai = k ? Ai[sl] : 0.f, bi = k ? Bi[sl] : 0.f;
-    z = make_float2(ar - bi, ai + br);
-  } else if (k >= I - N) {  // m = I - k
-    const int sl = q ? (R - q) * 17 + (31 - kl) : 32 - kl;
-    const float ar = Ar[sl], ai = Ai[sl], br = Br[sl], bi = Bi[sl];
-    z = make_float2(ar + bi, br - ai);
+  const int gap = I - 2 * N - 1;  // k = N+1 .. I-N-1
+#pragma unroll 1
+  for (int t = threadIdx.x; t < (gap << lbb); t += blockDim.x) {
+    const int k = N + 1 + (t >> lbb);
+    zs[(t & bmask) * ZB + (k % R) * 32 + brev5(k / R)] = make_float2(0.f, 0.f);
   }
-  return z;
 }
 
 template <int R>
 __device__ __forceinline__ void fft_inv_block(const FftGroup &G, int jj, int by, float *st) {
-  constexpr int I = 32 * R;
-  const int N = G.N, J = G.J, Jh = J / 2, lbb = G.lbb;
+  constexpr int I = 32 * R, ZB = zs_stride<R>();
+  const int J = G.J, Jh = J / 2;
   const int jn = Jh + jj, js = Jh - 1 - jj;
   const int b0 = by * G.BB;
   const int nb = min(G.BB, G.batch - b0);
-  stage_fourier<R>(G, jn, js, b0, nb, st);
+  float2 *zs = reinterpret_cast<float2 *>(st);
+  stage_z<R>(G, jn, js, b0, nb, zs);
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-  const int k2 = brev5(lane);
   float2 w[5];
   lane_twiddles<R>(G.tw, lane, true, w);
   for (int bl = warp; bl < nb; bl += nw) {
     float2 v[R];
 #pragma unroll
-    for (int k1 = 0; k1 < R; ++k1) v[k1] = inverse_input<R>(st, lbb, bl, N, k1, k2);
+    for (int k1 = 0; k1 < R; ++k1) v[k1] = zs[bl * ZB + k1 * 32 + lane];
     warp_fft_inv<R>(v, G.tw, G.twl, w, lane);
     double *gn = static_cast<double *>(G.out) + ((long long)(b0 + bl) * J + jn) * I;
     double *gs = static_cast<double *>(G.out) + ((long long)(b0 + bl) * J + js) * I;
@@ -343,6 +340,61 @@ __device__ __forceinline__ void write_g3(const FftGroup &G, int jj, int b0, int 
   const int N = G.N, Jh = G.J / 2, lcw = G.lbb + 1;
   unsigned short *G3 = static_cast<unsigned short *>(G.out);
   const size_t plane = (size_t)(N + 1) * 2 * Jh * G.C2Bp;
+  if (lcw >= 3) {
+    // Eight consecutive c a thread: one 16-byte store per plane (the run
+    // starts at 2 b0 + 8 q, a multiple of 8 bf16, in a row of C2Bp, a
+    // multiple of 8).  Splits two values at a time (packed conversions
+    // round each half as the scalar ones do).
+    const int lq = lcw - 3;
+    const int tot = (N + 1) << (lq + 1);  // (m, p, q), q fastest
+    for (int t = threadIdx.x; t < tot; t += blockDim.x) {
+      const int q = t & ((1 << lq) - 1);
+      const int p = (t >> lq) & 1;
+      const int m = t >> (lq + 1);
+      const int c0 = 8 * q;
+      if (c0 >= 2 * nb) continue;
+      const float *src = st + ((p << lcw) + c0) * PS + slot_of<R>(m);
+      float v[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) v[i] = src[i * PS];
+      unsigned short *o = G3 + ((size_t)(2 * m + p) * Jh + jj) * G.C2Bp + 2 * b0 + c0;
+      const bool full = c0 + 8 <= 2 * nb;
+      if (G.nsplit == 2) {
+        unsigned h[4], l[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {  // values 2i, 2i+1: field-level b0 + q*4 + i
+          const float sc = 4 * q + i < nb ? pow2f(13 - G.cexp[b0 + 4 * q + i]) : 0.f;  // no scale past the batch
+          split2h_x2(make_float2(v[2 * i] * sc, v[2 * i + 1] * sc), h[i], l[i]);
+        }
+        if (full) {
+          *reinterpret_cast<uint4 *>(o) = make_uint4(h[0], h[1], h[2], h[3]);
+          *reinterpret_cast<uint4 *>(o + plane) = make_uint4(l[0], l[1], l[2], l[3]);
+        } else {
+          for (int i = 0; c0 + i < 2 * nb; ++i) {
+            o[i] = (unsigned short)(h[i >> 1] >> (16 * (i & 1)));
+            o[plane + i] = (unsigned short)(l[i >> 1] >> (16 * (i & 1)));
+          }
+        }
+      } else {
+        unsigned h[4], md[4], l[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) split3f_x2(make_float2(v[2 * i], v[2 * i + 1]), h[i], md[i], l[i]);
+        if (full) {
+          *reinterpret_cast<uint4 *>(o) = make_uint4(h[0], h[1], h[2], h[3]);
+          *reinterpret_cast<uint4 *>(o + plane) = make_uint4(md[0], md[1], md[2], md[3]);
+          *reinterpret_cast<uint4 *>(o + 2 * plane) = make_uint4(l[0], l[1], l[2], l[3]);
+        } else {
+          for (int i = 0; c0 + i < 2 * nb; ++i) {
+            const int sh = 16 * (i & 1);
+            o[i] = (unsigned short)(h[i >> 1] >> sh);
+            o[plane + i] = (unsigned short)(md[i >> 1] >> sh);
+            o[2 * plane + i] = (unsigned short)(l[i >> 1] >> sh);
+          }
+        }
+      }
+    }
+    return;
+  }
   const int tot = (N + 1) << (lcw + 1);  // (m, p, c), c fastest
   for (int t = threadIdx.x; t < tot; t += blockDim.x) {
     const int c = t & ((1 << lcw) - 1);
@@ -439,23 +491,24 @@ constexpr int MW_R0 = 8;
 template <int W>
 __device__ __forceinline__ void fft_inv_block_mw(const FftGroup &G, int jj, int by, float *st) {
   constexpr int R = MW_R0 * W, I = 32 * R, L = 32 * W, PS = R * 17 + 1;
-  const int N = G.N, J = G.J, Jh = J / 2, lbb = G.lbb;
+  constexpr int ZB = zs_stride<R>();
+  const int J = G.J, Jh = J / 2;
   const int jn = Jh + jj, js = Jh - 1 - jj;
   const int b0 = by * G.BB;
   const int nb = min(G.BB, G.batch - b0);
-  stage_fourier<R>(G, jn, js, b0, nb, st);
+  float2 *zs = reinterpret_cast<float2 *>(st);
+  stage_z<R>(G, jn, js, b0, nb, zs);
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int bl = warp / W, wq = warp % W;
-  const bool own = bl < G.BB;  // this warp has staging planes and an exchange slot
-  const int kl = brev5(lane);
-  float2 *xb = reinterpret_cast<float2 *>(st + 4 * G.BB * PS) + (size_t)(own ? bl : 0) * MW_R0 * W * 32;
+  const bool own = bl < G.BB;  // this warp has a staged spectrum and an exchange slot
+  float2 *xb = zs + (size_t)G.BB * ZB + (size_t)(own ? bl : 0) * MW_R0 * W * 32;
   float2 w[5];
   lane_twiddles<R>(G.tw, lane, true, w);
   float2 v[MW_R0];
 #pragma unroll
   for (int k1 = 0; k1 < MW_R0; ++k1)
-    v[k1] = own ? inverse_input<R>(st, lbb, bl, N, k1 + MW_R0 * wq, kl) : make_float2(0.f, 0.f);
+    v[k1] = own ? zs[bl * ZB + (k1 + MW_R0 * wq) * 32 + lane] : make_float2(0.f, 0.f);
   lane_dit<MW_R0>(v, w, lane);
   const float2 tq = twid(G.tw, lane * wq * (I / L), +1);
 #pragma unroll
@@ -586,8 +639,12 @@ __device__ __forceinline__ void dispatch_case(const FftGroup &G, int jj, int by,
   }
 }
 
-// Up to 16 warps (512 threads) per CTA.
-template <int RMAX, bool FWD>
+// Up to 16 warps (512 threads) per CTA.  RFIX > 0: every group of the
+// launch has R = RFIX and only that case is compiled in (one case keeps the
+// register allocation of that case alone; a launch mixing lengths, e.g. an
+// ensemble of truncations, takes the RFIX = 0 kernel with every case up to
+// RMAX).
+template <int RFIX, int RMAX, bool FWD>
 __global__ void __launch_bounds__(512, 2) fft_multi_kernel(const __grid_constant__ FftLaunch L) {
   extern __shared__ __align__(16) float st[];
   pdl_wait();  // reads the previous kernel's output; the forward FFT overwrites the buffer it read
@@ -604,17 +661,21 @@ __global__ void __launch_bounds__(512, 2) fft_multi_kernel(const __grid_constant
   const int nby = (G.batch + G.BB - 1) / G.BB;
   const int Jh = G.J / 2;
   const int by = FWD ? lb % nby : lb / Jh, jj = FWD ? lb / nby : lb % Jh;
-  switch (G.R) {
-    case 2: dispatch_case<2, RMAX, FWD>(G, jj, by, st); break;
-    case 3: dispatch_case<3, RMAX, FWD>(G, jj, by, st); break;
-    case 4: dispatch_case<4, RMAX, FWD>(G, jj, by, st); break;
-    case 6: dispatch_case<6, RMAX, FWD>(G, jj, by, st); break;
-    case 8: dispatch_case<8, RMAX, FWD>(G, jj, by, st); break;
-    case 12: dispatch_case<12, RMAX, FWD>(G, jj, by, st); break;
-    case 16: dispatch_case<16, RMAX, FWD>(G, jj, by, st); break;
-    case 24: dispatch_case<24, RMAX, FWD>(G, jj, by, st); break;
-    case 32: dispatch_case<32, RMAX, FWD>(G, jj, by, st); break;
-    default: break;
+  if constexpr (RFIX > 0) {
+    dispatch_case<RFIX, RMAX, FWD>(G, jj, by, st);
+  } else {
+    switch (G.R) {
+      case 2: dispatch_case<2, RMAX, FWD>(G, jj, by, st); break;
+      case 3: dispatch_case<3, RMAX, FWD>(G, jj, by, st); break;
+      case 4: dispatch_case<4, RMAX, FWD>(G, jj, by, st); break;
+      case 6: dispatch_case<6, RMAX, FWD>(G, jj, by, st); break;
+      case 8: dispatch_case<8, RMAX, FWD>(G, jj, by, st); break;
+      case 12: dispatch_case<12, RMAX, FWD>(G, jj, by, st); break;
+      case 16: dispatch_case<16, RMAX, FWD>(G, jj, by, st); break;
+      case 24: dispatch_case<24, RMAX, FWD>(G, jj, by, st); break;
+      case 32: dispatch_case<32, RMAX, FWD>(G, jj, by, st); break;
+      default: break;
+    }
   }
 }
 
@@ -624,7 +685,9 @@ __global__ void __launch_bounds__(512, 2) fft_multi_kernel(const __grid_constant
 static int fft_warps_per_row(int R) { return R >= 16 ? R / MW_R0 : 1; }
 static size_t fft_smem(int R, int bb) {
   const int W = fft_warps_per_row(R);
-  size_t s = (size_t)4 * bb * (R * 17 + 1) * sizeof(float);
+  const size_t planes = (size_t)4 * bb * (R * 17 + 1) * sizeof(float);  // forward: E/O planes
+  const size_t zs = (size_t)bb * (32 * R + 1) * sizeof(float2);          // inverse: staged spectra
+  size_t s = planes > zs ? planes : zs;
   if (W > 1) s += (size_t)bb * MW_R0 * W * 32 * sizeof(float2);
   return s;
 }
@@ -685,8 +748,20 @@ int fft_multi(Plan *const *plans, const int *batch, const void *const *in, void 
     DCCM_CUDA(launch_pdl(kernel, dim3(nblk), dim3(32 * warps), smem, s, L));
     return DCCM_OK;
   };
-  if (rmax <= 8) return fwd ? go(fft_multi_kernel<8, true>) : go(fft_multi_kernel<8, false>);
-  return fwd ? go(fft_multi_kernel<32, true>) : go(fft_multi_kernel<32, false>);
+  bool one = true;  // every group of the same length
+  for (int g = 1; g < ng; ++g) one = one && L.g[g].R == L.g[0].R;
+  if (one) {
+#define DCCM_FFT_FIX(RR) \
+  case RR: return fwd ? go(fft_multi_kernel<RR, 32, true>) : go(fft_multi_kernel<RR, 32, false>);
+    switch (L.g[0].R) {
+      DCCM_FFT_FIX(2) DCCM_FFT_FIX(3) DCCM_FFT_FIX(4) DCCM_FFT_FIX(6) DCCM_FFT_FIX(8)
+      DCCM_FFT_FIX(12) DCCM_FFT_FIX(16) DCCM_FFT_FIX(24) DCCM_FFT_FIX(32)
+      default: return DCCM_ERR_UNSUPPORTED;
+    }
+#undef DCCM_FFT_FIX
+  }
+  if (rmax <= 8) return fwd ? go(fft_multi_kernel<0, 8, true>) : go(fft_multi_kernel<0, 8, false>);
+  return fwd ? go(fft_multi_kernel<0, 32, true>) : go(fft_multi_kernel<0, 32, false>);
 }
 
 bool fft_length_supported(int I) {

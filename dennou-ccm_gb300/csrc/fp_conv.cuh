@@ -31,20 +31,21 @@ __device__ __forceinline__ double f32_to_f64(float f) {
 __device__ __forceinline__ float f64_to_f32_rn(double d) {
   const unsigned hi = (unsigned)__double2hiint(d);
   const unsigned lo = (unsigned)__double2loint(d);
-  const unsigned sign = hi & 0x80000000u;
-  const int e = (int)((hi >> 20) & 0x7FFu);
-  const int e32 = e - 1023 + 127;
-  if (e32 <= 0 || e32 >= 255) {
-    if ((hi & 0x7FFFFFFFu) == 0u && lo == 0u) return __uint_as_float(sign);
+  // biased exponent e in [897, 1150]: the result is a normal FP32 number
+  // (or rounds up to infinity at the top, as IEEE rounding does)
+  if ((hi & 0x7FF00000u) - 0x38100000u >= 0x0FE00000u) {
+    if ((hi & 0x7FFFFFFFu) == 0u && lo == 0u) return __uint_as_float(hi & 0x80000000u);
     return __double2float_rn(d);  // FP32 subnormal, overflow, inf, nan
   }
-  const unsigned m = ((hi & 0xFFFFFu) << 3) | (lo >> 29);
-  const unsigned rem = lo & 0x1FFFFFFFu;
-  unsigned r = sign | ((unsigned)e32 << 23) | m;
-  // round to nearest, ties to even; a carry out of the mantissa correctly
-  // increments the exponent (and reaches infinity at the top of the range)
-  if (rem > 0x10000000u || (rem == 0x10000000u && (m & 1u))) r += 1u;
-  return __uint_as_float(r);
+  // (hi:lo) << 3 keeps e's low 9 bits above the top 23 mantissa bits;
+  // subtracting 384 << 23 turns them into e - 896 (mod 512, which fits 8 bits)
+  unsigned r = __funnelshift_l(lo, hi, 3) - 0xC0000000u;
+  // round to nearest, ties to even, on the 29 dropped bits: the carry out of
+  // dropped + (2^28 - 1) + lsb is 1 exactly when they exceed half, or equal
+  // half with an odd lsb; a carry out of the mantissa correctly increments
+  // the exponent
+  const unsigned up = ((lo & 0x1FFFFFFFu) + 0x0FFFFFFFu + (r & 1u)) >> 29;
+  return __uint_as_float((r | (hi & 0x80000000u)) + up);
 }
 
 // Exact split of an FP32 value into three BF16 numbers x = hi + mid + lo
@@ -60,6 +61,21 @@ __device__ __forceinline__ void split3f_bits(float x, unsigned short &h, unsigne
   l = __bfloat16_as_ushort(bl);
 }
 
+// The same split for two values at once with the packed conversions (each
+// half rounded as __float2bfloat16_rn rounds it, so the bits equal two
+// split3f_bits calls); .x in the low 16 bits of each word.
+__device__ __forceinline__ void split3f_x2(float2 x, unsigned &h, unsigned &m, unsigned &l) {
+  const __nv_bfloat162 bh = __float22bfloat162_rn(x);
+  const float2 fh = __bfloat1622float2(bh);
+  const float2 r1 = make_float2(x.x - fh.x, x.y - fh.y);
+  const __nv_bfloat162 bm = __float22bfloat162_rn(r1);
+  const float2 fm = __bfloat1622float2(bm);
+  const __nv_bfloat162 bl = __float22bfloat162_rn(make_float2(r1.x - fm.x, r1.y - fm.y));
+  h = *reinterpret_cast<const unsigned *>(&bh);
+  m = *reinterpret_cast<const unsigned *>(&bm);
+  l = *reinterpret_cast<const unsigned *>(&bl);
+}
+
 // Split of an FP32 value into two FP16 numbers x ~ hi + lo (22 significant
 // bits; the caller scales x by a power of two into FP16's range first),
 // returned as raw bits.  The residual x - hi is exact in FP32.
@@ -68,6 +84,15 @@ __device__ __forceinline__ void split2h_bits(float x, unsigned short &h, unsigne
   const __half hl = __float2half_rn(x - __half2float(hh));
   h = __half_as_ushort(hh);
   l = __half_as_ushort(hl);
+}
+
+// Two values at once (packed conversions; the same bits as split2h_bits).
+__device__ __forceinline__ void split2h_x2(float2 x, unsigned &h, unsigned &l) {
+  const __half2 hh = __float22half2_rn(x);
+  const float2 fh = __half22float2(hh);
+  const __half2 hl = __float22half2_rn(make_float2(x.x - fh.x, x.y - fh.y));
+  h = *reinterpret_cast<const unsigned *>(&hh);
+  l = *reinterpret_cast<const unsigned *>(&hl);
 }
 
 // 2^k as an FP32 number, for exponents of normal numbers (-126 <= k <= 127;

@@ -496,81 +496,81 @@ legendre_tc_kernel(const __grid_constant__ TcLaunch L) {
 }
 
 // ------------------------------------------------------------ spectra pack
-// Apack[s][2b + comp][xpos[i]] = split s of the FP32 rounding of spectral
-// coefficient i of field b (one thread per coefficient and field; the
-// (m, p) segment padding stays zero from plan creation).
+// Apack[s][2b + comp][x] = split s of the FP32 rounding of the spectral
+// coefficient of field-level b at column x of its (m, p) segment.  A unit
+// is 16 consecutive coefficients n = n0 .. n0 + 15 (n0 = m + 16 q) of one m,
+// i.e. columns 8q .. 8q + 7 of both parities' segments; one thread per
+// (field-level, unit, parity).  A unit's two threads read the interleaved
+// halves of one contiguous 256-byte run of the spectra (a warp's units are
+// neighbouring runs); each of a thread's stores is one 16-byte run of a
+// segment.  A segment of c coefficients is 16 ceil(c /
+// 16) columns long; a run is written only if it starts below c (then it
+// ends inside the segment; its entries past N are written as 0), and the
+// columns no run reaches stay zero from plan creation.
 struct PackGroup {
   const double2 *spec;
-  const int *xpos;
+  const int4 *units;  // (m, q, x of parity 0, x of parity 1)
   unsigned short *A;
   long long ncoef, KX;
-  long long blk0;  // first block of this group; bx blocks per field-level
-  int C2Bp, bx;
-  int nsplit;        // 3: BF16 x 3; 2: FP16 hi + lo scaled by 2^(14 - cexp[b])
-  const int *cexp;   // FP16: exponent of the field-level's largest |coefficient|
+  long long t0;       // first thread of this group; nunits threads per field-level
+  int nunits, N, C2Bp, batch;
+  int nsplit;         // 3: BF16 x 3; 2: FP16 hi + lo scaled by 2^(14 - cexp[b])
+  const int *cexp;    // FP16: exponent of the field-level's largest |coefficient|
 };
 struct PackLaunch {
   PackGroup g[MAXG];
   int ngroups;
+  long long total;
 };
 
-__global__ void __launch_bounds__(256) pack_spectra_kernel(const __grid_constant__ PackLaunch L) {
+__global__ void __launch_bounds__(128) pack_spectra_kernel(const __grid_constant__ PackLaunch L) {
   pdl_wait();  // Apack is read by the previous step's synthesis
   pdl_trigger();
-  // Block -> (group, field-level b, chunk cx): each group has its own number
-  // of chunks per field-level (a group of short spectra launches no empty
-  // blocks for the longest group's coefficient range).
-  const long long blk = blockIdx.x;
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= L.total) return;
   int gi = 0;
-  while (gi + 1 < L.ngroups && blk >= L.g[gi + 1].blk0) ++gi;
+  while (gi + 1 < L.ngroups && t >= L.g[gi + 1].t0) ++gi;
   const PackGroup &G = L.g[gi];
-  const int b = (int)((blk - G.blk0) / G.bx);
-  const int cx = (int)((blk - G.blk0) % G.bx);
+  // thread = (field-level, unit, parity), parity fastest: the two threads of
+  // a unit read the interleaved halves of one 256-byte run
+  const long long u2 = t - G.t0;
+  const int b = (int)(u2 / (2 * G.nunits));
+  const int r = (int)(u2 - (long long)b * 2 * G.nunits);
+  const int p = r & 1;
+  const int4 w = __ldg(G.units + (r >> 1));
+  const int m = w.x, n0 = m + 16 * w.y;
+  // columns 8q .. 8q+7 of this parity hold at least one coefficient, else
+  // the run lies past the segment (whose rounded length covers every run
+  // that starts inside it) and is not written
+  if (8 * w.y >= count_np(G.N, m, p)) return;
+  const double2 *src = G.spec + (size_t)b * G.ncoef + idx_mn(G.N, m, n0) + p;
+  double2 v[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) v[j] = n0 + p + 2 * j <= G.N ? __ldg(src + 2 * j) : make_double2(0.0, 0.0);
   const size_t plane = (size_t)G.C2Bp * G.KX;
-  const double2 *src = G.spec + (size_t)b * G.ncoef;
-  unsigned short *dst = G.A + (size_t)(2 * b) * G.KX;
-  if (G.nsplit == 2) {
-    const int sc = 14 - G.cexp[b];
-    for (long long i = cx * (long long)blockDim.x + threadIdx.x; i < G.ncoef; i += (long long)G.bx * blockDim.x) {
-      const double2 v = __ldg(src + i);
-      const int x = __ldg(G.xpos + i);
-      unsigned short h0, l0, h1, l1;
-      split2h_bits(f64_to_f32_rn(scale_pow2(v.x, sc)), h0, l0);
-      split2h_bits(f64_to_f32_rn(scale_pow2(v.y, sc)), h1, l1);
-      unsigned short *o = dst + x;
-      o[0] = h0;
-      o[G.KX] = h1;
-      o[plane] = l0;
-      o[plane + G.KX] = l1;
-    }
-    return;
-  }
-  // two coefficients a thread per round, both loads in flight together
-  const long long stride = (long long)G.bx * blockDim.x;
-  for (long long i0 = cx * (long long)blockDim.x + threadIdx.x; i0 < G.ncoef; i0 += 2 * stride) {
-    double2 v[2];
-    int x[2];
+  const int sc = G.nsplit == 2 ? 14 - G.cexp[b] : 0;
 #pragma unroll
-    for (int u = 0; u < 2; ++u) {
-      const long long i = i0 + u * stride;
-      if (i < G.ncoef) {
-        v[u] = __ldg(src + i);
-        x[u] = __ldg(G.xpos + i);
-      }
-    }
+  for (int comp = 0; comp < 2; ++comp) {
+    unsigned short *o = G.A + (size_t)(2 * b + comp) * G.KX + (p ? w.w : w.z);
+    float f[8];
 #pragma unroll
-    for (int u = 0; u < 2; ++u) {
-      if (i0 + u * stride >= G.ncoef) break;
-      unsigned short h0, m0, l0, h1, m1, l1;
-      split3f_bits(f64_to_f32_rn(v[u].x), h0, m0, l0);
-      split3f_bits(f64_to_f32_rn(v[u].y), h1, m1, l1);
-      unsigned short *o = dst + x[u];
-      o[0] = h0;
-      o[G.KX] = h1;
-      o[plane] = m0;
-      o[plane + G.KX] = m1;
-      o[2 * plane] = l0;
-      o[2 * plane + G.KX] = l1;
+    for (int j = 0; j < 8; ++j) {
+      const double x = comp ? v[j].y : v[j].x;
+      f[j] = f64_to_f32_rn(G.nsplit == 2 ? scale_pow2(x, sc) : x);
+    }
+    if (G.nsplit == 2) {
+      unsigned h[4], l[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) split2h_x2(make_float2(f[2 * i], f[2 * i + 1]), h[i], l[i]);
+      *reinterpret_cast<uint4 *>(o) = make_uint4(h[0], h[1], h[2], h[3]);
+      *reinterpret_cast<uint4 *>(o + plane) = make_uint4(l[0], l[1], l[2], l[3]);
+    } else {
+      unsigned h[4], md[4], l[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) split3f_x2(make_float2(f[2 * i], f[2 * i + 1]), h[i], md[i], l[i]);
+      *reinterpret_cast<uint4 *>(o) = make_uint4(h[0], h[1], h[2], h[3]);
+      *reinterpret_cast<uint4 *>(o + plane) = make_uint4(md[0], md[1], md[2], md[3]);
+      *reinterpret_cast<uint4 *>(o + 2 * plane) = make_uint4(l[0], l[1], l[2], l[3]);
     }
   }
 }
@@ -610,31 +610,33 @@ int pack_spectra(Plan *const *plans, const int *batch, const double *const *spec
   PackLaunch L;
   memset(&L, 0, sizeof L);
   int ng = 0;
-  long long nblk = 0;
+  long long total = 0;
   for (int g = 0; g < ngroups; ++g) {
     if (batch[g] <= 0) continue;
     const Plan &P = *plans[g];
-    if (!P.d_apack) return DCCM_ERR_UNSUPPORTED;
+    if (!P.d_apack || !P.d_punits) return DCCM_ERR_UNSUPPORTED;
     PackGroup &G = L.g[ng++];
     G.spec = reinterpret_cast<const double2 *>(spec[g]);
-    G.xpos = P.d_xpos;
+    G.units = P.d_punits;
     G.A = P.d_apack;
     G.ncoef = P.ncoef;
     G.KX = P.KX;
+    G.N = P.N;
     G.C2Bp = P.C2Bp;
+    G.batch = batch[g];
+    G.nunits = P.npunits;
     G.nsplit = P.nsplit;
     G.cexp = P.d_cexp;
-    // two coefficients a thread: ncoef / 512 blocks a field-level, at most 64
-    long long bx = (P.ncoef + 511) / 512;
-    G.bx = (int)(bx < 1 ? 1 : (bx > 64 ? 64 : bx));
-    G.blk0 = nblk;
-    nblk += (long long)G.bx * batch[g];
+    G.t0 = total;
+    total += 2LL * P.npunits * batch[g];  // a thread per (field-level, unit, parity)
     if (P.nsplit == 2) DCCM_TRY(field_exponents(spec[g], 2 * P.ncoef, batch[g], P.d_cexp, s));
   }
   L.ngroups = ng;
-  if (nblk == 0) return DCCM_OK;
+  L.total = total;
+  if (total == 0) return DCCM_OK;
+  const long long nblk = (total + 127) / 128;  // 128-thread blocks: a c3 batch (35 k units) spans every SM
   if (nblk > 0x7FFFFFFFLL) return DCCM_ERR_UNSUPPORTED;
-  DCCM_CUDA(launch_pdl(pack_spectra_kernel, dim3((unsigned)nblk), dim3(256), 0, s, L));
+  DCCM_CUDA(launch_pdl(pack_spectra_kernel, dim3((unsigned)nblk), dim3(128), 0, s, L));
   return DCCM_OK;
 }
 
@@ -877,14 +879,16 @@ static int build_pack(Plan &P) {
     }
   P.KX = x;
   if (P.KX >= (1LL << 31)) return DCCM_ERR_UNSUPPORTED;
-  std::vector<int> xpos((size_t)P.ncoef);
+  // pack units (m, q): coefficients n = m + 16 q .. + 15, columns 8 q .. 8 q + 7
+  // of both parity segments (the kernel skips a parity's run that starts at
+  // or past that parity's coefficient count)
+  std::vector<int4> units;
   for (int m = 0; m <= P.N; ++m)
-    for (int n = m; n <= P.N; ++n) {
-      const int p = (n - m) & 1;
-      xpos[(size_t)idx_mn(P.N, m, n)] = P.xoff[2 * m + p] + (n - m - p) / 2;
-    }
-  DCCM_CUDA(cudaMalloc(&P.d_xpos, xpos.size() * sizeof(int)));
-  DCCM_CUDA(cudaMemcpy(P.d_xpos, xpos.data(), xpos.size() * sizeof(int), cudaMemcpyHostToDevice));
+    for (int q = 0; m + 16 * q <= P.N; ++q)
+      units.push_back(make_int4(m, q, P.xoff[2 * m] + 8 * q, P.xoff[2 * m + 1] + 8 * q));
+  P.npunits = (int)units.size();
+  DCCM_CUDA(cudaMalloc(&P.d_punits, units.size() * sizeof(int4)));
+  DCCM_CUDA(cudaMemcpy(P.d_punits, units.data(), units.size() * sizeof(int4), cudaMemcpyHostToDevice));
   const size_t bytes = (size_t)P.nsplit * P.C2Bp * P.KX * sizeof(uint16_t);
   DCCM_CUDA(cudaMalloc(&P.d_apack, bytes));
   DCCM_CUDA(cudaMemset(P.d_apack, 0, bytes));

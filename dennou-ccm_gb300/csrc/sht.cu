@@ -94,7 +94,7 @@ __global__ void pnm_kernel(int N, int Jh, const double *__restrict__ mu, double 
 static void destroy(Plan &P) {
   void *ptrs[] = {P.d_mu,      P.d_w,        P.d_pnm,       P.d_tw64,  P.d_tw32,  P.d_twl32,
                   P.tinv.d,    P.tfwd.d,     P.tinv.d_mi,   P.tfwd.d_mi, P.tinv.d_items,
-                  P.tfwd.d_items, P.d_work,  P.d_err,       P.d_apack, P.d_xpos,   P.d_cexp,
+                  P.tfwd.d_items, P.d_work,  P.d_err,       P.d_apack, P.d_punits, P.d_cexp,
                   P.d_wa_pos, P.d_wa_src};
   for (void *p : ptrs)
     if (p) cudaFree(p);

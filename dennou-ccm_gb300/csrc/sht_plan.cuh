@@ -71,7 +71,8 @@ struct Plan {
   int64_t KX = 0;              // row length of Apack
   std::vector<int> xoff;       // Apack segment offset of (m, p) at [2m + p]
   uint16_t *d_apack = nullptr; // Apack[3][C2Bp][KX] (bf16 bits)
-  int *d_xpos = nullptr;       // Apack column x of each spectral coefficient
+  int4 *d_punits = nullptr;    // pack units (m, q, x of parity 0, x of parity 1): 16 coefficients each
+  int npunits = 0;
   int *d_err = nullptr;        // device error flag of bounded waits
   int nsplit = 3;              // tensor-path operand splits: 3 (BF16 x 3) or 2 (FP16 hi + lo)
   int *d_cexp = nullptr;       // FP16: per field-level scale exponents, [inverse | forward][max_batch]

@@ -505,8 +505,11 @@ int dccm_step_host_release(dccm_step *step);
  * the first downloads, so the fastest flux can win) and leaves the graph
  * recorded.  chosen (3 ints, may be NULL) receives the order, host_path and
  * the flux CTA cap of this graph (0: the full grid); all 0 with pageable
- * buffers, for which there is nothing to choose.  ms (32 floats, may be NULL)
- * receives each combination's device time per step at index 16 (order - 1) +
+ * buffers, for which there is nothing to choose.  Each candidate is timed
+ * as the caller sees it: host clock from the graph launch to the end of the
+ * stream synchronisation (kernels writing host memory through the mapping
+ * can finish before their writes land).  ms (32 floats, may be NULL)
+ * receives each combination's time per step at index 16 (order - 1) +
  * mask.  The process-wide knobs "upload_order", "host_path" and "flux_ctas"
  * (dccm_tune_set) apply to steps that have not been tuned this way. */
 int dccm_step_autotune_host(dccm_step *step, void *stream, const dccm_host_copy *h2d, int nh2d,
