@@ -442,12 +442,14 @@ def host_copies(S, groups, dccm, torch):
 # algorithmic bytes; the L2 bytes of the same launches (lts__t_bytes.sum,
 # every request L2 serves) are reported beside them.
 TRAFFIC = {
-    "c3": {"legendre_inverse": int((7.686912 + 12.131584) * 1e6 + 1280), "fft_inverse": int(11.341056e6 + 512),
-           "fft_forward": int(33.623296e6 + 56064), "legendre_forward": int(18.93888e6),
-           "remap": int(4.062976e6), "bulk_flux": int(7.707392e6 + 768)},
+    "c3": {"legendre_inverse": 7683584 + 12131328, "fft_inverse": 11305216, "fft_forward": 33598720 + 38144,
+           "legendre_forward": 18939136, "remap": 4120832, "bulk_flux": 7708160 + 512},
 }
-L2_BYTES = {}
-TRAFFIC_SOURCE = "ncu of bench.py --workload c3 --profile-steps 3 (profiles/stages_c3_ncu.md)"
+L2_BYTES = {
+    "c3": {"legendre_inverse": 30839968 + 50586784, "fft_inverse": 83083680, "fft_forward": 105767840,
+           "legendre_forward": 43723264, "remap": 16528832, "bulk_flux": 40442240},
+}
+TRAFFIC_SOURCE = "ncu of bench.py --workload c3 --profile-steps 3, third replay (profiles/step_c3_launches.md)"
 # FP64 peak: measured on the device by dccm_fp64_peak (independent DFMA
 # chains on every SM) at the start of the run; the nominal figure (2 DFMA
 # lanes per SM and clock at the maximum SM clock) is reported beside it.

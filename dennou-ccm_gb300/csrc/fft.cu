@@ -179,7 +179,7 @@ __device__ __forceinline__ void lane_dif(float2 (&v)[NV], const float2 (&w)[5], 
       // lower: a + b; upper: (a - b) w  (the lower lane holds a)
       const float2 p = shfl_xor_c(v[k], h);
       const float2 t = make_float2(fmaf(sg, v[k].x, p.x), fmaf(sg, v[k].y, p.y));
-      v[k] = cmul(t, w[s]);
+      v[k] = s == 4 ? t : cmul(t, w[s]);  // the last stage's twiddles are all 1
     }
   }
 }
@@ -194,7 +194,7 @@ __device__ __forceinline__ void lane_dit(float2 (&v)[NV], const float2 (&w)[5], 
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
       // lower: a + w b; upper: a - w b  (the upper lane holds b)
-      const float2 x = cmul(v[k], w[s]);
+      const float2 x = s == 0 ? v[k] : cmul(v[k], w[s]);  // the first stage's twiddles are all 1
       const float2 p = shfl_xor_c(x, h);
       v[k] = make_float2(fmaf(sg, x.x, p.x), fmaf(sg, x.y, p.y));
     }
@@ -249,15 +249,18 @@ template <int R> __device__ __forceinline__ int slot_of(int m) { return (m % R) 
 // One CTA: latitude pair jj, field-levels [by*BB, by*BB + BB); warp bl
 // transforms field-level b0 + bl.  The CTA first assembles the spectrum of
 // every packed row pair z = g(jn) + i g(js) in shared memory, in the order
-// the lanes read it: Zs[bl][k mod R][brev5(k / R)] (float2, field-level
-// stride 32 R + 1 so that the eight field-levels a warp writes at once fall
-// in different banks).  Z_m = A_m + i B_m and Z_{I-m} = conj(A_m) +
+// the lanes read it: Zs[bl][k mod R][brev5(k / R)] (float2, rows of 33,
+// field-level stride 33 R + 1, so that the field-levels and the consecutive
+// m that a warp writes at once fall in different banks).  Z_m = A_m + i B_m and Z_{I-m} = conj(A_m) +
 // i conj(B_m) from the Fourier coefficients A (row jn) and B (row js) in
 // F[m][j][c] (imaginary parts of m = 0 taken as 0), zero for N < k < I - N.
 // One thread per (m, field-level), field-levels fastest: a warp's float2
 // loads cover whole 64-byte runs of F per (m, row).  Each lane then reads
 // its R inputs with one conflict-free 64-bit load apiece.
-template <int R> __device__ __forceinline__ constexpr int zs_stride() { return 32 * R + 1; }
+// Residue rows of 33 float2 (32 lanes and one pad): consecutive m, which a
+// warp's staging threads write at once, fall in different banks.
+constexpr int ZQ = 33;
+template <int R> __device__ __forceinline__ constexpr int zs_stride() { return ZQ * R + 1; }
 
 template <int R>
 __device__ __forceinline__ void stage_z(const FftGroup &G, int jn, int js, int b0, int nb, float2 *zs) {
@@ -288,10 +291,10 @@ __device__ __forceinline__ void stage_z(const FftGroup &G, int jn, int js, int b
       const int bl = t & bmask, m = t >> lbb;
       float2 *z = zs + bl * ZB;
       const float ai = m ? a[u].y : 0.f, bi = m ? b[u].y : 0.f;
-      z[(m % R) * 32 + brev5(m / R)] = make_float2(a[u].x - bi, ai + b[u].x);
+      z[(m % R) * ZQ + brev5(m / R)] = make_float2(a[u].x - bi, ai + b[u].x);
       if (m) {
         const int k = I - m;
-        z[(k % R) * 32 + brev5(k / R)] = make_float2(a[u].x + bi, b[u].x - ai);
+        z[(k % R) * ZQ + brev5(k / R)] = make_float2(a[u].x + bi, b[u].x - ai);
       }
     }
   }
@@ -299,7 +302,7 @@ __device__ __forceinline__ void stage_z(const FftGroup &G, int jn, int js, int b
 #pragma unroll 1
   for (int t = threadIdx.x; t < (gap << lbb); t += blockDim.x) {
     const int k = N + 1 + (t >> lbb);
-    zs[(t & bmask) * ZB + (k % R) * 32 + brev5(k / R)] = make_float2(0.f, 0.f);
+    zs[(t & bmask) * ZB + (k % R) * ZQ + brev5(k / R)] = make_float2(0.f, 0.f);
   }
 }
 
@@ -319,7 +322,7 @@ __device__ __forceinline__ void fft_inv_block(const FftGroup &G, int jj, int by,
   for (int bl = warp; bl < nb; bl += nw) {
     float2 v[R];
 #pragma unroll
-    for (int k1 = 0; k1 < R; ++k1) v[k1] = zs[bl * ZB + k1 * 32 + lane];
+    for (int k1 = 0; k1 < R; ++k1) v[k1] = zs[bl * ZB + k1 * ZQ + lane];
     warp_fft_inv<R>(v, G.tw, G.twl, w, lane);
     double *gn = static_cast<double *>(G.out) + ((long long)(b0 + bl) * J + jn) * I;
     double *gs = static_cast<double *>(G.out) + ((long long)(b0 + bl) * J + js) * I;
@@ -508,7 +511,7 @@ __device__ __forceinline__ void fft_inv_block_mw(const FftGroup &G, int jj, int 
   float2 v[MW_R0];
 #pragma unroll
   for (int k1 = 0; k1 < MW_R0; ++k1)
-    v[k1] = own ? zs[bl * ZB + (k1 + MW_R0 * wq) * 32 + lane] : make_float2(0.f, 0.f);
+    v[k1] = own ? zs[bl * ZB + (k1 + MW_R0 * wq) * ZQ + lane] : make_float2(0.f, 0.f);
   lane_dit<MW_R0>(v, w, lane);
   const float2 tq = twid(G.tw, lane * wq * (I / L), +1);
 #pragma unroll
@@ -686,7 +689,7 @@ static int fft_warps_per_row(int R) { return R >= 16 ? R / MW_R0 : 1; }
 static size_t fft_smem(int R, int bb) {
   const int W = fft_warps_per_row(R);
   const size_t planes = (size_t)4 * bb * (R * 17 + 1) * sizeof(float);  // forward: E/O planes
-  const size_t zs = (size_t)bb * (32 * R + 1) * sizeof(float2);          // inverse: staged spectra
+  const size_t zs = (size_t)bb * (33 * R + 1) * sizeof(float2);          // inverse: staged spectra
   size_t s = planes > zs ? planes : zs;
   if (W > 1) s += (size_t)bb * MW_R0 * W * 32 * sizeof(float2);
   return s;

@@ -7,7 +7,8 @@
 // instead (integer ALU and moves only).  Both are exact restatements of
 // the IEEE rules: widening is exact; narrowing rounds to nearest, ties to
 // even.  Operands outside the normal FP32 range (zero excepted), infinities
-// and NaNs take the hardware instruction.
+// and NaNs take the hardware instruction (the narrowing's in a call of its
+// own).
 #pragma once
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
@@ -28,24 +29,30 @@ __device__ __forceinline__ double f32_to_f64(float f) {
   return __hiloint2double((int)hi, (int)lo);
 }
 
+// Operands outside FP32's normal range other than zero (subnormal results,
+// overflow, inf, nan): the hardware instruction, in a call of its own so that
+// the common path keeps a branch around it instead of issuing it predicated
+// (it runs on the FP64 pipe).
+static __device__ __noinline__ float f64_to_f32_special(double d) { return __double2float_rn(d); }
+
 __device__ __forceinline__ float f64_to_f32_rn(double d) {
   const unsigned hi = (unsigned)__double2hiint(d);
   const unsigned lo = (unsigned)__double2loint(d);
   // biased exponent e in [897, 1150]: the result is a normal FP32 number
   // (or rounds up to infinity at the top, as IEEE rounding does)
-  if ((hi & 0x7FF00000u) - 0x38100000u >= 0x0FE00000u) {
-    if ((hi & 0x7FFFFFFFu) == 0u && lo == 0u) return __uint_as_float(hi & 0x80000000u);
-    return __double2float_rn(d);  // FP32 subnormal, overflow, inf, nan
-  }
+  const bool normal = (hi & 0x7FF00000u) - 0x38100000u < 0x0FE00000u;
+  const bool zero = ((hi << 1) | lo) == 0u;
+  if (!normal && !zero) return f64_to_f32_special(d);
   // (hi:lo) << 3 keeps e's low 9 bits above the top 23 mantissa bits;
   // subtracting 384 << 23 turns them into e - 896 (mod 512, which fits 8 bits)
-  unsigned r = __funnelshift_l(lo, hi, 3) - 0xC0000000u;
+  const unsigned r = __funnelshift_l(lo, hi, 3) - 0xC0000000u;
   // round to nearest, ties to even, on the 29 dropped bits: the carry out of
   // dropped + (2^28 - 1) + lsb is 1 exactly when they exceed half, or equal
   // half with an odd lsb; a carry out of the mantissa correctly increments
   // the exponent
   const unsigned up = ((lo & 0x1FFFFFFFu) + 0x0FFFFFFFu + (r & 1u)) >> 29;
-  return __uint_as_float((r | (hi & 0x80000000u)) + up);
+  const unsigned sign = hi & 0x80000000u;
+  return __uint_as_float(zero ? sign : (r | sign) + up);
 }
 
 // Exact split of an FP32 value into three BF16 numbers x = hi + mid + lo

@@ -45,3 +45,4 @@ def test_range_test_sends_specials_to_the_hardware_path():
     vals = np.array([0.0, -0.0, 1e-40, 2.0 ** -127, 2.0 ** 128, np.inf, -np.inf, np.nan, 2.0 ** -126, 3.0e38])
     _, normal = narrow_bits(vals)
     assert list(normal) == [False, False, False, False, False, False, False, False, True, True]
+
