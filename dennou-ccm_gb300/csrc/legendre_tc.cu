@@ -40,7 +40,11 @@
 namespace dccm {
 namespace sht {
 
-constexpr int TC_THREADS = 192;
+// Threads of a CTA: warp 0 (TMA), warp 1 (TMEM, MMA) and the epilogue
+// warps, 4 (narrow shape) or 8 (wide shape: two warps per TMEM lane quarter
+// share each item's epilogue).
+template <bool NARROW> constexpr int tc_epi_warps() { return NARROW ? 4 : 8; }
+template <bool NARROW> constexpr int tc_threads() { return 64 + 32 * tc_epi_warps<NARROW>(); }
 constexpr int A_SPLIT_BYTES = 128 * 128;     // 128 rows (c) x 64 bf16 (K)
 // Two shapes of the same kernel:
 //   wide   (any table): two 96 KB stages (B boxes of up to 128 N rows), all
@@ -177,7 +181,15 @@ __device__ __forceinline__ void tmem_ld16_nw(uint32_t taddr, uint32_t (&r)[16]) 
 }
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 // Named barrier of the four epilogue warps (threads 64..191).
-__device__ __forceinline__ void epi_sync() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
+template <int NTHREADS> __device__ __forceinline__ void epi_sync() {
+  asm volatile("bar.sync 1, %0;" ::"n"(NTHREADS) : "memory");
+}
+// 8 consecutive TMEM columns of this thread's lane, without waiting.
+__device__ __forceinline__ void tmem_ld8_nw(uint32_t taddr, uint32_t (&r)[8]) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+}
 
 // FP64 split used once per table entry at plan creation.
 __device__ __forceinline__ void split3(double x, __nv_bfloat16 &h, __nv_bfloat16 &m, __nv_bfloat16 &l) {
@@ -228,7 +240,7 @@ __device__ __forceinline__ int group_of(const TcLaunch &L, int it) {
 }
 
 template <bool NARROW>
-__global__ void __launch_bounds__(TC_THREADS, TcShape<NARROW>::MIN_CTAS)
+__global__ void __launch_bounds__(tc_threads<NARROW>(), TcShape<NARROW>::MIN_CTAS)
 legendre_tc_kernel(const __grid_constant__ TcLaunch L) {
   using Sh = TcShape<NARROW>;
   constexpr int NSTAGE = Sh::NSTAGE, STAGE_BYTES = Sh::STAGE_BYTES, B_SPLIT_BYTES = Sh::B_SPLIT_BYTES;
@@ -249,7 +261,7 @@ legendre_tc_kernel(const __grid_constant__ TcLaunch L) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
       mbar_init(&accf[s], 1);
-      mbar_init(&acce[s], 128);
+      mbar_init(&acce[s], 32 * tc_epi_warps<NARROW>());
     }
     *abort_flag = 0;
     mbar_init_fence();
@@ -385,7 +397,10 @@ legendre_tc_kernel(const __grid_constant__ TcLaunch L) {
     __syncwarp();
   } else {
     // -------------------------------------------------------- epilogue
-    const int quad = warp & 3;
+    constexpr int EW = tc_epi_warps<NARROW>(), EH = EW / 4, ET = 32 * EW;
+    const int quad = warp & 3;             // TMEM lane quarter this warp may read
+    const int widx = warp - 2;             // 0 .. EW-1
+    const int half = widx >> 2;            // 0 .. EH-1: which share of the quarter's columns
     const int row = quad * 32 + lane;
     float *ep = reinterpret_cast<float *>(sm + NSTAGE * STAGE_BYTES + 128);  // [128][EP_LD]
     int li = 0;
@@ -418,7 +433,7 @@ legendre_tc_kernel(const __grid_constant__ TcLaunch L) {
       if (a.dir == 0) {
         const int J = 2 * a.Jh;
         const bool odd = mi.kv1 > 0;
-        for (int j0 = 0; j0 < nrow; j0 += 16) {
+        for (int j0 = 16 * half; j0 < nrow; j0 += 16 * EH) {
           // the four accumulators' columns j0..j0+15, one wait for all
           uint32_t re[16], rx[16], ro[16], ry[16];
           tmem_ld16_nw(tbase + j0, re);
@@ -455,23 +470,38 @@ legendre_tc_kernel(const __grid_constant__ TcLaunch L) {
         for (int k0 = 0; k0 < nrow; k0 += 16) {
           if (nt * 128 + k0 >= mi.nv0) break;  // nv0 >= nv1; uniform over the epilogue warps
           if (!dead) {
-            uint32_t r0[16], x0[16], r1[16], x1[16];
-            tmem_ld16_nw(tbase + k0, r0);
-            tmem_ld16_nw(tbase + NT + k0, x0);
-            tmem_ld16_nw(tbase + 2 * NT + k0, r1);
-            tmem_ld16_nw(tbase + 3 * NT + k0, x1);
-            tmem_wait_ld();
+            if constexpr (EH == 1) {
+              uint32_t r0[16], x0[16], r1[16], x1[16];
+              tmem_ld16_nw(tbase + k0, r0);
+              tmem_ld16_nw(tbase + NT + k0, x0);
+              tmem_ld16_nw(tbase + 2 * NT + k0, r1);
+              tmem_ld16_nw(tbase + 3 * NT + k0, x1);
+              tmem_wait_ld();
 #pragma unroll
-            for (int i = 0; i < 16; ++i) {
-              erow[2 * i] = (__uint_as_float(r0[i]) + __uint_as_float(x0[i])) * us;
-              erow[2 * i + 1] = (__uint_as_float(r1[i]) + __uint_as_float(x1[i])) * us;
+              for (int i = 0; i < 16; ++i) {
+                erow[2 * i] = (__uint_as_float(r0[i]) + __uint_as_float(x0[i])) * us;
+                erow[2 * i + 1] = (__uint_as_float(r1[i]) + __uint_as_float(x1[i])) * us;
+              }
+            } else {  // two warps a quarter: columns k0 + 8 half .. + 7 each
+              const int k8 = k0 + 8 * half;
+              uint32_t r0[8], x0[8], r1[8], x1[8];
+              tmem_ld8_nw(tbase + k8, r0);
+              tmem_ld8_nw(tbase + NT + k8, x0);
+              tmem_ld8_nw(tbase + 2 * NT + k8, r1);
+              tmem_ld8_nw(tbase + 3 * NT + k8, x1);
+              tmem_wait_ld();
+#pragma unroll
+              for (int i = 0; i < 8; ++i) {
+                erow[2 * (8 * half + i)] = (__uint_as_float(r0[i]) + __uint_as_float(x0[i])) * us;
+                erow[2 * (8 * half + i) + 1] = (__uint_as_float(r1[i]) + __uint_as_float(x1[i])) * us;
+              }
             }
           }
-          epi_sync();
+          epi_sync<ET>();
           const int n = nbase + 2 * k0 + lane;
           if (!dead && n <= a.N) {
             double2 *dst = reinterpret_cast<double2 *>(a.spec_out) + idx_mn(a.N, m, n);
-            for (int bl = quad; bl < 64; bl += 4) {
+            for (int bl = widx; bl < 64; bl += EW) {
               const int c0 = ct * 128 + 2 * bl;
               if (c0 >= C2B) break;
               const double re = f32_to_f64(ep[2 * bl * EP_LD + lane]);
@@ -479,7 +509,7 @@ legendre_tc_kernel(const __grid_constant__ TcLaunch L) {
               dst[(long long)(c0 >> 1) * a.ncoef] = make_double2(re, im);
             }
           }
-          epi_sync();
+          epi_sync<ET>();
         }
       }
       tc_fence_before();
@@ -934,7 +964,7 @@ int legendre_tc_multi(Plan *const *plans, const int *batch, const void *const *i
     if (!T.map_ok) return DCCM_ERR_UNSUPPORTED;
     ntmax = T.ntmax > ntmax ? T.ntmax : ntmax;
   }
-  const bool narrow = ntmax <= 64 && tunables().tc_shape == 0;
+  const bool narrow = ntmax <= 64 && tunables().tc_shape == 1;
   for (int g = 0; g < ngroups; ++g) {
     if (batch[g] <= 0) continue;
     Plan &P = *plans[g];
@@ -973,9 +1003,9 @@ int legendre_tc_multi(Plan *const *plans, const int *batch, const void *const *i
   ctas = ctas < resident ? ctas : resident;
   const int grid = items < ctas ? items : ctas;
   if (narrow)
-    DCCM_CUDA(launch_pdl(legendre_tc_kernel<true>, dim3(grid), dim3(TC_THREADS), tc_smem_bytes<true>(), s, L));
+    DCCM_CUDA(launch_pdl(legendre_tc_kernel<true>, dim3(grid), dim3(tc_threads<true>()), tc_smem_bytes<true>(), s, L));
   else
-    DCCM_CUDA(launch_pdl(legendre_tc_kernel<false>, dim3(grid), dim3(TC_THREADS), tc_smem_bytes<false>(), s, L));
+    DCCM_CUDA(launch_pdl(legendre_tc_kernel<false>, dim3(grid), dim3(tc_threads<false>()), tc_smem_bytes<false>(), s, L));
   return DCCM_OK;
 }
 

@@ -516,10 +516,11 @@ int dccm_step_autotune_host(dccm_step *step, void *stream, const dccm_host_copy 
                             const dccm_host_copy *d2h, int nd2h, int *chosen, float *ms);
 
 /* Autotuner: chooses the launch shapes of the step's kernels by timing
- * candidates of each knob on the stage it affects ("tc_shape": 0 lets the
- * tensor-core Legendre kernel run two CTAs an SM where its tables allow
- * (N tiles of at most 64 rows, e.g. up to T85 on its Gaussian grid), 1
- * keeps one CTA an SM with two load stages; "tc_ctas": persistent CTAs of
+ * candidates of each knob on the stage it affects ("tc_shape": 0 runs the
+ * tensor-core Legendre kernel one CTA an SM with two load stages and eight
+ * epilogue warps, 1 runs it two CTAs an SM with one load stage and four
+ * epilogue warps where its tables allow (N tiles of at most 64 rows, e.g.
+ * up to T85 on its Gaussian grid); "tc_ctas": persistent CTAs of
  * that kernel, at most one wave, "fft_bb": warps per FFT CTA
  * (4, 8 or 16), "flux_threads", "remap_threads": CTA sizes, "remap_fc":
  * fields per thread of the remap, 1, 2, 3, 4 or 6), then "serial"
