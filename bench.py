@@ -442,12 +442,12 @@ def host_copies(S, groups, dccm, torch):
 # algorithmic bytes; the L2 bytes of the same launches (lts__t_bytes.sum,
 # every request L2 serves) are reported beside them.
 TRAFFIC = {
-    "c3": {"legendre_inverse": 7683584 + 12131328, "fft_inverse": 11305216, "fft_forward": 33598720 + 38144,
-           "legendre_forward": 18939136, "remap": 4120832, "bulk_flux": 7708160 + 512},
+    "c3": {"legendre_inverse": 7685888 + 12132608, "fft_inverse": 11304192, "fft_forward": 33599488 + 10496,
+           "legendre_forward": 18938112, "remap": 4120320, "bulk_flux": 7707392},
 }
 L2_BYTES = {
-    "c3": {"legendre_inverse": 30839968 + 50586784, "fft_inverse": 83083680, "fft_forward": 105767840,
-           "legendre_forward": 43723264, "remap": 16528832, "bulk_flux": 40442240},
+    "c3": {"legendre_inverse": 30906464 + 50166720, "fft_inverse": 83859552, "fft_forward": 105713056,
+           "legendre_forward": 43206016, "remap": 16645600, "bulk_flux": 40529280},
 }
 TRAFFIC_SOURCE = "ncu of bench.py --workload c3 --profile-steps 3, third replay (profiles/step_c3_launches.md)"
 # FP64 peak: measured on the device by dccm_fp64_peak (independent DFMA
