@@ -64,7 +64,7 @@ struct dccm_step {
   bool sfc_first = false;         // that graph uploads the surface inputs first
   // choices of dccm_step_autotune_host (0: the process-wide knobs; flux
   // CTA cap -1: the process-wide knob)
-  int host_order = 0, host_path = 0, host_flux_ctas = -1;
+  int host_order = 0, host_path = 0, host_flux_ctas = -1, host_flux_threads = -1;
   // surface rows of that graph's copies bound to the flux kernel (host_path
   // bit 4), used while the graph is recorded
   dccm::flux::HostRows hrows = {};
@@ -832,12 +832,14 @@ static int build_host_graph(dccm_step *st, const dccm_host_copy *h2d, int nh2d, 
   DCCM_TRY(prepare_sets(st, hp, hs));
   cudaGraph_t g = nullptr;
   Tunables &T = tunables();
-  const int flux_ctas = T.flux_ctas;
+  const int flux_ctas = T.flux_ctas, flux_threads = T.flux_threads;
   if (st->host_flux_ctas >= 0) T.flux_ctas = st->host_flux_ctas;
+  if (st->host_flux_threads >= 0) T.flux_threads = st->host_flux_threads;
   st->host_capture = true;
   const int rc = capture(st, &hs, &g);
   st->host_capture = false;
   T.flux_ctas = flux_ctas;
+  T.flux_threads = flux_threads;
   DCCM_TRY(rc);
   st->hgraph = g;
   DCCM_CUDA(cudaGraphInstantiate(&st->hexec, g, 0));
@@ -920,6 +922,7 @@ extern "C" int dccm_step_autotune_host(dccm_step *st, void *stream, const dccm_h
   // (rounds interleave the candidates, so a drift of the clocks hits all
   // of them).  The flux grid follows the process-wide knob meanwhile.
   st->host_flux_ctas = -1;
+  st->host_flux_threads = -1;
   float best_t[NC];
   for (int c = 0; c < NC; ++c) best_t[c] = 1e30f;
   for (int round = 0; round < 2; ++round)
@@ -969,6 +972,26 @@ extern "C" int dccm_step_autotune_host(dccm_step *st, void *stream, const dccm_h
         tk[k] = std::min(tk[k], t);
       }
     st->host_flux_ctas = tk[1] < tk[0] ? 0 : -1;
+  }
+  // The flux kernel's CTA size for this graph (the step's choice favours
+  // the transforms beside the flux; here the flux's results are waited for
+  // on the host link): the process-wide size against 64, 128 and 256
+  // threads, two interleaved rounds.
+  if (st->d.flux) {
+    const int cand[4] = {-1, 64, 128, 256};
+    float tk[4] = {1e30f, 1e30f, 1e30f, 1e30f};
+    for (int round = 0; round < 2; ++round)
+      for (int k = 0; k < 4; ++k) {
+        if (k && cand[k] == tunables().flux_threads) continue;  // the same as the process-wide size
+        st->host_flux_threads = cand[k];
+        float t;
+        DCCM_TRY(time_one(&t));
+        tk[k] = std::min(tk[k], t);
+      }
+    int kb = 0;
+    for (int k = 1; k < 4; ++k)
+      if (tk[k] < tk[kb]) kb = k;
+    st->host_flux_threads = cand[kb];
   }
   DCCM_TRY(build_host_graph(st, h2d, nh2d, d2h, nd2h));
   if (chosen) {

@@ -502,8 +502,9 @@ int dccm_step_host_release(dccm_step *step);
  * same mask with bit 4 under either upload order and keeps the fastest of
  * the three, then times the winner with the flux kernel's full grid against
  * the process-wide "flux_ctas" cap (with host copies the surface results are
- * the first downloads, so the fastest flux can win) and leaves the graph
- * recorded.  chosen (3 ints, may be NULL) receives the order, host_path and
+ * the first downloads, so the fastest flux can win), then the flux kernel's
+ * CTA size for this graph (the process-wide "flux_threads" against 64, 128
+ * and 256), and leaves the graph recorded.  chosen (3 ints, may be NULL) receives the order, host_path and
  * the flux CTA cap of this graph (0: the full grid); all 0 with pageable
  * buffers, for which there is nothing to choose.  Each candidate is timed
  * as the caller sees it: host clock from the graph launch to the end of the
