@@ -588,12 +588,14 @@ def roofline_f64(groups, stage_ms, fp64_peak):
     return out
 
 
-# FP64 pipe work of the flux kernel per ocean column (DADD + DMUL + 2 DFMA
-# thread instructions per cycle x elapsed cycles, ncu sass counters, c3:
-# 25.4 M for 45,478 columns).  Every column does the same work when there
-# is no sea ice (all workloads here: the ice physics is skipped where
-# SIceCon = 0), so the per-column figure carries to every workload.
-FLUX_FP64_INSTR_PER_COLUMN = (20.948747 + 41.897494 + 2 * 114.69439) * 86836.697368 / 45478
+# FP64 pipe work of the flux kernel per ocean column: DADD + DMUL + 2 DFMA
+# thread instructions (ncu sass counters, c3, 45,478 columns: 1,364,340
+# DADD, 3,274,416 DMUL, 5,730,228 DFMA; the reciprocals, square roots, exp
+# and log are the kernel's own, csrc/fp64_fast.cuh).  Every column does the
+# same work when there is no sea ice (all workloads here: the ice physics is
+# skipped where SIceCon = 0), so the per-column figure carries to every
+# workload.
+FLUX_FP64_INSTR_PER_COLUMN = (1364340 + 3274416 + 2 * 5730228) / 45478
 
 
 # FP64 flops of the implicit-coupling sweeps per column and level, one

@@ -160,6 +160,8 @@ _SIGS = {
                                           ctypes.c_void_p, ctypes.c_int]),
     "dccm_step_host_release": (ctypes.c_int, [ctypes.c_void_p]),
     "dccm_fp64_peak": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "dccm_fp64_fn_dev": (ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+                                        ctypes.c_void_p]),
     "dccm_spec_apply": (ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                        ctypes.c_int]),
     "dccm_spec_apply_dev": (ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
@@ -238,6 +240,19 @@ def fp64_peak(stream=None):
     v = ctypes.c_double()
     _check(load().dccm_fp64_peak(_stream(stream), ctypes.byref(v)), "dccm_fp64_peak")
     return v.value
+
+
+FP64_RCP, FP64_EXP, FP64_LOG, FP64_SQRT, FP64_RSQRT = 0, 1, 2, 3, 4
+
+
+def fp64_fn_dev(fn, x, y, stream=None):
+    """dccm_fp64_fn_dev: the bulk-flux kernel's FP64 reciprocal (0), exp (1),
+    log (2), square root (3) or reciprocal square root (4) of the float64
+    device tensor x into y (same length), stream-ordered."""
+    if x.numel() != y.numel():
+        raise ValueError("x and y differ in length")
+    _check(load().dccm_fp64_fn_dev(int(fn), ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(y.data_ptr()),
+                                   int(x.numel()), _stream(stream)), "dccm_fp64_fn_dev")
 
 
 def tune_set(knob, value):

@@ -20,13 +20,13 @@
 // once per warp.
 //
 // Shared memory stages, per CTA (latitude pair jj, BB field-levels), the
-// Fourier coefficients of all m in planes of 17 R + 1 floats, one plane per
-// (row or parity, re/im, field-level); coefficient m sits at slot
-// (m mod R) * 17 + m / R.  A lane reads or writes the m = k1 + R k2 it owns
-// at k1 * 17 + k2 (consecutive across lanes), and the CTA-wide copy between
-// shared and global memory walks field-levels fastest over an odd plane
-// stride, consecutive m 17 words apart: both sides are free of bank
-// conflicts and the global side is coalesced.
+// spectra of the CTA's row pairs: the inverse in the order its lanes read
+// them (stage_z), the forward's results in planes of 17 R + 1 (re, im)
+// pairs, one plane per (parity, field-level), coefficient m at slot
+// (m mod R) * 17 + m / R.  A lane writes the m = k1 + R k2 it owns at
+// k1 * 17 + k2 (consecutive across lanes, free of bank conflicts), and the
+// copy to global memory takes up to four field-levels of one (m, parity)
+// a thread, one 16-byte store per BF16 plane.
 // Supported lengths: R in {2, 3, 4, 6, 8, 12, 16, 24, 32}, I = 64 ... 1024.
 //
 // Inverse: Z_m = A_m + i B_m and Z_{I-m} = conj(A_m) + i conj(B_m) from the
@@ -107,6 +107,18 @@ __device__ __forceinline__ float2 unit24(int a) {
   return make_float2(c, -sn);
 }
 
+// o e^{sign 2 pi i a / 24}: the quarter turns (1, -i, -1, i) as swaps and
+// negations, which the compiler cannot make of a multiply by 0 and -1 (x * 0
+// is not 0 for infinities, NaN and -0).
+__device__ __forceinline__ float2 mul_unit24(float2 o, int a, int sign) {
+  const int b = (((sign > 0 ? -a : a) % 24) + 24) % 24;
+  if (b == 0) return o;
+  if (b == 6) return make_float2(o.y, -o.x);  // -i
+  if (b == 12) return make_float2(-o.x, -o.y);
+  if (b == 18) return make_float2(-o.y, o.x);  // +i
+  return cmul(o, unit24(b));
+}
+
 // In-register DFT of length R: v[k] <- sum_r v[r] e^{sign 2 pi i r k / R}.
 // Even lengths split into two halves (decimation in time), 3 is direct.
 template <int R> struct RegDft {
@@ -142,9 +154,7 @@ template <int R> struct RegDft {
       RegDft<H>::run(o, tw, I, sign);
 #pragma unroll
       for (int k = 0; k < H; ++k) {
-        float2 w = unit24(k * (24 / R));
-        if (sign > 0) w.y = -w.y;
-        const float2 t = k == 0 ? o[0] : cmul(o[k], w);
+        const float2 t = mul_unit24(o[k], k * (24 / R), sign);
         v[k] = cadd(e[k], t);
         v[k + H] = csub(e[k], t);
       }
@@ -335,112 +345,91 @@ __device__ __forceinline__ void fft_inv_block(const FftGroup &G, int jj, int by,
 }
 
 // ------------------------------------------------------------- forward
-// Split the staged E/O values (planes (parity, c) with c = 2 bl + re/im, m
-// at slot (m mod R) * 17 + m / R) into G3[s][(2m + p) Jh + jj][2 b0 + c].
-template <int R>
-__device__ __forceinline__ void write_g3(const FftGroup &G, int jj, int b0, int nb, const float *st) {
-  constexpr int PS = R * 17 + 1;
-  const int N = G.N, Jh = G.J / 2, lcw = G.lbb + 1;
+// The forward stages E and O of every row pair in shared memory as (re, im)
+// pairs: plane (parity p, field-level bl) of 17 R + 1 float2, m at slot
+// (m mod R) * 17 + m / R.
+template <int R> __device__ __forceinline__ float2 *eo_plane(float *st, int BB, int p, int bl) {
+  return reinterpret_cast<float2 *>(st) + (size_t)(p * BB + bl) * (R * 17 + 1);
+}
+
+// Split the staged E/O values into G3[s][(2m + p) Jh + jj][2 b0 + c], c =
+// 2 bl + re/im.  A thread item is (m, p, FL consecutive field-levels): FL
+// float2 reads and one store of 2 FL bf16 per plane (16, 8 or 4 bytes: the
+// run starts at 2 b0 + 2 FL q in a row of C2Bp, a multiple of 8).  Values
+// are split two at a time (packed conversions round each half as the
+// scalar ones do).
+template <int R, int FL>
+__device__ __forceinline__ void write_g3_fl(const FftGroup &G, int jj, int b0, int nb, float *st) {
+  const int N = G.N, Jh = G.J / 2, BB = G.BB, nq = BB / FL;
   unsigned short *G3 = static_cast<unsigned short *>(G.out);
   const size_t plane = (size_t)(N + 1) * 2 * Jh * G.C2Bp;
-  if (lcw >= 3) {
-    // Eight consecutive c a thread: one 16-byte store per plane (the run
-    // starts at 2 b0 + 8 q, a multiple of 8 bf16, in a row of C2Bp, a
-    // multiple of 8).  Splits two values at a time (packed conversions
-    // round each half as the scalar ones do).
-    const int lq = lcw - 3;
-    const int tot = (N + 1) << (lq + 1);  // (m, p, q), q fastest
-    for (int t = threadIdx.x; t < tot; t += blockDim.x) {
-      const int q = t & ((1 << lq) - 1);
-      const int p = (t >> lq) & 1;
-      const int m = t >> (lq + 1);
-      const int c0 = 8 * q;
-      if (c0 >= 2 * nb) continue;
-      const float *src = st + ((p << lcw) + c0) * PS + slot_of<R>(m);
-      float v[8];
-#pragma unroll
-      for (int i = 0; i < 8; ++i) v[i] = src[i * PS];
-      unsigned short *o = G3 + ((size_t)(2 * m + p) * Jh + jj) * G.C2Bp + 2 * b0 + c0;
-      const bool full = c0 + 8 <= 2 * nb;
-      if (G.nsplit == 2) {
-        unsigned h[4], l[4];
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {  // values 2i, 2i+1: field-level b0 + q*4 + i
-          const float sc = 4 * q + i < nb ? pow2f(13 - G.cexp[b0 + 4 * q + i]) : 0.f;  // no scale past the batch
-          split2h_x2(make_float2(v[2 * i] * sc, v[2 * i + 1] * sc), h[i], l[i]);
-        }
-        if (full) {
-          *reinterpret_cast<uint4 *>(o) = make_uint4(h[0], h[1], h[2], h[3]);
-          *reinterpret_cast<uint4 *>(o + plane) = make_uint4(l[0], l[1], l[2], l[3]);
-        } else {
-          for (int i = 0; c0 + i < 2 * nb; ++i) {
-            o[i] = (unsigned short)(h[i >> 1] >> (16 * (i & 1)));
-            o[plane + i] = (unsigned short)(l[i >> 1] >> (16 * (i & 1)));
-          }
-        }
-      } else {
-        unsigned h[4], md[4], l[4];
-#pragma unroll
-        for (int i = 0; i < 4; ++i) split3f_x2(make_float2(v[2 * i], v[2 * i + 1]), h[i], md[i], l[i]);
-        if (full) {
-          *reinterpret_cast<uint4 *>(o) = make_uint4(h[0], h[1], h[2], h[3]);
-          *reinterpret_cast<uint4 *>(o + plane) = make_uint4(md[0], md[1], md[2], md[3]);
-          *reinterpret_cast<uint4 *>(o + 2 * plane) = make_uint4(l[0], l[1], l[2], l[3]);
-        } else {
-          for (int i = 0; c0 + i < 2 * nb; ++i) {
-            const int sh = 16 * (i & 1);
-            o[i] = (unsigned short)(h[i >> 1] >> sh);
-            o[plane + i] = (unsigned short)(md[i >> 1] >> sh);
-            o[2 * plane + i] = (unsigned short)(l[i >> 1] >> sh);
-          }
-        }
-      }
-    }
-    return;
-  }
-  const int tot = (N + 1) << (lcw + 1);  // (m, p, c), c fastest
+  const int tot = (N + 1) * 2 * nq;  // (m, p, q), q fastest
   for (int t = threadIdx.x; t < tot; t += blockDim.x) {
-    const int c = t & ((1 << lcw) - 1);
-    const int p = (t >> lcw) & 1;
-    const int m = t >> (lcw + 1);
-    if (c < 2 * nb) {
-      const float v = st[((p << lcw) + c) * PS + slot_of<R>(m)];
-      unsigned short *o = G3 + ((size_t)(2 * m + p) * Jh + jj) * G.C2Bp + 2 * b0 + c;
-      if (G.nsplit == 2) {
-        unsigned short h, lo;
-        split2h_bits(v * pow2f(13 - G.cexp[b0 + (c >> 1)]), h, lo);
-        o[0] = h;
-        o[plane] = lo;
-      } else {
-        unsigned short h, md, lo;
-        split3f_bits(v, h, md, lo);
-        o[0] = h;
-        o[plane] = md;
-        o[2 * plane] = lo;
+    const int q = t % nq, p = (t / nq) & 1, m = t / (2 * nq);
+    const int f0 = FL * q;
+    if (f0 >= nb) continue;
+    const int sl = slot_of<R>(m);
+    float2 v[FL];
+#pragma unroll
+    for (int i = 0; i < FL; ++i) v[i] = eo_plane<R>(st, BB, p, f0 + i)[sl];
+    unsigned short *o = G3 + ((size_t)(2 * m + p) * Jh + jj) * G.C2Bp + 2 * (b0 + f0);
+    const bool full = f0 + FL <= nb;
+    unsigned w[3][FL];
+    if (G.nsplit == 2) {
+#pragma unroll
+      for (int i = 0; i < FL; ++i) {  // no scale past the batch
+        const float sc = f0 + i < nb ? pow2f(13 - G.cexp[b0 + f0 + i]) : 0.f;
+        split2h_x2(make_float2(v[i].x * sc, v[i].y * sc), w[0][i], w[1][i]);
       }
+    } else {
+#pragma unroll
+      for (int i = 0; i < FL; ++i) split3f_x2(v[i], w[0][i], w[1][i], w[2][i]);
+    }
+    const int ns = G.nsplit;
+    if (full) {
+#pragma unroll
+      for (int s3 = 0; s3 < 3; ++s3) {
+        if (s3 >= ns) break;
+        unsigned short *os = o + s3 * plane;
+        if constexpr (FL == 4) *reinterpret_cast<uint4 *>(os) = make_uint4(w[s3][0], w[s3][1], w[s3][2], w[s3][3]);
+        else if constexpr (FL == 2) *reinterpret_cast<uint2 *>(os) = make_uint2(w[s3][0], w[s3][1]);
+        else *reinterpret_cast<unsigned *>(os) = w[s3][0];
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < FL; ++i)
+#pragma unroll
+        for (int s3 = 0; s3 < 3; ++s3)
+          if (f0 + i < nb && s3 < ns) {
+            o[s3 * plane + 2 * i] = (unsigned short)w[s3][i];
+            o[s3 * plane + 2 * i + 1] = (unsigned short)(w[s3][i] >> 16);
+          }
     }
   }
+}
+
+template <int R>
+__device__ __forceinline__ void write_g3(const FftGroup &G, int jj, int b0, int nb, float *st) {
+  if (G.BB >= 4) write_g3_fl<R, 4>(G, jj, b0, nb, st);
+  else if (G.BB == 2) write_g3_fl<R, 2>(G, jj, b0, nb, st);
+  else write_g3_fl<R, 1>(G, jj, b0, nb, st);
 }
 
 // E_m = (A + B)/I and O_m = (A - B)/I of field-level bl from Z_m and
 // Z_{I-m}, into the staging planes at slot sl (m = 0: imaginary parts 0).
 template <int R>
-__device__ __forceinline__ void store_eo(float *st, int lcw, int bl, int m, int sl, float2 zm, float2 zc,
+__device__ __forceinline__ void store_eo(float *st, int BB, int bl, int m, int sl, float2 zm, float2 zc,
                                          float invI) {
-  constexpr int PS = R * 17 + 1;
-  float *E = st + ((0 << lcw) + 2 * bl) * PS, *O = st + ((1 << lcw) + 2 * bl) * PS;
   const float ar = 0.5f * (zm.x + zc.x), ai = 0.5f * (zm.y - zc.y);
   const float br = 0.5f * (zm.y + zc.y), bi = -0.5f * (zm.x - zc.x);
-  E[sl] = (ar + br) * invI;
-  E[PS + sl] = m ? (ai + bi) * invI : 0.f;
-  O[sl] = (ar - br) * invI;
-  O[PS + sl] = m ? (ai - bi) * invI : 0.f;
+  eo_plane<R>(st, BB, 0, bl)[sl] = make_float2((ar + br) * invI, m ? (ai + bi) * invI : 0.f);
+  eo_plane<R>(st, BB, 1, bl)[sl] = make_float2((ar - br) * invI, m ? (ai - bi) * invI : 0.f);
 }
 
 template <int R>
 __device__ __forceinline__ void fft_fwd_block(const FftGroup &G, int jj, int by, float *st) {
   constexpr int I = 32 * R;
-  const int N = G.N, J = G.J, Jh = J / 2, lcw = G.lbb + 1;
+  const int N = G.N, J = G.J, Jh = J / 2;
   const int jn = Jh + jj, js = Jh - 1 - jj;
   const int b0 = by * G.BB;
   const int nb = min(G.BB, G.batch - b0);
@@ -468,7 +457,7 @@ __device__ __forceinline__ void fft_fwd_block(const FftGroup &G, int jj, int by,
     for (int k1 = 0; k1 < R; ++k1) {
       const float2 zc = k1 ? shfl_c(v[(R - k1) % R], 31 - lane) : shfl_c(v[0], src0);  // Z[I - m]
       const int m = k1 + R * k2;
-      if (m <= N) store_eo<R>(st, lcw, bl, m, k1 * 17 + k2, v[k1], zc, invI);
+      if (m <= N) store_eo<R>(st, G.BB, bl, m, k1 * 17 + k2, v[k1], zc, invI);
     }
   }
   __syncthreads();
@@ -549,7 +538,7 @@ __device__ __forceinline__ void fft_inv_block_mw(const FftGroup &G, int jj, int 
 template <int W>
 __device__ __forceinline__ void fft_fwd_block_mw(const FftGroup &G, int jj, int by, float *st) {
   constexpr int R = MW_R0 * W, I = 32 * R, L = 32 * W, PS = R * 17 + 1;
-  const int N = G.N, J = G.J, Jh = J / 2, lcw = G.lbb + 1;
+  const int N = G.N, J = G.J, Jh = J / 2;
   const int jn = Jh + jj, js = Jh - 1 - jj;
   const int b0 = by * G.BB;
   const int nb = min(G.BB, G.batch - b0);
@@ -617,8 +606,169 @@ __device__ __forceinline__ void fft_fwd_block_mw(const FftGroup &G, int jj, int 
         int src;
         if (q) src = ((((MW_R0 - k1) % MW_R0) * W) + (k1 ? W - 1 - wq : W - wq)) * 32 + (31 - lane);
         else src = brev5((32 - kl) & 31);
-        store_eo<R>(st, lcw, bl, m, q * 17 + kl, v[k1], xb[src], invI);
+        store_eo<R>(st, G.BB, bl, m, q * 17 + kl, v[k1], xb[src], invI);
       }
+    }
+  }
+  __syncthreads();
+  write_g3<R>(G, jj, b0, nb, st);
+}
+
+// ------------------------------- rows over two or four warps, one exchange
+// For W = 2 and 4 the W-point step runs where its inputs meet instead: warp
+// wq owns 8 / W of the residues k1 and all W indices of the cross-warp
+// step, so each value crosses the exchange buffer once, read once (the
+// variant above reads every entry W times, once per output warp).  The
+// residues are paired (k1, 8 - k1) within a warp: {0, 4} and {2, 6} (W = 2)
+// in warp 0, {1, 7} and {3, 5} in warp 1; for W = 4 {0, 4}, {1, 7}, {2, 6},
+// {3, 5}.  So the forward's partner Z_{I-m} is in the same warp, one
+// shuffle away.
+//   forward  thread (wq, l): z[L r + t] (t = 32 wq + l) -> 8-point DFT and
+//            twiddle e^{-2 pi i t k1 / I} as above -> exchange -> for each
+//            owned k1 the W-point DFT over t_w, twiddle e^{-2 pi i l k_w / L},
+//            32-point lane DFT: register (j, k_w) of lane l holds
+//            Z[k1_j + 8 k_w + R brev5(l)];
+//   inverse  the mirror: thread (wq, l) reads Z[k1_j + 8 k_w + R brev5(l)]
+//            from the staged spectrum, lane DFT, twiddle, W-point DFT to t_w,
+//            exchange, and continues as above with all k1 of t_w = wq.
+template <int W> __device__ __forceinline__ int mw_base(int wq, int j) { return wq + W * (j >> 1); }
+template <int W> __device__ __forceinline__ int mw_k1(int wq, int j) {
+  const int b = mw_base<W>(wq, j);
+  return (j & 1) ? (b ? MW_R0 - b : 4) : b;
+}
+
+template <int W>
+__device__ __forceinline__ void fft_inv_block_mwp(const FftGroup &G, int jj, int by, float *st) {
+  constexpr int R = MW_R0 * W, I = 32 * R, L = 32 * W, NK = MW_R0 / W;
+  constexpr int ZB = zs_stride<R>();
+  const int J = G.J, Jh = J / 2;
+  const int jn = Jh + jj, js = Jh - 1 - jj;
+  const int b0 = by * G.BB;
+  const int nb = min(G.BB, G.batch - b0);
+  float2 *zs = reinterpret_cast<float2 *>(st);
+  stage_z<R>(G, jn, js, b0, nb, zs);
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int bl = warp / W, wq = warp % W;
+  const bool own = bl < G.BB;
+  float2 *xb = zs + (size_t)G.BB * ZB + (size_t)(own ? bl : 0) * MW_R0 * W * 32;
+  float2 w[5];
+  lane_twiddles<R>(G.tw, lane, true, w);
+  float2 v[MW_R0];  // v[j W + k_w]
+#pragma unroll
+  for (int j = 0; j < NK; ++j)
+#pragma unroll
+    for (int kw = 0; kw < W; ++kw)
+      v[j * W + kw] = own ? zs[bl * ZB + (mw_k1<W>(wq, j) + MW_R0 * kw) * ZQ + lane] : make_float2(0.f, 0.f);
+  lane_dit<MW_R0>(v, w, lane);
+#pragma unroll
+  for (int kw = 1; kw < W; ++kw) {
+    const float2 tq = twid(G.tw, lane * kw * (I / L), +1);
+#pragma unroll
+    for (int j = 0; j < NK; ++j) v[j * W + kw] = cmul(v[j * W + kw], tq);
+  }
+#pragma unroll
+  for (int j = 0; j < NK; ++j) RegDft<W>::run(v + j * W, G.tw, I, +1);
+  if (own) {
+#pragma unroll
+    for (int j = 0; j < NK; ++j)
+#pragma unroll
+      for (int tx = 0; tx < W; ++tx) xb[(mw_k1<W>(wq, j) * W + tx) * 32 + lane] = v[j * W + tx];
+  }
+  __syncthreads();
+  if (own) {
+#pragma unroll
+    for (int k1 = 0; k1 < MW_R0; ++k1) v[k1] = xb[(k1 * W + wq) * 32 + lane];
+  }
+  const int t = 32 * wq + lane;
+#pragma unroll
+  for (int k1 = 1; k1 < MW_R0; ++k1) v[k1] = cmul(v[k1], twid(G.tw, t * k1, +1));
+  RegDft<MW_R0>::run(v, G.tw, I, +1);
+  if (bl < nb) {
+    double *gn = static_cast<double *>(G.out) + ((long long)(b0 + bl) * J + jn) * I;
+    double *gs = static_cast<double *>(G.out) + ((long long)(b0 + bl) * J + js) * I;
+#pragma unroll
+    for (int r = 0; r < MW_R0; ++r) {
+      gn[L * r + t] = f32_to_f64(v[r].x);
+      gs[L * r + t] = f32_to_f64(v[r].y);
+    }
+  }
+}
+
+template <int W>
+__device__ __forceinline__ void fft_fwd_block_mwp(const FftGroup &G, int jj, int by, float *st) {
+  constexpr int R = MW_R0 * W, I = 32 * R, L = 32 * W, PS = R * 17 + 1, NK = MW_R0 / W;
+  const int N = G.N, J = G.J, Jh = J / 2;
+  const int jn = Jh + jj, js = Jh - 1 - jj;
+  const int b0 = by * G.BB;
+  const int nb = min(G.BB, G.batch - b0);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int bl = warp / W, wq = warp % W;
+  const bool own = bl < G.BB;
+  const int kl = brev5(lane);
+  const int t = 32 * wq + lane;
+  float2 *xb = reinterpret_cast<float2 *>(st + 4 * G.BB * PS) + (size_t)(own ? bl : 0) * MW_R0 * W * 32;
+  float2 v[MW_R0];
+  if (bl < nb) {
+    const double *gn = static_cast<const double *>(G.in) + ((long long)(b0 + bl) * J + jn) * I;
+    const double *gs = static_cast<const double *>(G.in) + ((long long)(b0 + bl) * J + js) * I;
+    double xn[MW_R0], xs[MW_R0];  // all loads first, then the conversions
+#pragma unroll
+    for (int r = 0; r < MW_R0; ++r) {
+      xn[r] = gn[L * r + t];
+      xs[r] = gs[L * r + t];
+    }
+#pragma unroll
+    for (int r = 0; r < MW_R0; ++r) v[r] = make_float2(f64_to_f32_rn(xn[r]), f64_to_f32_rn(xs[r]));
+  } else {
+#pragma unroll
+    for (int r = 0; r < MW_R0; ++r) v[r] = make_float2(0.f, 0.f);
+  }
+  RegDft<MW_R0>::run(v, G.tw, I, -1);
+#pragma unroll
+  for (int k1 = 1; k1 < MW_R0; ++k1) v[k1] = cmul(v[k1], twid(G.tw, t * k1, -1));
+  if (own) {
+#pragma unroll
+    for (int k1 = 0; k1 < MW_R0; ++k1) xb[(k1 * W + wq) * 32 + lane] = v[k1];
+  }
+  __syncthreads();
+  if (own) {
+#pragma unroll
+    for (int j = 0; j < NK; ++j)
+#pragma unroll
+      for (int tx = 0; tx < W; ++tx) v[j * W + tx] = xb[(mw_k1<W>(wq, j) * W + tx) * 32 + lane];
+  }
+#pragma unroll
+  for (int j = 0; j < NK; ++j) RegDft<W>::run(v + j * W, G.tw, I, -1);
+#pragma unroll
+  for (int kw = 1; kw < W; ++kw) {
+    const float2 tq = twid(G.tw, lane * kw * (I / L), -1);
+#pragma unroll
+    for (int j = 0; j < NK; ++j) v[j * W + kw] = cmul(v[j * W + kw], tq);
+  }
+  float2 w[5];
+  lane_twiddles<R>(G.tw, lane, false, w);
+  lane_dif<MW_R0>(v, w, lane);
+  // Z[I - m] for m = k1 + 8 k_w + R kl, all within the warp:
+  //   k1 in {1, 2, 3, 5, 6, 7}: register (partner j, W-1-k_w), lane 31 - l;
+  //   k1 = 4: register (j, W-1-k_w), lane 31 - l;
+  //   k1 = 0: register (j, W-k_w), lane 31 - l; for k_w = 0 register (j, 0),
+  //   lane brev5(32 - kl).
+  const int src0 = brev5((32 - kl) & 31);
+  const float invI = 1.f / (float)I;
+#pragma unroll
+  for (int j = 0; j < NK; ++j) {
+    const bool paired = mw_base<W>(wq, j) != 0;  // warp-uniform
+    const int k1 = mw_k1<W>(wq, j);
+#pragma unroll
+    for (int kw = 0; kw < W; ++kw) {
+      float2 zc;
+      if (paired) zc = shfl_c(v[(j ^ 1) * W + (W - 1 - kw)], 31 - lane);
+      else if (j & 1) zc = shfl_c(v[j * W + (W - 1 - kw)], 31 - lane);
+      else zc = kw ? shfl_c(v[j * W + (W - kw)], 31 - lane) : shfl_c(v[j * W], src0);
+      const int q = k1 + MW_R0 * kw;
+      const int m = q + R * kl;
+      if (bl < nb && m <= N) store_eo<R>(st, G.BB, bl, m, q * 17 + kl, v[j * W + kw], zc, invI);
     }
   }
   __syncthreads();
@@ -632,9 +782,12 @@ __device__ __forceinline__ void fft_fwd_block_mw(const FftGroup &G, int jj, int 
 template <int R, int RMAX, bool FWD>
 __device__ __forceinline__ void dispatch_case(const FftGroup &G, int jj, int by, float *st) {
   if constexpr (R <= RMAX) {
-    if constexpr (R >= 16) {
+    if constexpr (R == 24) {
       if (FWD) fft_fwd_block_mw<R / MW_R0>(G, jj, by, st);
       else fft_inv_block_mw<R / MW_R0>(G, jj, by, st);
+    } else if constexpr (R >= 16) {
+      if (FWD) fft_fwd_block_mwp<R / MW_R0>(G, jj, by, st);
+      else fft_inv_block_mwp<R / MW_R0>(G, jj, by, st);
     } else {
       if (FWD) fft_fwd_block<R>(G, jj, by, st);
       else fft_inv_block<R>(G, jj, by, st);

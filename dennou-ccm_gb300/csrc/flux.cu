@@ -14,6 +14,7 @@
 
 #include "common.cuh"
 #include "flux_rows.cuh"
+#include "fp64_fast.cuh"
 #include "nvtx.cuh"
 
 namespace dccm {
@@ -64,12 +65,13 @@ __device__ __forceinline__ void bulk_coef_l82(double Ri, double z0m, double z0h,
   double vm, th;
   if (flag) {
     if (Ri > 0.0) {
-      const double r = sqrt(1.0 + 5.0 * Ri);
-      vm = cmn / (1.0 + 10.0 * Ri / r);
-      th = chn / (1.0 + 15.0 * Ri * r);
+      double h;  // 1 / (2 r)
+      const double r = fp64::sqrt_h(1.0 + 5.0 * Ri, h);
+      vm = cmn * fp64::rcp(1.0 + 20.0 * Ri * h);  // 10 Ri / r
+      th = chn * fp64::rcp(1.0 + 15.0 * Ri * r);
     } else {
-      vm = cmn * (1.0 - 10.0 * Ri / (1.0 + 75.0 * cmn * sqrt(-(z - zs + z0m) / z0m * Ri)));
-      th = chn * (1.0 - 15.0 * Ri / (1.0 + 75.0 * chn * sqrt(-(z - zs + z0h) / z0h * Ri)));
+      vm = cmn * (1.0 - 10.0 * Ri * fp64::rcp(1.0 + 75.0 * cmn * fp64::sqrt(-(z - zs + z0m) * (1.0 / z0m) * Ri)));
+      th = chn * (1.0 - 15.0 * Ri * fp64::rcp(1.0 + 75.0 * chn * fp64::sqrt(-(z - zs + z0h) * (1.0 / z0h) * Ri)));
     }
   } else {
     vm = 0.0;
@@ -102,7 +104,7 @@ __device__ __forceinline__ void wr(const HostRows &h, int k, double *dev, int64_
 }
 
 template <bool HOST>
-__global__ void __launch_bounds__(256) bulk_flux_column(Ptrs p, Geom g, const __grid_constant__ HostRows h) {
+__global__ void __launch_bounds__(256, 2) bulk_flux_column(Ptrs p, Geom g, const __grid_constant__ HostRows h) {
   constexpr double GasRDry = GasRUniv / MolWtDry;
   constexpr double GasRWet = GasRUniv / MolWtWet;
   constexpr double EpsV = MolWtWet / MolWtDry;
@@ -127,11 +129,13 @@ __global__ void __launch_bounds__(256) bulk_flux_column(Ptrs p, Geom g, const __
     const double humd = 1.0;
 
     // FP64 is the scarce pipe on this GPU: divisions that do not feed a
-    // cancelling difference become products with a shared reciprocal, and
-    // the two Exner functions share one exp/log pair, (ps/P0)^k = exp(k log),
-    // with Exner(sig1 ps) = Exner(ps) sig1^k.  Each rewrite moves a result by
-    // an ulp or two, far inside the 1e-13 agreement with the reference.
-    const double rPs = 1.0 / Ps;
+    // cancelling difference become products with a reciprocal (fp64::rcp,
+    // three DFMA from an FP32 seed), exp and log are the table-driven ones
+    // of fp64_fast.cuh, and the two Exner functions share one exp/log pair,
+    // (ps/P0)^k = exp(k log), with Exner(sig1 ps) = Exner(ps) sig1^k.  Each
+    // rewrite moves a result by an ulp or two, far inside the 1e-13
+    // agreement with the reference.
+    const double rPs = fp64::rcp(Ps);
     double Frac[2], QSat[2], SVT[2], Tsn[2], Albn[2], rTs[2];
     Frac[0] = 1.0 - SIceCon;
     Frac[1] = SIceCon;
@@ -148,26 +152,33 @@ __global__ void __launch_bounds__(256) bulk_flux_column(Ptrs p, Geom g, const __
         rTs[n] = QSat[n] = SVT[n] = 0.0;
         continue;
       }
-      rTs[n] = 1.0 / Tsn[n];
-      QSat[n] = (EpsV * Es0) * rPs * exp(aL[n] / GasRWet * (1.0 / 273.0 - rTs[n]));
+      rTs[n] = fp64::rcp(Tsn[n]);
+      QSat[n] = (EpsV * Es0) * rPs * fp64::exp(aL[n] / GasRWet * (1.0 / 273.0 - rTs[n]));
       SVT[n] = Tsn[n] * (1.0 + (((1.0 / EpsV) - 1.0) * QSat[n]));
     }
     const double VirTemp = Ta * (1.0 + (((1.0 / EpsV) - 1.0) * q1));
-    const double SfcExner = exp((GasRDry / CpDry) * log(Ps * (1.0 / RefPress)));
+    const double SfcExner = fp64::exp((GasRDry / CpDry) * fp64::log(Ps * (1.0 / RefPress)));
     const double Exner = SfcExner * g.sig1k;
-    const double rExner = 1.0 / Exner;
-    const double VelAbs = sqrt(U * U + V * V);
+    const double rExner = fp64::rcp(Exner);
+    const double rSfcExner = fp64::rcp(SfcExner);
+    const double VelAbs = fp64::sqrt(U * U + V * V);
     const double Height = zs + GasRDry / Grav * VirTemp * (1.0 - g.sig1);
 
     // Neutral coefficients (:250-260) depend only on the column (the
     // roughness lengths are the same constants for both surface types).
-    const double tmp = (FKarm / log((Height - zs + z0m) / z0m));
+    const double tmp = FKarm * fp64::rcp(fp64::log((Height - zs + z0m) * (1.0 / z0m)));
     const double cmn = tmp * tmp;
-    const double chn = tmp * (FKarm / log((Height - zs + z0h) / z0h));
+    // z0h = RoughLenHeatFactor z0m: with the factor 1 both logarithms are one
+    const double chn = RoughLenHeatFactor == 1.0
+                           ? cmn
+                           : tmp * (FKarm * fp64::rcp(fp64::log((Height - zs + z0h) * (1.0 / z0h))));
     const double vmx = fmax(VelAbs, VelMinForRi);
-    const double rvmx2 = 1.0 / (vmx * vmx);
-    const double VT_E = VirTemp / Exner;  // the Richardson number and the sensible heat
-    const double Ta_E = Ta / Exner;       // flux subtract nearly equal terms: true divisions
+    const double rvmx2 = fp64::rcp(vmx * vmx);
+    // The Richardson number and the sensible heat flux subtract nearly equal
+    // quotients: these keep correctly rounded divisions (Markstein's
+    // correction of a times the shared reciprocal).
+    const double VT_E = fp64::div_rb(VirTemp, Exner, rExner);
+    const double Ta_E = fp64::div_rb(Ta, Exner, rExner);
 
     double CVel[2], CTemp[2], CQ[2], WSX[2], WSY[2], Sen[2], QV[2], LatH[2], LUw[2], SUw[2];
     bool flag[2];
@@ -182,18 +193,18 @@ __global__ void __launch_bounds__(256) bulk_flux_column(Ptrs p, Geom g, const __
         WSX[n] = WSY[n] = Sen[n] = QV[n] = LatH[n] = LUw[n] = SUw[n] = 0.0;
         continue;
       }
-      const double SVT_SE = SVT[n] / SfcExner;
-      const double Ri = Grav / SVT_SE * (VT_E - SVT_SE) * rvmx2 * (Height - zs);
+      const double SVT_SE = fp64::div_rb(SVT[n], SfcExner, rSfcExner);
+      const double Ri = Grav * fp64::rcp(SVT_SE) * (VT_E - SVT_SE) * rvmx2 * (Height - zs);
       double cm, ch, cq;
       bulk_coef_l82(Ri, z0m, z0h, zs, Height, cmn, chn, f, cm, ch, cq);
-      const double rho = Ps / (GasRDry * SVT[n]);
+      const double rho = Ps * fp64::rcp(GasRDry * SVT[n]);
       CVel[n] = cm * rho * fmin(fmax(VelAbs, VelMinForVel), VelMaxForVel);
       CTemp[n] = ch * rho * fmin(fmax(VelAbs, VelMinForTemp), VelMaxForTemp);
       CQ[n] = cq * rho * fmin(fmax(VelAbs, VelMinForQVap), VelMaxForQVap);
       if (f) {
         WSX[n] = -CVel[n] * U;
         WSY[n] = -CVel[n] * V;
-        Sen[n] = -CpDry * SfcExner * CTemp[n] * (Ta_E - Tsn[n] / SfcExner);
+        Sen[n] = -CpDry * SfcExner * CTemp[n] * (Ta_E - fp64::div_rb(Tsn[n], SfcExner, rSfcExner));
         QV[n] = -humd * CQ[n] * (q1 - QSat[n]);
         LatH[n] = aL[n] * QV[n];
         const double T2 = Tsn[n] * Tsn[n];
@@ -228,10 +239,10 @@ __global__ void __launch_bounds__(256) bulk_flux_column(Ptrs p, Geom g, const __
       for (int k = 0; k < NIN; ++k) mirror<HOST>(h, k, t, vin[k]);
     }
     const double DFsDT1 = -CpDry * SfcExner * CTemp3 * rExner;
-    const double f1 = 1.0 / (c11 + CVel3) * (WSX3 + c21);
-    const double f2 = 1.0 / (c12 + CVel3) * (WSY3 + c22);
-    const double f3 = 1.0 / (c13 - DFsDT1) * (Sen3 + c23);
-    const double f4 = 1.0 / (c14 + humd * CQ3) * (QV3 + c24);
+    const double f1 = fp64::rcp(c11 + CVel3) * (WSX3 + c21);
+    const double f2 = fp64::rcp(c12 + CVel3) * (WSY3 + c22);
+    const double f3 = fp64::rcp(c13 - DFsDT1) * (Sen3 + c23);
+    const double f4 = fp64::rcp(c14 + humd * CQ3) * (QV3 + c24);
     wr<HOST>(h, O_DELV, p.DelV, c, t, f1);
     wr<HOST>(h, O_DELV + 1, p.DelV, c + P, t, f2);
     wr<HOST>(h, O_DELV + 2, p.DelV, c + 2 * P, t, f3);
@@ -241,6 +252,7 @@ __global__ void __launch_bounds__(256) bulk_flux_column(Ptrs p, Geom g, const __
     double Lat3 = 0.0;
 #pragma unroll
     for (int n = 0; n < 2; ++n) {
+      if (n == 1 && !ice) break;  // the ice slot's zeros stay zeros (0 - 0 f = 0 for finite f)
       WSX[n] = WSX[n] - CVel[n] * f1;
       WSY[n] = WSY[n] - CVel[n] * f2;
       Sen[n] = Sen[n] - sfac * CTemp[n] * f3;

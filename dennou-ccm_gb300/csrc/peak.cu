@@ -3,6 +3,7 @@
 // thread runs 8 independent DFMA chains; the result is stored only under
 // a condition the values never meet, so no chain can be removed.
 #include "common.cuh"
+#include "fp64_fast.cuh"
 #include "nvtx.cuh"
 
 namespace dccm {
@@ -22,6 +23,23 @@ __global__ void __launch_bounds__(256) dfma_kernel(int iters, double b, double c
 #pragma unroll
   for (int k = 0; k < CHAINS; ++k) s += a[k];
   if (s == -1.0) sink[blockIdx.x] = s;
+}
+
+// The column physics' FP64 elementary functions on an array (their tests).
+__global__ void __launch_bounds__(256) fn_kernel(int fn, const double *x, double *y, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double v = x[i];
+    double r, h;
+    if (fn == DCCM_FP64_RCP) r = fp64::rcp(v);
+    else if (fn == DCCM_FP64_EXP) r = fp64::exp(v);
+    else if (fn == DCCM_FP64_LOG) r = fp64::log(v);
+    else if (fn == DCCM_FP64_SQRT) r = fp64::sqrt(v);
+    else {
+      fp64::sqrt_h(v, h);
+      r = 2.0 * h;
+    }
+    y[i] = r;
+  }
 }
 
 }  // namespace peak
@@ -61,5 +79,17 @@ extern "C" int dccm_fp64_peak(void *stream, double *tflops) {
   if (rc != DCCM_OK) return rc;
   const double flops = 2.0 * peak::CHAINS * (double)iters * blocks * threads;
   *tflops = flops / (best * 1e-3) / 1e12;
+  return DCCM_OK;
+}
+
+extern "C" int dccm_fp64_fn_dev(int fn, const double *x, double *y, int64_t n, void *stream) {
+  DCCM_NVTX_FUNC();
+  if (fn < DCCM_FP64_RCP || fn > DCCM_FP64_RSQRT) return DCCM_ERR_INVALID_ARG;
+  if (n < 0 || (n > 0 && (!x || !y))) return DCCM_ERR_INVALID_ARG;
+  if (n == 0) return DCCM_OK;
+  const int64_t cap = (int64_t)sm_count() * 8, want = (n + 255) / 256;
+  const int64_t blocks = want < cap ? want : cap;
+  peak::fn_kernel<<<(unsigned)blocks, 256, 0, as_stream(stream)>>>(fn, x, y, n);
+  DCCM_CUDA(cudaGetLastError());
   return DCCM_OK;
 }

@@ -591,6 +591,18 @@ int dccm_spec_apply(int nmax, const dccm_spec_op *op, const double *spec_in, dou
  * of the FP64-bound kernels' roofline fractions. */
 int dccm_fp64_peak(void *stream, double *tflops);
 
+/* The bulk-flux kernel's FP64 reciprocal, exp, log, square root and
+ * reciprocal square root (fewer FP64 operations than the correctly rounded
+ * library calls; within about 2 units in the last place) evaluated
+ * elementwise on device arrays, y[i] = f(x[i]), stream-ordered: the entry
+ * point their accuracy tests call. */
+#define DCCM_FP64_RCP 0
+#define DCCM_FP64_EXP 1
+#define DCCM_FP64_LOG 2
+#define DCCM_FP64_SQRT 3
+#define DCCM_FP64_RSQRT 4
+int dccm_fp64_fn_dev(int fn, const double *x, double *y, int64_t n, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
