@@ -18,8 +18,11 @@
 // of (M(k,-1) M(k+1,0)) per level and matrix and multiplies every
 // right-hand side by it (the momentum matrix serves U and V, the tracer
 // matrix every tracer), the mass term uses 1 / (g 2 dt), and each level's
-// full Exner function is inverted once.  Results agree with the
-// reference's operation order to rounding (the tests hold 1e-13).  Level 1
+// full Exner function is inverted once.  The reciprocals are fp64::rcp
+// (an FP32 seed and one cubic Newton step: 3 DFMA, within half an ulp
+// and a little; zeros, infinities and out-of-range values take the exact
+// division).  Results agree with the reference's operation order to
+// rounding (the tests hold 1e-13).  Level 1
 // of the eliminated systems divides by the zero sub-diagonal the reference
 // sets at k = 1 (:199, :237, :272), as the reference does: the coupler
 // replaces U, V, T and the vapour tracer there with the surface solution
@@ -27,6 +30,7 @@
 #include <new>
 
 #include "common.cuh"
+#include "fp64_fast.cuh"
 #include "nvtx.cuh"
 
 struct dccm_implcpl {
@@ -65,15 +69,17 @@ constexpr int LVB = 8;  // backward sweep
 // once per system: G(j) = P_h(j) / (R Tv_h(j) (z(j+1) - z(j))) at half level
 // j = 1..kmax-1 (the transfer coefficient of :182-195 is K(j) G(j)), and the
 // reciprocal Exner function 1 / Exner_f(j) at full level j (0-based index,
-// the temperature rows of :222-260).  Same expressions, same rounding.
+// the temperature rows of :222-260).  Same expressions; G as a product
+// with the reciprocal.
 __global__ void __launch_bounds__(256) geo_kernel(const Fwd a) {
   const long long n = a.ncol;
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= n * a.kmax) return;
   const int j = (int)(t / n);
   const long long c = t - j * n;
-  a.IEF[t] = 1.0 / a.Ef[c + n * j];
-  if (j >= 1) a.G[t] = a.P[c + n * j] / (a.GasR * a.Tv[c + n * j] * (a.Z[c + n * j] - a.Z[c + n * (j - 1)]));
+  a.IEF[t] = fp64::rcp(a.Ef[c + n * j]);
+  if (j >= 1)
+    a.G[t] = a.P[c + n * j] * fp64::rcp(a.GasR * a.Tv[c + n * j] * (a.Z[c + n * j] - a.Z[c + n * (j - 1)]));
 }
 
 template <int SYS>
@@ -156,10 +162,10 @@ __device__ __forceinline__ void forward_column(const Fwd &a, long long c, int tr
       if (k == 1) tc1 = tck;
       double inv, m0e;
       if (k == K) {
-        inv = 1.0 / mm;
+        inv = fp64::rcp(mm);
         m0e = m0 * inv;
       } else {
-        inv = 1.0 / (mm * m0p);
+        inv = fp64::rcp(mm * m0p);
         m0e = (m0 * m0p - mp) * inv;
       }
 #pragma unroll
@@ -188,7 +194,7 @@ __device__ __forceinline__ void forward_column(const Fwd &a, long long c, int tr
   }
   // coupling coefficients (:342-375); DFADUV1 = -DFADUV2 = TC(1)
   const double Tmp = -(a.P[c + n] - a.P[c]) * a.inv_g2dt;
-  const double i2 = 1.0 / m0_2;
+  const double i2 = fp64::rcp(m0_2);
   if constexpr (SYS == 0) {
     const double cu = Tmp + tc1 + tc1 * i2;
     a.C1[c + n * 0] = cu;
@@ -254,7 +260,7 @@ __device__ __forceinline__ void backward_chains(const double *__restrict__ mat, 
     for (int i = 0; i < LVB; ++i) {
       const int k = k0 + i;
       if (k > K) break;
-      const double im = 1.0 / m0[i];
+      const double im = fp64::rcp(m0[i]);
 #pragma unroll
       for (int r = 0; r < NR; ++r) {
         v[r] = (xs[i][r] - mm[i] * v[r]) * im;

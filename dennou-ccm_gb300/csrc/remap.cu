@@ -19,10 +19,15 @@
 //
 // Apply.  The table is grouped by destination, so a stable counting sort
 // groups it by row without changing the per-row order.  The rows are then
-// stored as a sliced ELL matrix: slices of 32 consecutive destination rows
-// (one warp), each slice as many record columns wide as its longest row,
-// record k of lane r at slice_base + 32 k + r, so that a warp's k-th records
-// are one coalesced 512-byte load.  A record is 16 bytes (weight, source
+// stored as a sliced ELL matrix: slices of 32 destination rows (one warp),
+// each slice as many record columns wide as its longest row, record k of
+// lane r at slice_base + 32 k + r, so that a warp's k-th records are one
+// coalesced 512-byte load.  Within each window of 256 consecutive rows the
+// rows are ordered by length (stable) before they are cut into slices, so
+// that a slice's rows are about equally long: the padding records, which
+// cost FP64 instructions like real ones, fall from 19 % to 5 % of the
+// records at c3 (17 % to 3 % at c5); each lane reads its row number from
+// the plan.  A record is 16 bytes (weight, source
 // column; column -1 pads a short row).  One thread owns a destination row
 // and FC of the fields: it loads each record once and gathers the FC source
 // values of its column (all of a round's gathers in flight together);
@@ -50,6 +55,7 @@ struct dccm_remap_plan {
   int64_t n_send = 0, n_recv = 0, nnz = 0;
   int64_t nslice = 0, nrec = 0;  // 32-row slices; records including padding
   int2 *d_slices = nullptr;      // per slice: (first record / 32, width in records)
+  int *d_rows = nullptr;         // per slice lane: its destination row (0-based), -1 past the last
   double2 *d_ent = nullptr;      // nrec records: x = weight, y = column (0-based, -1 pad) bits
   dccm::DevBuf stage;            // host entry point staging
   cudaStream_t stream = nullptr;
@@ -61,21 +67,21 @@ namespace remap {
 constexpr int UNSET = -2147483647;
 
 // ---------------------------------------------------------------- apply
-// Thread = destination row r (lane of its slice) x fields f0 .. f0+FC-1
+// Thread = destination row r (lane of its slice, rows[]) x fields f0 .. f0+FC-1
 // (f0 = FC blockIdx.y).  Field f is read at src + f ld_src and written at
 // (f % nsub) ld_dst + (f / nsub) ld_dst2.  U records a round: their loads,
 // then their U x FC source gathers, are in flight before the in-order sums.
 template <int FC>
 __global__ void __launch_bounds__(256)
-sell_apply(const int2 *__restrict__ slices, const double2 *__restrict__ ent, const double *__restrict__ src,
-           int64_t ld_src, double *__restrict__ dst, int64_t ld_dst, int nrow, int nslice, int nfields,
-           int nsub, int64_t ld_dst2) {
+sell_apply(const int2 *__restrict__ slices, const int *__restrict__ rows, const double2 *__restrict__ ent,
+           const double *__restrict__ src, int64_t ld_src, double *__restrict__ dst, int64_t ld_dst, int nslice,
+           int nfields, int nsub, int64_t ld_dst2) {
   constexpr int U = FC >= 6 ? 2 : 4;
   const int lane = threadIdx.x & 31;
   const int sl_i = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
   if (sl_i >= nslice) return;
   const int f0 = blockIdx.y * FC;
-  const int r = sl_i * 32 + lane;
+  const int r = __ldg(rows + sl_i * 32 + lane);
   const int2 sl = __ldg(slices + sl_i);
   const double2 *e = ent + (int64_t)sl.x * 32 + lane;
   const double *sp[FC];
@@ -113,7 +119,7 @@ sell_apply(const int2 *__restrict__ slices, const double2 *__restrict__ ent, con
       }
     }
   }
-  if (r >= nrow) return;
+  if (r < 0) return;
 #pragma unroll
   for (int f = 0; f < FC; ++f) {
     const int fg = f0 + f;
@@ -139,14 +145,18 @@ int apply2(dccm_remap_plan *p, const double *src, int64_t ld_src, double *dst, i
   const int64_t ychunks = (nfields + fc - 1) / fc;
   if (blocks > 0x7FFFFFFF || ychunks > 65535) return DCCM_ERR_UNSUPPORTED;
   const dim3 grid((unsigned)blocks, (unsigned)ychunks);
-  const int nr = (int)p->n_recv, ns = (int)p->nslice;
+  const int ns = (int)p->nslice;
+#define DCCM_SELL(FC_)                                                                                   \
+  sell_apply<FC_><<<grid, threads, 0, s>>>(p->d_slices, p->d_rows, p->d_ent, src, ld_src, dst, ld_dst, ns, \
+                                           nfields, nsub, ld_dst2)
   switch (fc) {
-    case 6: sell_apply<6><<<grid, threads, 0, s>>>(p->d_slices, p->d_ent, src, ld_src, dst, ld_dst, nr, ns, nfields, nsub, ld_dst2); break;
-    case 4: sell_apply<4><<<grid, threads, 0, s>>>(p->d_slices, p->d_ent, src, ld_src, dst, ld_dst, nr, ns, nfields, nsub, ld_dst2); break;
-    case 3: sell_apply<3><<<grid, threads, 0, s>>>(p->d_slices, p->d_ent, src, ld_src, dst, ld_dst, nr, ns, nfields, nsub, ld_dst2); break;
-    case 2: sell_apply<2><<<grid, threads, 0, s>>>(p->d_slices, p->d_ent, src, ld_src, dst, ld_dst, nr, ns, nfields, nsub, ld_dst2); break;
-    default: sell_apply<1><<<grid, threads, 0, s>>>(p->d_slices, p->d_ent, src, ld_src, dst, ld_dst, nr, ns, nfields, nsub, ld_dst2); break;
+    case 6: DCCM_SELL(6); break;
+    case 4: DCCM_SELL(4); break;
+    case 3: DCCM_SELL(3); break;
+    case 2: DCCM_SELL(2); break;
+    default: DCCM_SELL(1); break;
   }
+#undef DCCM_SELL
   DCCM_LAUNCH_CHECK();
   return DCCM_OK;
 }
@@ -698,14 +708,28 @@ extern "C" int dccm_remap_plan_create(int64_t n_send, int64_t n_recv, int64_t no
   std::vector<int64_t> rowptr(n_recv + 1, 0);
   for (int64_t k = 0; k < nop; ++k) rowptr[recv_index[k]]++;
   for (int64_t r = 0; r < n_recv; ++r) rowptr[r + 1] += rowptr[r];
-  // Sliced ELL: slice of rows 32 q .. 32 q + 31, width = its longest row.
+  // Row order of the slices: by length within windows of 256 rows (stable).
+  constexpr int64_t WIN = 256;
+  std::vector<int> order((size_t)n_recv);
+  for (int64_t r = 0; r < n_recv; ++r) order[(size_t)r] = (int)r;
+  for (int64_t w0 = 0; w0 < n_recv; w0 += WIN)
+    std::stable_sort(order.begin() + w0, order.begin() + std::min<int64_t>(n_recv, w0 + WIN), [&](int a, int b) {
+      return rowptr[a + 1] - rowptr[a] < rowptr[b + 1] - rowptr[b];
+    });
+  // Sliced ELL: slice q holds rows order[32 q .. 32 q + 31], width = its longest row.
   const int64_t nslice = (n_recv + 31) / 32;
   std::vector<int2> slices((size_t)nslice);
+  std::vector<int> rows((size_t)nslice * 32, -1);
+  std::vector<int64_t> pos((size_t)n_recv);  // slice position of each row
   int64_t nrec = 0;
   for (int64_t q = 0; q < nslice; ++q) {
     int64_t wmax = 0;
-    for (int64_t r = q * 32; r < std::min<int64_t>(n_recv, q * 32 + 32); ++r)
+    for (int64_t i = q * 32; i < std::min<int64_t>(n_recv, q * 32 + 32); ++i) {
+      const int r = order[(size_t)i];
       wmax = std::max<int64_t>(wmax, rowptr[r + 1] - rowptr[r]);
+      rows[(size_t)i] = r;
+      pos[(size_t)r] = i;
+    }
     if (nrec / 32 > 0x7FFFFFFF || wmax > 0x7FFFFFFF) return DCCM_ERR_UNSUPPORTED;
     slices[(size_t)q] = make_int2((int)(nrec / 32), (int)wmax);
     nrec += 32 * wmax;
@@ -721,7 +745,8 @@ extern "C" int dccm_remap_plan_create(int64_t n_send, int64_t n_recv, int64_t no
     double colbits;
     memcpy(&colbits, &col, sizeof col);
     const int64_t kk = fill[r]++ - rowptr[r];  // position of the entry within its row
-    ent[(size_t)((int64_t)slices[(size_t)(r / 32)].x * 32 + kk * 32 + r % 32)] = make_double2(coef[k], colbits);
+    const int64_t i = pos[(size_t)r];
+    ent[(size_t)((int64_t)slices[(size_t)(i / 32)].x * 32 + kk * 32 + i % 32)] = make_double2(coef[k], colbits);
   }
   dccm_remap_plan *p = new (std::nothrow) dccm_remap_plan();
   if (!p) return DCCM_ERR_NOMEM;
@@ -732,9 +757,12 @@ extern "C" int dccm_remap_plan_create(int64_t n_send, int64_t n_recv, int64_t no
   p->nrec = nrec;
   cudaError_t e = cudaSuccess;
   if (nslice > 0) e = cudaMalloc(&p->d_slices, nslice * sizeof(int2));
+  if (e == cudaSuccess && nslice > 0) e = cudaMalloc(&p->d_rows, nslice * 32 * sizeof(int));
   if (e == cudaSuccess && nrec > 0) e = cudaMalloc(&p->d_ent, nrec * sizeof(double2));
   if (e == cudaSuccess && nslice > 0)
     e = cudaMemcpy(p->d_slices, slices.data(), nslice * sizeof(int2), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && nslice > 0)
+    e = cudaMemcpy(p->d_rows, rows.data(), nslice * 32 * sizeof(int), cudaMemcpyHostToDevice);
   if (e == cudaSuccess && nrec > 0)
     e = cudaMemcpy(p->d_ent, ent.data(), nrec * sizeof(double2), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
@@ -750,6 +778,7 @@ extern "C" int dccm_remap_plan_destroy(dccm_remap_plan *p) {
   DCCM_NVTX_FUNC();
   if (!p) return DCCM_OK;
   if (p->d_slices) cudaFree(p->d_slices);
+  if (p->d_rows) cudaFree(p->d_rows);
   if (p->d_ent) cudaFree(p->d_ent);
   p->stage.release();
   if (p->stream) cudaStreamDestroy(p->stream);
