@@ -328,7 +328,7 @@ legendre_tc_kernel(const __grid_constant__ TcLaunch L) {
                 tma_load_3d(Ad, &L.amap[gi], ct * 128, x0 + 64 * q, sp, &full[s]);
                 tma_load_3d(Ad + 8192, &L.amap[gi], ct * 128 + 64, x0 + 64 * q, sp, &full[s]);
               }
-              const long long row0 = mi.base + ((long long)(p * mi.nq + q) * a.nsplit + sp) * mi.nr + nt * 128;
+              const long long row0 = mi.base + ((long long)(p * mi.nq + q) * a.nsplit + sp) * mi.nr + nt * a.brows;
               tma_load_2d(Bs + sp * B_SPLIT_BYTES, &L.map[gi], 0, (int)row0, &full[s]);
             }
           }
@@ -347,7 +347,7 @@ legendre_tc_kernel(const __grid_constant__ TcLaunch L) {
         int m, ct, nt;
         item_of(a, it - L.start[gi], m, ct, nt);
         const MInfo mi = a.mi[m];
-        const int nrow = min(128, mi.nr - nt * 128);
+        const int nrow = min(a.brows, mi.nr - nt * a.brows);
         const int amn = a.dir;  // forward A is MN-major
         const uint32_t idesc = idesc_f16kind(nrow, amn, a.nsplit == 3);
         const int ncross = a.nsplit == 3 ? 5 : 2;
@@ -415,7 +415,7 @@ legendre_tc_kernel(const __grid_constant__ TcLaunch L) {
       item_of(a, it - L.start[gi], m, ct, nt);
       const int C2B = 2 * a.batch;
       const MInfo mi = a.mi[m];
-      const int nrow = min(128, mi.nr - nt * 128);
+      const int nrow = min(a.brows, mi.nr - nt * a.brows);
       const int ab = a.nacc == 2 ? (li & 1) : 0;
       const int ar = a.nacc == 2 ? (li >> 1) : li;
       if (dead || !mbar_wait(&accf[ab], ar & 1, a.err, abort_flag, 4, L.wait_ns)) {
@@ -452,7 +452,7 @@ legendre_tc_kernel(const __grid_constant__ TcLaunch L) {
           if (c < C2B) {
 #pragma unroll
             for (int i = 0; i < 16; ++i) {
-              const int jj = nt * 128 + j0 + i;
+              const int jj = nt * a.brows + j0 + i;
               if (jj < a.Jh) {
                 a.F[((long long)m * J + (a.Jh + jj)) * C2B + c] = (e[i] + o[i]) * us;
                 a.F[((long long)m * J + (a.Jh - 1 - jj)) * C2B + c] = (e[i] - o[i]) * us;
@@ -466,9 +466,9 @@ legendre_tc_kernel(const __grid_constant__ TcLaunch L) {
         // writes the contiguous runs of n of field-levels w, w + 4, ...:
         // 16-byte stores of consecutive coefficients.
         float *erow = ep + row * EP_LD;
-        const int nbase = m + 2 * nt * 128;
+        const int nbase = m + 2 * nt * a.brows;
         for (int k0 = 0; k0 < nrow; k0 += 16) {
-          if (nt * 128 + k0 >= mi.nv0) break;  // nv0 >= nv1; uniform over the epilogue warps
+          if (nt * a.brows + k0 >= mi.nv0) break;  // nv0 >= nv1; uniform over the epilogue warps
           if (!dead) {
             if constexpr (EH == 1) {
               uint32_t r0[16], x0[16], r1[16], x1[16];
@@ -759,7 +759,7 @@ struct TabMeta {
   long long rows = 0, rows0 = 0;
 };
 
-static TabMeta make_meta(int dir, const Plan &P, const std::vector<int> &emax) {
+static TabMeta make_meta(int dir, const Plan &P, const std::vector<int> &emax, int tn) {
   const int N = P.N, Jh = P.Jh;
   TabMeta t;
   t.mi.resize(N + 1);
@@ -788,7 +788,7 @@ static TabMeta make_meta(int dir, const Plan &P, const std::vector<int> &emax) {
     t.rowstart[m] = r0;
     base += 2LL * M.nq * P.nsplit * M.nr;
     r0 += 2LL * M.nq * M.nr;
-    for (int nt = 0; nt < (M.nr + 127) / 128; ++nt) t.items.push_back(make_int4(m, 0, nt, 0));
+    for (int nt = 0; nt < (M.nr + tn - 1) / tn; ++nt) t.items.push_back(make_int4(m, 0, nt, 0));
   }
   t.rowstart[N + 1] = r0;
   t.rows = base;
@@ -842,7 +842,19 @@ static int build_one(Plan &P, int dir, TileTable &T) {
     cudaFree(de);
     for (int &e : emax) e = e < -1000 ? -1000 : e;  // an all-zero m: any scale
   }
-  TabMeta meta = make_meta(dir, P, emax);
+  // N rows of a tile (B box rows, TMEM columns of an accumulator): 64 where
+  // every tile fits, and always for the analysis, whose epilogue (through
+  // shared memory) then overlaps the next item's MMAs in the second
+  // accumulator set (T341 x 192 field-levels: 184 -> 162 us); the
+  // synthesis keeps 128-row tiles for larger tables (with 64 it reloads
+  // each spectra tile twice as often: 194 -> 214 us).
+  int nrmax = 16;
+  for (int m = 0; m <= P.N; ++m) {
+    const int nr = dir == 0 ? (P.Jh + 15) / 16 * 16 : (count_np(P.N, m, 0) + 15) / 16 * 16;
+    nrmax = nr > nrmax ? nr : nrmax;
+  }
+  const int tn = (nrmax <= 64 || dir == 1) ? 64 : 128;
+  TabMeta meta = make_meta(dir, P, emax, tn);
   T.rows = meta.rows;
   T.base.assign(P.N + 1, 0);
   for (int m = 0; m <= P.N; ++m) T.base[m] = meta.mi[m].base;
@@ -868,10 +880,8 @@ static int build_one(Plan &P, int dir, TileTable &T) {
   }
   DCCM_CUDA(cudaDeviceSynchronize());
   cudaFree(drs);
-  int nrmax = 16;
-  for (const MInfo &M : meta.mi) nrmax = M.nr > nrmax ? M.nr : nrmax;
-  T.ntmax = nrmax <= 64 ? 64 : 128;
-  {  // B boxes of ntmax rows: every N tile of an ntmax = 64 table fits 64
+  T.ntmax = tn;
+  {  // B boxes of ntmax rows
     const cuuint64_t dims[2] = {64, (cuuint64_t)meta.rows};
     const cuuint64_t str[1] = {128};
     const cuuint32_t box[2] = {64, (cuuint32_t)T.ntmax};
