@@ -599,11 +599,10 @@ FLUX_FP64_INSTR_PER_COLUMN = (1364340 + 3274416 + 2 * 5730228) / 45478
 
 
 # FP64 flops of the implicit-coupling sweeps per column and level, one
-# tracer (DADD + DMUL + 2 DFMA thread instructions per cycle x elapsed
-# cycles, ncu, 32768 columns x 32 levels):
-# per 32-level column forward 3915 (shared factors 878 + elimination 3037),
-# backward 1430.
-IMPLCPL_FP64_FLOPS = {"forward": 3915 / 32, "backward": 1430 / 32}
+# tracer (DADD + DMUL + 2 DFMA thread instructions, ncu sass counters,
+# 32768 columns x 32 levels): per 32-level column forward 3163 (shared
+# factors 502 + elimination 2661), backward 1058.
+IMPLCPL_FP64_FLOPS = {"forward": 3163 / 32, "backward": 1058 / 32}
 
 
 def dccm_stages():
