@@ -33,6 +33,7 @@ struct Tunables {
   int tc_ctas = 0;        // persistent CTAs of the tensor-core Legendre kernel (at most one wave)
   int tc_shape = 0;       // tensor-core Legendre kernel: 0 wide, 1 narrow where the table allows (2 CTAs an SM)
   int fft_bb = 0;         // warps per FFT CTA (4, 8, 16)
+  int fft_rpw = 0;        // row pairs per FFT warp where a row pair takes one warp (1, 2; 0: 1)
   int flux_threads = 0;   // threads per CTA of the bulk-flux kernel
   int flux_ctas = 0;      // CTA cap of the bulk-flux kernel's grid-stride loop (0: 16 per SM)
   int remap_threads = 0;  // threads per CTA of the remap kernel

@@ -854,10 +854,13 @@ int fft_multi(Plan *const *plans, const int *batch, const void *const *in, void 
               cudaStream_t s) {
   if (ngroups < 1 || ngroups > FFT_MAXG) return DCCM_ERR_UNSUPPORTED;
   // Warps per CTA (the fft_bb knob); each group fits as many row pairs as
-  // its warps per row allow (a power of two), within the smem budget.
+  // its warps per row allow (a power of two), within the smem budget.  The
+  // fft_rpw knob (2) gives each warp of a one-warp-per-row length two row
+  // pairs in turn: half the warps, one wave instead of 1.7 at c3.
   const size_t budget = 100 * 1024;
   const int tb = tunables().fft_bb;
   const int WPC = (tb == 4 || tb == 8 || tb == 16) ? tb : 8;
+  const int rpw = tunables().fft_rpw == 2 ? 2 : 1;
   int rmax = 2, warps = 1;
   for (int g = 0; g < ngroups; ++g)
     if (!fft_length_supported(plans[g]->I)) return DCCM_ERR_UNSUPPORTED;
@@ -869,12 +872,14 @@ int fft_multi(Plan *const *plans, const int *batch, const void *const *in, void 
     if (batch[g] <= 0) continue;
     const Plan &P = *plans[g];
     const int R = P.I / 32, W = fft_warps_per_row(R);
+    const int rp = W == 1 ? rpw : 1;
     int BB = 1;
-    while (2 * BB * W <= WPC && fft_smem(R, 2 * BB) <= budget) BB *= 2;
+    while (2 * BB * W <= WPC * rp && fft_smem(R, 2 * BB) <= budget) BB *= 2;
     int lbb = 0;
     while ((1 << lbb) < BB) ++lbb;
     rmax = R > rmax ? R : rmax;
-    warps = BB * W > warps ? BB * W : warps;
+    const int wg = (BB * W + rp - 1) / rp;
+    warps = wg > warps ? wg : warps;
     FftGroup &G = L.g[ng++];
     G.N = P.N;
     G.J = P.J;

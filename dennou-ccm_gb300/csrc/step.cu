@@ -1074,6 +1074,7 @@ static bool cache_lookup(const char *path, const std::string &key, Tunables &t) 
     if ((p = strstr(line, "\"tc_ctas\": "))) v.tc_ctas = atoi(p + 11);
     if ((p = strstr(line, "\"tc_shape\": "))) v.tc_shape = atoi(p + 12);
     if ((p = strstr(line, "\"fft_bb\": "))) v.fft_bb = atoi(p + 10);
+    if ((p = strstr(line, "\"fft_rpw\": "))) v.fft_rpw = atoi(p + 11);
     if ((p = strstr(line, "\"flux_threads\": "))) v.flux_threads = atoi(p + 16);
     if ((p = strstr(line, "\"remap_threads\": "))) v.remap_threads = atoi(p + 17);
     if ((p = strstr(line, "\"remap_fc\": "))) v.remap_fc = atoi(p + 12);
@@ -1092,10 +1093,11 @@ static void cache_store(const char *path, const std::string &key, const Tunables
   FILE *fp = fopen(path, "a");
   if (!fp) return;
   fprintf(fp,
-          "{\"key\": \"%s\", \"tc_shape\": %d, \"tc_ctas\": %d, \"fft_bb\": %d, \"flux_threads\": %d, \"remap_threads\": %d, "
+          "{\"key\": \"%s\", \"tc_shape\": %d, \"tc_ctas\": %d, \"fft_bb\": %d, \"fft_rpw\": %d, \"flux_threads\": %d, \"remap_threads\": %d, "
           "\"remap_fc\": %d, \"serial\": %d, \"flux_ctas\": %d, \"step_ms\": %.4f, "
           "\"stage_ms\": [%.4f, %.4f, %.4f, %.4f, %.4f, %.4f]}\n",
-          key.c_str(), t.tc_shape, t.tc_ctas, t.fft_bb, t.flux_threads, t.remap_threads, t.remap_fc, t.serial, t.flux_ctas,
+          key.c_str(), t.tc_shape, t.tc_ctas, t.fft_bb, t.fft_rpw, t.flux_threads, t.remap_threads, t.remap_fc, t.serial,
+          t.flux_ctas,
           step_ms, ms[0],
           ms[1], ms[2], ms[3], ms[4], ms[5]);
   fclose(fp);
@@ -1193,6 +1195,7 @@ extern "C" int dccm_step_autotune(dccm_step *st, const char *cache_path, int *ch
     Knob stage_knobs[] = {
         {&T.tc_shape, {0, 1}, 0, 4},
         {&T.tc_ctas, {2 * sms, sms, sms * 3 / 4, sms / 2}, 0, 4},
+        {&T.fft_rpw, {1, 2}, 1, 3},
         {&T.fft_bb, {16, 8, 4}, 1, 3},
         {&T.flux_threads, {64, 128, 256}, 5, 6},
         {&T.remap_fc, {3, 6, 2}, 4, 5},
@@ -1254,6 +1257,7 @@ extern "C" int dccm_tune_set(const char *knob, int value) {
   if (!strcmp(knob, "tc_ctas")) T.tc_ctas = value;
   else if (!strcmp(knob, "tc_shape")) T.tc_shape = value ? 1 : 0;
   else if (!strcmp(knob, "fft_bb")) T.fft_bb = value;
+  else if (!strcmp(knob, "fft_rpw")) T.fft_rpw = value;
   else if (!strcmp(knob, "flux_threads")) T.flux_threads = value;
   else if (!strcmp(knob, "remap_threads")) T.remap_threads = value;
   else if (!strcmp(knob, "remap_fc")) T.remap_fc = value;
@@ -1281,6 +1285,7 @@ extern "C" int dccm_tune_get(const char *knob, int *value) {
   if (!strcmp(knob, "tc_ctas")) *value = T.tc_ctas;
   else if (!strcmp(knob, "tc_shape")) *value = T.tc_shape;
   else if (!strcmp(knob, "fft_bb")) *value = T.fft_bb;
+  else if (!strcmp(knob, "fft_rpw")) *value = T.fft_rpw;
   else if (!strcmp(knob, "flux_threads")) *value = T.flux_threads;
   else if (!strcmp(knob, "remap_threads")) *value = T.remap_threads;
   else if (!strcmp(knob, "remap_fc")) *value = T.remap_fc;

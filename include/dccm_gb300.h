@@ -522,7 +522,8 @@ int dccm_step_autotune_host(dccm_step *step, void *stream, const dccm_host_copy 
  * epilogue warps, 1 runs it two CTAs an SM with one load stage and four
  * epilogue warps where its tables allow (N tiles of at most 64 rows, e.g.
  * up to T85 on its Gaussian grid); "tc_ctas": persistent CTAs of
- * that kernel, at most one wave, "fft_bb": warps per FFT CTA
+ * that kernel, at most one wave, "fft_rpw": row pairs per FFT warp for
+ * rows of one warp (I <= 384; 1 or 2, in turn), "fft_bb": warps per FFT CTA
  * (4, 8 or 16), "flux_threads", "remap_threads": CTA sizes, "remap_fc":
  * fields per thread of the remap, 1, 2, 3, 4 or 6), then "serial"
  * (1: ordinary launches instead of programmatic dependent launches along
@@ -535,7 +536,7 @@ int dccm_step_autotune_host(dccm_step *step, void *stream, const dccm_host_copy 
  * from / appended to that file (one JSON object per line, keyed by the
  * GPU name and SM count and the step's shapes).  chosen (4 ints, may be
  * NULL) receives tc_ctas, fft_bb, flux_threads, remap_threads (read
- * "serial", "flux_ctas", "remap_fc" and "tc_shape" with dccm_tune_get).  The knobs are
+ * "serial", "flux_ctas", "remap_fc", "tc_shape" and "fft_rpw" with dccm_tune_get).  The knobs are
  * process-wide defaults of later launches too. */
 int dccm_step_autotune(dccm_step *step, const char *cache_path, int *chosen);
 /* Process-wide knobs of later launches (and of graphs recorded later): the

@@ -195,3 +195,30 @@ def test_zero_and_single_field_level(dccm, oracle, synth, cuda, prec):
     assert rel_l2(g, go) <= tol
     assert rel_l2(plan.forward(go), oracle.sht_forward(N, I, J, go)) <= tol
     assert plan.status() == (0, 0)
+
+
+@pytest.mark.parametrize("rpw,bb", [(2, 4), (2, 8), (2, 16), (1, 4)])
+@pytest.mark.parametrize("N,I,J", TRUNC + [(127, 384, 192)])
+def test_fft_launch_shapes_match_oracle(dccm, oracle, synth, N, I, J, rpw, bb):
+    """Every FFT launch shape the autotuner can pick (warps per CTA, two
+    row pairs a warp for the one-warp lengths): the same results, with a
+    batch that leaves the last CTA of field-levels partial (13 field-levels,
+    CTAs of 4 to 32)."""
+    B = 13
+    s = synth.spectra(N, B, seed=N + 5)
+    saved = {k: dccm.tune_get(k) for k in ("fft_rpw", "fft_bb")}
+    try:
+        dccm.tune_set("fft_rpw", rpw)
+        dccm.tune_set("fft_bb", bb)
+        plan = dccm.ShtPlan(N, I, J, 1, B)
+        g = plan.inverse(s)
+        go = oracle.sht_inverse(N, I, J, s)
+        s2 = plan.forward(go)
+        so = oracle.sht_forward(N, I, J, go)
+        assert plan.status() == (0, 0)
+        assert rel_l2(g, go) <= 2e-6 and rel_l2(s2, so) <= 2e-6
+        for b in range(B):
+            assert rel_l2(g[b], go[b]) <= 4e-6 and rel_l2(s2[b], so[b]) <= 4e-6, b
+    finally:
+        for k, v in saved.items():
+            dccm.tune_set(k, v)

@@ -187,8 +187,8 @@ def test_remap_two_level_destination(dccm, oracle, synth, cuda):
 
 def test_autotune_keeps_results_and_caches(dccm, oracle, synth, cuda, tmp_path):
     """Every launch shape the autotuner can pick (Legendre CTA count, FFT
-    CTA size, flux and remap CTA sizes, plain or programmatic dependent
-    launches) computes each output element the same way, so the step's
+    CTA size and row pairs per warp, flux and remap CTA sizes, plain or
+    programmatic dependent launches) computes each output element the same way, so the step's
     outputs are bit-identical before and after tuning; the cache file
     returns the same choice on a second call."""
     torch = cuda
@@ -203,12 +203,13 @@ def test_autotune_keeps_results_and_caches(dccm, oracle, synth, cuda, tmp_path):
         torch.cuda.synchronize()
         return [o.cpu().clone() for o in outs]
 
-    saved = {k: dccm.tune_get(k) for k in dccm.Step.KNOBS + ["serial", "flux_ctas", "remap_fc", "tc_shape"]}
+    extra = ["serial", "flux_ctas", "remap_fc", "tc_shape", "fft_rpw"]
+    saved = {k: dccm.tune_get(k) for k in dccm.Step.KNOBS + extra}
     try:
         want = run()
         cache = str(tmp_path / "tune.jsonl")
         first = step.autotune(cache)
-        assert set(first) == set(dccm.Step.KNOBS + ["serial", "flux_ctas", "remap_fc", "tc_shape"])
+        assert set(first) == set(dccm.Step.KNOBS + extra)
         assert first["serial"] in (0, 1)
         assert all(torch.equal(a, b) for a, b in zip(run(), want))
         line = open(cache).read()
@@ -218,7 +219,7 @@ def test_autotune_keeps_results_and_caches(dccm, oracle, synth, cuda, tmp_path):
         # at a few CTAs (each walks many columns), gives the same bits
         for knob, v in (("serial", 0), ("serial", 1), ("flux_ctas", 3), ("remap_fc", 1), ("remap_fc", 6),
                         ("remap_fc", 4), ("remap_threads", 32), ("tc_shape", 1), ("tc_shape", 0),
-                        ("tc_ctas", 7)):
+                        ("tc_ctas", 7), ("fft_rpw", 2), ("fft_bb", 4), ("fft_bb", 16), ("fft_rpw", 1)):
             dccm.tune_set(knob, v)
             S = bench.gpu_setup(w, inp, dccm, synth, torch, torch.device("cuda", 0))
             step = S["steps"]["mixed"]
