@@ -637,6 +637,11 @@ template <int W> __device__ __forceinline__ int mw_k1(int wq, int j) {
   return (j & 1) ? (b ? MW_R0 - b : 4) : b;
 }
 
+// A CTA's warps form groups of W, one row pair per group at a time; with
+// more row pairs than groups (the fft_rpw knob) a group takes them in
+// rounds, every round ending at a CTA barrier before the group's exchange
+// buffer is written again.  More field-levels a CTA make the forward's G3
+// runs longer (a whole 32-byte sector per BF16 plane from 8 field-levels).
 template <int W>
 __device__ __forceinline__ void fft_inv_block_mwp(const FftGroup &G, int jj, int by, float *st) {
   constexpr int R = MW_R0 * W, I = 32 * R, L = 32 * W, NK = MW_R0 / W;
@@ -649,49 +654,54 @@ __device__ __forceinline__ void fft_inv_block_mwp(const FftGroup &G, int jj, int
   stage_z<R>(G, jn, js, b0, nb, zs);
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int bl = warp / W, wq = warp % W;
-  const bool own = bl < G.BB;
-  float2 *xb = zs + (size_t)G.BB * ZB + (size_t)(own ? bl : 0) * MW_R0 * W * 32;
+  const int ng = (int)(blockDim.x >> 5) / W, grp = warp / W, wq = warp % W;
+  float2 *xb = zs + (size_t)G.BB * ZB + (size_t)grp * MW_R0 * W * 32;
   float2 w[5];
   lane_twiddles<R>(G.tw, lane, true, w);
-  float2 v[MW_R0];  // v[j W + k_w]
-#pragma unroll
-  for (int j = 0; j < NK; ++j)
-#pragma unroll
-    for (int kw = 0; kw < W; ++kw)
-      v[j * W + kw] = own ? zs[bl * ZB + (mw_k1<W>(wq, j) + MW_R0 * kw) * ZQ + lane] : make_float2(0.f, 0.f);
-  lane_dit<MW_R0>(v, w, lane);
-#pragma unroll
-  for (int kw = 1; kw < W; ++kw) {
-    const float2 tq = twid(G.tw, lane * kw * (I / L), +1);
-#pragma unroll
-    for (int j = 0; j < NK; ++j) v[j * W + kw] = cmul(v[j * W + kw], tq);
-  }
-#pragma unroll
-  for (int j = 0; j < NK; ++j) RegDft<W>::run(v + j * W, G.tw, I, +1);
-  if (own) {
+  const int t = 32 * wq + lane;
+  const int rounds = (G.BB + ng - 1) / ng;
+  for (int rd = 0; rd < rounds; ++rd) {
+    const int bl = rd * ng + grp;
+    const bool own = grp < ng && bl < G.BB;  // this group has a staged spectrum this round
+    float2 v[MW_R0];  // v[j W + k_w]
 #pragma unroll
     for (int j = 0; j < NK; ++j)
 #pragma unroll
-      for (int tx = 0; tx < W; ++tx) xb[(mw_k1<W>(wq, j) * W + tx) * 32 + lane] = v[j * W + tx];
-  }
-  __syncthreads();
-  if (own) {
+      for (int kw = 0; kw < W; ++kw)
+        v[j * W + kw] = own ? zs[bl * ZB + (mw_k1<W>(wq, j) + MW_R0 * kw) * ZQ + lane] : make_float2(0.f, 0.f);
+    lane_dit<MW_R0>(v, w, lane);
 #pragma unroll
-    for (int k1 = 0; k1 < MW_R0; ++k1) v[k1] = xb[(k1 * W + wq) * 32 + lane];
-  }
-  const int t = 32 * wq + lane;
+    for (int kw = 1; kw < W; ++kw) {
+      const float2 tq = twid(G.tw, lane * kw * (I / L), +1);
 #pragma unroll
-  for (int k1 = 1; k1 < MW_R0; ++k1) v[k1] = cmul(v[k1], twid(G.tw, t * k1, +1));
-  RegDft<MW_R0>::run(v, G.tw, I, +1);
-  if (bl < nb) {
-    double *gn = static_cast<double *>(G.out) + ((long long)(b0 + bl) * J + jn) * I;
-    double *gs = static_cast<double *>(G.out) + ((long long)(b0 + bl) * J + js) * I;
-#pragma unroll
-    for (int r = 0; r < MW_R0; ++r) {
-      gn[L * r + t] = f32_to_f64(v[r].x);
-      gs[L * r + t] = f32_to_f64(v[r].y);
+      for (int j = 0; j < NK; ++j) v[j * W + kw] = cmul(v[j * W + kw], tq);
     }
+#pragma unroll
+    for (int j = 0; j < NK; ++j) RegDft<W>::run(v + j * W, G.tw, I, +1);
+    if (own) {
+#pragma unroll
+      for (int j = 0; j < NK; ++j)
+#pragma unroll
+        for (int tx = 0; tx < W; ++tx) xb[(mw_k1<W>(wq, j) * W + tx) * 32 + lane] = v[j * W + tx];
+    }
+    __syncthreads();
+    if (own) {
+#pragma unroll
+      for (int k1 = 0; k1 < MW_R0; ++k1) v[k1] = xb[(k1 * W + wq) * 32 + lane];
+    }
+#pragma unroll
+    for (int k1 = 1; k1 < MW_R0; ++k1) v[k1] = cmul(v[k1], twid(G.tw, t * k1, +1));
+    RegDft<MW_R0>::run(v, G.tw, I, +1);
+    if (own && bl < nb) {
+      double *gn = static_cast<double *>(G.out) + ((long long)(b0 + bl) * J + jn) * I;
+      double *gs = static_cast<double *>(G.out) + ((long long)(b0 + bl) * J + js) * I;
+#pragma unroll
+      for (int r = 0; r < MW_R0; ++r) {
+        gn[L * r + t] = f32_to_f64(v[r].x);
+        gs[L * r + t] = f32_to_f64(v[r].y);
+      }
+    }
+    if (rd + 1 < rounds) __syncthreads();  // the exchange buffer is read before the next round writes it
   }
 }
 
@@ -703,75 +713,79 @@ __device__ __forceinline__ void fft_fwd_block_mwp(const FftGroup &G, int jj, int
   const int b0 = by * G.BB;
   const int nb = min(G.BB, G.batch - b0);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int bl = warp / W, wq = warp % W;
-  const bool own = bl < G.BB;
+  const int ng = (int)(blockDim.x >> 5) / W, grp = warp / W, wq = warp % W;
   const int kl = brev5(lane);
   const int t = 32 * wq + lane;
-  float2 *xb = reinterpret_cast<float2 *>(st + 4 * G.BB * PS) + (size_t)(own ? bl : 0) * MW_R0 * W * 32;
-  float2 v[MW_R0];
-  if (bl < nb) {
-    const double *gn = static_cast<const double *>(G.in) + ((long long)(b0 + bl) * J + jn) * I;
-    const double *gs = static_cast<const double *>(G.in) + ((long long)(b0 + bl) * J + js) * I;
-    double xn[MW_R0], xs[MW_R0];  // all loads first, then the conversions
-#pragma unroll
-    for (int r = 0; r < MW_R0; ++r) {
-      xn[r] = gn[L * r + t];
-      xs[r] = gs[L * r + t];
-    }
-#pragma unroll
-    for (int r = 0; r < MW_R0; ++r) v[r] = make_float2(f64_to_f32_rn(xn[r]), f64_to_f32_rn(xs[r]));
-  } else {
-#pragma unroll
-    for (int r = 0; r < MW_R0; ++r) v[r] = make_float2(0.f, 0.f);
-  }
-  RegDft<MW_R0>::run(v, G.tw, I, -1);
-#pragma unroll
-  for (int k1 = 1; k1 < MW_R0; ++k1) v[k1] = cmul(v[k1], twid(G.tw, t * k1, -1));
-  if (own) {
-#pragma unroll
-    for (int k1 = 0; k1 < MW_R0; ++k1) xb[(k1 * W + wq) * 32 + lane] = v[k1];
-  }
-  __syncthreads();
-  if (own) {
-#pragma unroll
-    for (int j = 0; j < NK; ++j)
-#pragma unroll
-      for (int tx = 0; tx < W; ++tx) v[j * W + tx] = xb[(mw_k1<W>(wq, j) * W + tx) * 32 + lane];
-  }
-#pragma unroll
-  for (int j = 0; j < NK; ++j) RegDft<W>::run(v + j * W, G.tw, I, -1);
-#pragma unroll
-  for (int kw = 1; kw < W; ++kw) {
-    const float2 tq = twid(G.tw, lane * kw * (I / L), -1);
-#pragma unroll
-    for (int j = 0; j < NK; ++j) v[j * W + kw] = cmul(v[j * W + kw], tq);
-  }
+  float2 *xb = reinterpret_cast<float2 *>(st + 4 * G.BB * PS) + (size_t)grp * MW_R0 * W * 32;
   float2 w[5];
   lane_twiddles<R>(G.tw, lane, false, w);
-  lane_dif<MW_R0>(v, w, lane);
-  // Z[I - m] for m = k1 + 8 k_w + R kl, all within the warp:
-  //   k1 in {1, 2, 3, 5, 6, 7}: register (partner j, W-1-k_w), lane 31 - l;
-  //   k1 = 4: register (j, W-1-k_w), lane 31 - l;
-  //   k1 = 0: register (j, W-k_w), lane 31 - l; for k_w = 0 register (j, 0),
-  //   lane brev5(32 - kl).
   const int src0 = brev5((32 - kl) & 31);
   const float invI = 1.f / (float)I;
+  const int rounds = (G.BB + ng - 1) / ng;
+  for (int rd = 0; rd < rounds; ++rd) {
+    const int bl = rd * ng + grp;
+    const bool own = grp < ng && bl < G.BB;  // this group has an exchange slot and staging planes this round
+    float2 v[MW_R0];
+    if (own && bl < nb) {
+      const double *gn = static_cast<const double *>(G.in) + ((long long)(b0 + bl) * J + jn) * I;
+      const double *gs = static_cast<const double *>(G.in) + ((long long)(b0 + bl) * J + js) * I;
+      double xn[MW_R0], xs[MW_R0];  // all loads first, then the conversions
 #pragma unroll
-  for (int j = 0; j < NK; ++j) {
-    const bool paired = mw_base<W>(wq, j) != 0;  // warp-uniform
-    const int k1 = mw_k1<W>(wq, j);
+      for (int r = 0; r < MW_R0; ++r) {
+        xn[r] = gn[L * r + t];
+        xs[r] = gs[L * r + t];
+      }
 #pragma unroll
-    for (int kw = 0; kw < W; ++kw) {
-      float2 zc;
-      if (paired) zc = shfl_c(v[(j ^ 1) * W + (W - 1 - kw)], 31 - lane);
-      else if (j & 1) zc = shfl_c(v[j * W + (W - 1 - kw)], 31 - lane);
-      else zc = kw ? shfl_c(v[j * W + (W - kw)], 31 - lane) : shfl_c(v[j * W], src0);
-      const int q = k1 + MW_R0 * kw;
-      const int m = q + R * kl;
-      if (bl < nb && m <= N) store_eo<R>(st, G.BB, bl, m, q * 17 + kl, v[j * W + kw], zc, invI);
+      for (int r = 0; r < MW_R0; ++r) v[r] = make_float2(f64_to_f32_rn(xn[r]), f64_to_f32_rn(xs[r]));
+    } else {
+#pragma unroll
+      for (int r = 0; r < MW_R0; ++r) v[r] = make_float2(0.f, 0.f);
     }
+    RegDft<MW_R0>::run(v, G.tw, I, -1);
+#pragma unroll
+    for (int k1 = 1; k1 < MW_R0; ++k1) v[k1] = cmul(v[k1], twid(G.tw, t * k1, -1));
+    if (own) {
+#pragma unroll
+      for (int k1 = 0; k1 < MW_R0; ++k1) xb[(k1 * W + wq) * 32 + lane] = v[k1];
+    }
+    __syncthreads();
+    if (own) {
+#pragma unroll
+      for (int j = 0; j < NK; ++j)
+#pragma unroll
+        for (int tx = 0; tx < W; ++tx) v[j * W + tx] = xb[(mw_k1<W>(wq, j) * W + tx) * 32 + lane];
+    }
+#pragma unroll
+    for (int j = 0; j < NK; ++j) RegDft<W>::run(v + j * W, G.tw, I, -1);
+#pragma unroll
+    for (int kw = 1; kw < W; ++kw) {
+      const float2 tq = twid(G.tw, lane * kw * (I / L), -1);
+#pragma unroll
+      for (int j = 0; j < NK; ++j) v[j * W + kw] = cmul(v[j * W + kw], tq);
+    }
+    lane_dif<MW_R0>(v, w, lane);
+    // Z[I - m] for m = k1 + 8 k_w + R kl, all within the warp:
+    //   k1 in {1, 2, 3, 5, 6, 7}: register (partner j, W-1-k_w), lane 31 - l;
+    //   k1 = 4: register (j, W-1-k_w), lane 31 - l;
+    //   k1 = 0: register (j, W-k_w), lane 31 - l; for k_w = 0 register (j, 0),
+    //   lane brev5(32 - kl).
+#pragma unroll
+    for (int j = 0; j < NK; ++j) {
+      const bool paired = mw_base<W>(wq, j) != 0;  // warp-uniform
+      const int k1 = mw_k1<W>(wq, j);
+#pragma unroll
+      for (int kw = 0; kw < W; ++kw) {
+        float2 zc;
+        if (paired) zc = shfl_c(v[(j ^ 1) * W + (W - 1 - kw)], 31 - lane);
+        else if (j & 1) zc = shfl_c(v[j * W + (W - 1 - kw)], 31 - lane);
+        else zc = kw ? shfl_c(v[j * W + (W - kw)], 31 - lane) : shfl_c(v[j * W], src0);
+        const int q = k1 + MW_R0 * kw;
+        const int m = q + R * kl;
+        if (own && bl < nb && m <= N) store_eo<R>(st, G.BB, bl, m, q * 17 + kl, v[j * W + kw], zc, invI);
+      }
+    }
+    __syncthreads();  // the exchange buffer is read before the next round writes it; the planes are complete
   }
-  __syncthreads();
   write_g3<R>(G, jj, b0, nb, st);
 }
 
@@ -835,16 +849,17 @@ __global__ void __launch_bounds__(512, 2) fft_multi_kernel(const __grid_constant
   }
 }
 
-// Warps per row pair and shared memory of one CTA: four planes of 17 R + 1
-// floats per field-level, and for rows over several warps the exchange
-// buffer of 8 x W x 32 complex values per row pair.
+// Warps per row pair and shared memory of one CTA: the staged spectra
+// (inverse) or the E/O planes (forward) of its bb row pairs, and for rows
+// over several warps the exchange buffers, 8 x W x 32 complex values for
+// each of the CTA's nx warp groups (W = 3: one per row pair).
 static int fft_warps_per_row(int R) { return R >= 16 ? R / MW_R0 : 1; }
-static size_t fft_smem(int R, int bb) {
+static size_t fft_smem(int R, int bb, int nx) {
   const int W = fft_warps_per_row(R);
   const size_t planes = (size_t)4 * bb * (R * 17 + 1) * sizeof(float);  // forward: E/O planes
   const size_t zs = (size_t)bb * (33 * R + 1) * sizeof(float2);          // inverse: staged spectra
   size_t s = planes > zs ? planes : zs;
-  if (W > 1) s += (size_t)bb * MW_R0 * W * 32 * sizeof(float2);
+  if (W > 1) s += (size_t)(W == 3 ? bb : nx) * MW_R0 * W * 32 * sizeof(float2);
   return s;
 }
 
@@ -855,9 +870,10 @@ int fft_multi(Plan *const *plans, const int *batch, const void *const *in, void 
   if (ngroups < 1 || ngroups > FFT_MAXG) return DCCM_ERR_UNSUPPORTED;
   // Warps per CTA (the fft_bb knob); each group fits as many row pairs as
   // its warps per row allow (a power of two), within the smem budget.  The
-  // fft_rpw knob (2) gives each warp of a one-warp-per-row length two row
-  // pairs in turn: half the warps, one wave instead of 1.7 at c3.
-  const size_t budget = 100 * 1024;
+  // fft_rpw knob (2) gives each warp (group of W warps) two row pairs in
+  // turn: half the warps for the same row pairs, twice the field-levels a
+  // CTA (W = 3 rows keep one row pair a group).
+  const size_t budget = 110 * 1024;  // two CTAs an SM
   const int tb = tunables().fft_bb;
   const int WPC = (tb == 4 || tb == 8 || tb == 16) ? tb : 8;
   const int rpw = tunables().fft_rpw == 2 ? 2 : 1;
@@ -872,9 +888,9 @@ int fft_multi(Plan *const *plans, const int *batch, const void *const *in, void 
     if (batch[g] <= 0) continue;
     const Plan &P = *plans[g];
     const int R = P.I / 32, W = fft_warps_per_row(R);
-    const int rp = W == 1 ? rpw : 1;
+    const int rp = W == 3 ? 1 : rpw;
     int BB = 1;
-    while (2 * BB * W <= WPC * rp && fft_smem(R, 2 * BB) <= budget) BB *= 2;
+    while (2 * BB * W <= WPC * rp && fft_smem(R, 2 * BB, WPC / W) <= budget) BB *= 2;
     int lbb = 0;
     while ((1 << lbb) < BB) ++lbb;
     rmax = R > rmax ? R : rmax;
@@ -899,10 +915,13 @@ int fft_multi(Plan *const *plans, const int *batch, const void *const *in, void 
     if (fwd && P.nsplit == 2)
       DCCM_TRY(field_exponents(static_cast<const double *>(in[g]), (long long)P.J * P.I, batch[g], P.d_cexp + P.max_batch, s));
     nblk += P.Jh * ((batch[g] + BB - 1) / BB);
-    const size_t sm = fft_smem(G.R, BB);
-    smem = sm > smem ? sm : smem;
   }
   L.ngroups = ng;
+  // the kernel forms warps / W groups of W warps whatever this group needed
+  for (int g = 0; g < ng; ++g) {
+    const size_t sm = fft_smem(L.g[g].R, L.g[g].BB, warps / L.g[g].W);
+    smem = sm > smem ? sm : smem;
+  }
   if (nblk == 0) return DCCM_OK;
   auto go = [&](auto kernel) -> int {
     DCCM_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

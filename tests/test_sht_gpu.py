@@ -198,12 +198,12 @@ def test_zero_and_single_field_level(dccm, oracle, synth, cuda, prec):
 
 
 @pytest.mark.parametrize("rpw,bb", [(2, 4), (2, 8), (2, 16), (1, 4)])
-@pytest.mark.parametrize("N,I,J", TRUNC + [(127, 384, 192)])
+@pytest.mark.parametrize("N,I,J", TRUNC + LONG)
 def test_fft_launch_shapes_match_oracle(dccm, oracle, synth, N, I, J, rpw, bb):
     """Every FFT launch shape the autotuner can pick (warps per CTA, two
-    row pairs a warp for the one-warp lengths): the same results, with a
+    row pairs a warp or a warp group in turn): the same results, with a
     batch that leaves the last CTA of field-levels partial (13 field-levels,
-    CTAs of 4 to 32)."""
+    CTAs of 1 to 32)."""
     B = 13
     s = synth.spectra(N, B, seed=N + 5)
     saved = {k: dccm.tune_get(k) for k in ("fft_rpw", "fft_bb")}
