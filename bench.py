@@ -442,12 +442,12 @@ def host_copies(S, groups, dccm, torch):
 # algorithmic bytes; the L2 bytes of the same launches (lts__t_bytes.sum,
 # every request L2 serves) are reported beside them.
 TRAFFIC = {
-    "c3": {"legendre_inverse": 7685888 + 12132608, "fft_inverse": 11304192, "fft_forward": 33599488 + 10496,
-           "legendre_forward": 18938112, "remap": 4120320, "bulk_flux": 7707392},
+    "c3": {"legendre_inverse": 7685632 + 12131072, "fft_inverse": 11304192, "fft_forward": 33602304,
+           "legendre_forward": 18938368, "remap": 3995904, "bulk_flux": 7722240},
 }
 L2_BYTES = {
-    "c3": {"legendre_inverse": 30906464 + 50166720, "fft_inverse": 83859552, "fft_forward": 105713056,
-           "legendre_forward": 43206016, "remap": 16645600, "bulk_flux": 40529280},
+    "c3": {"legendre_inverse": 30760000 + 49978368, "fft_inverse": 85293248, "fft_forward": 79587712,
+           "legendre_forward": 43426816, "remap": 20492224, "bulk_flux": 41896288},
 }
 TRAFFIC_SOURCE = "ncu of bench.py --workload c3 --profile-steps 3, third replay (profiles/step_c3_launches.md)"
 # FP64 peak: measured on the device by dccm_fp64_peak (independent DFMA
@@ -611,13 +611,14 @@ def dccm_stages():
 
 def profile_run(args, w, inp):
     """Graph replays of the mixed-precision step only (default launch
-    shapes, no autotuning, no host copies): a small, countable launch
-    sequence for ncu.  Each replay launches, in order, the spectra pack,
-    Legendre synthesis, inverse FFT, forward FFT, Legendre analysis, one
-    remap per truncation group and the flux kernel."""
+    shapes or --knobs, no autotuning, no host copies): a small, countable
+    launch sequence for ncu.  Each replay launches, in order, the spectra
+    pack, Legendre synthesis, inverse FFT, forward FFT, Legendre analysis,
+    one remap per truncation group and the flux kernel."""
     import torch
     dccm = importlib.import_module("dennou-ccm_gb300")
     synth = importlib.import_module("dennou-ccm_gb300.synth")
+    set_knobs(dccm, args.knobs)
     dev = torch.device("cuda", 0)
     S = gpu_setup(w, inp, dccm, synth, torch, dev)
     step = S["steps"]["mixed"]
@@ -646,7 +647,14 @@ def profile_run(args, w, inp):
 GAUSSIAN_GRIDS = {21: (64, 32), 42: (128, 64), 63: (192, 96), 85: (256, 128), 170: (512, 256), 341: (1024, 512)}
 
 
-def profile_sht(spec):
+def set_knobs(dccm, knobs):
+    """"k=v,k=v" -> dccm_tune_set for each (the profiling modes' launch shapes)."""
+    for kv in filter(None, knobs.split(",")):
+        k, v = kv.split("=")
+        dccm.tune_set(k.strip(), int(v))
+
+
+def profile_sht(spec, knobs=""):
     """Mixed-precision transforms only, for ncu on a small case: "N:B"
     (truncation, field-levels) on the truncation's Gaussian grid; three
     inverse + forward round trips on the device (each: the spectra pack,
@@ -654,6 +662,7 @@ def profile_sht(spec):
     import torch
     dccm = importlib.import_module("dennou-ccm_gb300")
     synth = importlib.import_module("dennou-ccm_gb300.synth")
+    set_knobs(dccm, knobs)
     N, B = (int(x) for x in spec.split(":"))
     I, J = GAUSSIAN_GRIDS[N]
     plan = dccm.ShtPlan(N, I, J, dccm.SHT_MIXED, max_batch=B)
@@ -938,9 +947,11 @@ def main():
                     help="only replay the mixed step this many times (for ncu) and exit")
     ap.add_argument("--profile-sht", default=None, metavar="N:B",
                     help="only run 3 mixed SHT round trips of B field-levels at truncation N (for ncu) and exit")
+    ap.add_argument("--knobs", default="", metavar="K=V,...",
+                    help="launch-shape knobs (dccm_tune_set) for --profile-steps / --profile-sht")
     args = ap.parse_args()
     if args.profile_sht:
-        profile_sht(args.profile_sht)
+        profile_sht(args.profile_sht, args.knobs)
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
