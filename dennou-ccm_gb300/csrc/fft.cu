@@ -639,8 +639,8 @@ template <int W> __device__ __forceinline__ int mw_k1(int wq, int j) {
 
 // A CTA's warps form groups of W, one row pair per group at a time; with
 // more row pairs than groups (the fft_rpw knob) a group takes them in
-// rounds, every round ending at a CTA barrier before the group's exchange
-// buffer is written again.  More field-levels a CTA make the forward's G3
+// turns (passes), every pass ending at a CTA barrier before the group's
+// exchange buffer is written again.  More field-levels a CTA make the forward's G3
 // runs longer (a whole 32-byte sector per BF16 plane from 8 field-levels).
 template <int W>
 __device__ __forceinline__ void fft_inv_block_mwp(const FftGroup &G, int jj, int by, float *st) {
@@ -659,10 +659,10 @@ __device__ __forceinline__ void fft_inv_block_mwp(const FftGroup &G, int jj, int
   float2 w[5];
   lane_twiddles<R>(G.tw, lane, true, w);
   const int t = 32 * wq + lane;
-  const int rounds = (G.BB + ng - 1) / ng;
-  for (int rd = 0; rd < rounds; ++rd) {
+  const int passes = (G.BB + ng - 1) / ng;
+  for (int rd = 0; rd < passes; ++rd) {
     const int bl = rd * ng + grp;
-    const bool own = grp < ng && bl < G.BB;  // this group has a staged spectrum this round
+    const bool own = grp < ng && bl < G.BB;  // this group has a staged spectrum in this pass
     float2 v[MW_R0];  // v[j W + k_w]
 #pragma unroll
     for (int j = 0; j < NK; ++j)
@@ -701,7 +701,7 @@ __device__ __forceinline__ void fft_inv_block_mwp(const FftGroup &G, int jj, int
         gs[L * r + t] = f32_to_f64(v[r].y);
       }
     }
-    if (rd + 1 < rounds) __syncthreads();  // the exchange buffer is read before the next round writes it
+    if (rd + 1 < passes) __syncthreads();  // the exchange buffer is read before the next pass writes it
   }
 }
 
@@ -721,10 +721,10 @@ __device__ __forceinline__ void fft_fwd_block_mwp(const FftGroup &G, int jj, int
   lane_twiddles<R>(G.tw, lane, false, w);
   const int src0 = brev5((32 - kl) & 31);
   const float invI = 1.f / (float)I;
-  const int rounds = (G.BB + ng - 1) / ng;
-  for (int rd = 0; rd < rounds; ++rd) {
+  const int passes = (G.BB + ng - 1) / ng;
+  for (int rd = 0; rd < passes; ++rd) {
     const int bl = rd * ng + grp;
-    const bool own = grp < ng && bl < G.BB;  // this group has an exchange slot and staging planes this round
+    const bool own = grp < ng && bl < G.BB;  // this group has an exchange slot and staging planes in this pass
     float2 v[MW_R0];
     if (own && bl < nb) {
       const double *gn = static_cast<const double *>(G.in) + ((long long)(b0 + bl) * J + jn) * I;
@@ -784,7 +784,7 @@ __device__ __forceinline__ void fft_fwd_block_mwp(const FftGroup &G, int jj, int
         if (own && bl < nb && m <= N) store_eo<R>(st, G.BB, bl, m, q * 17 + kl, v[j * W + kw], zc, invI);
       }
     }
-    __syncthreads();  // the exchange buffer is read before the next round writes it; the planes are complete
+    __syncthreads();  // the exchange buffer is read before the next pass writes it; the planes are complete
   }
   write_g3<R>(G, jj, b0, nb, st);
 }
