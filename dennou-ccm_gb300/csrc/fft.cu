@@ -482,7 +482,7 @@ constexpr int MW_R0 = 8;
 
 template <int W>
 __device__ __forceinline__ void fft_inv_block_mw(const FftGroup &G, int jj, int by, float *st) {
-  constexpr int R = MW_R0 * W, I = 32 * R, L = 32 * W, PS = R * 17 + 1;
+  constexpr int R = MW_R0 * W, I = 32 * R, L = 32 * W;
   constexpr int ZB = zs_stride<R>();
   const int J = G.J, Jh = J / 2;
   const int jn = Jh + jj, js = Jh - 1 - jj;
