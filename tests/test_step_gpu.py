@@ -292,3 +292,34 @@ def test_coupled_step_matches_pieces(dccm, oracle, synth, cuda):
             dccm.tune_set("upload_order", 0)
         for (h, _), k in zip(d2h, out):
             assert torch.equal(h, want[k].cpu()), (order, k)
+
+
+@pytest.mark.parametrize("rpw", [1, 2])
+def test_ensemble_mixed_row_lengths_match_oracle(dccm, oracle, synth, cuda, rpw):
+    """One FFT launch over groups of one-warp and several-warp rows (T42:
+    I = 128, T170: I = 512 over two warps, T255: I = 768 over three, T85:
+    I = 256): the launch's CTA size is the largest any group needs, the
+    other groups' extra warps idle, each group's exchange buffers are sized
+    for the launch's warp groups; with two row pairs a warp (group) or one.
+    Mixed path against the oracle at the long-row tolerance."""
+    torch = cuda
+    groups = [(42, 128, 64, 5), (170, 512, 256, 3), (255, 768, 384, 2), (85, 256, 128, 7)]
+    saved = dccm.tune_get("fft_rpw")
+    try:
+        dccm.tune_set("fft_rpw", rpw)
+        ens = dccm.Ensemble(groups, 1)
+        specs = [synth.spectra(N, B, seed=N + 7) for N, I, J, B in groups]
+        ds = [torch.from_numpy(s.view(np.float64).copy()).cuda() for s in specs]
+        dg = [torch.empty((B, J, I), dtype=torch.float64, device="cuda") for N, I, J, B in groups]
+        ds2 = [torch.empty_like(x) for x in ds]
+        batch = [B for *_, B in groups]
+        ens.inverse_dev(ds, dg, batch)
+        ens.forward_dev(dg, ds2, batch)
+        torch.cuda.synchronize()
+        assert ens.status() == (0, 0)
+        for (N, I, J, B), s, g, s2 in zip(groups, specs, dg, ds2):
+            go = oracle.sht_inverse(N, I, J, s)
+            assert rel_l2(g.cpu().numpy(), go) <= 2e-6, N
+            assert rel_l2(s2.cpu().numpy().view(np.complex128), s) <= 2e-6, N
+    finally:
+        dccm.tune_set("fft_rpw", saved)
