@@ -3,7 +3,8 @@
 // equatorial symmetry, in split BF16 x 3 with FP32 accumulation in TMEM.
 //
 // A work item is (m, 128 columns c of the batch, up to 128 columns of the
-// N dimension) and computes both parities p (n - m even / odd):
+// N dimension: 64 for the analysis and for tables whose tiles fit 64) and
+// computes both parities p (n - m even / odd):
 //   inverse  D_p[c][jj] = sum_k S_p[c][k] Pbar_p[jj][k]   (K = n index)
 //            F(jn) = D_0 + D_1, F(js) = D_0 - D_1
 //   forward  D_p[c][k]  = sum_jj X_p[c][jj] PW_p[k][jj]   (K = latitude pair)
