@@ -57,10 +57,12 @@ struct Geom {
   int64_t ncol;  // NI*NJ
   double sig1;
   double sig1k;  // sig1^(R/Cp): Exner(p1) = Exner(ps) * sig1k
+  double hfac;   // (R/g) (1 - sig1): the first level's height above the surface is hfac VirTemp
 };
 
-__device__ __forceinline__ void bulk_coef_l82(double Ri, double z0m, double z0h, double zs,
-                                              double z, double cmn, double chn, bool flag,
+// qm = (z - zs + z0m) / z0m and qh = (z - zs + z0h) / z0h, the arguments of
+// the neutral coefficients' logarithms (computed once by the caller).
+__device__ __forceinline__ void bulk_coef_l82(double Ri, double qm, double qh, double cmn, double chn, bool flag,
                                               double &cm, double &ch, double &cq) {
   double vm, th;
   if (flag) {
@@ -70,8 +72,8 @@ __device__ __forceinline__ void bulk_coef_l82(double Ri, double z0m, double z0h,
       vm = cmn * fp64::rcp(1.0 + 20.0 * Ri * h);  // 10 Ri / r
       th = chn * fp64::rcp(1.0 + 15.0 * Ri * r);
     } else {
-      vm = cmn * (1.0 - 10.0 * Ri * fp64::rcp(1.0 + 75.0 * cmn * fp64::sqrt(-(z - zs + z0m) * (1.0 / z0m) * Ri)));
-      th = chn * (1.0 - 15.0 * Ri * fp64::rcp(1.0 + 75.0 * chn * fp64::sqrt(-(z - zs + z0h) * (1.0 / z0h) * Ri)));
+      vm = cmn * (1.0 - 10.0 * Ri * fp64::rcp(1.0 + 75.0 * cmn * fp64::sqrt(-(qm * Ri))));
+      th = chn * (1.0 - 15.0 * Ri * fp64::rcp(1.0 + 75.0 * chn * fp64::sqrt(-(qh * Ri))));
     }
   } else {
     vm = 0.0;
@@ -153,7 +155,7 @@ __global__ void __launch_bounds__(256, 2) bulk_flux_column(Ptrs p, Geom g, const
         continue;
       }
       rTs[n] = fp64::rcp(Tsn[n]);
-      QSat[n] = (EpsV * Es0) * rPs * fp64::exp(aL[n] / GasRWet * (1.0 / 273.0 - rTs[n]));
+      QSat[n] = (EpsV * Es0) * rPs * fp64::exp(fma(-aL[n] / GasRWet, rTs[n], aL[n] / GasRWet * (1.0 / 273.0)));
       SVT[n] = Tsn[n] * (1.0 + (((1.0 / EpsV) - 1.0) * QSat[n]));
     }
     const double VirTemp = Ta * (1.0 + (((1.0 / EpsV) - 1.0) * q1));
@@ -162,18 +164,19 @@ __global__ void __launch_bounds__(256, 2) bulk_flux_column(Ptrs p, Geom g, const
     const double rExner = fp64::rcp(Exner);
     const double rSfcExner = fp64::rcp(SfcExner);
     const double VelAbs = fp64::sqrt(U * U + V * V);
-    const double Height = zs + GasRDry / Grav * VirTemp * (1.0 - g.sig1);
+    // Height - zs, the reference's Height (:223-225) less the surface height
+    const double dH = g.hfac * VirTemp;
 
     // Neutral coefficients (:250-260) depend only on the column (the
     // roughness lengths are the same constants for both surface types).
-    const double tmp = FKarm * fp64::rcp(fp64::log((Height - zs + z0m) * (1.0 / z0m)));
+    const double qm = (dH + z0m) * (1.0 / z0m);
+    const double qh = RoughLenHeatFactor == 1.0 ? qm : (dH + z0h) * (1.0 / z0h);
+    const double tmp = FKarm * fp64::rcp(fp64::log(qm));
     const double cmn = tmp * tmp;
     // z0h = RoughLenHeatFactor z0m: with the factor 1 both logarithms are one
-    const double chn = RoughLenHeatFactor == 1.0
-                           ? cmn
-                           : tmp * (FKarm * fp64::rcp(fp64::log((Height - zs + z0h) * (1.0 / z0h))));
+    const double chn = RoughLenHeatFactor == 1.0 ? cmn : tmp * (FKarm * fp64::rcp(fp64::log(qh)));
     const double vmx = fmax(VelAbs, VelMinForRi);
-    const double rvmx2 = fp64::rcp(vmx * vmx);
+    const double vmx2 = vmx * vmx;
     // The Richardson number and the sensible heat flux subtract nearly equal
     // quotients: these keep correctly rounded divisions (Markstein's
     // correction of a times the shared reciprocal).
@@ -194,10 +197,13 @@ __global__ void __launch_bounds__(256, 2) bulk_flux_column(Ptrs p, Geom g, const
         continue;
       }
       const double SVT_SE = fp64::div_rb(SVT[n], SfcExner, rSfcExner);
-      const double Ri = Grav * fp64::rcp(SVT_SE) * (VT_E - SVT_SE) * rvmx2 * (Height - zs);
+      // Ri = g / SVT_SE (VT_E - SVT_SE) / vmx^2 dH and rho = Ps / (R SVT)
+      // from one reciprocal y = 1 / (SVT vmx^2): 1 / SVT_SE = SfcExner y vmx^2
+      const double y = fp64::rcp(SVT[n] * vmx2);
+      const double Ri = (Grav * SfcExner) * (VT_E - SVT_SE) * dH * y;
       double cm, ch, cq;
-      bulk_coef_l82(Ri, z0m, z0h, zs, Height, cmn, chn, f, cm, ch, cq);
-      const double rho = Ps * fp64::rcp(GasRDry * SVT[n]);
+      bulk_coef_l82(Ri, qm, qh, cmn, chn, f, cm, ch, cq);
+      const double rho = (Ps * (1.0 / GasRDry)) * (vmx2 * y);
       CVel[n] = cm * rho * fmin(fmax(VelAbs, VelMinForVel), VelMaxForVel);
       CTemp[n] = ch * rho * fmin(fmax(VelAbs, VelMinForTemp), VelMaxForTemp);
       CQ[n] = cq * rho * fmin(fmax(VelAbs, VelMinForQVap), VelMaxForQVap);
@@ -273,7 +279,7 @@ __global__ void __launch_bounds__(256, 2) bulk_flux_column(Ptrs p, Geom g, const
         fns = +LUw[n] - LDw + LatH[n] + Sen[n];
         fsr = SUw[n] - SDw;
         dfdt = +4.0 * StB * (Tsn[n] * Tsn[n] * Tsn[n]) + CpDry * CTemp[n] +
-               aL[n] * humd * CQ[n] * (aL[n] * QSat[n] * (1.0 / GasRWet) * (rTs[n] * rTs[n]));
+               (aL[n] * aL[n] * humd / GasRWet) * (CQ[n] * QSat[n]) * (rTs[n] * rTs[n]);
       }
       const int64_t cn = c + P * n;
       wr<HOST>(h, O_FNS + n, p.Fns, cn, t, fns);
@@ -351,6 +357,7 @@ int launch(const Ptrs &p, const dccm_sfc_grid *g, double sig1, cudaStream_t s, c
   geo.ncol = (int64_t)geo.NI * NJ;
   geo.sig1 = sig1;
   geo.sig1k = pow(sig1, (GasRUniv / MolWtDry) / CpDry);
+  geo.hfac = (GasRUniv / MolWtDry) / Grav * (1.0 - sig1);
   const int threads = tunables().flux_threads > 0 ? tunables().flux_threads : 128;
   int64_t blocks = (geo.ncol + threads - 1) / threads;
   // In the coupling step the flux runs beside the transforms: fewer CTAs
