@@ -283,18 +283,24 @@ def cpu_measure(oracle, synth, w, inp, tables, steps, warmup, budget_s=20.0):
 
 
 # ------------------------------------------------------------------ GPU
-def gpu_setup(w, inp, dccm, synth, torch, dev):
-    """Device buffers, plans and the two steps (mixed and FP64)."""
+def gpu_setup(w, inp, dccm, synth, torch, dev, keys=("mixed", "fp16", "fp64"), reuse=None):
+    """Device buffers, plans and the steps of the given precisions (mixed
+    BF16 x 3, FP16 hi + lo, FP64).  reuse: another setup of the same
+    workload whose remap tables and plans this one shares (its own device
+    buffers and transform plans: a second, independent instance)."""
     groups = inp["groups"]
     n1 = len(inp["ocean"])
-    tables = []
-    for g in groups:
-        def gen(A, O):
-            t = dccm.gen_gridmapfile_lonlat2lonlat(A[0], A[1], O[0], O[1], A[2], A[3], O[2], O[3],
-                                                   accuracy_order=1, weight_mode=w["mode"])
-            return t.rows()
-        tables.append(remap_index(w, inp, g, gen))
-    plans = [dccm.RemapPlan(g.I * g.J, n1, *tb) for g, tb in zip(groups, tables)]
+    if reuse is not None:
+        tables, plans = reuse["tables"], reuse["remap_plans"]
+    else:
+        tables = []
+        for g in groups:
+            def gen(A, O):
+                t = dccm.gen_gridmapfile_lonlat2lonlat(A[0], A[1], O[0], O[1], A[2], A[3], O[2], O[3],
+                                                       accuracy_order=1, weight_mode=w["mode"])
+                return t.rows()
+            tables.append(remap_index(w, inp, g, gen))
+        plans = [dccm.RemapPlan(g.I * g.J, n1, *tb) for g, tb in zip(groups, tables)]
     arrs, fgrid = ocean_columns(inp)
     arrs.update(synth.flux_outputs(fgrid[0], fgrid[1], fill=0.0))
     IA, JA = fgrid[0], fgrid[1]
@@ -324,6 +330,8 @@ def gpu_setup(w, inp, dccm, synth, torch, dev):
     steps = {}
     keep = {}
     for prec, key in ((dccm.SHT_MIXED, "mixed"), (dccm.SHT_MIXED_FP16, "fp16"), (dccm.SHT_FP64, "fp64")):
+        if key not in keys:
+            continue
         if len(groups) == 1:
             sp = dccm.ShtPlan(groups[0].N, groups[0].I, groups[0].J, prec, groups[0].nfl)
             steps[key] = dccm.Step(sht=sp, nfl=groups[0].nfl, spec_in=spec_in[0], grid=grid[0],
@@ -828,6 +836,7 @@ def gpu_bench(args, w, inp, rank, world):
         S["steps"]["mixed"].run_host(hc, stream=stream)
         te.append(time.perf_counter() - t0)
     t_e2e, = max_over_ranks([float(np.mean(te))], world, dev)
+    e2e2 = e2e_two_in_flight(args, w, inp, S, hc, host_tuned, dccm, synth, torch, dev, world, cache)
     launches = 5 + len(groups) + 1  # pack + 2 Legendre + 2 FFT + one remap per group + flux
     ic = implcpl_leg(args, groups, dccm, synth, torch, dev, stream, flush, fp64_peak)
     so = spec_ops_leg(args, groups, S, dccm, torch, stream, flush)
@@ -847,7 +856,84 @@ def gpu_bench(args, w, inp, rank, world):
     return dict(t_mixed=t_mixed, t_fp64=t_fp64, t_fp16=t_fp16, err_fp16=err_fp16, t_e2e=t_e2e, clocks=ck, roof=roof,
                 roof_f64=roof_f64, stage_f64=[float(x) for x in stage_f64], err=err, h2d=h2d_bytes,
                 d2h=d2h_bytes, nfl=nfl, launches=launches, tables=S["tables"], tuned=dict(tuned, host=host_tuned),
-                implcpl=ic, spec_ops=so, coupled=coupled)
+                implcpl=ic, spec_ops=so, coupled=coupled, e2e2=e2e2)
+
+
+def e2e_two_in_flight(args, w, inp, S, hc, host_tuned, dccm, synth, torch, dev, world, cache):
+    """End to end with two independent instances of the step in flight
+    (ensemble members or separate runs: each its own device buffers,
+    transform plans and page-locked host buffers, the remap plans shared),
+    each through dccm_step_launch_host on a stream of its own, the steps
+    issued to the two in turn, so one instance's downloads share the host
+    link with the other's uploads.  Every step still copies all its inputs
+    in and its results out.  Time per step = the span of K steps (CUDA
+    events on a stream that waits for both) / K; no L2 flush between steps
+    (two are in flight; every step's inputs arrive over the host link).
+    Host-copy choices tried (dccm_step_host_choice): each instance's own
+    choice from dccm_step_autotune_host, and the copy engines alone under
+    either upload order; the fastest is reported, all are listed.  The
+    second instance's downloads are compared with the first's (same
+    inputs, bit-identical)."""
+    groups = inp["groups"]
+    S2 = gpu_setup(w, inp, dccm, synth, torch, dev, keys=("mixed",), reuse=S)
+    step1, step2 = S["steps"]["mixed"], S2["steps"]["mixed"]
+    step2.autotune(cache)
+    hc2 = dccm.HostCopies(*host_copies(S2, groups, dccm, torch))
+    cur = torch.cuda.current_stream(dev)
+    t2 = step2.autotune_host(hc2, stream=cur)
+    own = [(host_tuned["upload_order"], host_tuned["host_path"], host_tuned["flux_ctas"]),
+           (t2["upload_order"], t2["host_path"], t2["flux_ctas"])]
+    cands = {"each instance's own tuned choice": own,
+             "copy engines, transforms' inputs first": [(1, 1, c[2]) for c in own],
+             "copy engines, surface inputs first": [(2, 1, c[2]) for c in own]}
+    streams = [torch.cuda.Stream(dev), torch.cuda.Stream(dev)]
+    inst = [(step1, hc, streams[0]), (step2, hc2, streams[1])]
+    K = max(10, args.steps)
+
+    def issue(n):
+        for k in range(n):
+            st, h, sx = inst[k % 2]
+            st.launch_host(h, stream=sx)
+
+    def span():
+        torch.cuda.synchronize()
+        issue(2 * max(3, args.warmup))
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(cur)
+        for sx in streams:
+            sx.wait_event(ev0)
+        issue(K)
+        for sx in streams:
+            e = torch.cuda.Event()
+            e.record(sx)
+            cur.wait_event(e)
+        ev1.record(cur)
+        torch.cuda.synchronize()
+        t, = max_over_ranks([ev0.elapsed_time(ev1) / 1e3 / K], world, dev)
+        return t
+
+    times = {}
+    for name, ch in cands.items():
+        for st, c in zip((step1, step2), ch):
+            st.host_choice(*c)
+        times[name] = span()
+    best = min(times, key=times.get)
+    for st, c in zip((step1, step2), cands[best]):
+        st.host_choice(*c)
+    t = span()
+    same = all(torch.equal(a[0], b[0]) for a, b in zip(hc.pairs[1], hc2.pairs[1]))
+    step1.host_choice(*own[0])
+    h2d, d2h = hc.nbytes()
+    del S2
+    return {"value": job_throughput(world, inp["nfl"], t), "unit": "field-levels/s", "ms_per_step": t * 1e3,
+            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "instances": 2, "steps": K,
+            "downloads_equal": bool(same), "host_copies": best,
+            "candidates_ms": {k: v * 1e3 for k, v in times.items()},
+            "how": "two independent instances (own device and page-locked host buffers), "
+                   "dccm_step_launch_host on two streams in turn; span of K steps / K, no L2 flush"}
 
 
 def spec_ops_leg(args, groups, S, dccm, torch, stream, flush):
@@ -1032,6 +1118,7 @@ def main():
         "roofline": roof,
         "e2e": {"value": job_throughput(world, nfl, r["t_e2e"]), "unit": "field-levels/s", "h2d_bytes_per_step": r["h2d"],
                 "d2h_bytes_per_step": r["d2h"], "ms_per_step": r["t_e2e"] * 1e3},
+        "e2e_two_in_flight": r["e2e2"],
         "stage_ms": {n: round(v["ms"], 5) for n, v in stages.items()},
         "fp64_gpu": {"value": job_throughput(world, nfl, r["t_fp64"]), "ms_per_step": r["t_fp64"] * 1e3,
                      "mixed_over_fp64": r["t_fp64"] / r["t_mixed"],

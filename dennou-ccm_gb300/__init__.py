@@ -158,6 +158,9 @@ _SIGS = {
     "dccm_step_run_timed": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "dccm_step_run_host": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                           ctypes.c_void_p, ctypes.c_int]),
+    "dccm_step_launch_host": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                             ctypes.c_void_p, ctypes.c_int]),
+    "dccm_step_host_choice": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "dccm_step_host_release": (ctypes.c_int, [ctypes.c_void_p]),
     "dccm_fp64_peak": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "dccm_fp64_fn_dev": (ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
@@ -748,6 +751,14 @@ class Step:
         _check(load().dccm_step_run_host(self.h, _stream(stream), c.h2d, c.nh2d, c.d2h, c.nd2h),
                "dccm_step_run_host")
 
+    def launch_host(self, h2d, d2h=None, stream=None):
+        """dccm_step_launch_host: run_host without the final synchronisation
+        (page-locked buffers only); the downloads are in host memory once
+        the stream has synchronised."""
+        c = h2d if isinstance(h2d, HostCopies) else HostCopies(h2d, d2h or [])
+        _check(load().dccm_step_launch_host(self.h, _stream(stream), c.h2d, c.nh2d, c.d2h, c.nd2h),
+               "dccm_step_launch_host")
+
     def autotune_host(self, h2d, d2h=None, stream=None):
         """dccm_step_autotune_host: upload order, copy path and flux CTA cap
         for these copy lists, by timing (the step runs about 420 times);
@@ -761,6 +772,12 @@ class Step:
                "dccm_step_autotune_host")
         return {"upload_order": out[0], "host_path": out[1], "flux_ctas": out[2],
                 "candidates_ms": {"%d,%d" % (1 + k // 16, 1 + k % 16): ms[k] for k in range(32)}}
+
+    def host_choice(self, upload_order=0, host_path=0, flux_ctas=-1):
+        """dccm_step_host_choice: this step's upload order, copy path and
+        host-graph flux CTA cap (0, 0, -1: the process-wide knobs)."""
+        _check(load().dccm_step_host_choice(self.h, int(upload_order), int(host_path), int(flux_ctas)),
+               "dccm_step_host_choice")
 
     def host_release(self):
         """dccm_step_host_release: forget the recorded copy graph."""

@@ -507,6 +507,8 @@ static int capture(dccm_step *st, const HostSets *hp, cudaGraph_t *out) {
 }
 
 static void drop_host_graph(dccm_step *st) {
+  // a launch by dccm_step_launch_host may still be running on its stream
+  if (st->hexec || !st->host_tabs.empty()) cudaDeviceSynchronize();
   if (st->hexec) cudaGraphExecDestroy(st->hexec);
   if (st->hgraph) cudaGraphDestroy(st->hgraph);
   st->hexec = nullptr;
@@ -859,33 +861,46 @@ static bool page_locked(const dccm_host_copy *h2d, int nh2d, const dccm_host_cop
   return locked;
 }
 
+// Launches the host-copy graph for these copy lists on s (recording it
+// first if the lists changed); page-locked buffers only.
+static int launch_host_graph(dccm_step *st, cudaStream_t s, const dccm_host_copy *h2d, int nh2d,
+                             const dccm_host_copy *d2h, int nd2h) {
+  if (!(st->hexec && same_copies(st->host_h2d, h2d, nh2d) && same_copies(st->host_d2h, d2h, nd2h)))
+    DCCM_TRY(build_host_graph(st, h2d, nh2d, d2h, nd2h));
+  DCCM_CUDA(cudaGraphLaunch(st->hexec, s));
+  return DCCM_OK;
+}
+
 extern "C" int dccm_step_run_host(dccm_step *st, void *stream, const dccm_host_copy *h2d, int nh2d,
                                   const dccm_host_copy *d2h, int nd2h) {
   DCCM_NVTX_FUNC();
   if (!st || (nh2d > 0 && !h2d) || (nd2h > 0 && !d2h) || nh2d < 0 || nd2h < 0) return DCCM_ERR_INVALID_ARG;
   cudaStream_t s = as_stream(stream);
-  // The copy lists of the recorded host graph again: replay it.
-  if (st->hexec && same_copies(st->host_h2d, h2d, nh2d) && same_copies(st->host_d2h, d2h, nd2h)) {
-    DCCM_CUDA(cudaGraphLaunch(st->hexec, s));
-    DCCM_CUDA(cudaStreamSynchronize(s));
-    return DCCM_OK;
-  }
-  // Page-locked host buffers: the copies join the step's graph, each next to
-  // the stage that needs or produces its data.  Otherwise (pageable memory)
-  // copy in, replay, copy out.
-  if (!page_locked(h2d, nh2d, d2h, nd2h)) {
+  // The copy lists of the recorded host graph again: replay it.  Page-locked
+  // host buffers otherwise: the copies join the step's graph, each next to
+  // the stage that needs or produces its data.  Pageable memory: copy in,
+  // replay, copy out.
+  const bool recorded = st->hexec && same_copies(st->host_h2d, h2d, nh2d) && same_copies(st->host_d2h, d2h, nd2h);
+  if (recorded || page_locked(h2d, nh2d, d2h, nd2h)) {
+    DCCM_TRY(launch_host_graph(st, s, h2d, nh2d, d2h, nd2h));
+  } else {
     for (int k = 0; k < nh2d; ++k)
       DCCM_CUDA(cudaMemcpyAsync(h2d[k].dev, h2d[k].host, h2d[k].bytes, cudaMemcpyHostToDevice, s));
     DCCM_CUDA(cudaGraphLaunch(st->exec, s));
     for (int k = 0; k < nd2h; ++k)
       DCCM_CUDA(cudaMemcpyAsync(d2h[k].host, d2h[k].dev, d2h[k].bytes, cudaMemcpyDeviceToHost, s));
-    DCCM_CUDA(cudaStreamSynchronize(s));
-    return DCCM_OK;
   }
-  DCCM_TRY(build_host_graph(st, h2d, nh2d, d2h, nd2h));
-  DCCM_CUDA(cudaGraphLaunch(st->hexec, s));
   DCCM_CUDA(cudaStreamSynchronize(s));
   return DCCM_OK;
+}
+
+extern "C" int dccm_step_launch_host(dccm_step *st, void *stream, const dccm_host_copy *h2d, int nh2d,
+                                     const dccm_host_copy *d2h, int nd2h) {
+  DCCM_NVTX_FUNC();
+  if (!st || (nh2d > 0 && !h2d) || (nd2h > 0 && !d2h) || nh2d < 0 || nd2h < 0) return DCCM_ERR_INVALID_ARG;
+  const bool recorded = st->hexec && same_copies(st->host_h2d, h2d, nh2d) && same_copies(st->host_d2h, d2h, nd2h);
+  if (!recorded && !page_locked(h2d, nh2d, d2h, nd2h)) return DCCM_ERR_UNSUPPORTED;
+  return launch_host_graph(st, as_stream(stream), h2d, nh2d, d2h, nd2h);
 }
 
 extern "C" int dccm_step_autotune_host(dccm_step *st, void *stream, const dccm_host_copy *h2d, int nh2d,
@@ -1001,6 +1016,17 @@ extern "C" int dccm_step_autotune_host(dccm_step *st, void *stream, const dccm_h
   }
   if (ms)
     for (int k = 0; k < NC; ++k) ms[k] = best_t[k];
+  return DCCM_OK;
+}
+
+extern "C" int dccm_step_host_choice(dccm_step *st, int upload_order, int host_path, int flux_ctas) {
+  DCCM_NVTX_FUNC();
+  if (!st || upload_order < 0 || upload_order > 2 || host_path < 0 || host_path > 32 || flux_ctas < -1)
+    return DCCM_ERR_INVALID_ARG;
+  drop_host_graph(st);
+  st->host_order = upload_order;
+  st->host_path = host_path;
+  st->host_flux_ctas = flux_ctas;
   return DCCM_OK;
 }
 

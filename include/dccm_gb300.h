@@ -481,6 +481,26 @@ int dccm_step_run_timed(dccm_step *step, void *stream, float *ms);
  * dccm_step_host_release after freeing or unpinning one of them). */
 int dccm_step_run_host(dccm_step *step, void *stream, const dccm_host_copy *h2d, int nh2d,
                        const dccm_host_copy *d2h, int nd2h);
+/* dccm_step_run_host without the final synchronisation: the copies and the
+ * step are enqueued on stream and the call returns; the downloads are in
+ * host memory once the stream has synchronised (or an event recorded on
+ * it after this call has completed).  Page-locked host buffers only
+ * (DCCM_ERR_UNSUPPORTED otherwise).  A step's graph runs once at a time:
+ * calls on one step are ordered by passing the same stream.  For
+ * independent problems (ensemble members, runs, snapshots), each with its
+ * own step, device buffers and host buffers, calls on different streams
+ * overlap one problem's downloads with the next one's uploads on the
+ * host link, which moves data both ways at once. */
+int dccm_step_launch_host(dccm_step *step, void *stream, const dccm_host_copy *h2d, int nh2d,
+                          const dccm_host_copy *d2h, int nd2h);
+/* Sets this step's host-copy choices as dccm_step_autotune_host would:
+ * upload_order (0: the process-wide knob), host_path (0: the process-wide
+ * knob, else 1 + the copy-group mask) and the flux CTA cap of the host
+ * graph (-1: the process-wide knob, 0: the full grid), and drops the
+ * recorded host graph.  For a caller that times its own schedule, e.g.
+ * two instances in flight, where the copy engines alone (host_path 1)
+ * leave the SMs to the other instance's kernels. */
+int dccm_step_host_choice(dccm_step *step, int upload_order, int host_path, int flux_ctas);
 /* Drops the graph and the staging buffers dccm_step_run_host keeps for its
  * copy lists (the next call records them again). */
 int dccm_step_host_release(dccm_step *step);

@@ -323,3 +323,41 @@ def test_ensemble_mixed_row_lengths_match_oracle(dccm, oracle, synth, cuda, rpw)
             assert rel_l2(s2.cpu().numpy().view(np.complex128), s) <= 2e-6, N
     finally:
         dccm.tune_set("fft_rpw", saved)
+
+
+def test_launch_host_two_instances_in_flight(dccm, oracle, synth, cuda):
+    """dccm_step_launch_host: two independent instances of the c1 step (own
+    device buffers and transform plans, shared remap plans), their steps
+    issued in turn on two streams without synchronising, return exactly
+    what dccm_step_run_host returns; pageable buffers are refused."""
+    torch = cuda
+    bench, w, inp, S = _small_step(dccm, synth, oracle, torch, 1)
+    groups = inp["groups"]
+    dev = torch.device("cuda", 0)
+    S2 = bench.gpu_setup(w, inp, dccm, synth, torch, dev, keys=("mixed",), reuse=S)
+    steps = [S["steps"]["mixed"], S2["steps"]["mixed"]]
+    hcs = [dccm.HostCopies(*bench.host_copies(X, groups, dccm, torch)) for X in (S, S2)]
+    steps[0].run_host(hcs[0])
+    want = [h.clone() for h, _ in hcs[0].pairs[1]]
+    streams = [torch.cuda.Stream(dev), torch.cuda.Stream(dev)]
+    # the process-wide choices, the copy engines alone, everything mapped
+    for choice in ((0, 0, -1), (1, 1, -1), (2, 16, 0)):
+        for st in steps:
+            st.host_choice(*choice)
+        for hc in hcs:
+            for h, _ in hc.pairs[1]:
+                h.zero_()
+        for k in range(6):
+            steps[k % 2].launch_host(hcs[k % 2], stream=streams[k % 2])
+        torch.cuda.synchronize()
+        for hc in hcs:
+            for (h, _), ref in zip(hc.pairs[1], want):
+                assert torch.equal(h, ref), choice
+    assert S["plans"]["mixed"].status() == (0, 0) and S2["plans"]["mixed"].status() == (0, 0)
+    for bad in ((3, 1, -1), (1, 33, -1), (1, 1, -2)):
+        with pytest.raises(dccm.DccmError):
+            steps[0].host_choice(*bad)
+    # pageable host buffers cannot be left in flight
+    h_in = torch.from_numpy(groups[0].spec.view(np.float64).copy())
+    with pytest.raises(dccm.DccmError):
+        steps[1].launch_host([(h_in, S2["spec_in"][0])], [])
