@@ -69,6 +69,14 @@ __device__ __forceinline__ float2 shfl_c(float2 v, int src) {
 }
 __device__ __forceinline__ int brev5(int l) { return (int)(__brev((unsigned)l) >> 27); }
 
+// Barrier of the nw warps of one row-pair group (named barrier 1 + g; 0 is
+// __syncthreads): the groups' exchange buffers are their own, so one group's
+// loads and arithmetic can overlap another's.  Every warp of the group
+// executes it; warps outside every group execute none.
+__device__ __forceinline__ void group_sync(int g, int nw) {
+  asm volatile("bar.sync %0, %1;" ::"r"(1 + g), "r"(32 * nw) : "memory");
+}
+
 // e^{-2 pi i a / 24} (a multiple of 15 degrees) as literal constants: the
 // in-register DFT lengths (2, 3, 4, 6, 8, 12) all divide 24, so their
 // twiddles fold into the instructions instead of being loaded.  The values
@@ -508,9 +516,7 @@ __device__ __forceinline__ void fft_inv_block_mw(const FftGroup &G, int jj, int 
   if (own) {
 #pragma unroll
     for (int k1 = 0; k1 < MW_R0; ++k1) xb[(k1 * W + wq) * 32 + lane] = v[k1];
-  }
-  __syncthreads();
-  if (own) {
+    group_sync(bl, W);
 #pragma unroll
     for (int k1 = 0; k1 < MW_R0; ++k1) {
       float2 acc = xb[(k1 * W) * 32 + lane];
@@ -572,9 +578,7 @@ __device__ __forceinline__ void fft_fwd_block_mw(const FftGroup &G, int jj, int 
   if (own) {
 #pragma unroll
     for (int k1 = 0; k1 < MW_R0; ++k1) xb[(k1 * W + wq) * 32 + lane] = v[k1];
-  }
-  __syncthreads();
-  if (own) {
+    group_sync(bl, W);
 #pragma unroll
     for (int k1 = 0; k1 < MW_R0; ++k1) {
       float2 acc = xb[(k1 * W) * 32 + lane];
@@ -588,12 +592,12 @@ __device__ __forceinline__ void fft_fwd_block_mw(const FftGroup &G, int jj, int 
 #pragma unroll
   for (int k1 = 0; k1 < MW_R0; ++k1) v[k1] = cmul(v[k1], tq);
   lane_dif<MW_R0>(v, w, lane);
-  __syncthreads();  // every warp is done reading the exchange buffer
   if (own) {
+    group_sync(bl, W);  // every warp of the group is done reading the exchange buffer
 #pragma unroll
     for (int k1 = 0; k1 < MW_R0; ++k1) xb[(k1 * W + wq) * 32 + lane] = v[k1];
+    group_sync(bl, W);
   }
-  __syncthreads();
   if (bl < nb) {
     const float invI = 1.f / (float)I;
 #pragma unroll
@@ -684,7 +688,7 @@ __device__ __forceinline__ void fft_inv_block_mwp(const FftGroup &G, int jj, int
 #pragma unroll
         for (int tx = 0; tx < W; ++tx) xb[(mw_k1<W>(wq, j) * W + tx) * 32 + lane] = v[j * W + tx];
     }
-    __syncthreads();
+    if (grp < ng) group_sync(grp, W);
     if (own) {
 #pragma unroll
       for (int k1 = 0; k1 < MW_R0; ++k1) v[k1] = xb[(k1 * W + wq) * 32 + lane];
@@ -701,7 +705,7 @@ __device__ __forceinline__ void fft_inv_block_mwp(const FftGroup &G, int jj, int
         gs[L * r + t] = f32_to_f64(v[r].y);
       }
     }
-    if (rd + 1 < passes) __syncthreads();  // the exchange buffer is read before the next pass writes it
+    if (rd + 1 < passes && grp < ng) group_sync(grp, W);  // the exchange buffer is read before the next pass writes it
   }
 }
 
@@ -748,7 +752,7 @@ __device__ __forceinline__ void fft_fwd_block_mwp(const FftGroup &G, int jj, int
 #pragma unroll
       for (int k1 = 0; k1 < MW_R0; ++k1) xb[(k1 * W + wq) * 32 + lane] = v[k1];
     }
-    __syncthreads();
+    if (grp < ng) group_sync(grp, W);
     if (own) {
 #pragma unroll
       for (int j = 0; j < NK; ++j)
@@ -784,8 +788,9 @@ __device__ __forceinline__ void fft_fwd_block_mwp(const FftGroup &G, int jj, int
         if (own && bl < nb && m <= N) store_eo<R>(st, G.BB, bl, m, q * 17 + kl, v[j * W + kw], zc, invI);
       }
     }
-    __syncthreads();  // the exchange buffer is read before the next pass writes it; the planes are complete
+    if (rd + 1 < passes && grp < ng) group_sync(grp, W);  // the exchange buffer is read before the next pass writes it
   }
+  __syncthreads();  // every group's planes are complete
   write_g3<R>(G, jj, b0, nb, st);
 }
 
