@@ -18,15 +18,14 @@ namespace dccm {
 
 __device__ __forceinline__ double f32_to_f64(float f) {
   const unsigned u = __float_as_uint(f);
-  const unsigned e = (u >> 23) & 0xFFu;
-  if (e == 0u || e == 0xFFu) {
-    if ((u & 0x7FFFFFFFu) == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
-    return (double)f;  // subnormal, inf, nan
+  const unsigned a = u & 0x7FFFFFFFu;
+  if (a - 0x00800000u >= 0x7F000000u) {  // zero, subnormal, inf, nan
+    if (a == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
+    return (double)f;
   }
-  const unsigned m = u & 0x7FFFFFu;
-  const unsigned hi = (u & 0x80000000u) | ((e + (1023u - 127u)) << 20) | (m >> 3);
-  const unsigned lo = m << 29;
-  return __hiloint2double((int)hi, (int)lo);
+  // exponent and mantissa move down 3 bits as one field; the bias grows by
+  // 1023 - 127 = 896 (896 << 20 = 0x38000000)
+  return __hiloint2double((int)(((a >> 3) + 0x38000000u) | (u & 0x80000000u)), (int)(u << 29));
 }
 
 // Operands outside FP32's normal range other than zero (subnormal results,
@@ -37,22 +36,28 @@ static __device__ __noinline__ float f64_to_f32_special(double d) { return __dou
 
 __device__ __forceinline__ float f64_to_f32_rn(double d) {
   const unsigned hi = (unsigned)__double2hiint(d);
-  const unsigned lo = (unsigned)__double2loint(d);
   // biased exponent e in [897, 1150]: the result is a normal FP32 number
-  // (or rounds up to infinity at the top, as IEEE rounding does)
-  const bool normal = (hi & 0x7FF00000u) - 0x38100000u < 0x0FE00000u;
-  const bool zero = ((hi << 1) | lo) == 0u;
-  if (!normal && !zero) return f64_to_f32_special(d);
+  // (or rounds up to infinity at the top, as IEEE rounding does); zero
+  // takes the hardware path with the other operands outside that range
+  if ((hi & 0x7FF00000u) - 0x38100000u >= 0x0FE00000u) return f64_to_f32_special(d);
+  // round to nearest, ties to even, at bit 29: adding 2^28 - 1 + lsb to
+  // the 64-bit pattern carries out of the 29 dropped bits exactly when they
+  // exceed half, or equal half with an odd lsb; a carry out of the mantissa
+  // correctly increments the exponent
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const unsigned long long rb = b + (0x0FFFFFFFull + ((b >> 29) & 1ull));
   // (hi:lo) << 3 keeps e's low 9 bits above the top 23 mantissa bits;
   // subtracting 384 << 23 turns them into e - 896 (mod 512, which fits 8 bits)
-  const unsigned r = __funnelshift_l(lo, hi, 3) - 0xC0000000u;
-  // round to nearest, ties to even, on the 29 dropped bits: the carry out of
-  // dropped + (2^28 - 1) + lsb is 1 exactly when they exceed half, or equal
-  // half with an odd lsb; a carry out of the mantissa correctly increments
-  // the exponent
-  const unsigned up = ((lo & 0x1FFFFFFFu) + 0x0FFFFFFFu + (r & 1u)) >> 29;
-  const unsigned sign = hi & 0x80000000u;
-  return __uint_as_float(zero ? sign : (r | sign) + up);
+  const unsigned r = __funnelshift_l((unsigned)rb, (unsigned)(rb >> 32), 3) - 0xC0000000u;
+  return __uint_as_float(r | (hi & 0x80000000u));
+}
+
+// The same for inputs where zeros are common (padding, the imaginary parts
+// of m = 0 coefficients): zero on the integer path, the rest as above.
+__device__ __forceinline__ float f64_to_f32_rn_z(double d) {
+  const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
+  if (((hi << 1) | lo) == 0u) return __uint_as_float(hi & 0x80000000u);
+  return f64_to_f32_rn(d);
 }
 
 // Exact split of an FP32 value into three BF16 numbers x = hi + mid + lo

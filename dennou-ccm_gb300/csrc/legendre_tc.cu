@@ -587,7 +587,7 @@ __global__ void __launch_bounds__(128) pack_spectra_kernel(const __grid_constant
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
       const double x = comp ? v[j].y : v[j].x;
-      f[j] = f64_to_f32_rn(G.nsplit == 2 ? scale_pow2(x, sc) : x);
+      f[j] = f64_to_f32_rn_z(G.nsplit == 2 ? scale_pow2(x, sc) : x);
     }
     if (G.nsplit == 2) {
       unsigned h[4], l[4];
