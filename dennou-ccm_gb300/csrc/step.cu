@@ -1249,8 +1249,6 @@ extern "C" int dccm_step_autotune(dccm_step *st, const char *cache_path, int *ch
     Knob graph_knobs[] = {
         {&T.serial, {0, 1}, -1, -1},
         {&T.tc_ctas, first(T.tc_ctas, {2 * sms, sms, sms * 3 / 4, sms / 2}), -1, -1},
-        {&T.flux_threads, first(T.flux_threads, {64, 128, 256}), -1, -1},
-        {&T.flux_ctas, {0, sms * 4, sms * 2, sms}, -1, -1},
     };
     float step_ms = 0.f;
     for (Knob &kb : graph_knobs) {
@@ -1260,6 +1258,35 @@ extern "C" int dccm_step_autotune(dccm_step *st, const char *cache_path, int *ch
         rerecord(st);
         return rc;
       }
+    }
+    // The flux CTA size and grid cap together: how many flux warps an SM
+    // holds beside the transforms depends on both (e.g. at T341 one
+    // 128-thread CTA an SM beat the best cap for the stage pass's 64).
+    if (st->d.flux) {
+      const std::vector<int> fts = first(T.flux_threads, {64, 128, 256});
+      const int fcs[] = {0, sms * 4, sms * 2, sms};
+      int bft = T.flux_threads, bfc = 0;
+      float bt = 1e30f;
+      for (int a : fts)
+        for (int c : fcs) {
+          T.flux_threads = a;
+          T.flux_ctas = c;
+          float t;
+          const int rc = time_graph(st, s, 7, &t);
+          if (rc != DCCM_OK) {
+            T = saved;
+            rerecord(st);
+            return rc;
+          }
+          if (t < bt * 0.98f || bt == 1e30f) {
+            bt = t;
+            bft = a;
+            bfc = c;
+          }
+        }
+      T.flux_threads = bft;
+      T.flux_ctas = bfc;
+      step_ms = bt;
     }
     best = T;
     DCCM_TRY(dccm_step_run_timed(st, s, ms));

@@ -547,8 +547,9 @@ int dccm_step_autotune_host(dccm_step *step, void *stream, const dccm_host_copy 
  * (4, 8 or 16), "flux_threads", "remap_threads": CTA sizes, "remap_fc":
  * fields per thread of the remap, 1, 2, 3, 4 or 6), then "serial"
  * (1: ordinary launches instead of programmatic dependent launches along
- * the transform chain), "tc_ctas" again and "flux_ctas" (CTA cap of the
- * flux kernel's grid, 0: 16 per SM) on replays of the whole step graph,
+ * the transform chain), "tc_ctas" again, and "flux_threads" with
+ * "flux_ctas" (CTA cap of the flux kernel's grid, 0: 16 per SM) as pairs
+ * (3 x 4 candidates) on replays of the whole step graph,
  * where the two branches run concurrently; applies the winners and
  * records the step's graph again.  Every timed run follows a 256 MB
  * device write, so that the step finds L2 as it does between the model's
