@@ -597,13 +597,13 @@ def roofline_f64(groups, stage_ms, fp64_peak):
 
 
 # FP64 pipe work of the flux kernel per ocean column: DADD + DMUL + 2 DFMA
-# thread instructions (ncu sass counters, c3, 45,478 columns: 1,227,906
-# DADD, 3,183,460 DMUL, 5,457,360 DFMA; the reciprocals, square roots, exp
+# thread instructions (ncu sass counters, c3, 45,478 columns: 1,182,428
+# DADD, 3,137,982 DMUL, 5,002,580 DFMA; the reciprocals, square roots, exp
 # and log are the kernel's own, csrc/fp64_fast.cuh).  Every column does the
-# same work when there is no sea ice (all workloads here: the ice physics is
-# skipped where SIceCon = 0), so the per-column figure carries to every
-# workload.
-FLUX_FP64_INSTR_PER_COLUMN = (1227906 + 3183460 + 2 * 5457360) / 45478
+# same work when there is no sea ice (all workloads here: warps whose
+# columns all have SIceCon = 0 skip the ice physics and the merging), so
+# the per-column figure carries to every workload.
+FLUX_FP64_INSTR_PER_COLUMN = (1182428 + 3137982 + 2 * 5002580) / 45478
 
 
 # FP64 flops of the implicit-coupling sweeps per column and level, one

@@ -105,118 +105,131 @@ __device__ __forceinline__ void wr(const HostRows &h, int k, double *dev, int64_
   if (HOST && h.out[k]) h.out[k][t] = v;
 }
 
-template <bool HOST>
-__global__ void __launch_bounds__(256, 2) bulk_flux_column(Ptrs p, Geom g, const __grid_constant__ HostRows h) {
+// One column t (device element c).  PURE: the caller's whole warp has no
+// sea ice at all (SIceCon = 0), so Frac = (1, 0), the ice slot is skipped
+// and every merged value 0 + 1 X[0] is X[0] (up to the sign of an exact
+// zero) with no FP64 operation; PURE = false is the general column.  The
+// two are separate code paths so that the general one keeps its register
+// allocation.
+template <bool HOST, bool PURE>
+__device__ __forceinline__ void flux_column(const Ptrs &p, const Geom &g, const HostRows &h, int64_t t, int64_t c,
+                                            double SIceCon) {
   constexpr double GasRDry = GasRUniv / MolWtDry;
   constexpr double GasRWet = GasRUniv / MolWtWet;
   constexpr double EpsV = MolWtWet / MolWtDry;
   const double aL[2] = {LatentHeat, LatentHeat + LatentHeatFusion};
+  const int64_t P = g.plane;
+  const double Ps = rd<HOST>(h, I_PS, p.Ps, c, t);
+  const double Ta = rd<HOST>(h, I_TA, p.Ta, c, t);
+  const double q1 = rd<HOST>(h, I_Q1, p.q1, c, t);
+  const double U = rd<HOST>(h, I_U, p.U, c, t), V = rd<HOST>(h, I_V, p.V, c, t);
+  const double zs = rd<HOST>(h, I_ZS, p.Zs, c, t);
+  const double SDw = rd<HOST>(h, I_SDW, p.SDw, c, t), LDw = rd<HOST>(h, I_LDW, p.LDw, c, t);
+  const double z0m = RoughLength;
+  const double z0h = RoughLenHeatFactor * z0m;
+  const double humd = 1.0;
 
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < g.ncol;
-       t += (int64_t)gridDim.x * blockDim.x) {
-    const int ii = (int)(t % g.NI);
-    const int jj = (int)(t / g.NI);
-    const int64_t c = (int64_t)(g.IS - 1 + ii) + (int64_t)g.IA * (g.JS - 1 + jj);
-    const int64_t P = g.plane;
-
-    const double SIceCon = rd<HOST>(h, I_ICE, p.Ice, c, t);
-    const double Ps = rd<HOST>(h, I_PS, p.Ps, c, t);
-    const double Ta = rd<HOST>(h, I_TA, p.Ta, c, t);
-    const double q1 = rd<HOST>(h, I_Q1, p.q1, c, t);
-    const double U = rd<HOST>(h, I_U, p.U, c, t), V = rd<HOST>(h, I_V, p.V, c, t);
-    const double zs = rd<HOST>(h, I_ZS, p.Zs, c, t);
-    const double SDw = rd<HOST>(h, I_SDW, p.SDw, c, t), LDw = rd<HOST>(h, I_LDW, p.LDw, c, t);
-    const double z0m = RoughLength;
-    const double z0h = RoughLenHeatFactor * z0m;
-    const double humd = 1.0;
-
-    // FP64 is the scarce pipe on this GPU: divisions that do not feed a
-    // cancelling difference become products with a reciprocal (fp64::rcp,
-    // three DFMA from an FP32 seed), exp and log are the table-driven ones
-    // of fp64_fast.cuh, and the two Exner functions share one exp/log pair,
-    // (ps/P0)^k = exp(k log), with Exner(sig1 ps) = Exner(ps) sig1^k.  Each
-    // rewrite moves a result by an ulp or two, far inside the 1e-13
-    // agreement with the reference.
-    const double rPs = fp64::rcp(Ps);
-    double Frac[2], QSat[2], SVT[2], Tsn[2], Albn[2], rTs[2];
-    Frac[0] = 1.0 - SIceCon;
-    Frac[1] = SIceCon;
-    // Sea-ice flag (:269-273, :389-393): with no ice the reference still
-    // evaluates the ice column, but every ice output is then an exact zero
-    // (bulk coefficients clamp to 0); the ice physics is skipped here.  The
-    // results are the same for any positive finite ice temperature.
-    const bool ice = Frac[1] > 1e-12;
+  // FP64 is the scarce pipe on this GPU: divisions that do not feed a
+  // cancelling difference become products with a reciprocal (fp64::rcp,
+  // three DFMA from an FP32 seed), exp and log are the table-driven ones
+  // of fp64_fast.cuh, and the two Exner functions share one exp/log pair,
+  // (ps/P0)^k = exp(k log), with Exner(sig1 ps) = Exner(ps) sig1^k.  Each
+  // rewrite moves a result by an ulp or two, far inside the 1e-13
+  // agreement with the reference.
+  const double rPs = fp64::rcp(Ps);
+  double Frac[2], QSat[2], SVT[2], Tsn[2], Albn[2], rTs[2];
+  Frac[0] = 1.0 - SIceCon;
+  Frac[1] = SIceCon;
+  // Sea-ice flag (:269-273, :389-393): with no ice the reference still
+  // evaluates the ice column, but every ice output is then an exact zero
+  // (bulk coefficients clamp to 0); the ice physics is skipped here.  The
+  // results are the same for any positive finite ice temperature.
+  const bool ice = !PURE && Frac[1] > 1e-12;
+  constexpr bool pure = PURE;
 #pragma unroll
-    for (int n = 0; n < 2; ++n) {
-      Tsn[n] = rd<HOST>(h, I_TS + n, p.Ts, c + P * n, t);
-      Albn[n] = rd<HOST>(h, I_ALB + n, p.Alb, c + P * n, t);
-      if (n == 1 && !ice) {
-        rTs[n] = QSat[n] = SVT[n] = 0.0;
-        continue;
-      }
-      rTs[n] = fp64::rcp(Tsn[n]);
-      QSat[n] = (EpsV * Es0) * rPs * fp64::exp(fma(-aL[n] / GasRWet, rTs[n], aL[n] / GasRWet * (1.0 / 273.0)));
-      SVT[n] = Tsn[n] * (1.0 + (((1.0 / EpsV) - 1.0) * QSat[n]));
+  for (int n = 0; n < 2; ++n) {
+    Tsn[n] = rd<HOST>(h, I_TS + n, p.Ts, c + P * n, t);
+    Albn[n] = rd<HOST>(h, I_ALB + n, p.Alb, c + P * n, t);
+    if (n == 1 && !ice) {
+      rTs[n] = QSat[n] = SVT[n] = 0.0;
+      continue;
     }
-    const double VirTemp = Ta * (1.0 + (((1.0 / EpsV) - 1.0) * q1));
-    const double SfcExner = fp64::exp((GasRDry / CpDry) * fp64::log(Ps * (1.0 / RefPress)));
-    const double Exner = SfcExner * g.sig1k;
-    const double rExner = fp64::rcp(Exner);
-    const double rSfcExner = fp64::rcp(SfcExner);
-    const double VelAbs = fp64::sqrt(U * U + V * V);
-    // Height - zs, the reference's Height (:223-225) less the surface height
-    const double dH = g.hfac * VirTemp;
+    rTs[n] = fp64::rcp(Tsn[n]);
+    QSat[n] = (EpsV * Es0) * rPs * fp64::exp(fma(-aL[n] / GasRWet, rTs[n], aL[n] / GasRWet * (1.0 / 273.0)));
+    SVT[n] = Tsn[n] * (1.0 + (((1.0 / EpsV) - 1.0) * QSat[n]));
+  }
+  const double VirTemp = Ta * (1.0 + (((1.0 / EpsV) - 1.0) * q1));
+  const double SfcExner = fp64::exp((GasRDry / CpDry) * fp64::log(Ps * (1.0 / RefPress)));
+  const double Exner = SfcExner * g.sig1k;
+  const double rExner = fp64::rcp(Exner);
+  const double rSfcExner = fp64::rcp(SfcExner);
+  const double VelAbs = fp64::sqrt(U * U + V * V);
+  // Height - zs, the reference's Height (:223-225) less the surface height
+  const double dH = g.hfac * VirTemp;
 
-    // Neutral coefficients (:250-260) depend only on the column (the
-    // roughness lengths are the same constants for both surface types).
-    const double qm = (dH + z0m) * (1.0 / z0m);
-    const double qh = RoughLenHeatFactor == 1.0 ? qm : (dH + z0h) * (1.0 / z0h);
-    const double tmp = FKarm * fp64::rcp(fp64::log(qm));
-    const double cmn = tmp * tmp;
-    // z0h = RoughLenHeatFactor z0m: with the factor 1 both logarithms are one
-    const double chn = RoughLenHeatFactor == 1.0 ? cmn : tmp * (FKarm * fp64::rcp(fp64::log(qh)));
-    const double vmx = fmax(VelAbs, VelMinForRi);
-    const double vmx2 = vmx * vmx;
-    // The Richardson number and the sensible heat flux subtract nearly equal
-    // quotients: these keep correctly rounded divisions (Markstein's
-    // correction of a times the shared reciprocal).
-    const double VT_E = fp64::div_rb(VirTemp, Exner, rExner);
-    const double Ta_E = fp64::div_rb(Ta, Exner, rExner);
+  // Neutral coefficients (:250-260) depend only on the column (the
+  // roughness lengths are the same constants for both surface types).
+  const double qm = (dH + z0m) * (1.0 / z0m);
+  const double qh = RoughLenHeatFactor == 1.0 ? qm : (dH + z0h) * (1.0 / z0h);
+  const double tmp = FKarm * fp64::rcp(fp64::log(qm));
+  const double cmn = tmp * tmp;
+  // z0h = RoughLenHeatFactor z0m: with the factor 1 both logarithms are one
+  const double chn = RoughLenHeatFactor == 1.0 ? cmn : tmp * (FKarm * fp64::rcp(fp64::log(qh)));
+  const double vmx = fmax(VelAbs, VelMinForRi);
+  const double vmx2 = vmx * vmx;
+  // The Richardson number and the sensible heat flux subtract nearly equal
+  // quotients: these keep correctly rounded divisions (Markstein's
+  // correction of a times the shared reciprocal).
+  const double VT_E = fp64::div_rb(VirTemp, Exner, rExner);
+  const double Ta_E = fp64::div_rb(Ta, Exner, rExner);
 
-    double CVel[2], CTemp[2], CQ[2], WSX[2], WSY[2], Sen[2], QV[2], LatH[2], LUw[2], SUw[2];
-    bool flag[2];
-    double WSX3 = 0.0, WSY3 = 0.0, Sen3 = 0.0, QV3 = 0.0, SUw3 = 0.0, LUw3 = 0.0, Ts3 = 0.0,
-           Alb3 = 0.0, CVel3 = 0.0, CTemp3 = 0.0, CQ3 = 0.0;
+  double CVel[2], CTemp[2], CQ[2], WSX[2], WSY[2], Sen[2], QV[2], LatH[2], LUw[2], SUw[2];
+  bool flag[2];
+  double WSX3 = 0.0, WSY3 = 0.0, Sen3 = 0.0, QV3 = 0.0, SUw3 = 0.0, LUw3 = 0.0, Ts3 = 0.0,
+         Alb3 = 0.0, CVel3 = 0.0, CTemp3 = 0.0, CQ3 = 0.0;
 #pragma unroll
-    for (int n = 0; n < 2; ++n) {
-      const bool f = (n == 0) ? true : ice;
-      flag[n] = f;
-      if (!f) {
-        CVel[n] = CTemp[n] = CQ[n] = 0.0;
-        WSX[n] = WSY[n] = Sen[n] = QV[n] = LatH[n] = LUw[n] = SUw[n] = 0.0;
-        continue;
-      }
-      const double SVT_SE = fp64::div_rb(SVT[n], SfcExner, rSfcExner);
-      // Ri = g / SVT_SE (VT_E - SVT_SE) / vmx^2 dH and rho = Ps / (R SVT)
-      // from one reciprocal y = 1 / (SVT vmx^2): 1 / SVT_SE = SfcExner y vmx^2
-      const double y = fp64::rcp(SVT[n] * vmx2);
-      const double Ri = (Grav * SfcExner) * (VT_E - SVT_SE) * dH * y;
-      double cm, ch, cq;
-      bulk_coef_l82(Ri, qm, qh, cmn, chn, f, cm, ch, cq);
-      const double rho = (Ps * (1.0 / GasRDry)) * (vmx2 * y);
-      CVel[n] = cm * rho * fmin(fmax(VelAbs, VelMinForVel), VelMaxForVel);
-      CTemp[n] = ch * rho * fmin(fmax(VelAbs, VelMinForTemp), VelMaxForTemp);
-      CQ[n] = cq * rho * fmin(fmax(VelAbs, VelMinForQVap), VelMaxForQVap);
-      if (f) {
-        WSX[n] = -CVel[n] * U;
-        WSY[n] = -CVel[n] * V;
-        Sen[n] = -CpDry * SfcExner * CTemp[n] * (Ta_E - fp64::div_rb(Tsn[n], SfcExner, rSfcExner));
-        QV[n] = -humd * CQ[n] * (q1 - QSat[n]);
-        LatH[n] = aL[n] * QV[n];
-        const double T2 = Tsn[n] * Tsn[n];
-        const double T4 = T2 * T2;
-        LUw[n] = StB * T4;
-        SUw[n] = Albn[n] * SDw;
+  for (int n = 0; n < 2; ++n) {
+    const bool f = (n == 0) ? true : ice;
+    flag[n] = f;
+    if (!f) {
+      CVel[n] = CTemp[n] = CQ[n] = 0.0;
+      WSX[n] = WSY[n] = Sen[n] = QV[n] = LatH[n] = LUw[n] = SUw[n] = 0.0;
+      continue;
+    }
+    const double SVT_SE = fp64::div_rb(SVT[n], SfcExner, rSfcExner);
+    // Ri = g / SVT_SE (VT_E - SVT_SE) / vmx^2 dH and rho = Ps / (R SVT)
+    // from one reciprocal y = 1 / (SVT vmx^2): 1 / SVT_SE = SfcExner y vmx^2
+    const double y = fp64::rcp(SVT[n] * vmx2);
+    const double Ri = (Grav * SfcExner) * (VT_E - SVT_SE) * dH * y;
+    double cm, ch, cq;
+    bulk_coef_l82(Ri, qm, qh, cmn, chn, f, cm, ch, cq);
+    const double rho = (Ps * (1.0 / GasRDry)) * (vmx2 * y);
+    CVel[n] = cm * rho * fmin(fmax(VelAbs, VelMinForVel), VelMaxForVel);
+    CTemp[n] = ch * rho * fmin(fmax(VelAbs, VelMinForTemp), VelMaxForTemp);
+    CQ[n] = cq * rho * fmin(fmax(VelAbs, VelMinForQVap), VelMaxForQVap);
+    if (f) {
+      WSX[n] = -CVel[n] * U;
+      WSY[n] = -CVel[n] * V;
+      Sen[n] = -CpDry * SfcExner * CTemp[n] * (Ta_E - fp64::div_rb(Tsn[n], SfcExner, rSfcExner));
+      QV[n] = -humd * CQ[n] * (q1 - QSat[n]);
+      LatH[n] = aL[n] * QV[n];
+      const double T2 = Tsn[n] * Tsn[n];
+      const double T4 = T2 * T2;
+      LUw[n] = StB * T4;
+      SUw[n] = Albn[n] * SDw;
+      if (pure) {  // n = 0 only
+        Ts3 = T4;
+        Alb3 = Albn[n];
+        WSX3 = WSX[n];
+        WSY3 = WSY[n];
+        Sen3 = Sen[n];
+        QV3 = QV[n];
+        LUw3 = LUw[n];
+        SUw3 = SUw[n];
+        CVel3 = CVel[n];
+        CTemp3 = CTemp[n];
+        CQ3 = CQ[n];
+      } else {
         Ts3 = Ts3 + Frac[n] * T4;
         Alb3 = Alb3 + Frac[n] * Albn[n];
         WSX3 = WSX3 + Frac[n] * WSX[n];
@@ -228,87 +241,109 @@ __global__ void __launch_bounds__(256, 2) bulk_flux_column(Ptrs p, Geom g, const
         CVel3 = CVel3 + Frac[n] * CVel[n];
         CTemp3 = CTemp3 + Frac[n] * CTemp[n];
         CQ3 = CQ3 + Frac[n] * CQ[n];
-      } else {
-        WSX[n] = WSY[n] = Sen[n] = QV[n] = LatH[n] = LUw[n] = SUw[n] = 0.0;
       }
+    } else {
+      WSX[n] = WSY[n] = Sen[n] = QV[n] = LatH[n] = LUw[n] = SUw[n] = 0.0;
     }
+  }
 
-    // Implicit-coupling back-substitution (:355-382).
-    const double c11 = rd<HOST>(h, I_C1, p.C1, c, t), c12 = rd<HOST>(h, I_C1 + 1, p.C1, c + P, t),
-                 c13 = rd<HOST>(h, I_C1 + 2, p.C1, c + 2 * P, t), c14 = rd<HOST>(h, I_C1 + 3, p.C1, c + 3 * P, t);
-    const double c21 = rd<HOST>(h, I_C2, p.C2, c, t), c22 = rd<HOST>(h, I_C2 + 1, p.C2, c + P, t),
-                 c23 = rd<HOST>(h, I_C2 + 2, p.C2, c + 2 * P, t), c24 = rd<HOST>(h, I_C2 + 3, p.C2, c + 3 * P, t);
-    if (HOST) {  // every input has been read: the bound ones into their device rows
-      const double vin[NIN] = {SIceCon, Ps, Ta, q1, U, V, zs, SDw, LDw, Tsn[0], Tsn[1], Albn[0], Albn[1],
-                               c11, c12, c13, c14, c21, c22, c23, c24};
+  // Implicit-coupling back-substitution (:355-382).
+  const double c11 = rd<HOST>(h, I_C1, p.C1, c, t), c12 = rd<HOST>(h, I_C1 + 1, p.C1, c + P, t),
+               c13 = rd<HOST>(h, I_C1 + 2, p.C1, c + 2 * P, t), c14 = rd<HOST>(h, I_C1 + 3, p.C1, c + 3 * P, t);
+  const double c21 = rd<HOST>(h, I_C2, p.C2, c, t), c22 = rd<HOST>(h, I_C2 + 1, p.C2, c + P, t),
+               c23 = rd<HOST>(h, I_C2 + 2, p.C2, c + 2 * P, t), c24 = rd<HOST>(h, I_C2 + 3, p.C2, c + 3 * P, t);
+  if (HOST) {  // every input has been read: the bound ones into their device rows
+    const double vin[NIN] = {SIceCon, Ps, Ta, q1, U, V, zs, SDw, LDw, Tsn[0], Tsn[1], Albn[0], Albn[1],
+                             c11, c12, c13, c14, c21, c22, c23, c24};
 #pragma unroll
-      for (int k = 0; k < NIN; ++k) mirror<HOST>(h, k, t, vin[k]);
-    }
-    const double DFsDT1 = -CpDry * SfcExner * CTemp3 * rExner;
-    const double f1 = fp64::rcp(c11 + CVel3) * (WSX3 + c21);
-    const double f2 = fp64::rcp(c12 + CVel3) * (WSY3 + c22);
-    const double f3 = fp64::rcp(c13 - DFsDT1) * (Sen3 + c23);
-    const double f4 = fp64::rcp(c14 + humd * CQ3) * (QV3 + c24);
-    wr<HOST>(h, O_DELV, p.DelV, c, t, f1);
-    wr<HOST>(h, O_DELV + 1, p.DelV, c + P, t, f2);
-    wr<HOST>(h, O_DELV + 2, p.DelV, c + 2 * P, t, f3);
-    wr<HOST>(h, O_DELV + 3, p.DelV, c + 3 * P, t, f4);
+    for (int k = 0; k < NIN; ++k) mirror<HOST>(h, k, t, vin[k]);
+  }
+  const double DFsDT1 = -CpDry * SfcExner * CTemp3 * rExner;
+  const double f1 = fp64::rcp(c11 + CVel3) * (WSX3 + c21);
+  const double f2 = fp64::rcp(c12 + CVel3) * (WSY3 + c22);
+  const double f3 = fp64::rcp(c13 - DFsDT1) * (Sen3 + c23);
+  const double f4 = fp64::rcp(c14 + humd * CQ3) * (QV3 + c24);
+  wr<HOST>(h, O_DELV, p.DelV, c, t, f1);
+  wr<HOST>(h, O_DELV + 1, p.DelV, c + P, t, f2);
+  wr<HOST>(h, O_DELV + 2, p.DelV, c + 2 * P, t, f3);
+  wr<HOST>(h, O_DELV + 3, p.DelV, c + 3 * P, t, f4);
 
-    const double sfac = CpDry * SfcExner * rExner;
-    double Lat3 = 0.0;
+  const double sfac = CpDry * SfcExner * rExner;
+  double Lat3 = 0.0;
 #pragma unroll
-    for (int n = 0; n < 2; ++n) {
-      if (n == 1 && !ice) break;  // the ice slot's zeros stay zeros (0 - 0 f = 0 for finite f)
-      WSX[n] = WSX[n] - CVel[n] * f1;
-      WSY[n] = WSY[n] - CVel[n] * f2;
-      Sen[n] = Sen[n] - sfac * CTemp[n] * f3;
-      QV[n] = QV[n] - humd * CQ[n] * f4;
-      LatH[n] = aL[n] * QV[n];
-      if (flag[n]) Lat3 = Lat3 + Frac[n] * LatH[n];
-    }
+  for (int n = 0; n < 2; ++n) {
+    if (n == 1 && !ice) break;  // the ice slot's zeros stay zeros (0 - 0 f = 0 for finite f)
+    WSX[n] = WSX[n] - CVel[n] * f1;
+    WSY[n] = WSY[n] - CVel[n] * f2;
+    Sen[n] = Sen[n] - sfac * CTemp[n] * f3;
+    QV[n] = QV[n] - humd * CQ[n] * f4;
+    LatH[n] = aL[n] * QV[n];
+    if (flag[n] && !pure) Lat3 = Lat3 + Frac[n] * LatH[n];
+  }
+  if (pure) {  // the merged values are slot 0's and get its update
+    WSX3 = WSX[0];
+    WSY3 = WSY[0];
+    Sen3 = Sen[0];
+    QV3 = QV[0];
+    Lat3 = LatH[0];
+  } else {
     WSX3 = WSX3 - CVel3 * f1;
     WSY3 = WSY3 - CVel3 * f2;
     Sen3 = Sen3 - sfac * CTemp3 * f3;
     QV3 = QV3 - humd * CQ3 * f4;
+  }
 
-    // Net heat fluxes and dF/dTs (:384-415), flag per surface type.
+  // Net heat fluxes and dF/dTs (:384-415), flag per surface type.
 #pragma unroll
-    for (int n = 0; n < 2; ++n) {
-      double fns = 0.0, fsr = 0.0, dfdt = 0.0;
-      if (flag[n]) {
-        fns = +LUw[n] - LDw + LatH[n] + Sen[n];
-        fsr = SUw[n] - SDw;
-        dfdt = +4.0 * StB * (Tsn[n] * Tsn[n] * Tsn[n]) + CpDry * CTemp[n] +
-               (aL[n] * aL[n] * humd / GasRWet) * (CQ[n] * QSat[n]) * (rTs[n] * rTs[n]);
-      }
-      const int64_t cn = c + P * n;
-      wr<HOST>(h, O_FNS + n, p.Fns, cn, t, fns);
-      wr<HOST>(h, O_FSR + n, p.Fsr, cn, t, fsr);
-      wr<HOST>(h, O_DFDT + n, p.DFdT, cn, t, dfdt);
-      wr<HOST>(h, O_WSX + n, p.WSX, cn, t, WSX[n]);
-      wr<HOST>(h, O_WSY + n, p.WSY, cn, t, WSY[n]);
-      wr<HOST>(h, O_SEN + n, p.Sen, cn, t, Sen[n]);
-      wr<HOST>(h, O_QV + n, p.QV, cn, t, QV[n]);
-      wr<HOST>(h, O_LAT + n, p.Lat, cn, t, LatH[n]);
-      wr<HOST>(h, O_CVEL + n, p.CVel, cn, t, CVel[n]);
-      wr<HOST>(h, O_CTEMP + n, p.CTemp, cn, t, CTemp[n]);
-      wr<HOST>(h, O_CQ + n, p.CQ, cn, t, CQ[n]);
-      wr<HOST>(h, O_SUW + n, p.SUw, cn, t, SUw[n]);
-      wr<HOST>(h, O_LUW + n, p.LUw, cn, t, LUw[n]);
+  for (int n = 0; n < 2; ++n) {
+    double fns = 0.0, fsr = 0.0, dfdt = 0.0;
+    if (flag[n]) {
+      fns = +LUw[n] - LDw + LatH[n] + Sen[n];
+      fsr = SUw[n] - SDw;
+      dfdt = +4.0 * StB * (Tsn[n] * Tsn[n] * Tsn[n]) + CpDry * CTemp[n] +
+             (aL[n] * aL[n] * humd / GasRWet) * (CQ[n] * QSat[n]) * (rTs[n] * rTs[n]);
     }
-    const int64_t c3 = c + 2 * P;
-    wr<HOST>(h, O_WSX + 2, p.WSX, c3, t, WSX3);
-    wr<HOST>(h, O_WSY + 2, p.WSY, c3, t, WSY3);
-    wr<HOST>(h, O_SEN + 2, p.Sen, c3, t, Sen3);
-    wr<HOST>(h, O_QV + 2, p.QV, c3, t, QV3);
-    wr<HOST>(h, O_LAT + 2, p.Lat, c3, t, Lat3);
-    wr<HOST>(h, O_CVEL + 2, p.CVel, c3, t, CVel3);
-    wr<HOST>(h, O_CTEMP + 2, p.CTemp, c3, t, CTemp3);
-    wr<HOST>(h, O_CQ + 2, p.CQ, c3, t, CQ3);
-    wr<HOST>(h, O_SUW + 2, p.SUw, c3, t, SUw3);
-    wr<HOST>(h, O_LUW + 2, p.LUw, c3, t, LUw3);
-    wr<HOST>(h, O_TS3, p.Ts, c3, t, Ts3);
-    wr<HOST>(h, O_ALB3, p.Alb, c3, t, Alb3);
+    const int64_t cn = c + P * n;
+    wr<HOST>(h, O_FNS + n, p.Fns, cn, t, fns);
+    wr<HOST>(h, O_FSR + n, p.Fsr, cn, t, fsr);
+    wr<HOST>(h, O_DFDT + n, p.DFdT, cn, t, dfdt);
+    wr<HOST>(h, O_WSX + n, p.WSX, cn, t, WSX[n]);
+    wr<HOST>(h, O_WSY + n, p.WSY, cn, t, WSY[n]);
+    wr<HOST>(h, O_SEN + n, p.Sen, cn, t, Sen[n]);
+    wr<HOST>(h, O_QV + n, p.QV, cn, t, QV[n]);
+    wr<HOST>(h, O_LAT + n, p.Lat, cn, t, LatH[n]);
+    wr<HOST>(h, O_CVEL + n, p.CVel, cn, t, CVel[n]);
+    wr<HOST>(h, O_CTEMP + n, p.CTemp, cn, t, CTemp[n]);
+    wr<HOST>(h, O_CQ + n, p.CQ, cn, t, CQ[n]);
+    wr<HOST>(h, O_SUW + n, p.SUw, cn, t, SUw[n]);
+    wr<HOST>(h, O_LUW + n, p.LUw, cn, t, LUw[n]);
+  }
+  const int64_t c3 = c + 2 * P;
+  wr<HOST>(h, O_WSX + 2, p.WSX, c3, t, WSX3);
+  wr<HOST>(h, O_WSY + 2, p.WSY, c3, t, WSY3);
+  wr<HOST>(h, O_SEN + 2, p.Sen, c3, t, Sen3);
+  wr<HOST>(h, O_QV + 2, p.QV, c3, t, QV3);
+  wr<HOST>(h, O_LAT + 2, p.Lat, c3, t, Lat3);
+  wr<HOST>(h, O_CVEL + 2, p.CVel, c3, t, CVel3);
+  wr<HOST>(h, O_CTEMP + 2, p.CTemp, c3, t, CTemp3);
+  wr<HOST>(h, O_CQ + 2, p.CQ, c3, t, CQ3);
+  wr<HOST>(h, O_SUW + 2, p.SUw, c3, t, SUw3);
+  wr<HOST>(h, O_LUW + 2, p.LUw, c3, t, LUw3);
+  wr<HOST>(h, O_TS3, p.Ts, c3, t, Ts3);
+  wr<HOST>(h, O_ALB3, p.Alb, c3, t, Alb3);
+}
+
+template <bool HOST>
+__global__ void __launch_bounds__(256, 2) bulk_flux_column(Ptrs p, Geom g, const __grid_constant__ HostRows h) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < g.ncol;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int ii = (int)(t % g.NI);
+    const int jj = (int)(t / g.NI);
+    const int64_t c = (int64_t)(g.IS - 1 + ii) + (int64_t)g.IA * (g.JS - 1 + jj);
+    const double SIceCon = rd<HOST>(h, I_ICE, p.Ice, c, t);
+    const bool pure = ((unsigned long long)__double_as_longlong(SIceCon) << 1) == 0ull;
+    if (__all_sync(__activemask(), pure)) flux_column<HOST, true>(p, g, h, t, c, SIceCon);
+    else flux_column<HOST, false>(p, g, h, t, c, SIceCon);
   }
 }
 
