@@ -261,7 +261,7 @@ def fp64_fn_dev(fn, x, y, stream=None):
 def tune_set(knob, value):
     """dccm_tune_set: process-wide knob (launch shapes tc_shape, tc_ctas,
     fft_bb, fft_rpw, flux_threads, flux_ctas, remap_threads, remap_fc,
-    serial; host copies upload_order,
+    serial, prio; host copies upload_order,
     host_path; failure path wait_limit_ms, tc_withhold_loads); 0 = the
     default."""
     _check(load().dccm_tune_set(knob.encode(), int(value)), "dccm_tune_set")
@@ -735,6 +735,7 @@ class Step:
         chosen["remap_fc"] = tune_get("remap_fc")
         chosen["tc_shape"] = tune_get("tc_shape")
         chosen["fft_rpw"] = tune_get("fft_rpw")
+        chosen["prio"] = tune_get("prio")
         return chosen
 
     def run_timed(self, stream=None):

@@ -39,6 +39,9 @@ struct Tunables {
   int remap_threads = 0;  // threads per CTA of the remap kernel
   int remap_fc = 0;       // fields per thread of the remap kernel (1, 2, 3, 4, 6; 0: 3, or all below 6)
   int serial = 0;         // 1: launch_pdl makes ordinary launches
+  int prio = 0;           // 1: the transform chain's launches (launch_pdl), 2: the surface branch's
+                          // (launch_surface) at the device's greatest priority; the step graphs
+                          // then run their nodes at their own priorities
   int upload_order = 0;   // dccm_step_run_host: 1 transforms' inputs first, 2 surface inputs first
   int host_path = 0;      // dccm_step_run_host: 1 + mask of the copy groups moved through the host mapping (0: 1)
   int wait_limit_ms = 0;  // limit of the tensor-core kernel's bounded waits (0: 1000 ms)
@@ -58,6 +61,9 @@ Tunables &tunables();
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
+// The device's greatest (most urgent) stream priority (cached).
+int greatest_priority();
+
 template <typename... KArgs, typename... Args>
 inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
                               Args &&...args) {
@@ -66,11 +72,36 @@ inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, s
   cfg.blockDim = block;
   cfg.dynamicSmemBytes = smem;
   cfg.stream = s;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchAttribute attr[2];
+  unsigned n = 0;
+  if (!tunables().serial) {
+    attr[n].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[n++].val.programmaticStreamSerializationAllowed = 1;
+  }
+  if (tunables().prio == 1) {
+    attr[n].id = cudaLaunchAttributePriority;
+    attr[n++].val.priority = greatest_priority();
+  }
   cfg.attrs = attr;
-  cfg.numAttrs = tunables().serial ? 0 : 1;
+  cfg.numAttrs = n;
+  return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
+// Launch of a surface-branch kernel (remap, flux): at the device's greatest
+// priority with the "prio" knob at 2, else an ordinary launch.
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_surface(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                                  Args &&...args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributePriority;
+  attr[0].val.priority = greatest_priority();
+  cfg.attrs = attr;
+  cfg.numAttrs = tunables().prio == 2 ? 1 : 0;
   return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
 }
 

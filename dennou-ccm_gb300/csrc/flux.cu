@@ -405,9 +405,9 @@ int launch(const Ptrs &p, const dccm_sfc_grid *g, double sig1, cudaStream_t s, c
     hr = &none;
   }
   if (hr->any)
-    bulk_flux_column<true><<<(unsigned)blocks, threads, 0, s>>>(p, geo, *hr);
+    DCCM_CUDA(launch_surface(bulk_flux_column<true>, dim3((unsigned)blocks), dim3(threads), 0, s, p, geo, *hr));
   else
-    bulk_flux_column<false><<<(unsigned)blocks, threads, 0, s>>>(p, geo, *hr);
+    DCCM_CUDA(launch_surface(bulk_flux_column<false>, dim3((unsigned)blocks), dim3(threads), 0, s, p, geo, *hr));
   DCCM_LAUNCH_CHECK();
   return DCCM_OK;
 }

@@ -147,8 +147,9 @@ int apply2(dccm_remap_plan *p, const double *src, int64_t ld_src, double *dst, i
   const dim3 grid((unsigned)blocks, (unsigned)ychunks);
   const int ns = (int)p->nslice;
 #define DCCM_SELL(FC_)                                                                                   \
-  sell_apply<FC_><<<grid, threads, 0, s>>>(p->d_slices, p->d_rows, p->d_ent, src, ld_src, dst, ld_dst, ns, \
-                                           nfields, nsub, ld_dst2)
+  DCCM_CUDA(launch_surface(sell_apply<FC_>, grid, dim3(threads), 0, s, (const int2 *)p->d_slices,          \
+                           (const int *)p->d_rows, (const double2 *)p->d_ent, src, ld_src, dst, ld_dst, ns, \
+                           nfields, nsub, ld_dst2))
   switch (fc) {
     case 6: DCCM_SELL(6); break;
     case 4: DCCM_SELL(4); break;

@@ -22,6 +22,16 @@ int sm_count() {
   }
   return cached[dev];
 }
+
+int greatest_priority() {
+  static int cached = 1;  // 1: not read yet (priorities are 0 or negative)
+  if (cached == 1) {
+    int least = 0, greatest = 0;
+    if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) greatest = 0;
+    cached = greatest;
+  }
+  return cached;
+}
 }  // namespace dccm
 
 extern "C" {

@@ -506,6 +506,16 @@ static int capture(dccm_step *st, const HostSets *hp, cudaGraph_t *out) {
   return DCCM_OK;
 }
 
+// With the "prio" knob one branch's kernels are recorded at the device's
+// greatest priority (1: the transform chain, launch_pdl; 2: the remaps and
+// the flux, launch_surface) and the graph is instantiated to run every node
+// at its own priority (otherwise all run at the launching stream's), so
+// that SMs freed while both branches have CTAs waiting go to that branch
+// first.
+static unsigned long long instantiate_flags() {
+  return tunables().prio ? (unsigned long long)cudaGraphInstantiateFlagUseNodePriority : 0ull;
+}
+
 static void drop_host_graph(dccm_step *st) {
   // a launch by dccm_step_launch_host may still be running on its stream
   if (st->hexec || !st->host_tabs.empty()) cudaDeviceSynchronize();
@@ -543,7 +553,7 @@ static int record(dccm_step *st) {
   cudaGraph_t g = nullptr;
   DCCM_TRY(capture(st, nullptr, &g));
   st->graph = g;
-  DCCM_CUDA(cudaGraphInstantiate(&st->exec, g, 0));
+  DCCM_CUDA(cudaGraphInstantiate(&st->exec, g, instantiate_flags()));
   return DCCM_OK;
 }
 
@@ -844,7 +854,7 @@ static int build_host_graph(dccm_step *st, const dccm_host_copy *h2d, int nh2d, 
   T.flux_threads = flux_threads;
   DCCM_TRY(rc);
   st->hgraph = g;
-  DCCM_CUDA(cudaGraphInstantiate(&st->hexec, g, 0));
+  DCCM_CUDA(cudaGraphInstantiate(&st->hexec, g, instantiate_flags()));
   st->host_h2d.assign(h2d, h2d + nh2d);
   st->host_d2h.assign(d2h, d2h + nd2h);
   return DCCM_OK;
@@ -1105,6 +1115,7 @@ static bool cache_lookup(const char *path, const std::string &key, Tunables &t) 
     if ((p = strstr(line, "\"remap_threads\": "))) v.remap_threads = atoi(p + 17);
     if ((p = strstr(line, "\"remap_fc\": "))) v.remap_fc = atoi(p + 12);
     if ((p = strstr(line, "\"serial\": "))) v.serial = atoi(p + 10);
+    if ((p = strstr(line, "\"prio\": "))) v.prio = atoi(p + 8);
     if ((p = strstr(line, "\"flux_ctas\": "))) v.flux_ctas = atoi(p + 13);
     t = v;
     found = true;
@@ -1120,10 +1131,10 @@ static void cache_store(const char *path, const std::string &key, const Tunables
   if (!fp) return;
   fprintf(fp,
           "{\"key\": \"%s\", \"tc_shape\": %d, \"tc_ctas\": %d, \"fft_bb\": %d, \"fft_rpw\": %d, \"flux_threads\": %d, \"remap_threads\": %d, "
-          "\"remap_fc\": %d, \"serial\": %d, \"flux_ctas\": %d, \"step_ms\": %.4f, "
+          "\"remap_fc\": %d, \"serial\": %d, \"prio\": %d, \"flux_ctas\": %d, \"step_ms\": %.4f, "
           "\"stage_ms\": [%.4f, %.4f, %.4f, %.4f, %.4f, %.4f]}\n",
           key.c_str(), t.tc_shape, t.tc_ctas, t.fft_bb, t.fft_rpw, t.flux_threads, t.remap_threads, t.remap_fc, t.serial,
-          t.flux_ctas,
+          t.prio, t.flux_ctas,
           step_ms, ms[0],
           ms[1], ms[2], ms[3], ms[4], ms[5]);
   fclose(fp);
@@ -1249,6 +1260,7 @@ extern "C" int dccm_step_autotune(dccm_step *st, const char *cache_path, int *ch
     Knob graph_knobs[] = {
         {&T.serial, {0, 1}, -1, -1},
         {&T.tc_ctas, first(T.tc_ctas, {2 * sms, sms, sms * 3 / 4, sms / 2}), -1, -1},
+        {&T.prio, {0, 2, 1}, -1, -1},
     };
     float step_ms = 0.f;
     for (Knob &kb : graph_knobs) {
@@ -1259,31 +1271,39 @@ extern "C" int dccm_step_autotune(dccm_step *st, const char *cache_path, int *ch
         return rc;
       }
     }
-    // The flux CTA size and grid cap together: how many flux warps an SM
-    // holds beside the transforms depends on both (e.g. at T341 one
-    // 128-thread CTA an SM beat the best cap for the stage pass's 64).
+    // The branch priority, the flux CTA size and the flux grid cap
+    // together: how many flux warps an SM holds beside the transforms, and
+    // when, depends on all three (e.g. at T341 one 128-thread CTA an SM
+    // beat the best cap for the stage pass's 64; the ensemble of 64 small
+    // transforms gained most from the flux first with that shape, which
+    // neither knob found alone).
     if (st->d.flux) {
+      const std::vector<int> prs = first(T.prio, {0, 2, 1});
       const std::vector<int> fts = first(T.flux_threads, {64, 128, 256});
       const int fcs[] = {0, sms * 4, sms * 2, sms};
-      int bft = T.flux_threads, bfc = 0;
+      int bpr = T.prio, bft = T.flux_threads, bfc = 0;
       float bt = 1e30f;
-      for (int a : fts)
-        for (int c : fcs) {
-          T.flux_threads = a;
-          T.flux_ctas = c;
-          float t;
-          const int rc = time_graph(st, s, 7, &t);
-          if (rc != DCCM_OK) {
-            T = saved;
-            rerecord(st);
-            return rc;
+      for (int q : prs)
+        for (int a : fts)
+          for (int c : fcs) {
+            T.prio = q;
+            T.flux_threads = a;
+            T.flux_ctas = c;
+            float t;
+            const int rc = time_graph(st, s, 7, &t);
+            if (rc != DCCM_OK) {
+              T = saved;
+              rerecord(st);
+              return rc;
+            }
+            if (t < bt * 0.98f || bt == 1e30f) {
+              bt = t;
+              bpr = q;
+              bft = a;
+              bfc = c;
+            }
           }
-          if (t < bt * 0.98f || bt == 1e30f) {
-            bt = t;
-            bft = a;
-            bfc = c;
-          }
-        }
+      T.prio = bpr;
       T.flux_threads = bft;
       T.flux_ctas = bfc;
       step_ms = bt;
@@ -1316,6 +1336,10 @@ extern "C" int dccm_tune_set(const char *knob, int value) {
   else if (!strcmp(knob, "remap_fc")) T.remap_fc = value;
   else if (!strcmp(knob, "flux_ctas")) T.flux_ctas = value;
   else if (!strcmp(knob, "serial")) T.serial = value ? 1 : 0;
+  else if (!strcmp(knob, "prio")) {
+    if (value > 2) return DCCM_ERR_INVALID_ARG;
+    T.prio = value;
+  }
   else if (!strcmp(knob, "upload_order")) {
     if (value > 2) return DCCM_ERR_INVALID_ARG;
     T.upload_order = value;
@@ -1344,6 +1368,7 @@ extern "C" int dccm_tune_get(const char *knob, int *value) {
   else if (!strcmp(knob, "remap_fc")) *value = T.remap_fc;
   else if (!strcmp(knob, "flux_ctas")) *value = T.flux_ctas;
   else if (!strcmp(knob, "serial")) *value = T.serial;
+  else if (!strcmp(knob, "prio")) *value = T.prio;
   else if (!strcmp(knob, "upload_order")) *value = T.upload_order;
   else if (!strcmp(knob, "host_path")) *value = T.host_path;
   else if (!strcmp(knob, "wait_limit_ms")) *value = T.wait_limit_ms;

@@ -547,9 +547,13 @@ int dccm_step_autotune_host(dccm_step *step, void *stream, const dccm_host_copy 
  * (4, 8 or 16), "flux_threads", "remap_threads": CTA sizes, "remap_fc":
  * fields per thread of the remap, 1, 2, 3, 4 or 6), then "serial"
  * (1: ordinary launches instead of programmatic dependent launches along
- * the transform chain), "tc_ctas" again, and "flux_threads" with
- * "flux_ctas" (CTA cap of the flux kernel's grid, 0: 16 per SM) as pairs
- * (3 x 4 candidates) on replays of the whole step graph,
+ * the transform chain), "tc_ctas" again, "prio" (0: every kernel at the
+ * launching stream's priority; 1: the transform chain's, 2: the remaps'
+ * and the flux's kernels at the device's greatest priority, so that SMs
+ * freed while both branches have CTAs waiting go to that branch first),
+ * and, with a flux, "prio", "flux_threads" and "flux_ctas" (CTA cap of the
+ * flux kernel's grid, 0: 16 per SM) together (3 x 3 x 4 candidates), on
+ * replays of the whole step graph,
  * where the two branches run concurrently; applies the winners and
  * records the step's graph again.  Every timed run follows a 256 MB
  * device write, so that the step finds L2 as it does between the model's
@@ -557,7 +561,7 @@ int dccm_step_autotune_host(dccm_step *step, void *stream, const dccm_host_copy 
  * from / appended to that file (one JSON object per line, keyed by the
  * GPU name and SM count and the step's shapes).  chosen (4 ints, may be
  * NULL) receives tc_ctas, fft_bb, flux_threads, remap_threads (read
- * "serial", "flux_ctas", "remap_fc", "tc_shape" and "fft_rpw" with dccm_tune_get).  The knobs are
+ * "serial", "prio", "flux_ctas", "remap_fc", "tc_shape" and "fft_rpw" with dccm_tune_get).  The knobs are
  * process-wide defaults of later launches too. */
 int dccm_step_autotune(dccm_step *step, const char *cache_path, int *chosen);
 /* Process-wide knobs of later launches (and of graphs recorded later): the

@@ -90,7 +90,7 @@ def test_failure_path_knobs(dccm):
     try:
         dccm.tune_set("wait_limit_ms", 60000)
         assert dccm.tune_get("wait_limit_ms") == 60000
-        for bad in (("wait_limit_ms", 60001), ("wait_limit_ms", -1), ("no_such_knob", 1)):
+        for bad in (("wait_limit_ms", 60001), ("wait_limit_ms", -1), ("no_such_knob", 1), ("prio", 3)):
             try:
                 dccm.tune_set(*bad)
                 raise AssertionError("accepted %r" % (bad,))

@@ -188,7 +188,8 @@ def test_remap_two_level_destination(dccm, oracle, synth, cuda):
 def test_autotune_keeps_results_and_caches(dccm, oracle, synth, cuda, tmp_path):
     """Every launch shape the autotuner can pick (Legendre CTA count, FFT
     CTA size and row pairs per warp, flux and remap CTA sizes, plain or
-    programmatic dependent launches) computes each output element the same way, so the step's
+    programmatic dependent launches, either branch at the greatest
+    priority) computes each output element the same way, so the step's
     outputs are bit-identical before and after tuning; the cache file
     returns the same choice on a second call."""
     torch = cuda
@@ -203,7 +204,7 @@ def test_autotune_keeps_results_and_caches(dccm, oracle, synth, cuda, tmp_path):
         torch.cuda.synchronize()
         return [o.cpu().clone() for o in outs]
 
-    extra = ["serial", "flux_ctas", "remap_fc", "tc_shape", "fft_rpw"]
+    extra = ["serial", "flux_ctas", "remap_fc", "tc_shape", "fft_rpw", "prio"]
     saved = {k: dccm.tune_get(k) for k in dccm.Step.KNOBS + extra}
     try:
         want = run()
@@ -219,7 +220,8 @@ def test_autotune_keeps_results_and_caches(dccm, oracle, synth, cuda, tmp_path):
         # at a few CTAs (each walks many columns), gives the same bits
         for knob, v in (("serial", 0), ("serial", 1), ("flux_ctas", 3), ("remap_fc", 1), ("remap_fc", 6),
                         ("remap_fc", 4), ("remap_threads", 32), ("tc_shape", 1), ("tc_shape", 0),
-                        ("tc_ctas", 7), ("fft_rpw", 2), ("fft_bb", 4), ("fft_bb", 16), ("fft_rpw", 1)):
+                        ("tc_ctas", 7), ("fft_rpw", 2), ("fft_bb", 4), ("fft_bb", 16), ("fft_rpw", 1),
+                        ("prio", 1), ("prio", 2), ("prio", 0)):
             dccm.tune_set(knob, v)
             S = bench.gpu_setup(w, inp, dccm, synth, torch, torch.device("cuda", 0))
             step = S["steps"]["mixed"]
