@@ -643,9 +643,10 @@ template <int W> __device__ __forceinline__ int mw_k1(int wq, int j) {
 
 // A CTA's warps form groups of W, one row pair per group at a time; with
 // more row pairs than groups (the fft_rpw knob) a group takes them in
-// turns (passes), every pass ending at a CTA barrier before the group's
-// exchange buffer is written again.  More field-levels a CTA make the forward's G3
-// runs longer (a whole 32-byte sector per BF16 plane from 8 field-levels).
+// turns (passes), every pass ending at the group's own barrier before its
+// exchange buffer is written again.  More field-levels a CTA make the
+// forward's G3 runs longer (a whole 32-byte sector per BF16 plane from 8
+// field-levels).
 template <int W>
 __device__ __forceinline__ void fft_inv_block_mwp(const FftGroup &G, int jj, int by, float *st) {
   constexpr int R = MW_R0 * W, I = 32 * R, L = 32 * W, NK = MW_R0 / W;
