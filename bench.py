@@ -547,21 +547,33 @@ def roofline(S, inp, groups, stage_ms, workload, fp64_peak, flux_alone=None, pro
     if flux_alone:
         stages["bulk_flux"]["launch"] = ("full grid, timed alone; in the step its grid is capped at %d CTAs "
                                          "(%.4f ms there)" % (flux_alone["step_cta_cap"], flux_alone["ms_in_step"]))
+    # FP64 pipe occupancy beside the flop rate: a DADD, a DMUL and a DFMA
+    # each take one issue slot of the FP64 pipe (2 lanes per SM and clock),
+    # so the pipe's operation rate is half the measured DFMA flop rate and a
+    # kernel of separate multiplies and adds is bound there, at half the
+    # flop peak.
+    def pipe(ops, ms):
+        rate = ops / (ms / 1e3) / 1e12
+        return {"ops_per_launch": ops, "achieved": rate, "unit": "T ops/s", "peak": fp64_peak / 2,
+                "frac": rate / (fp64_peak / 2), "floor_ms": ops / (fp64_peak / 2 * 1e12) * 1e3}
     f64 = FLUX_FP64_INSTR_PER_COLUMN * S["ncol"]
     tf = f64 / (stages["bulk_flux"]["ms"] / 1e3) / 1e12
     stages["bulk_flux"]["fp64"] = {"achieved": tf, "unit": "TFLOP/s", "peak": fp64_peak,
                                    "peak_source": "measured (dccm_fp64_peak)", "frac": tf / fp64_peak,
                                    "flops_per_launch": f64,
                                    "count": "FP64 pipe work per column from ncu instruction counts (DADD + DMUL "
-                                            "+ 2 DFMA), the same for every ice-free column"}
+                                            "+ 2 DFMA), the same for every ice-free column",
+                                   "pipe": pipe(FLUX_FP64_PIPE_OPS_PER_COLUMN * S["ncol"], stages["bulk_flux"]["ms"])}
     # the remap keeps the reference's separately rounded products and sums
-    # (bit-exact): one DMUL and one DADD per table entry and field, reported
-    # beside its bytes
+    # (bit-exact): one DMUL per table entry and field, and one DADD per
+    # entry and field after each row's first (the first addition, 0 + p, is
+    # done on the integer pipes), reported beside its bytes
     rf = sum(2.0 * len(t[2]) * 6 * len(g.members) for g, t in zip(groups, S["tables"]))
+    rops = sum((2.0 * len(t[2]) - len(np.unique(t[1]))) * 6 * len(g.members) for g, t in zip(groups, S["tables"]))
     tf = rf / (stages["remap"]["ms"] / 1e3) / 1e12
     stages["remap"]["fp64"] = {"achieved": tf, "unit": "TFLOP/s", "peak": fp64_peak,
                                "peak_source": "measured (dccm_fp64_peak)", "frac": tf / fp64_peak,
-                               "flops_per_launch": rf}
+                               "flops_per_launch": rf, "pipe": pipe(rops, stages["remap"]["ms"])}
     cq = sum(work[n][0] for n in CHAIN)
     cms = sum(stage_ms[names.index(n)] for n in CHAIN)
     ctr = [traffic.get(n) for n in CHAIN]
@@ -604,6 +616,8 @@ def roofline_f64(groups, stage_ms, fp64_peak):
 # columns all have SIceCon = 0 skip the ice physics and the merging), so
 # the per-column figure carries to every workload.
 FLUX_FP64_INSTR_PER_COLUMN = (1182428 + 3137982 + 2 * 5002580) / 45478
+# the same counts as FP64 pipe operations (one issue slot each)
+FLUX_FP64_PIPE_OPS_PER_COLUMN = (1182428 + 3137982 + 5002580) / 45478
 
 
 # FP64 flops of the implicit-coupling sweeps per column and level, one
