@@ -6,7 +6,11 @@
 // keeps ~25 full-grid temporaries; here every statement is column-local,
 // so one thread evaluates the whole routine for one column in registers:
 // 21 FP64 reads and 42 FP64 writes per column, nothing else touches HBM.
-// Expressions keep the reference's evaluation order.  The two reference
+// Expressions follow the reference's, except that divisions not followed
+// by a cancelling difference are products with a shared reciprocal, the
+// elementary functions are those of fp64_fast.cuh (within 2 ulp), and a
+// few common factors are computed once; each such step moves a result by
+// an ulp or two, far inside the 1e-13 agreement tested.  The two reference
 // behaviours without a single defined result are given the meaning stated
 // in dccm_gb300.h (per-type sea-ice flag in the final loop; slot-3 latent
 // heat flux as the fraction-weighted merge of slots 1 and 2).
