@@ -511,6 +511,26 @@ def stage_work_f64(groups):
 CHAIN = ["legendre_inverse", "fft_inverse", "fft_forward", "legendre_forward"]
 
 
+def fp64_pipe(ops, ms, fp64_peak):
+    """FP64 pipe occupancy of a stage: a DADD, a DMUL and a DFMA each take
+    one issue slot of the FP64 pipe (2 lanes per SM and clock), so the
+    pipe's operation rate is half the measured DFMA flop rate (TFLOP/s)
+    and a kernel of separate multiplies and adds is bound there.  ops: FP64
+    operations per launch; ms: the launch's time; floor_ms: the time those
+    operations need on the whole GPU's pipe."""
+    rate = ops / (ms / 1e3) / 1e12
+    return {"ops_per_launch": ops, "achieved": rate, "unit": "T ops/s", "peak": fp64_peak / 2,
+            "frac": rate / (fp64_peak / 2), "floor_ms": ops / (fp64_peak / 2 * 1e12) * 1e3}
+
+
+def remap_pipe_ops(tables, members, fields=6):
+    """FP64 operations of the remap apply: one DMUL per table entry and
+    field, one DADD per entry and field after each destination row's first
+    (the first addition, 0 + p, is done on the integer pipes); tables are
+    (send, recv, coef) per group, each applied to fields x members columns."""
+    return sum((2.0 * len(t[2]) - len(np.unique(t[1]))) * fields * m for t, m in zip(tables, members))
+
+
 def roofline(S, inp, groups, stage_ms, workload, fp64_peak, flux_alone=None, products=6):
     """Per-stage roofline against the copy bandwidth, and the headline: the
     transform chain (spectra pack + Legendre synthesis, inverse FFT, forward
@@ -547,15 +567,6 @@ def roofline(S, inp, groups, stage_ms, workload, fp64_peak, flux_alone=None, pro
     if flux_alone:
         stages["bulk_flux"]["launch"] = ("full grid, timed alone; in the step its grid is capped at %d CTAs "
                                          "(%.4f ms there)" % (flux_alone["step_cta_cap"], flux_alone["ms_in_step"]))
-    # FP64 pipe occupancy beside the flop rate: a DADD, a DMUL and a DFMA
-    # each take one issue slot of the FP64 pipe (2 lanes per SM and clock),
-    # so the pipe's operation rate is half the measured DFMA flop rate and a
-    # kernel of separate multiplies and adds is bound there, at half the
-    # flop peak.
-    def pipe(ops, ms):
-        rate = ops / (ms / 1e3) / 1e12
-        return {"ops_per_launch": ops, "achieved": rate, "unit": "T ops/s", "peak": fp64_peak / 2,
-                "frac": rate / (fp64_peak / 2), "floor_ms": ops / (fp64_peak / 2 * 1e12) * 1e3}
     f64 = FLUX_FP64_INSTR_PER_COLUMN * S["ncol"]
     tf = f64 / (stages["bulk_flux"]["ms"] / 1e3) / 1e12
     stages["bulk_flux"]["fp64"] = {"achieved": tf, "unit": "TFLOP/s", "peak": fp64_peak,
@@ -563,17 +574,18 @@ def roofline(S, inp, groups, stage_ms, workload, fp64_peak, flux_alone=None, pro
                                    "flops_per_launch": f64,
                                    "count": "FP64 pipe work per column from ncu instruction counts (DADD + DMUL "
                                             "+ 2 DFMA), the same for every ice-free column",
-                                   "pipe": pipe(FLUX_FP64_PIPE_OPS_PER_COLUMN * S["ncol"], stages["bulk_flux"]["ms"])}
+                                   "pipe": fp64_pipe(FLUX_FP64_PIPE_OPS_PER_COLUMN * S["ncol"],
+                                                     stages["bulk_flux"]["ms"], fp64_peak)}
     # the remap keeps the reference's separately rounded products and sums
     # (bit-exact): one DMUL per table entry and field, and one DADD per
     # entry and field after each row's first (the first addition, 0 + p, is
     # done on the integer pipes), reported beside its bytes
     rf = sum(2.0 * len(t[2]) * 6 * len(g.members) for g, t in zip(groups, S["tables"]))
-    rops = sum((2.0 * len(t[2]) - len(np.unique(t[1]))) * 6 * len(g.members) for g, t in zip(groups, S["tables"]))
+    rops = remap_pipe_ops(S["tables"], [len(g.members) for g in groups])
     tf = rf / (stages["remap"]["ms"] / 1e3) / 1e12
     stages["remap"]["fp64"] = {"achieved": tf, "unit": "TFLOP/s", "peak": fp64_peak,
                                "peak_source": "measured (dccm_fp64_peak)", "frac": tf / fp64_peak,
-                               "flops_per_launch": rf, "pipe": pipe(rops, stages["remap"]["ms"])}
+                               "flops_per_launch": rf, "pipe": fp64_pipe(rops, stages["remap"]["ms"], fp64_peak)}
     cq = sum(work[n][0] for n in CHAIN)
     cms = sum(stage_ms[names.index(n)] for n in CHAIN)
     ctr = [traffic.get(n) for n in CHAIN]
